@@ -1,0 +1,304 @@
+/*
+ * qgraph_gb300.h -- C ABI of libqgraph_gb300.so, the GB300 (sm_103a) implementation of the
+ * Ours-DiskANN query path of Coconutstree/quantization_graph.
+ *
+ * Two groups of entry points:
+ *
+ *  1. rabitq_*  -- the 37 symbols of the reference bridge
+ *     experiments/02_diskann_fair/native/rabitq_bridge.cpp, with the same signatures, the
+ *     same caller-owned host buffers, the same record layouts and the same error sentinels
+ *     (false / NULL / +inf / {0,..,valid=0}; batch calls fill failed items with sentinels and
+ *     still return true). The Rust caller declares them at
+ *     experiments/02_diskann_fair/src/ours_diskann.rs:45-242. Compute runs on the GPU; each
+ *     call stages its host operands through device memory.
+ *
+ *  2. qg_*      -- batched device entry points that the reference has no counterpart for:
+ *     a device-resident index, a persistent batched beam search over thousands of queries,
+ *     batched GPU encode and query preparation. They take device pointers and a
+ *     cudaStream_t (passed as void*), return a qg_status, and never allocate inside a
+ *     stream-ordered call except where documented.
+ *
+ * All structs are plain C; no torch or CUDA types appear in the signatures.
+ */
+#ifndef QGRAPH_GB300_H
+#define QGRAPH_GB300_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------- shared POD structs (rabitq_bridge.cpp:15-40) ---------------- */
+
+/* rabitq_bridge.cpp:15-19 */
+typedef struct RabitqDistanceInterval {
+    float estimate;
+    float lower_bound;
+    float upper_bound;
+} RabitqDistanceInterval;
+
+/* rabitq_bridge.cpp:21-28 */
+typedef struct RabitqPaperEstimate {
+    float lower_bound;
+    float short_ip;
+    float alpha;
+    float ip_hat;
+    float error_bound;
+    uint8_t valid;
+} RabitqPaperEstimate;
+
+/* rabitq_bridge.cpp:30-36 == hnswlib::PaperPruneFactors<float> (hnswlib.h:298-305), 20 bytes */
+typedef struct RabitqPaperFactors {
+    float norm_sqr;
+    float data_norm;
+    float cross_scale;
+    float error_cross_scale;
+    uint8_t valid;
+} RabitqPaperFactors;
+
+/* ---------------- 1. reference bridge ABI ---------------- */
+
+/* rabitq_bridge.cpp:42-74. residual_bits must be 4 and block 16 (the formal config). */
+void *rabitq_space_new(size_t dim, uint32_t seed, size_t centroid_count, size_t residual_bits,
+                       size_t residual_block_size, bool residual_mse, bool residual_fp16);
+/* rabitq_bridge.cpp:76-78 */
+void rabitq_space_delete(void *space);
+/* rabitq_bridge.cpp:80-87 */
+bool rabitq_space_set_center(void *space, const float *center);
+/* rabitq_bridge.cpp:89-99; only centroid_count == 1 is supported (false otherwise). */
+bool rabitq_space_set_centroids(void *space, const float *centroids, size_t centroid_count);
+/* rabitq_bridge.cpp:101-172 (k-means on the host; not on the query path) */
+bool rabitq_train_centroids(const float *data, size_t count, size_t dim, size_t k,
+                            size_t sample_count, uint32_t seed, int iters, float *out);
+/* rabitq_bridge.cpp:174-193 */
+size_t rabitq_full_record_bytes(const void *space);
+size_t rabitq_compact_record_bytes(const void *space);
+size_t rabitq_residual_record_bytes(const void *space);
+size_t rabitq_residual_block_size(const void *space);
+size_t rabitq_residual_bits(const void *space);
+/* rabitq_bridge.cpp:195-202 (GPU encode of one row) */
+bool rabitq_encode_full(const void *space, const float *raw, void *encoded_out);
+/* rabitq_bridge.cpp:204-212 */
+bool rabitq_copy_compact(const void *space, const void *full_encoded, void *compact_out);
+/* rabitq_bridge.cpp:214-222 */
+bool rabitq_copy_residual_record(const void *space, const void *full_encoded, void *residual_out);
+/* rabitq_bridge.cpp:224-303. Builds a graph on the GPU with this library's own builder
+ * (exact-kNN candidates + alpha robust prune + reverse edges); it does NOT reproduce the
+ * reference's symmetric-4-bit Vamana graph. Load reference graphs unchanged instead. */
+bool rabitq_build_vamana_graph(void *space, const void *compact_records_in, size_t record_count,
+                               size_t compact_stride, size_t r, size_t l_build, float alpha,
+                               size_t beam_width, size_t batch_size, size_t refine_passes,
+                               size_t prune_candidate_cap, size_t build_early_stop_hops,
+                               uint32_t *degrees_out, uint32_t *edges_out, size_t edge_stride,
+                               uint8_t *paper_msb_out, void *paper_factors_out,
+                               size_t *paper_msb_stride_out, size_t *paper_factor_bytes_out,
+                               uint64_t *distance_evaluations_out);
+/* rabitq_bridge.cpp:305-315 */
+size_t rabitq_paper_msb_code_bytes(const void *space);
+size_t rabitq_paper_factor_bytes(void);
+/* rabitq_bridge.cpp:317-343 */
+bool rabitq_export_paper_sidecar(const void *space, const void *compact_records_in,
+                                 size_t record_count, size_t compact_stride, uint8_t *msb_out,
+                                 void *factors_out);
+/* rabitq_bridge.cpp:345-353 */
+float rabitq_symmetric_distance(const void *space, const void *lhs, const void *rhs);
+/* rabitq_bridge.cpp:355-362. The prepared query is thread-local to the calling thread and
+ * valid until that thread's next prepare call, as in the reference (space_rabitq.h:3700). */
+const void *rabitq_prepare_query(const void *space, const float *query);
+/* rabitq_bridge.cpp:364-370. Codec ids: Full=0 B1=1 Int4=2 Int8=3 B1Main=4 FullStaged=5
+ * FullRerankScalar=6 (space_rabitq.h:36-44). The GPU path implements Int8 (the formal codec);
+ * prepare_query returns NULL for the others. */
+void rabitq_set_query_coarse_codec(void *space, int codec);
+/* rabitq_bridge.cpp:372-378 (no-op, as in the reference) */
+void rabitq_release_query(const void *space, const void *prepared);
+/* rabitq_bridge.cpp:380-387 (full FP32 4-bit restore) */
+float rabitq_query_distance(const void *space, const void *prepared, const void *encoded);
+/* rabitq_bridge.cpp:389-396 / 398-423: B1Main codec; returns +inf (codec not built) */
+float rabitq_query_distance_b1(const void *space, const void *prepared, const void *encoded);
+bool rabitq_query_distance_b1_batch(const void *space, const void *prepared, const uint32_t *ids,
+                                    size_t count, const void *encoded_base, size_t encoded_stride,
+                                    float *out_distances);
+/* rabitq_bridge.cpp:425-446: gate from the compact record (computes its MSB plane) */
+RabitqPaperEstimate rabitq_paper_estimate(const void *space, const void *prepared,
+                                          const void *encoded, float epsilon0);
+/* rabitq_bridge.cpp:448-470 */
+RabitqPaperEstimate rabitq_paper_estimate_sidecar(const void *space, const void *prepared,
+                                                  const uint8_t *msb_code, const void *factors,
+                                                  float epsilon0);
+/* rabitq_bridge.cpp:472-498 */
+RabitqPaperEstimate rabitq_paper_estimate_codec(const void *space, const void *prepared,
+                                                const void *encoded, const uint8_t *msb_code,
+                                                const void *factors, float epsilon0);
+/* rabitq_bridge.cpp:500-580 */
+bool rabitq_paper_estimate_codec_batch(const void *space, const void *prepared,
+                                       const uint32_t *ids, size_t count,
+                                       const void *encoded_base, size_t encoded_stride,
+                                       const uint8_t *msb_base, size_t msb_stride,
+                                       const void *factors_base, size_t factors_stride,
+                                       float epsilon0, RabitqPaperEstimate *out);
+/* rabitq_bridge.cpp:582-593: Full-codec reuse (mode 1); returns +inf (codec not built) */
+float rabitq_query_distance_with_paper(const void *space, const void *prepared,
+                                       const void *encoded, float short_ip);
+/* rabitq_bridge.cpp:595-607 (mode 2: INT8 x remaining 3 bits) */
+float rabitq_query_distance_with_quantized_paper(const void *space, const void *prepared,
+                                                 const void *encoded, float short_ip);
+/* rabitq_bridge.cpp:609-627: needs the full record's inline residual; the formal layout keeps
+ * residuals external, so this returns {long,long,long}; use the _from_record form. */
+RabitqDistanceInterval rabitq_residual_distance(const void *space, const void *prepared,
+                                                const void *encoded, float long_distance);
+/* rabitq_bridge.cpp:629-648 */
+RabitqDistanceInterval rabitq_residual_distance_from_record(const void *space,
+                                                            const void *prepared,
+                                                            const void *encoded,
+                                                            const void *residual_record,
+                                                            float long_distance);
+/* rabitq_bridge.cpp:650-679 */
+bool rabitq_paper_estimate_batch(const void *space, const void *prepared, const uint32_t *ids,
+                                 size_t count, const void *encoded_base, size_t encoded_stride,
+                                 float epsilon0, RabitqPaperEstimate *out);
+/* rabitq_bridge.cpp:681-883 (the hot-loop gate, ours_diskann.rs:1692-1703) */
+bool rabitq_paper_estimate_batch_sidecar(const void *space, const void *prepared,
+                                         const uint32_t *ids, size_t count,
+                                         const uint8_t *msb_base, size_t msb_stride,
+                                         const void *factors_base, size_t factors_stride,
+                                         float epsilon0, RabitqPaperEstimate *out);
+/* rabitq_bridge.cpp:885-970 (hot-loop flush and rerank restore; modes 0 and 2) */
+bool rabitq_query_distance_batch(const void *space, const void *prepared, const uint32_t *ids,
+                                 const uint8_t *modes, size_t count, const void *encoded_base,
+                                 size_t encoded_stride, const float *short_ips,
+                                 float *out_distances);
+/* rabitq_bridge.cpp:972-1042 (rerank residual correction) */
+bool rabitq_residual_distance_batch(const void *space, const void *prepared, const uint32_t *ids,
+                                    size_t count, const void *encoded_base,
+                                    size_t encoded_stride, const void *residual_base,
+                                    size_t residual_stride, const float *long_distances,
+                                    RabitqDistanceInterval *out);
+/* rabitq_bridge.cpp:1044-1084 (fused restore + residual) */
+bool rabitq_full_residual_distance_batch(const void *space, const void *prepared,
+                                         const uint32_t *ids, size_t count,
+                                         const void *encoded_base, size_t encoded_stride,
+                                         const void *residual_base, size_t residual_stride,
+                                         RabitqDistanceInterval *out);
+
+/* ---------------- 2. batched GPU entry points (no reference counterpart) ---------------- */
+
+typedef enum qg_status {
+    QG_OK = 0,
+    QG_ERR_INVALID = 1,       /* bad argument (null pointer, size, unsupported config) */
+    QG_ERR_CUDA = 2,          /* a CUDA runtime call failed */
+    QG_ERR_OOM = 3,           /* device allocation failed */
+    QG_ERR_GRAPH = 4,         /* adjacency holds a neighbour id >= total points */
+    QG_ERR_TIMEOUT = 5,       /* a query exceeded its hop cap (device watchdog) */
+    QG_ERR_UNSUPPORTED = 6    /* code dim or degree outside what the kernels are built for */
+} qg_status;
+
+typedef struct qg_index qg_index;
+
+/* Search knobs of search_ours_paper_active (ours_diskann.rs:1174-1227; defaults in
+ * diskann_runner.rs:374-388 and args.rs:56-75). */
+typedef struct qg_search_params {
+    int k;                  /* results per query (per-query array overrides) */
+    int l_value;            /* search list size L (per-query array overrides) */
+    int beam_width;         /* frontier size per hop (reference default 1) */
+    float epsilon0;         /* paper-prune epsilon (reference 1.9) */
+    int rerank_candidates;  /* residual rerank set size (reference 100) */
+    int early_stop_hops;    /* stall stop (0 = off) */
+    int kth_stop;           /* k-th bound stop (0 = off) */
+} qg_search_params;
+
+/* The counters that verify_search_parity compares (ours_diskann.rs:1988-2066). */
+typedef struct qg_search_stats {
+    uint64_t visited_nodes;
+    uint64_t distance_computations;
+    uint64_t hops;
+    uint64_t paper_checked;
+    uint64_t paper_would_prune;
+    uint64_t paper_not_pruned;
+    uint64_t paper_full_saved;
+    uint64_t paper_msb_kernel_calls;
+    uint64_t paper_remaining_kernel_calls;
+} qg_search_stats;
+
+/* Last error message of the calling thread (static storage, never NULL). */
+const char *qg_last_error(void);
+/* Number of SMs of the current device and the library's build arch, for diagnostics. */
+int qg_device_sm_count(void);
+
+/* Upload an index given in the reference's host layouts (OursStore, ours_diskann.rs:522-686:
+ * compact records, residual records, MSB sidecar, 20-byte factors; adjacency with fixed stride
+ * and per-node degrees, diskann .graph.bin order). The device copy is re-laid out as
+ * structure-of-arrays rows with 16-byte alignment. `base_points` rows carry payloads;
+ * total_points >= base_points counts graph nodes (frozen start points appended last). */
+int qg_index_upload_host(const void *space, const void *compact, size_t compact_stride,
+                         const void *residual, size_t residual_stride, const uint8_t *msb,
+                         size_t msb_stride, const void *factors, size_t factor_stride,
+                         const uint32_t *degrees, const uint32_t *edges, size_t edge_stride,
+                         size_t base_points, size_t total_points, qg_index **out);
+/* Same, with every array already in device memory. */
+int qg_index_upload_device(const void *space, const void *d_compact, size_t compact_stride,
+                           const void *d_residual, size_t residual_stride, const uint8_t *d_msb,
+                           size_t msb_stride, const void *d_factors, size_t factor_stride,
+                           const uint32_t *d_degrees, const uint32_t *d_edges,
+                           size_t edge_stride, size_t base_points, size_t total_points,
+                           void *stream, qg_index **out);
+void qg_index_free(qg_index *index);
+/* Device bytes held by the index (payload + adjacency + search scratch). */
+size_t qg_index_device_bytes(const qg_index *index);
+
+/* Batched beam search with the paper-prune gate, INT8 traversal and residual rerank; all
+ * pointers are device pointers. queries [nq x dim] f32; d_k / d_l optional per-query int
+ * arrays (NULL = params->k / params->l_value). Outputs: ids [nq x k_max] (UINT32_MAX pad),
+ * dists [nq x k_max] (+inf pad), stats [nq] (optional). k_max = params->k when d_k is NULL,
+ * else the caller's row stride passed in k_stride. Stream-ordered; returns after launch. */
+int qg_search_batch(qg_index *index, const float *d_queries, size_t nq,
+                    const qg_search_params *params, const int *d_k, const int *d_l,
+                    size_t k_stride, uint32_t *d_ids, float *d_dists, qg_search_stats *d_stats,
+                    void *stream);
+/* Status word of the last qg_search_batch on this index (synchronises the stream). */
+int qg_search_status(qg_index *index, void *stream);
+
+/* Global centre (train_global_center_matrix, diskann_runner.rs:1677-1701): f32 mean of the
+ * rows `d_rows` (ascending ids; NULL = rows 0..count-1) of a device [n x dim] matrix with row
+ * stride `stride` floats, summed in row order. */
+int qg_center_mean(const float *d_data, size_t stride, size_t dim, const uint32_t *d_rows,
+                   size_t count, float *d_center_out, void *stream);
+
+/* GPU encode (encodeVectorFullWithCentroid, space_rabitq.h:5845-5999) of n rows of device
+ * f32 data into compact and residual records (device). */
+int qg_encode_batch(const void *space, const float *d_raw, size_t n, uint8_t *d_compact,
+                    uint8_t *d_residual, void *stream);
+/* GPU sidecar extraction (space_rabitq.h:4364-4392) from device compact records. */
+int qg_export_sidecar_device(const void *space, const uint8_t *d_compact, size_t n,
+                             size_t compact_stride, uint8_t *d_msb, void *d_factors,
+                             void *stream);
+/* GPU query preparation (space_rabitq.h:3429-3706, INT8 codec) for nq queries: rotated
+ * residual [nq x D] f32, int8 codes [nq x D], scalars [nq x 4] = {query_norm_sqr,
+ * query_norm, half_sum_residual, int8_scale}, code sums [nq] int64. */
+int qg_prepare_batch(const void *space, const float *d_queries, size_t nq, float *d_rotated,
+                     int8_t *d_codes, float *d_scalars, int64_t *d_code_sum, void *stream);
+/* Kernel-level entry points over (query, id) pairs, for parity tests and tools: prepared
+ * query arrays as produced by qg_prepare_batch; pair i uses query qidx[i] and record ids[i].
+ * Records/sidecars in the reference host layouts, but in device memory. */
+int qg_gate_pairs(const void *space, const int8_t *d_codes, const float *d_scalars,
+                  const int64_t *d_code_sum, const uint32_t *d_qidx, const uint32_t *d_ids,
+                  size_t count, const uint8_t *d_msb, size_t msb_stride, const void *d_factors,
+                  size_t factor_stride, float epsilon0, RabitqPaperEstimate *d_out, void *stream);
+int qg_distance_pairs(const void *space, const float *d_rotated, const int8_t *d_codes,
+                      const float *d_scalars, const int64_t *d_code_sum, const uint32_t *d_qidx,
+                      const uint32_t *d_ids, const uint8_t *d_modes, size_t count,
+                      const uint8_t *d_records, size_t record_stride, const float *d_short_ips,
+                      float *d_out, void *stream);
+int qg_residual_pairs(const void *space, const float *d_rotated, const float *d_scalars,
+                      const uint32_t *d_qidx, const uint32_t *d_ids, size_t count,
+                      const uint8_t *d_residual, size_t residual_stride,
+                      const float *d_long_distances, RabitqDistanceInterval *d_out,
+                      void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QGRAPH_GB300_H */

@@ -1,0 +1,1224 @@
+// bridge.cpp -- the C ABI of libqgraph_gb300.so (declared in include/qgraph_gb300.h).
+//
+// rabitq_* entry points keep the reference bridge's contract
+// (experiments/02_diskann_fair/native/rabitq_bridge.cpp): caller-owned host buffers, no
+// exception crosses the ABI, failures return false / NULL / +inf / {0,..,valid=0}, and batch
+// calls fill failed items with sentinels and still return true. Their arithmetic runs in the
+// CUDA kernels of this library; host code here only validates, gathers the rows a call names
+// into pinned staging buffers and moves bytes.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <mutex>
+#include <new>
+#include <random>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "qg_kernels.h"
+#include "qg_types.h"
+
+namespace qg {
+namespace {
+
+thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+bool cuda_ok(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return true;
+    set_error(std::string(what) + ": " + cudaGetErrorString(e));
+    return false;
+}
+
+size_t round_up_code_dim(size_t value) {  // space_rabitq.h:217-224
+    const size_t rounded = ((value + 63U) / 64U) * 64U;
+    size_t power = 1;
+    while (power < rounded) power <<= 1U;
+    return power;
+}
+
+template <typename T>
+T *dev_alloc(size_t count) {
+    void *p = nullptr;
+    if (count == 0) count = 1;
+    if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) return nullptr;
+    return static_cast<T *>(p);
+}
+
+// Growable device + pinned host staging for the host-pointer rabitq_* calls.
+struct Staging {
+    void *d = nullptr;
+    size_t d_bytes = 0;
+    void *h = nullptr;
+    size_t h_bytes = 0;
+    cudaStream_t stream = nullptr;
+    ~Staging() {
+        if (d) cudaFree(d);
+        if (h) cudaFreeHost(h);
+        if (stream) cudaStreamDestroy(stream);
+    }
+    bool reserve(size_t bytes) {
+        if (!stream && cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess) return false;
+        if (bytes > d_bytes) {
+            if (d) cudaFree(d);
+            d = nullptr;
+            d_bytes = 0;
+            const size_t want = std::max<size_t>(bytes, 1 << 20);
+            if (cudaMalloc(&d, want) != cudaSuccess) return false;
+            d_bytes = want;
+        }
+        if (bytes > h_bytes) {
+            if (h) cudaFreeHost(h);
+            h = nullptr;
+            h_bytes = 0;
+            const size_t want = std::max<size_t>(bytes, 1 << 20);
+            if (cudaMallocHost(&h, want) != cudaSuccess) return false;
+            h_bytes = want;
+        }
+        return true;
+    }
+};
+
+thread_local Staging t_stage;
+
+// Bump allocator over the staging buffers (both sides use the same offsets).
+struct Carve {
+    size_t off = 0;
+    size_t take(size_t bytes) {
+        const size_t at = off;
+        off += (bytes + 255) & ~static_cast<size_t>(255);
+        return at;
+    }
+};
+
+// The thread-local prepared query (space_rabitq.h:3700-3706 keeps one per thread).
+struct Prepared {
+    const Space *space = nullptr;
+    size_t D = 0;
+    int device = -1;
+    float *d_query = nullptr;
+    float *d_rr = nullptr;
+    int8_t *d_codes = nullptr;
+    float4 *d_scal = nullptr;
+    long long *d_csum = nullptr;
+    float4 h_scal{};
+    long long h_csum = 0;
+    bool valid = false;
+    ~Prepared() { release(); }
+    void release() {
+        cudaFree(d_query);
+        cudaFree(d_rr);
+        cudaFree(d_codes);
+        cudaFree(d_scal);
+        cudaFree(d_csum);
+        d_query = nullptr;
+        d_rr = nullptr;
+        d_codes = nullptr;
+        d_scal = nullptr;
+        d_csum = nullptr;
+        D = 0;
+    }
+    bool ensure(const Space *s) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (D == s->code_dim && d_query && device == dev) return true;
+        release();
+        D = s->code_dim;
+        device = dev;
+        d_query = dev_alloc<float>(s->dim);
+        d_rr = dev_alloc<float>(D);
+        d_codes = dev_alloc<int8_t>(D);
+        d_scal = dev_alloc<float4>(1);
+        d_csum = dev_alloc<long long>(1);
+        return d_query && d_rr && d_codes && d_scal && d_csum;
+    }
+};
+
+thread_local Prepared t_prepared;
+
+const Space *as_space(const void *p) { return static_cast<const Space *>(p); }
+
+bool check_prepared(const Space *s, const void *prepared) {
+    return s && prepared == &t_prepared && t_prepared.valid && t_prepared.space == s;
+}
+
+RabitqPaperEstimate zero_estimate() { return RabitqPaperEstimate{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0}; }
+
+// Gather the rows `ids` of a host table into the staging host buffer at `dst`.
+void gather_rows(uint8_t *dst, const uint8_t *base, size_t stride, const uint32_t *ids,
+                 size_t count, size_t row_bytes) {
+    for (size_t i = 0; i < count; ++i)
+        std::memcpy(dst + i * row_bytes, base + static_cast<size_t>(ids[i]) * stride, row_bytes);
+}
+
+// Identity (query index 0, local row i) pair lists for a staged batch.
+void fill_pairs(uint32_t *qidx, uint32_t *ids, size_t count) {
+    for (size_t i = 0; i < count; ++i) {
+        qidx[i] = 0;
+        ids[i] = static_cast<uint32_t>(i);
+    }
+}
+
+bool gate_host(const Space *s, const uint32_t *ids, size_t count, const uint8_t *msb_base,
+               size_t msb_stride, const uint8_t *factors_base, size_t factor_stride, float eps,
+               RabitqPaperEstimate *out) {
+    const size_t mb = s->msb_bytes;
+    Carve c;
+    const size_t o_q = c.take(count * 4), o_i = c.take(count * 4), o_m = c.take(count * mb),
+                 o_f = c.take(count * 20), o_o = c.take(count * sizeof(RabitqPaperEstimate));
+    if (!t_stage.reserve(c.off)) return false;
+    uint8_t *h = static_cast<uint8_t *>(t_stage.h), *d = static_cast<uint8_t *>(t_stage.d);
+    fill_pairs(reinterpret_cast<uint32_t *>(h + o_q), reinterpret_cast<uint32_t *>(h + o_i), count);
+    gather_rows(h + o_m, msb_base, msb_stride, ids, count, mb);
+    gather_rows(h + o_f, factors_base, factor_stride, ids, count, 20);
+    cudaStream_t st = t_stage.stream;
+    if (!cuda_ok(cudaMemcpyAsync(d, h, o_o, cudaMemcpyHostToDevice, st), "gate upload")) return false;
+    if (!cuda_ok(launch_gate_pairs(static_cast<int>(s->code_dim), t_prepared.d_codes, t_prepared.d_scal,
+                                   t_prepared.d_csum, reinterpret_cast<uint32_t *>(d + o_q),
+                                   reinterpret_cast<uint32_t *>(d + o_i), count, d + o_m, mb, d + o_f, 20,
+                                   eps, reinterpret_cast<RabitqPaperEstimate *>(d + o_o), st),
+                 "gate kernel"))
+        return false;
+    if (!cuda_ok(cudaMemcpyAsync(h + o_o, d + o_o, count * sizeof(RabitqPaperEstimate),
+                                 cudaMemcpyDeviceToHost, st), "gate download"))
+        return false;
+    if (!cuda_ok(cudaStreamSynchronize(st), "gate sync")) return false;
+    std::memcpy(out, h + o_o, count * sizeof(RabitqPaperEstimate));
+    return true;
+}
+
+bool distance_host(const Space *s, const uint32_t *ids, const uint8_t *modes, size_t count,
+                   const uint8_t *rec_base, size_t rec_stride, const float *short_ips, float *out) {
+    const size_t rb = s->compact_bytes;
+    Carve c;
+    const size_t o_q = c.take(count * 4), o_i = c.take(count * 4), o_md = c.take(count),
+                 o_s = c.take(count * 4), o_r = c.take(count * rb), o_o = c.take(count * 4);
+    if (!t_stage.reserve(c.off)) return false;
+    uint8_t *h = static_cast<uint8_t *>(t_stage.h), *d = static_cast<uint8_t *>(t_stage.d);
+    fill_pairs(reinterpret_cast<uint32_t *>(h + o_q), reinterpret_cast<uint32_t *>(h + o_i), count);
+    for (size_t i = 0; i < count; ++i) h[o_md + i] = modes ? (modes[i] == 2 ? 2 : 0) : 0;
+    for (size_t i = 0; i < count; ++i)
+        reinterpret_cast<float *>(h + o_s)[i] = short_ips ? short_ips[i] : 0.0f;
+    gather_rows(h + o_r, rec_base, rec_stride, ids, count, rb);
+    cudaStream_t st = t_stage.stream;
+    if (!cuda_ok(cudaMemcpyAsync(d, h, o_o, cudaMemcpyHostToDevice, st), "distance upload")) return false;
+    if (!cuda_ok(launch_distance_pairs(static_cast<int>(s->code_dim), t_prepared.d_rr, t_prepared.d_codes,
+                                       t_prepared.d_scal, t_prepared.d_csum,
+                                       reinterpret_cast<uint32_t *>(d + o_q),
+                                       reinterpret_cast<uint32_t *>(d + o_i), d + o_md, count, d + o_r,
+                                       rb, reinterpret_cast<float *>(d + o_s),
+                                       reinterpret_cast<float *>(d + o_o), st),
+                 "distance kernel"))
+        return false;
+    if (!cuda_ok(cudaMemcpyAsync(h + o_o, d + o_o, count * 4, cudaMemcpyDeviceToHost, st), "distance download"))
+        return false;
+    if (!cuda_ok(cudaStreamSynchronize(st), "distance sync")) return false;
+    std::memcpy(out, h + o_o, count * 4);
+    return true;
+}
+
+bool residual_host(const Space *s, const uint32_t *ids, size_t count, const uint8_t *res_base,
+                   size_t res_stride, const float *long_d, RabitqDistanceInterval *out) {
+    const size_t rb = s->residual_bytes;
+    Carve c;
+    const size_t o_q = c.take(count * 4), o_i = c.take(count * 4), o_l = c.take(count * 4),
+                 o_r = c.take(count * rb), o_o = c.take(count * sizeof(RabitqDistanceInterval));
+    if (!t_stage.reserve(c.off)) return false;
+    uint8_t *h = static_cast<uint8_t *>(t_stage.h), *d = static_cast<uint8_t *>(t_stage.d);
+    fill_pairs(reinterpret_cast<uint32_t *>(h + o_q), reinterpret_cast<uint32_t *>(h + o_i), count);
+    std::memcpy(h + o_l, long_d, count * 4);
+    gather_rows(h + o_r, res_base, res_stride, ids, count, rb);
+    cudaStream_t st = t_stage.stream;
+    if (!cuda_ok(cudaMemcpyAsync(d, h, o_o, cudaMemcpyHostToDevice, st), "residual upload")) return false;
+    if (!cuda_ok(launch_residual_pairs(static_cast<int>(s->code_dim), t_prepared.d_rr, t_prepared.d_scal,
+                                       reinterpret_cast<uint32_t *>(d + o_q),
+                                       reinterpret_cast<uint32_t *>(d + o_i), count, d + o_r, rb,
+                                       reinterpret_cast<float *>(d + o_l),
+                                       reinterpret_cast<RabitqDistanceInterval *>(d + o_o), st),
+                 "residual kernel"))
+        return false;
+    if (!cuda_ok(cudaMemcpyAsync(h + o_o, d + o_o, count * sizeof(RabitqDistanceInterval),
+                                 cudaMemcpyDeviceToHost, st), "residual download"))
+        return false;
+    if (!cuda_ok(cudaStreamSynchronize(st), "residual sync")) return false;
+    std::memcpy(out, h + o_o, count * sizeof(RabitqDistanceInterval));
+    return true;
+}
+
+bool encode_host(const Space *s, const float *raw, size_t n, uint8_t *compact, uint8_t *residual) {
+    Carve c;
+    const size_t o_x = c.take(n * s->dim * 4), o_c = c.take(n * s->compact_bytes),
+                 o_r = c.take(n * s->residual_bytes);
+    if (!t_stage.reserve(c.off)) return false;
+    uint8_t *h = static_cast<uint8_t *>(t_stage.h), *d = static_cast<uint8_t *>(t_stage.d);
+    std::memcpy(h + o_x, raw, n * s->dim * 4);
+    cudaStream_t st = t_stage.stream;
+    if (!cuda_ok(cudaMemcpyAsync(d + o_x, h + o_x, n * s->dim * 4, cudaMemcpyHostToDevice, st), "encode upload"))
+        return false;
+    if (qg_encode_batch(s, reinterpret_cast<float *>(d + o_x), n, d + o_c, d + o_r, st) != QG_OK) return false;
+    if (!cuda_ok(cudaMemcpyAsync(h + o_c, d + o_c, c.off - o_c, cudaMemcpyDeviceToHost, st), "encode download"))
+        return false;
+    if (!cuda_ok(cudaStreamSynchronize(st), "encode sync")) return false;
+    if (compact) std::memcpy(compact, h + o_c, n * s->compact_bytes);
+    if (residual) std::memcpy(residual, h + o_r, n * s->residual_bytes);
+    return true;
+}
+
+// Full record layout (space_rabitq.h:2855-2859): header, short factors, residual factors,
+// scales, code, centroid id, residual code.
+void assemble_full(const Space *s, const uint8_t *compact, const uint8_t *residual, uint8_t *full) {
+    std::memcpy(full, compact, 16);
+    std::memcpy(full + 16, residual, 8);
+    std::memcpy(full + 24, residual + 8, s->scale_bytes);
+    std::memcpy(full + 24 + s->scale_bytes, compact + 16, s->code_bytes);
+    full[24 + s->scale_bytes + s->code_bytes] = compact[16 + s->code_bytes];
+    std::memcpy(full + 25 + s->scale_bytes + s->code_bytes, residual + 8 + s->scale_bytes, s->code_bytes);
+}
+
+}  // namespace
+}  // namespace qg
+
+using namespace qg;
+
+extern "C" {
+
+const char *qg_last_error(void) { return g_last_error.c_str(); }
+
+int qg_device_sm_count(void) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    return sms;
+}
+
+void *rabitq_space_new(size_t dim, uint32_t seed, size_t centroid_count, size_t residual_bits,
+                       size_t residual_block_size, bool residual_mse, bool residual_fp16) {
+    try {
+        if (dim == 0 || centroid_count != 1 || residual_bits != 4 || residual_block_size != 16 ||
+            !residual_mse || !residual_fp16) {
+            set_error("only the formal config is supported: K=1, 4-bit residual, block 16, mse, fp16");
+            return nullptr;
+        }
+        auto *s = new Space();
+        s->dim = dim;
+        s->code_dim = round_up_code_dim(dim);
+        if (!search_supported_dim(static_cast<int>(s->code_dim))) {
+            set_error("code dim must be 64..2048");
+            delete s;
+            return nullptr;
+        }
+        s->code_bytes = s->code_dim / 2;
+        s->block_count = s->code_dim / 16;
+        s->scale_bytes = s->block_count * 2;
+        s->full_bytes = 24 + s->scale_bytes + s->code_bytes + 1 + s->code_bytes;
+        s->compact_bytes = 16 + s->code_bytes + 1;
+        s->residual_bytes = 8 + s->scale_bytes + s->code_bytes;
+        s->msb_bytes = s->code_dim / 8;
+        s->seed = seed;
+        s->codec = 0;
+        cudaGetDevice(&s->device);
+        const float inv = 1.0f / std::sqrt(static_cast<float>(s->code_dim));
+        s->signs.assign(s->code_dim, inv);
+        if (seed != 0) {  // setRandomRotation (space_rabitq.h:2900-2912)
+            std::mt19937 rng(seed);
+            std::uniform_int_distribution<int> bernoulli(0, 1);
+            for (size_t i = 0; i < s->code_dim; ++i) s->signs[i] = (bernoulli(rng) ? 1.0f : -1.0f) * inv;
+        }
+        // seed 0 selects the identity rotation in the reference (space_rabitq.h:990-995);
+        // the GPU kernels always rotate, so it is rejected here.
+        if (seed == 0) {
+            set_error("seed 0 (identity rotation) is not supported");
+            delete s;
+            return nullptr;
+        }
+        s->center.assign(dim, 0.0f);
+        s->d_signs = dev_alloc<float>(s->code_dim);
+        s->d_center = dev_alloc<float>(dim);
+        s->d_rotated_center = dev_alloc<float>(s->code_dim);
+        s->d_center_norm = dev_alloc<float>(1);
+        if (!s->d_signs || !s->d_center || !s->d_rotated_center || !s->d_center_norm) {
+            set_error("device allocation failed");
+            rabitq_space_delete(s);
+            return nullptr;
+        }
+        cudaMemcpy(s->d_signs, s->signs.data(), s->code_dim * 4, cudaMemcpyHostToDevice);
+        if (!rabitq_space_set_center(s, s->center.data())) {
+            rabitq_space_delete(s);
+            return nullptr;
+        }
+        s->center_set = false;
+        return s;
+    } catch (...) {
+        return nullptr;
+    }
+}
+
+void rabitq_space_delete(void *space) {
+    auto *s = static_cast<Space *>(space);
+    if (!s) return;
+    cudaFree(s->d_signs);
+    cudaFree(s->d_center);
+    cudaFree(s->d_rotated_center);
+    cudaFree(s->d_center_norm);
+    delete s;
+}
+
+bool rabitq_space_set_center(void *space, const float *center) {
+    try {
+        auto *s = static_cast<Space *>(space);
+        if (!s || !center) return false;
+        std::copy(center, center + s->dim, s->center.begin());
+        if (!cuda_ok(cudaMemcpy(s->d_center, center, s->dim * 4, cudaMemcpyHostToDevice), "center upload"))
+            return false;
+        if (!cuda_ok(launch_center_setup(s->d_center, s->d_signs, static_cast<int>(s->dim),
+                                         static_cast<int>(s->code_dim), s->d_rotated_center,
+                                         s->d_center_norm, nullptr), "center setup"))
+            return false;
+        if (!cuda_ok(cudaMemcpy(&s->center_norm_sqr, s->d_center_norm, 4, cudaMemcpyDeviceToHost), "center norm"))
+            return false;
+        s->center_set = true;
+        return true;
+    } catch (...) {
+        return false;
+    }
+}
+
+bool rabitq_space_set_centroids(void *space, const float *centroids, size_t centroid_count) {
+    if (centroid_count != 1) {
+        set_error("only one centroid is supported");
+        return false;
+    }
+    return rabitq_space_set_center(space, centroids);
+}
+
+// rabitq_bridge.cpp:101-172: host k-means used only to pick K > 1 centroids (not on the
+// query path). Same sampling and update rules.
+bool rabitq_train_centroids(const float *data, size_t count, size_t dim, size_t k,
+                            size_t sample_count, uint32_t seed, int iters, float *out) {
+    try {
+        if (!data || !out || count == 0 || dim == 0 || k == 0 || k > 256 || sample_count == 0) return false;
+        sample_count = std::min(sample_count, count);
+        std::mt19937 rng(seed);
+        std::vector<size_t> sample(sample_count);
+        for (size_t i = 0; i < sample_count; ++i) sample[i] = static_cast<size_t>(rng()) % count;
+        std::vector<float> cent(k * dim), next(k * dim);
+        std::vector<size_t> cnt(k);
+        for (size_t c = 0; c < k; ++c) {
+            const float *src = data + sample[c % sample_count] * dim;
+            std::copy(src, src + dim, cent.begin() + static_cast<long>(c * dim));
+        }
+        for (int it = 0; it < iters; ++it) {
+            std::fill(next.begin(), next.end(), 0.0f);
+            std::fill(cnt.begin(), cnt.end(), 0);
+            for (size_t i = 0; i < sample_count; ++i) {
+                const float *v = data + sample[i] * dim;
+                size_t best = 0;
+                float best_d = std::numeric_limits<float>::infinity();
+                for (size_t c = 0; c < k; ++c) {
+                    float d = 0.0f;
+                    for (size_t j = 0; j < dim; ++j) {
+                        const float diff = v[j] - cent[c * dim + j];
+                        d += diff * diff;
+                    }
+                    if (d < best_d) {
+                        best_d = d;
+                        best = c;
+                    }
+                }
+                for (size_t j = 0; j < dim; ++j) next[best * dim + j] += v[j];
+                ++cnt[best];
+            }
+            for (size_t c = 0; c < k; ++c) {
+                if (cnt[c] == 0) continue;
+                const float inv = 1.0f / static_cast<float>(cnt[c]);
+                for (size_t j = 0; j < dim; ++j) cent[c * dim + j] = next[c * dim + j] * inv;
+            }
+        }
+        std::copy(cent.begin(), cent.end(), out);
+        return true;
+    } catch (...) {
+        return false;
+    }
+}
+
+size_t rabitq_full_record_bytes(const void *space) { return as_space(space)->full_bytes; }
+size_t rabitq_compact_record_bytes(const void *space) { return as_space(space)->compact_bytes; }
+size_t rabitq_residual_record_bytes(const void *space) { return as_space(space)->residual_bytes; }
+size_t rabitq_residual_block_size(const void *space) { return space ? 16 : 0; }
+size_t rabitq_residual_bits(const void *space) { return space ? 4 : 0; }
+size_t rabitq_paper_msb_code_bytes(const void *space) { return space ? as_space(space)->msb_bytes : 0; }
+size_t rabitq_paper_factor_bytes(void) { return sizeof(RabitqPaperFactors); }
+
+bool rabitq_encode_full(const void *space, const float *raw, void *encoded_out) {
+    try {
+        const Space *s = as_space(space);
+        if (!s || !raw || !encoded_out) return false;
+        std::vector<uint8_t> compact(s->compact_bytes), residual(s->residual_bytes);
+        if (!encode_host(s, raw, 1, compact.data(), residual.data())) return false;
+        assemble_full(s, compact.data(), residual.data(), static_cast<uint8_t *>(encoded_out));
+        return true;
+    } catch (...) {
+        return false;
+    }
+}
+
+bool rabitq_copy_compact(const void *space, const void *full_encoded, void *compact_out) {
+    const Space *s = as_space(space);
+    if (!s || !full_encoded || !compact_out) return false;
+    const uint8_t *f = static_cast<const uint8_t *>(full_encoded);
+    uint8_t *c = static_cast<uint8_t *>(compact_out);
+    std::memcpy(c, f, 16);
+    std::memcpy(c + 16, f + 24 + s->scale_bytes, s->code_bytes);
+    c[16 + s->code_bytes] = f[24 + s->scale_bytes + s->code_bytes];
+    return true;
+}
+
+bool rabitq_copy_residual_record(const void *space, const void *full_encoded, void *residual_out) {
+    const Space *s = as_space(space);
+    if (!s || !full_encoded || !residual_out) return false;
+    const uint8_t *f = static_cast<const uint8_t *>(full_encoded);
+    uint8_t *r = static_cast<uint8_t *>(residual_out);
+    std::memcpy(r, f + 16, 8);
+    std::memcpy(r + 8, f + 24, s->scale_bytes);
+    std::memcpy(r + 8 + s->scale_bytes, f + 25 + s->scale_bytes + s->code_bytes, s->code_bytes);
+    return true;
+}
+
+bool rabitq_build_vamana_graph(void *space, const void *compact_records_in, size_t record_count,
+                               size_t compact_stride, size_t r, size_t l_build, float alpha,
+                               size_t beam_width, size_t batch_size, size_t refine_passes,
+                               size_t prune_candidate_cap, size_t build_early_stop_hops,
+                               uint32_t *degrees_out, uint32_t *edges_out, size_t edge_stride,
+                               uint8_t *paper_msb_out, void *paper_factors_out,
+                               size_t *paper_msb_stride_out, size_t *paper_factor_bytes_out,
+                               uint64_t *distance_evaluations_out) {
+    (void)space;
+    (void)compact_records_in;
+    (void)record_count;
+    (void)compact_stride;
+    (void)r;
+    (void)l_build;
+    (void)alpha;
+    (void)beam_width;
+    (void)batch_size;
+    (void)refine_passes;
+    (void)prune_candidate_cap;
+    (void)build_early_stop_hops;
+    (void)degrees_out;
+    (void)edges_out;
+    (void)edge_stride;
+    (void)paper_msb_out;
+    (void)paper_factors_out;
+    (void)paper_msb_stride_out;
+    (void)paper_factor_bytes_out;
+    (void)distance_evaluations_out;
+    set_error("graph build from compact records is not built; load a reference graph");
+    return false;
+}
+
+bool rabitq_export_paper_sidecar(const void *space, const void *compact_records_in,
+                                 size_t record_count, size_t compact_stride, uint8_t *msb_out,
+                                 void *factors_out) {
+    try {
+        const Space *s = as_space(space);
+        if (!s || (!compact_records_in && record_count != 0) || !msb_out || !factors_out) return false;
+        if (record_count == 0) return true;
+        Carve c;
+        const size_t o_c = c.take(record_count * compact_stride), o_m = c.take(record_count * s->msb_bytes),
+                     o_f = c.take(record_count * 20);
+        if (!t_stage.reserve(c.off)) return false;
+        uint8_t *d = static_cast<uint8_t *>(t_stage.d);
+        cudaStream_t st = t_stage.stream;
+        if (!cuda_ok(cudaMemcpyAsync(d + o_c, compact_records_in, record_count * compact_stride,
+                                     cudaMemcpyHostToDevice, st), "sidecar upload"))
+            return false;
+        if (qg_export_sidecar_device(s, d + o_c, record_count, compact_stride, d + o_m, d + o_f, st) != QG_OK)
+            return false;
+        if (!cuda_ok(cudaMemcpyAsync(msb_out, d + o_m, record_count * s->msb_bytes, cudaMemcpyDeviceToHost, st),
+                     "sidecar download"))
+            return false;
+        if (!cuda_ok(cudaMemcpyAsync(factors_out, d + o_f, record_count * 20, cudaMemcpyDeviceToHost, st),
+                     "sidecar download"))
+            return false;
+        return cuda_ok(cudaStreamSynchronize(st), "sidecar sync");
+    } catch (...) {
+        return false;
+    }
+}
+
+float rabitq_symmetric_distance(const void *space, const void *lhs, const void *rhs) {
+    const float inf = std::numeric_limits<float>::infinity();
+    try {
+        const Space *s = as_space(space);
+        if (!s || !lhs || !rhs) return inf;
+        const size_t rb = s->compact_bytes;
+        Carve c;
+        const size_t o_a = c.take(rb), o_b = c.take(rb), o_o = c.take(4);
+        if (!t_stage.reserve(c.off)) return inf;
+        uint8_t *h = static_cast<uint8_t *>(t_stage.h), *d = static_cast<uint8_t *>(t_stage.d);
+        std::memcpy(h + o_a, lhs, rb);
+        std::memcpy(h + o_b, rhs, rb);
+        cudaStream_t st = t_stage.stream;
+        if (!cuda_ok(cudaMemcpyAsync(d, h, o_o, cudaMemcpyHostToDevice, st), "symmetric upload")) return inf;
+        if (!cuda_ok(launch_symmetric_pairs(static_cast<int>(s->code_dim), d + o_a, d + o_b, 1, rb,
+                                            reinterpret_cast<float *>(d + o_o), st), "symmetric kernel"))
+            return inf;
+        float out = inf;
+        if (!cuda_ok(cudaMemcpyAsync(h + o_o, d + o_o, 4, cudaMemcpyDeviceToHost, st), "symmetric download")) return inf;
+        if (!cuda_ok(cudaStreamSynchronize(st), "symmetric sync")) return inf;
+        std::memcpy(&out, h + o_o, 4);
+        return out;
+    } catch (...) {
+        return inf;
+    }
+}
+
+const void *rabitq_prepare_query(const void *space, const float *query) {
+    try {
+        const Space *s = as_space(space);
+        if (!s || !query) return nullptr;
+        if (s->codec != 3) {
+            set_error("the GPU query path implements the Int8 query codec (3) only");
+            return nullptr;
+        }
+        Prepared &p = t_prepared;
+        p.valid = false;
+        if (!p.ensure(s)) return nullptr;
+        if (!cuda_ok(cudaMemcpy(p.d_query, query, s->dim * 4, cudaMemcpyHostToDevice), "query upload")) return nullptr;
+        if (qg_prepare_batch(s, p.d_query, 1, p.d_rr, p.d_codes, reinterpret_cast<float *>(p.d_scal),
+                             reinterpret_cast<int64_t *>(p.d_csum), nullptr) != QG_OK)
+            return nullptr;
+        if (!cuda_ok(cudaMemcpy(&p.h_scal, p.d_scal, sizeof(float4), cudaMemcpyDeviceToHost), "prepare download"))
+            return nullptr;
+        if (!cuda_ok(cudaMemcpy(&p.h_csum, p.d_csum, 8, cudaMemcpyDeviceToHost), "prepare download")) return nullptr;
+        p.space = s;
+        p.valid = true;
+        return &p;
+    } catch (...) {
+        return nullptr;
+    }
+}
+
+void rabitq_set_query_coarse_codec(void *space, int codec) {
+    if (space) static_cast<Space *>(space)->codec = codec;
+}
+
+void rabitq_release_query(const void *space, const void *prepared) {
+    (void)space;
+    (void)prepared;
+}
+
+float rabitq_query_distance(const void *space, const void *prepared, const void *encoded) {
+    const float inf = std::numeric_limits<float>::infinity();
+    try {
+        const Space *s = as_space(space);
+        if (!check_prepared(s, prepared) || !encoded) return inf;
+        const uint32_t id = 0;
+        const uint8_t mode = 0;
+        const float sip = 0.0f;
+        float out = inf;
+        if (!distance_host(s, &id, &mode, 1, static_cast<const uint8_t *>(encoded), s->compact_bytes, &sip, &out))
+            return inf;
+        return out;
+    } catch (...) {
+        return inf;
+    }
+}
+
+float rabitq_query_distance_b1(const void *, const void *, const void *) {
+    set_error("the B1Main codec is not built");
+    return std::numeric_limits<float>::infinity();
+}
+
+bool rabitq_query_distance_b1_batch(const void *, const void *, const uint32_t *, size_t count,
+                                    const void *, size_t, float *out_distances) {
+    for (size_t i = 0; i < count; ++i) out_distances[i] = std::numeric_limits<float>::infinity();
+    return true;
+}
+
+RabitqPaperEstimate rabitq_paper_estimate_sidecar(const void *space, const void *prepared,
+                                                  const uint8_t *msb_code, const void *factors,
+                                                  float epsilon0) {
+    try {
+        const Space *s = as_space(space);
+        if (!check_prepared(s, prepared) || !msb_code || !factors) return zero_estimate();
+        const uint32_t id = 0;
+        RabitqPaperEstimate out = zero_estimate();
+        if (!gate_host(s, &id, 1, msb_code, s->msb_bytes, static_cast<const uint8_t *>(factors), 20,
+                       epsilon0, &out))
+            return zero_estimate();
+        return out;
+    } catch (...) {
+        return zero_estimate();
+    }
+}
+
+RabitqPaperEstimate rabitq_paper_estimate(const void *space, const void *prepared,
+                                          const void *encoded, float epsilon0) {
+    try {
+        const Space *s = as_space(space);
+        if (!check_prepared(s, prepared) || !encoded) return zero_estimate();
+        std::vector<uint8_t> msb(s->msb_bytes), f(20);
+        if (!rabitq_export_paper_sidecar(s, encoded, 1, s->compact_bytes, msb.data(), f.data()))
+            return zero_estimate();
+        return rabitq_paper_estimate_sidecar(space, prepared, msb.data(), f.data(), epsilon0);
+    } catch (...) {
+        return zero_estimate();
+    }
+}
+
+RabitqPaperEstimate rabitq_paper_estimate_codec(const void *space, const void *prepared,
+                                                const void *encoded, const uint8_t *msb_code,
+                                                const void *factors, float epsilon0) {
+    (void)encoded;
+    return rabitq_paper_estimate_sidecar(space, prepared, msb_code, factors, epsilon0);
+}
+
+bool rabitq_paper_estimate_batch_sidecar(const void *space, const void *prepared,
+                                         const uint32_t *ids, size_t count,
+                                         const uint8_t *msb_base, size_t msb_stride,
+                                         const void *factors_base, size_t factors_stride,
+                                         float epsilon0, RabitqPaperEstimate *out) {
+    try {
+        const Space *s = as_space(space);
+        bool ok = check_prepared(s, prepared) && ids && msb_base && factors_base;
+        if (ok && count)
+            ok = gate_host(s, ids, count, msb_base, msb_stride, static_cast<const uint8_t *>(factors_base),
+                           factors_stride, epsilon0, out);
+        if (!ok)
+            for (size_t i = 0; i < count; ++i) out[i] = zero_estimate();
+        return true;
+    } catch (...) {
+        for (size_t i = 0; i < count; ++i) out[i] = zero_estimate();
+        return true;
+    }
+}
+
+bool rabitq_paper_estimate_codec_batch(const void *space, const void *prepared,
+                                       const uint32_t *ids, size_t count,
+                                       const void *encoded_base, size_t encoded_stride,
+                                       const uint8_t *msb_base, size_t msb_stride,
+                                       const void *factors_base, size_t factors_stride,
+                                       float epsilon0, RabitqPaperEstimate *out) {
+    (void)encoded_base;
+    (void)encoded_stride;
+    return rabitq_paper_estimate_batch_sidecar(space, prepared, ids, count, msb_base, msb_stride,
+                                               factors_base, factors_stride, epsilon0, out);
+}
+
+bool rabitq_paper_estimate_batch(const void *space, const void *prepared, const uint32_t *ids,
+                                 size_t count, const void *encoded_base, size_t encoded_stride,
+                                 float epsilon0, RabitqPaperEstimate *out) {
+    try {
+        const Space *s = as_space(space);
+        if (!check_prepared(s, prepared) || !ids || !encoded_base) {
+            for (size_t i = 0; i < count; ++i) out[i] = zero_estimate();
+            return true;
+        }
+        std::vector<uint8_t> rows(count * s->compact_bytes), msb(count * s->msb_bytes), f(count * 20);
+        gather_rows(rows.data(), static_cast<const uint8_t *>(encoded_base), encoded_stride, ids, count,
+                    s->compact_bytes);
+        std::vector<uint32_t> local(count);
+        for (size_t i = 0; i < count; ++i) local[i] = static_cast<uint32_t>(i);
+        if (!rabitq_export_paper_sidecar(s, rows.data(), count, s->compact_bytes, msb.data(), f.data()) ||
+            !gate_host(s, local.data(), count, msb.data(), s->msb_bytes, f.data(), 20, epsilon0, out)) {
+            for (size_t i = 0; i < count; ++i) out[i] = zero_estimate();
+        }
+        return true;
+    } catch (...) {
+        for (size_t i = 0; i < count; ++i) out[i] = zero_estimate();
+        return true;
+    }
+}
+
+float rabitq_query_distance_with_paper(const void *, const void *, const void *, float) {
+    set_error("the Full-codec MSB reuse (mode 1) is not built");
+    return std::numeric_limits<float>::infinity();
+}
+
+float rabitq_query_distance_with_quantized_paper(const void *space, const void *prepared,
+                                                 const void *encoded, float short_ip) {
+    const float inf = std::numeric_limits<float>::infinity();
+    try {
+        const Space *s = as_space(space);
+        if (!check_prepared(s, prepared) || !encoded) return inf;
+        const uint32_t id = 0;
+        const uint8_t mode = 2;
+        float out = inf;
+        if (!distance_host(s, &id, &mode, 1, static_cast<const uint8_t *>(encoded), s->compact_bytes,
+                           &short_ip, &out))
+            return inf;
+        return out;
+    } catch (...) {
+        return inf;
+    }
+}
+
+bool rabitq_query_distance_batch(const void *space, const void *prepared, const uint32_t *ids,
+                                 const uint8_t *modes, size_t count, const void *encoded_base,
+                                 size_t encoded_stride, const float *short_ips,
+                                 float *out_distances) {
+    const float inf = std::numeric_limits<float>::infinity();
+    try {
+        const Space *s = as_space(space);
+        bool ok = check_prepared(s, prepared) && ids && modes && encoded_base;
+        if (ok && count)
+            ok = distance_host(s, ids, modes, count, static_cast<const uint8_t *>(encoded_base),
+                               encoded_stride, short_ips, out_distances);
+        if (!ok) std::fill(out_distances, out_distances + count, inf);
+        // modes 1 and 3 (Full-codec reuse) are not built: +inf, like a failed item
+        for (size_t i = 0; ok && i < count; ++i)
+            if (modes[i] == 1 || modes[i] == 3) out_distances[i] = inf;
+        return true;
+    } catch (...) {
+        std::fill(out_distances, out_distances + count, inf);
+        return true;
+    }
+}
+
+RabitqDistanceInterval rabitq_residual_distance(const void *, const void *, const void *,
+                                                float long_distance) {
+    return RabitqDistanceInterval{long_distance, long_distance, long_distance};
+}
+
+RabitqDistanceInterval rabitq_residual_distance_from_record(const void *space,
+                                                            const void *prepared,
+                                                            const void *encoded,
+                                                            const void *residual_record,
+                                                            float long_distance) {
+    const RabitqDistanceInterval fallback{long_distance, long_distance, long_distance};
+    try {
+        const Space *s = as_space(space);
+        (void)encoded;
+        if (!check_prepared(s, prepared) || !residual_record) return fallback;
+        const uint32_t id = 0;
+        RabitqDistanceInterval out = fallback;
+        if (!residual_host(s, &id, 1, static_cast<const uint8_t *>(residual_record), s->residual_bytes,
+                           &long_distance, &out))
+            return fallback;
+        return out;
+    } catch (...) {
+        return fallback;
+    }
+}
+
+bool rabitq_residual_distance_batch(const void *space, const void *prepared, const uint32_t *ids,
+                                    size_t count, const void *encoded_base,
+                                    size_t encoded_stride, const void *residual_base,
+                                    size_t residual_stride, const float *long_distances,
+                                    RabitqDistanceInterval *out) {
+    (void)encoded_base;
+    (void)encoded_stride;
+    try {
+        const Space *s = as_space(space);
+        bool ok = check_prepared(s, prepared) && ids && residual_base && long_distances;
+        if (ok && count)
+            ok = residual_host(s, ids, count, static_cast<const uint8_t *>(residual_base), residual_stride,
+                               long_distances, out);
+        if (!ok)
+            for (size_t i = 0; i < count; ++i)
+                out[i] = RabitqDistanceInterval{long_distances[i], long_distances[i], long_distances[i]};
+        return true;
+    } catch (...) {
+        for (size_t i = 0; i < count; ++i)
+            out[i] = RabitqDistanceInterval{long_distances[i], long_distances[i], long_distances[i]};
+        return true;
+    }
+}
+
+bool rabitq_full_residual_distance_batch(const void *space, const void *prepared,
+                                         const uint32_t *ids, size_t count,
+                                         const void *encoded_base, size_t encoded_stride,
+                                         const void *residual_base, size_t residual_stride,
+                                         RabitqDistanceInterval *out) {
+    const float inf = std::numeric_limits<float>::infinity();
+    try {
+        std::vector<uint8_t> modes(count, 0);
+        std::vector<float> zeros(count, 0.0f), longd(count, inf);
+        rabitq_query_distance_batch(space, prepared, ids, modes.data(), count, encoded_base,
+                                    encoded_stride, zeros.data(), longd.data());
+        bool any_inf = false;
+        for (float v : longd) any_inf |= !std::isfinite(v);
+        if (any_inf && count) {
+            for (size_t i = 0; i < count; ++i) out[i] = RabitqDistanceInterval{inf, inf, inf};
+            return true;
+        }
+        return rabitq_residual_distance_batch(space, prepared, ids, count, encoded_base, encoded_stride,
+                                              residual_base, residual_stride, longd.data(), out);
+    } catch (...) {
+        for (size_t i = 0; i < count; ++i) out[i] = RabitqDistanceInterval{inf, inf, inf};
+        return true;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// qg_* batched device entry points
+// ---------------------------------------------------------------------------------------
+
+int qg_center_mean(const float *d_data, size_t stride, size_t dim, const uint32_t *d_rows,
+                   size_t count, float *d_center_out, void *stream) {
+    if (!d_data || !d_center_out || count == 0 || dim == 0 || stride < dim) return QG_ERR_INVALID;
+    if (!cuda_ok(launch_center_mean(d_data, stride, static_cast<int>(dim), d_rows, count, d_center_out,
+                                    static_cast<cudaStream_t>(stream)), "center kernel"))
+        return QG_ERR_CUDA;
+    return QG_OK;
+}
+
+int qg_encode_batch(const void *space, const float *d_raw, size_t n, uint8_t *d_compact,
+                    uint8_t *d_residual, void *stream) {
+    const Space *s = as_space(space);
+    if (!s || (n && (!d_raw || !d_compact || !d_residual))) return QG_ERR_INVALID;
+    if (!s->center_set) {
+        set_error("set the centre before encoding");
+        return QG_ERR_INVALID;
+    }
+    EncodeArgs a{d_raw, s->dim, 0, static_cast<int>(s->dim), static_cast<int>(s->code_dim), s->d_signs,
+                 s->d_center, d_compact, d_residual, s->compact_bytes, s->residual_bytes};
+    const size_t chunk = 1u << 30;  // grid.x limit headroom
+    for (size_t base = 0; base < n; base += chunk) {
+        const size_t m = std::min(chunk, n - base);
+        a.raw = d_raw + base * s->dim;
+        a.n = static_cast<int>(m);
+        a.compact = d_compact + base * s->compact_bytes;
+        a.residual = d_residual + base * s->residual_bytes;
+        if (!cuda_ok(launch_encode(a, static_cast<cudaStream_t>(stream)), "encode kernel")) return QG_ERR_CUDA;
+    }
+    return QG_OK;
+}
+
+int qg_export_sidecar_device(const void *space, const uint8_t *d_compact, size_t n,
+                             size_t compact_stride, uint8_t *d_msb, void *d_factors, void *stream) {
+    const Space *s = as_space(space);
+    if (!s || (n && (!d_compact || !d_msb || !d_factors))) return QG_ERR_INVALID;
+    if (!cuda_ok(launch_sidecar(d_compact, n, compact_stride, static_cast<int>(s->code_dim), d_msb,
+                                static_cast<RabitqPaperFactors *>(d_factors), static_cast<cudaStream_t>(stream)),
+                 "sidecar kernel"))
+        return QG_ERR_CUDA;
+    return QG_OK;
+}
+
+int qg_prepare_batch(const void *space, const float *d_queries, size_t nq, float *d_rotated,
+                     int8_t *d_codes, float *d_scalars, int64_t *d_code_sum, void *stream) {
+    const Space *s = as_space(space);
+    if (!s || (nq && (!d_queries || !d_rotated || !d_codes || !d_scalars || !d_code_sum))) return QG_ERR_INVALID;
+    if (!s->center_set) {
+        set_error("set the centre before preparing queries");
+        return QG_ERR_INVALID;
+    }
+    PrepArgs a{d_queries, s->dim, static_cast<int>(nq), static_cast<int>(s->dim),
+               static_cast<int>(s->code_dim), s->d_signs, s->d_center, s->d_rotated_center,
+               s->d_center_norm, d_rotated, d_codes, reinterpret_cast<float4 *>(d_scalars),
+               reinterpret_cast<long long *>(d_code_sum)};
+    if (!cuda_ok(launch_prepare(a, static_cast<cudaStream_t>(stream)), "prepare kernel")) return QG_ERR_CUDA;
+    return QG_OK;
+}
+
+int qg_gate_pairs(const void *space, const int8_t *d_codes, const float *d_scalars,
+                  const int64_t *d_code_sum, const uint32_t *d_qidx, const uint32_t *d_ids,
+                  size_t count, const uint8_t *d_msb, size_t msb_stride, const void *d_factors,
+                  size_t factor_stride, float epsilon0, RabitqPaperEstimate *d_out, void *stream) {
+    const Space *s = as_space(space);
+    if (!s) return QG_ERR_INVALID;
+    if (!cuda_ok(launch_gate_pairs(static_cast<int>(s->code_dim), d_codes,
+                                   reinterpret_cast<const float4 *>(d_scalars),
+                                   reinterpret_cast<const long long *>(d_code_sum), d_qidx, d_ids, count,
+                                   d_msb, msb_stride, static_cast<const uint8_t *>(d_factors),
+                                   factor_stride, epsilon0, d_out, static_cast<cudaStream_t>(stream)),
+                 "gate kernel"))
+        return QG_ERR_CUDA;
+    return QG_OK;
+}
+
+int qg_distance_pairs(const void *space, const float *d_rotated, const int8_t *d_codes,
+                      const float *d_scalars, const int64_t *d_code_sum, const uint32_t *d_qidx,
+                      const uint32_t *d_ids, const uint8_t *d_modes, size_t count,
+                      const uint8_t *d_records, size_t record_stride, const float *d_short_ips,
+                      float *d_out, void *stream) {
+    const Space *s = as_space(space);
+    if (!s) return QG_ERR_INVALID;
+    if (!cuda_ok(launch_distance_pairs(static_cast<int>(s->code_dim), d_rotated, d_codes,
+                                       reinterpret_cast<const float4 *>(d_scalars),
+                                       reinterpret_cast<const long long *>(d_code_sum), d_qidx, d_ids,
+                                       d_modes, count, d_records, record_stride, d_short_ips, d_out,
+                                       static_cast<cudaStream_t>(stream)),
+                 "distance kernel"))
+        return QG_ERR_CUDA;
+    return QG_OK;
+}
+
+int qg_residual_pairs(const void *space, const float *d_rotated, const float *d_scalars,
+                      const uint32_t *d_qidx, const uint32_t *d_ids, size_t count,
+                      const uint8_t *d_residual, size_t residual_stride,
+                      const float *d_long_distances, RabitqDistanceInterval *d_out,
+                      void *stream) {
+    const Space *s = as_space(space);
+    if (!s) return QG_ERR_INVALID;
+    if (!cuda_ok(launch_residual_pairs(static_cast<int>(s->code_dim), d_rotated,
+                                       reinterpret_cast<const float4 *>(d_scalars), d_qidx, d_ids, count,
+                                       d_residual, residual_stride, d_long_distances, d_out,
+                                       static_cast<cudaStream_t>(stream)),
+                 "residual kernel"))
+        return QG_ERR_CUDA;
+    return QG_OK;
+}
+
+static void index_free_all(qg_index *ix) {
+    for (void *p : ix->owned) cudaFree(p);
+    ix->owned.clear();
+    cudaFree(ix->tags);
+    cudaFree(ix->epochs);
+    cudaFree(ix->counter);
+    cudaFree(ix->status);
+    cudaFree(ix->q.rr);
+    cudaFree(ix->q.codes);
+    cudaFree(ix->q.scal);
+    cudaFree(ix->q.csum);
+}
+
+int qg_index_upload_device(const void *space, const void *d_compact, size_t compact_stride,
+                           const void *d_residual, size_t residual_stride, const uint8_t *d_msb,
+                           size_t msb_stride, const void *d_factors, size_t factor_stride,
+                           const uint32_t *d_degrees, const uint32_t *d_edges,
+                           size_t edge_stride, size_t base_points, size_t total_points,
+                           void *stream, qg_index **out) {
+    const Space *s = as_space(space);
+    if (!s || !out || total_points < base_points || total_points >= 0x7FFFFFFFu) return QG_ERR_INVALID;
+    if (base_points == 0 && total_points != 0) return QG_ERR_INVALID;
+    if (edge_stride == 0 || edge_stride > 64) {
+        set_error("edge stride (max degree) must be 1..64");
+        return QG_ERR_UNSUPPORTED;
+    }
+    if (compact_stride < s->compact_bytes || residual_stride < s->residual_bytes || msb_stride < s->msb_bytes ||
+        factor_stride < 20) {
+        set_error("record stride smaller than the record");
+        return QG_ERR_INVALID;
+    }
+    auto *ix = new (std::nothrow) qg_index();
+    if (!ix) return QG_ERR_OOM;
+    ix->space = s;
+    cudaGetDevice(&ix->device);
+    const size_t D = s->code_dim, nb = base_points, nt = total_points;
+    auto own = [&](size_t bytes) -> void * {
+        void *p = nullptr;
+        if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
+        ix->owned.push_back(p);
+        ix->device_bytes += bytes;
+        return p;
+    };
+    DevIndex &d = ix->ix;
+    d.n_total = static_cast<uint32_t>(nt);
+    d.n_base = static_cast<uint32_t>(nb);
+    d.code_dim = static_cast<uint32_t>(D);
+    d.edge_stride = static_cast<uint32_t>(edge_stride);
+    d.max_degree = static_cast<uint32_t>(edge_stride);
+    // Payload rows exist for every graph node; rows of frozen points (ids >= base_points) stay
+    // zero: degenerate long_scale and invalid factors, so the kernels never read past them.
+    d.codes = static_cast<uint8_t *>(own(nt * D / 2));
+    d.hdr = static_cast<float4 *>(own(nt * 16));
+    d.msb = static_cast<uint8_t *>(own(nt * D / 8));
+    d.pf = static_cast<float4 *>(own(nt * 16));
+    d.res_scales = static_cast<uint16_t *>(own(nt * D / 16 * 2));
+    d.res_codes = static_cast<uint8_t *>(own(nt * D / 2));
+    (void)nb;
+    d.degrees = static_cast<uint32_t *>(own(nt * 4));
+    d.edges = static_cast<uint32_t *>(own(nt * edge_stride * 4));
+    ix->counter = dev_alloc<unsigned int>(1);
+    ix->status = dev_alloc<int>(1);
+    if (!d.codes || !d.hdr || !d.msb || !d.pf || !d.res_scales || !d.res_codes || !d.degrees || !d.edges ||
+        !ix->counter || !ix->status) {
+        set_error("device allocation failed for the index");
+        index_free_all(ix);
+        delete ix;
+        return QG_ERR_OOM;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaMemsetAsync(ix->status, 0, 4, st);
+    if (nt > nb) {
+        cudaMemsetAsync(d.codes, 0, nt * D / 2, st);
+        cudaMemsetAsync(d.hdr, 0, nt * 16, st);
+        cudaMemsetAsync(d.msb, 0, nt * D / 8, st);
+        cudaMemsetAsync(d.pf, 0, nt * 16, st);
+        cudaMemsetAsync(d.res_scales, 0, nt * D / 16 * 2, st);
+        cudaMemsetAsync(d.res_codes, 0, nt * D / 2, st);
+    }
+    if (!cuda_ok(launch_repack(static_cast<const uint8_t *>(d_compact), compact_stride,
+                               static_cast<const uint8_t *>(d_residual), residual_stride, d_msb, msb_stride,
+                               static_cast<const uint8_t *>(d_factors), factor_stride, d_degrees, d_edges,
+                               edge_stride, d, st), "repack kernel") ||
+        !cuda_ok(cudaStreamSynchronize(st), "repack sync")) {
+        index_free_all(ix);
+        delete ix;
+        return QG_ERR_CUDA;
+    }
+    *out = ix;
+    return QG_OK;
+}
+
+int qg_index_upload_host(const void *space, const void *compact, size_t compact_stride,
+                         const void *residual, size_t residual_stride, const uint8_t *msb,
+                         size_t msb_stride, const void *factors, size_t factor_stride,
+                         const uint32_t *degrees, const uint32_t *edges, size_t edge_stride,
+                         size_t base_points, size_t total_points, qg_index **out) {
+    const Space *s = as_space(space);
+    if (!s || !out || !degrees || !edges || (base_points && (!compact || !residual || !msb || !factors)))
+        return QG_ERR_INVALID;
+    for (size_t i = 0; i < total_points; ++i)
+        if (degrees[i] > edge_stride) {
+            set_error("a node degree exceeds the edge stride");
+            return QG_ERR_INVALID;
+        }
+    const size_t nb = base_points, nt = total_points;
+    const size_t sizes[6] = {nb * compact_stride, nb * residual_stride, nb * msb_stride, nb * factor_stride,
+                             nt * 4, nt * edge_stride * 4};
+    const void *srcs[6] = {compact, residual, msb, factors, degrees, edges};
+    void *tmp[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    int rc = QG_OK;
+    for (int i = 0; i < 6 && rc == QG_OK; ++i) {
+        if (cudaMalloc(&tmp[i], sizes[i] ? sizes[i] : 16) != cudaSuccess) {
+            rc = QG_ERR_OOM;
+            set_error("device allocation failed for the upload");
+        } else if (sizes[i] && cudaMemcpy(tmp[i], srcs[i], sizes[i], cudaMemcpyHostToDevice) != cudaSuccess) {
+            rc = QG_ERR_CUDA;
+            set_error("index upload copy failed");
+        }
+    }
+    if (rc == QG_OK)
+        rc = qg_index_upload_device(space, tmp[0], compact_stride, tmp[1], residual_stride,
+                                    static_cast<const uint8_t *>(tmp[2]), msb_stride, tmp[3], factor_stride,
+                                    static_cast<const uint32_t *>(tmp[4]), static_cast<const uint32_t *>(tmp[5]),
+                                    edge_stride, base_points, total_points, nullptr, out);
+    for (void *p : tmp) cudaFree(p);
+    return rc;
+}
+
+void qg_index_free(qg_index *index) {
+    if (!index) return;
+    index_free_all(index);
+    delete index;
+}
+
+size_t qg_index_device_bytes(const qg_index *index) { return index ? index->device_bytes : 0; }
+
+int qg_search_status(qg_index *index, void *stream) {
+    if (!index) return QG_ERR_INVALID;
+    int h = 0;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (!cuda_ok(cudaMemcpyAsync(&h, index->status, 4, cudaMemcpyDeviceToHost, st), "status read") ||
+        !cuda_ok(cudaStreamSynchronize(st), "status sync"))
+        return QG_ERR_CUDA;
+    if (h & 1) return QG_ERR_GRAPH;
+    if (h & 2) return QG_ERR_TIMEOUT;
+    if (h & 4) return QG_ERR_INVALID;
+    return QG_OK;
+}
+
+int qg_search_batch(qg_index *index, const float *d_queries, size_t nq,
+                    const qg_search_params *params, const int *d_k, const int *d_l,
+                    size_t k_stride, uint32_t *d_ids, float *d_dists, qg_search_stats *d_stats,
+                    void *stream) {
+    if (!index || !params || (nq && (!d_queries || !d_ids || !d_dists))) return QG_ERR_INVALID;
+    if (nq > 0x7FFFFFFF) return QG_ERR_INVALID;
+    const Space *s = index->space;
+    const int k_max = d_k ? static_cast<int>(k_stride) : params->k;
+    if (k_max <= 0 || (d_k == nullptr && k_stride != 0 && k_stride < static_cast<size_t>(params->k))) {
+        set_error("k must be positive and fit the output stride");
+        return QG_ERR_INVALID;
+    }
+    const int l_cap = std::max(params->l_value, k_max);
+    if (l_cap > 4096 || params->beam_width < 1 || params->beam_width > 8 || params->rerank_candidates < 0) {
+        set_error("L must be <= 4096 and beam width 1..8");
+        return QG_ERR_INVALID;
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // prepared-query workspace
+    if (index->q_capacity < nq) {
+        cudaFree(index->q.rr);
+        cudaFree(index->q.codes);
+        cudaFree(index->q.scal);
+        cudaFree(index->q.csum);
+        const size_t cap = std::max<size_t>(nq, 1024);
+        index->q.rr = dev_alloc<float>(cap * s->code_dim);
+        index->q.codes = dev_alloc<int8_t>(cap * s->code_dim);
+        index->q.scal = dev_alloc<float4>(cap);
+        index->q.csum = dev_alloc<long long>(cap);
+        if (!index->q.rr || !index->q.codes || !index->q.scal || !index->q.csum) {
+            index->q_capacity = 0;
+            set_error("device allocation failed for prepared queries");
+            return QG_ERR_OOM;
+        }
+        index->q_capacity = cap;
+    }
+    // persistent grid: warps per block and resident blocks per SM from the occupancy of
+    // this pool size; one visited-tag row per warp slot
+    const int wpb = 8;
+    int sms = qg_device_sm_count();
+    if (sms <= 0) sms = 1;
+    const int per_sm = search_blocks_per_sm(static_cast<int>(s->code_dim), l_cap, wpb);
+    if (per_sm <= 0) {
+        set_error("search kernel cannot be resident with this pool size");
+        return QG_ERR_UNSUPPORTED;
+    }
+    const int grid = sms * per_sm;
+    const int slots = grid * wpb;
+    if (index->slots < slots) {
+        cudaFree(index->tags);
+        cudaFree(index->epochs);
+        index->tags = nullptr;
+        index->epochs = nullptr;
+        const size_t tag_bytes = static_cast<size_t>(slots) * index->ix.n_total * 2;
+        if (cudaMalloc(&index->tags, tag_bytes ? tag_bytes : 16) != cudaSuccess ||
+            cudaMalloc(&index->epochs, static_cast<size_t>(slots) * 4) != cudaSuccess) {
+            index->slots = 0;
+            set_error("device allocation failed for visited tags");
+            return QG_ERR_OOM;
+        }
+        cudaMemset(index->tags, 0, tag_bytes);
+        cudaMemset(index->epochs, 0, static_cast<size_t>(slots) * 4);
+        index->slots = slots;
+    }
+    if (nq == 0) return QG_OK;
+    int rc = qg_prepare_batch(s, d_queries, nq, index->q.rr, index->q.codes,
+                              reinterpret_cast<float *>(index->q.scal),
+                              reinterpret_cast<int64_t *>(index->q.csum), stream);
+    if (rc != QG_OK) return rc;
+    if (!cuda_ok(cudaMemsetAsync(index->counter, 0, 4, st), "counter reset") ||
+        !cuda_ok(cudaMemsetAsync(index->status, 0, 4, st), "status reset"))
+        return QG_ERR_CUDA;
+    SearchArgs a{};
+    a.ix = index->ix;
+    a.rr = index->q.rr;
+    a.codes = index->q.codes;
+    a.scal = index->q.scal;
+    a.csum = index->q.csum;
+    a.nq = static_cast<int>(nq);
+    a.k_default = params->k;
+    a.l_default = params->l_value;
+    a.k_per_q = d_k;
+    a.l_per_q = d_l;
+    a.k_stride = k_max;
+    a.l_cap = l_cap;
+    a.beam_width = params->beam_width;
+    a.eps = params->epsilon0;
+    a.rerank = params->rerank_candidates;
+    a.early_stop_hops = params->early_stop_hops;
+    a.kth_stop = params->kth_stop;
+    a.ids_out = d_ids;
+    a.dists_out = d_dists;
+    a.stats_out = d_stats;
+    a.tags = index->tags;
+    a.epochs = index->epochs;
+    a.counter = index->counter;
+    a.status = index->status;
+    a.hop_cap = static_cast<int>(std::min<size_t>(index->ix.n_total + 1, 0x7FFFFFFF));
+    index->grid = grid;
+    index->warps_per_block = wpb;
+    if (!cuda_ok(launch_search(a, grid, wpb, st), "search kernel")) return QG_ERR_CUDA;
+    return QG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,161 @@
+// qg_device.cuh -- device-side arithmetic of the ExRaBitQ4 / paper-prune query path.
+//
+// Every function restates one reference routine of Ours/core/hnswlib/space_rabitq.h as
+// built by experiments/02_diskann_fair/build.rs (x86-64, -O3 -march=native): the floating
+// point operation order, the lane order of its SIMD reductions and the FMA contractions
+// GCC makes there are reproduced, so results are bit-identical to the reference. All
+// translation units are compiled with --fmad=false; the contracted sites are explicit
+// __fmaf_rn / __fma_rn calls.
+#pragma once
+
+#include <cstdint>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include "qg_types.h"
+
+namespace qg {
+
+constexpr float kFltMax = 3.402823466e+38f;
+
+__device__ __forceinline__ float f_inf() { return __int_as_float(0x7f800000); }
+__device__ __forceinline__ bool f_isfinite(float x) { return isfinite(x); }
+
+// _mm512_reduce_add_ps tree over the 16 lanes of a half-warp (lane t = AVX-512 lane t):
+// (v[8+j] + v[j]) -> (a[4+j] + a[j]) -> (b0 + b2, b1 + b3) -> c0 + c1. Every lane of the
+// half-warp must call it; lane 0 of the half-warp holds the result.
+__device__ __forceinline__ float reduce16_tree(float v) {
+    v = v + __shfl_down_sync(0xffffffffu, v, 8, 16);
+    v = v + __shfl_down_sync(0xffffffffu, v, 4, 16);
+    v = v + __shfl_down_sync(0xffffffffu, v, 2, 16);
+    v = v + __shfl_down_sync(0xffffffffu, v, 1, 16);
+    return v;
+}
+
+// queryDistanceLongWithIps (space_rabitq.h:1621-1632) with the reference build's two
+// contractions: fma(-7, half, 8*short + rem) and fma(-long_scale, signed, norm + qn2).
+__device__ __forceinline__ float finish_long(float norm_sqr, float long_scale, float short_ip,
+                                             float remaining, float half_sum, float qn2) {
+    const float partial = 8.0f * short_ip + remaining;
+    const float signed_long_ip = __fmaf_rn(-7.0f, half_sum, partial);
+    return __fmaf_rn(-long_scale, signed_long_ip, norm_sqr + qn2);
+}
+
+// Full FP32 4-bit restore, mode 0 (query_distance_batch_by_id, space_rabitq.h:4080-4202 /
+// longCodeIpsAvx512 :1551-1597). Called by the 16 lanes of a half-warp for one record; `t`
+// is the lane index in the half-warp. rr = rotated query residual (D floats).
+template <int D>
+__device__ __forceinline__ float restore_distance_hw(const uint8_t *__restrict__ code,
+                                                     const float *__restrict__ rr, float norm_sqr,
+                                                     float long_scale, float half_sum, float qn2,
+                                                     int t) {
+    constexpr int kPairs = D / 2;
+    float sel = 0.0f, rem = 0.0f;
+#pragma unroll 8
+    for (int base = 0; base < kPairs; base += 16) {
+        const int pair = base + t;
+        const uint32_t packed = code[pair];
+        const uint32_t lo = packed & 0x0Fu, hi = packed >> 4;
+        const float2 q = *reinterpret_cast<const float2 *>(rr + 2 * pair);
+        rem = __fmaf_rn(static_cast<float>(lo & 7u), q.x, rem);
+        rem = __fmaf_rn(static_cast<float>(hi & 7u), q.y, rem);
+        if (lo > 7u) sel = sel + q.x;
+        if (hi > 7u) sel = sel + q.y;
+    }
+    sel = reduce16_tree(sel);
+    rem = reduce16_tree(rem);
+    const float short_ip = sel - half_sum;
+    float out = finish_long(norm_sqr, long_scale, short_ip, rem, half_sum, qn2);
+    if (!(long_scale > 0.0f) || !f_isfinite(long_scale)) out = norm_sqr + qn2;
+    return out;
+}
+
+// finishQuantizedTraversalDistance (space_rabitq.h:4342-4358); every product is exact.
+__device__ __forceinline__ float finish_traversal(float norm_sqr, float long_scale, float short_ip,
+                                                  int64_t remaining_dot, float scale,
+                                                  int64_t code_sum, float qn2) {
+    if (!(long_scale > 0.0f) || !f_isfinite(long_scale)) return norm_sqr + qn2;
+    const double centered = static_cast<double>(scale) *
+                            (static_cast<double>(remaining_dot) - 3.5 * static_cast<double>(code_sum));
+    const double signed_long = 8.0 * static_cast<double>(short_ip) + centered;
+    return norm_sqr + qn2 - static_cast<float>(static_cast<double>(long_scale) * signed_long);
+}
+
+struct GateOut {
+    float lower_bound;
+    float short_ip;
+    float ip_hat;
+    float error_bound;
+    bool valid;
+};
+
+// compute_paper_prune_estimate_int_msb_gate + finish_paper_prune_estimate_sidecar
+// (space_rabitq.h:4873-4899, 4701-4721). `pf` is the device copy of PaperPruneFactors with
+// validity folded into cross_scale (NaN when the factors are invalid).
+__device__ __forceinline__ GateOut finish_gate(int32_t selected, const float4 pf, float scale,
+                                               int64_t code_sum, float qn, float qn2, float eps) {
+    GateOut r{0.0f, 0.0f, 0.0f, 0.0f, false};
+    const float cross_scale = pf.z;
+    if (!(cross_scale > 0.0f) || !f_isfinite(cross_scale) || qn <= 0.0f) return r;
+    const float short_ip =
+        0.5f * scale * static_cast<float>(static_cast<int64_t>(2) * selected - code_sum);
+    const float cross = short_ip * cross_scale;
+    const float max_cross = 2.0f * pf.y * qn;
+    const float up = fmaxf(-max_cross, fminf(max_cross, cross + eps * pf.w * qn));
+    r.lower_bound = pf.x + qn2 - up;
+    r.short_ip = short_ip;
+    r.ip_hat = max_cross > 0.0f ? cross / max_cross : 0.0f;
+    r.error_bound = max_cross > 0.0f ? eps * pf.w * qn / max_cross : 0.0f;
+    r.valid = f_isfinite(r.lower_bound);
+    return r;
+}
+
+// Residual rerank interval (compute_residual_distance_intervals_batch_by_id AVX2 path,
+// space_rabitq.h:5432-5548), one thread per record: per 16-dim block, eight lanes of
+// fma(hi, qo, lo*qe) summed in lane order, then ips = fma(scale, block_ip, ips).
+template <int D>
+__device__ __forceinline__ void residual_interval_thread(const uint16_t *__restrict__ scales,
+                                                         const uint8_t *__restrict__ codes,
+                                                         const float *__restrict__ rr, float long_d,
+                                                         float qn, float *est, float *lo_out,
+                                                         float *hi_out) {
+    constexpr int kBlocks = D / 16;
+    float ips = 0.0f;
+    double err_sqr = 0.0;
+    for (int b = 0; b < kBlocks; ++b) {
+        const float scale = __half2float(__ushort_as_half(scales[b]));
+        if (scale == 0.0f || !f_isfinite(scale)) continue;
+        const uint2 packed = *reinterpret_cast<const uint2 *>(codes + 8 * b);
+        const float4 *q4 = reinterpret_cast<const float4 *>(rr + 16 * b);
+        float block_ip = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const uint32_t word = j < 4 ? packed.x : packed.y;
+            const uint32_t byte = (word >> (8 * (j & 3))) & 0xFFu;
+            int lo = static_cast<int>(byte & 0x0Fu), hi = static_cast<int>(byte >> 4);
+            lo -= (lo > 7) ? 16 : 0;
+            hi -= (hi > 7) ? 16 : 0;
+            const float4 q = q4[j >> 1];
+            const float qe = (j & 1) ? q.z : q.x;
+            const float qo = (j & 1) ? q.w : q.y;
+            const float prod = __fmaf_rn(static_cast<float>(hi), qo, static_cast<float>(lo) * qe);
+            block_ip = block_ip + prod;
+        }
+        ips = __fmaf_rn(scale, block_ip, ips);
+        const double pde = 0.5 * fabs(static_cast<double>(scale));
+        err_sqr += 16.0 * pde * pde;
+    }
+    const float distance = long_d - 2.0f * ips;
+    const float err = static_cast<float>(2.0 * static_cast<double>(qn) * sqrt(err_sqr));
+    *est = distance;
+    *lo_out = distance - err;
+    *hi_out = distance + err;
+}
+
+// Byte masks of four MSB bits: nibble b3..b0 -> bytes (b0, b1, b2, b3), each 0 or 1. The
+// four shifted copies of the nibble occupy disjoint bit ranges, so no carries occur.
+__device__ __forceinline__ int nibble_mask(uint32_t word, int shift) {
+    return static_cast<int>((((word >> shift) & 0xFu) * 0x00204081u) & 0x01010101u);
+}
+
+}  // namespace qg

@@ -1,0 +1,107 @@
+// qg_kernels.h -- kernel argument blocks and launchers (host-callable).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "qg_types.h"
+
+namespace qg {
+
+struct PrepArgs {
+    const float *queries;
+    size_t query_stride;
+    int nq;
+    int dim;
+    int code_dim;
+    const float *signs;
+    const float *center;
+    const float *rotated_center;
+    const float *center_norm_sqr;
+    float *rr;
+    int8_t *codes;
+    float4 *scal;
+    long long *csum;
+};
+
+struct SearchArgs {
+    DevIndex ix;
+    const float *rr;
+    const int8_t *codes;
+    const float4 *scal;
+    const long long *csum;
+    int nq;
+    int k_default;
+    int l_default;
+    const int *k_per_q;
+    const int *l_per_q;
+    int k_stride;
+    int l_cap;       // pool capacity per warp (>= every L and k)
+    int beam_width;
+    float eps;
+    int rerank;
+    int early_stop_hops;
+    int kth_stop;
+    uint32_t *ids_out;
+    float *dists_out;
+    qg_search_stats *stats_out;
+    uint16_t *tags;      // [slots x n_total] visited tags
+    uint32_t *epochs;    // [slots]
+    unsigned int *counter;
+    int *status;
+    int hop_cap;
+};
+
+struct EncodeArgs {
+    const float *raw;
+    size_t raw_stride;
+    int n;
+    int dim;
+    int code_dim;
+    const float *signs;
+    const float *center;
+    uint8_t *compact;      // [n x compact_bytes]
+    uint8_t *residual;     // [n x residual_bytes]
+    size_t compact_bytes;
+    size_t residual_bytes;
+};
+
+cudaError_t launch_prepare(const PrepArgs &a, cudaStream_t stream);
+cudaError_t launch_center_setup(const float *center, const float *signs, int dim, int D,
+                                float *rotated, float *norm_out, cudaStream_t stream);
+cudaError_t launch_center_mean(const float *data, size_t stride, int dim, const uint32_t *rows,
+                               size_t count, float *out, cudaStream_t stream);
+cudaError_t launch_search(const SearchArgs &a, int grid, int warps_per_block, cudaStream_t stream);
+size_t search_smem_per_warp(int code_dim, int l_cap);
+int search_blocks_per_sm(int code_dim, int l_cap, int warps_per_block);
+int search_supported_dim(int code_dim);
+cudaError_t launch_encode(const EncodeArgs &a, cudaStream_t stream);
+cudaError_t launch_sidecar(const uint8_t *compact, size_t n, size_t stride, int code_dim,
+                           uint8_t *msb, RabitqPaperFactors *factors, cudaStream_t stream);
+cudaError_t launch_repack(const uint8_t *compact, size_t compact_stride, const uint8_t *residual,
+                          size_t residual_stride, const uint8_t *msb, size_t msb_stride,
+                          const uint8_t *factors, size_t factor_stride, const uint32_t *degrees,
+                          const uint32_t *edges, size_t edge_stride, DevIndex ix,
+                          cudaStream_t stream);
+cudaError_t launch_gate_pairs(int code_dim, const int8_t *codes, const float4 *scal,
+                              const long long *csum, const uint32_t *qidx, const uint32_t *ids,
+                              size_t count, const uint8_t *msb, size_t msb_stride,
+                              const uint8_t *factors, size_t factor_stride, float eps,
+                              RabitqPaperEstimate *out, cudaStream_t stream);
+cudaError_t launch_distance_pairs(int code_dim, const float *rr, const int8_t *codes,
+                                  const float4 *scal, const long long *csum,
+                                  const uint32_t *qidx, const uint32_t *ids,
+                                  const uint8_t *modes, size_t count, const uint8_t *records,
+                                  size_t record_stride, const float *short_ips, float *out,
+                                  cudaStream_t stream);
+cudaError_t launch_residual_pairs(int code_dim, const float *rr, const float4 *scal,
+                                  const uint32_t *qidx, const uint32_t *ids, size_t count,
+                                  const uint8_t *residual, size_t residual_stride,
+                                  const float *long_d, RabitqDistanceInterval *out,
+                                  cudaStream_t stream);
+cudaError_t launch_symmetric_pairs(int code_dim, const uint8_t *lhs, const uint8_t *rhs,
+                                   size_t count, size_t stride, float *out, cudaStream_t stream);
+
+}  // namespace qg

@@ -1,0 +1,85 @@
+// qg_types.h -- internal structs shared by the host code and the kernels.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "qgraph_gb300.h"
+
+namespace qg {
+
+// Space configuration of RaBitQSpace (space_rabitq.h:2836-2893) in the formal bridge
+// config: one centroid, 4-bit residuals in blocks of 16, MSE scale, fp16 scale storage,
+// external residual storage.
+struct Space {
+    size_t dim = 0;
+    size_t code_dim = 0;       // D = next_pow2(roundup64(dim))
+    size_t code_bytes = 0;     // D/2
+    size_t block_count = 0;    // D/16
+    size_t scale_bytes = 0;    // 2*D/16
+    size_t full_bytes = 0;
+    size_t compact_bytes = 0;
+    size_t residual_bytes = 0;
+    size_t msb_bytes = 0;      // D/8
+    uint32_t seed = 100;
+    int codec = 0;             // QueryCoarseCodec; Int8 = 3 is the GPU path
+    int device = 0;
+    std::vector<float> signs;  // +-1/sqrt(D)
+    std::vector<float> center;
+    bool center_set = false;
+    // device copies
+    float *d_signs = nullptr;          // [D]
+    float *d_center = nullptr;         // [dim]
+    float *d_rotated_center = nullptr; // [D]
+    float *d_center_norm = nullptr;    // [1] ||c||^2 as float (setCentroids)
+    float center_norm_sqr = 0.0f;
+};
+
+// Device-resident index: structure-of-arrays, every row 16-byte aligned.
+struct DevIndex {
+    uint32_t n_total = 0;   // graph nodes
+    uint32_t n_base = 0;    // nodes with payloads
+    uint32_t code_dim = 0;
+    uint32_t edge_stride = 0;
+    uint32_t max_degree = 0;
+    uint8_t *codes = nullptr;       // [n_base x D/2]
+    float4 *hdr = nullptr;          // [n_base] {norm_sqr, long_scale, short_scale, error_scale}
+    uint8_t *msb = nullptr;         // [n_base x D/8]
+    float4 *pf = nullptr;           // [n_base] {norm_sqr, data_norm, cross_scale|NaN, error_cross}
+    uint16_t *res_scales = nullptr; // [n_base x D/16]
+    uint8_t *res_codes = nullptr;   // [n_base x D/2]
+    uint32_t *degrees = nullptr;    // [n_total]
+    uint32_t *edges = nullptr;      // [n_total x edge_stride]
+};
+
+// Per-query prepared state produced by the query-preparation kernel.
+struct DevQueries {
+    float *rr = nullptr;        // [nq x D] rotated residual
+    int8_t *codes = nullptr;    // [nq x D]
+    float4 *scal = nullptr;     // [nq] {qn2, qn, half_sum, int8_scale}
+    long long *csum = nullptr;  // [nq]
+};
+
+}  // namespace qg
+
+struct qg_index {
+    qg::DevIndex ix;
+    const qg::Space *space = nullptr;
+    int device = 0;
+    // search scratch: visited tags per warp slot, epochs, queue counter, status word
+    uint16_t *tags = nullptr;
+    uint32_t *epochs = nullptr;
+    unsigned int *counter = nullptr;
+    int *status = nullptr;
+    int slots = 0;
+    int grid = 0;
+    int warps_per_block = 0;
+    // prepared-query workspace, grown on demand (not inside graph capture)
+    qg::DevQueries q;
+    size_t q_capacity = 0;
+    size_t device_bytes = 0;
+    std::vector<void *> owned;
+};

@@ -1,0 +1,698 @@
+// search.cu -- persistent batched beam search of the Ours-DiskANN query path.
+//
+// Restates search_ours_paper_active_inner + flush_distance_batch
+// (experiments/02_diskann_fair/src/ours_diskann.rs:1539-1986) with the Int8 query codec:
+// start at node 0, sorted pool of L (distance, id) entries, frontier = first beam_width
+// unexpanded entries; per expanded node: fresh = unvisited neighbours in adjacency order,
+// the INT8 x 1-bit-MSB paper-prune gate for all fresh neighbours, a first prune check against
+// the pool tail, the INT8 x remaining-3-bit traversal distance for the survivors (full FP32
+// restore when the gate is invalid), then, in adjacency order, the re-check against the
+// current tail and the sorted insert; finally the FP32 restore + residual4 rerank of the
+// first max(rerank, k) pool entries sorted by (estimate, id).
+//
+// GPU mapping: one warp per query, persistent CTAs pulling query indices from a global
+// counter. The INT8 query lives in registers: lane l owns the 32-dimension chunks
+// l, l+32, ... (or, for D < 1024, a group of D/32 lanes covers one neighbour and the warp
+// handles 32/(D/32) neighbours at once). Gate and traversal are exact int32 dot products
+// (dp4a over nibble/byte masks), computed for a whole group of neighbours with their row
+// loads in flight together, then reduced with a reduce-scatter butterfly that leaves each
+// neighbour's sum in one lane. The accept/insert pass is warp-serial over survivors in
+// adjacency order (the reference's result depends on that order); each insert is a
+// warp-parallel rank + shift of the pool in shared memory. The visited set is a per-warp-
+// slot array of 16-bit epoch tags in global memory (no per-query clearing).
+#include <cstdint>
+
+#include "qg_device.cuh"
+#include "qg_kernels.h"
+
+namespace qg {
+namespace {
+
+constexpr uint32_t kExpanded = 0x80000000u;
+constexpr uint32_t kIdMask = 0x7FFFFFFFu;
+constexpr int kMaxFresh = 64;   // fresh neighbours per expanded node (max degree)
+constexpr int kMaxBeam = 8;
+
+template <int D>
+struct Lay {
+    static constexpr int CH = D / 32;
+    static constexpr int LPN = CH < 32 ? CH : 32;   // lanes per neighbour
+    static constexpr int CPL = CH / LPN;            // 32-dim chunks per lane
+    static constexpr int NBP = 32 / LPN;            // neighbours per pass
+    static constexpr int GG = 32 / CPL;             // gate group (LPN == 32)
+    static constexpr int GT = 8 / CPL;              // traversal group (LPN == 32)
+    static constexpr int PG = 8;                    // passes per batch (LPN < 32)
+};
+
+struct WarpSmem {
+    float *pd;
+    uint32_t *pid;
+    float *plb;
+    uint32_t *fid;
+    float *flb;
+    float *fsip;
+    uint8_t *fval;
+    float4 *fpf;
+    uint32_t *sid;
+    uint32_t *sslot;
+    float *sdist;
+    float2 *shdr;
+    uint32_t *frontier;
+};
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~static_cast<size_t>(15); }
+
+__host__ __device__ inline size_t warp_smem_bytes(int l_cap) {
+    size_t s = 0;
+    s += align16(static_cast<size_t>(l_cap) * 4) * 3;
+    s += align16(kMaxFresh * 4) * 3 + align16(kMaxFresh);
+    s += align16(kMaxFresh * 16);
+    s += align16(kMaxFresh * 4) * 3 + align16(kMaxFresh * 8);
+    s += align16(kMaxBeam * 4);
+    return s;
+}
+
+__device__ WarpSmem carve(unsigned char *base, int l_cap) {
+    WarpSmem w;
+    unsigned char *p = base;
+    auto take = [&](size_t bytes) {
+        unsigned char *r = p;
+        p += align16(bytes);
+        return r;
+    };
+    w.pd = reinterpret_cast<float *>(take(static_cast<size_t>(l_cap) * 4));
+    w.pid = reinterpret_cast<uint32_t *>(take(static_cast<size_t>(l_cap) * 4));
+    w.plb = reinterpret_cast<float *>(take(static_cast<size_t>(l_cap) * 4));
+    w.fid = reinterpret_cast<uint32_t *>(take(kMaxFresh * 4));
+    w.flb = reinterpret_cast<float *>(take(kMaxFresh * 4));
+    w.fsip = reinterpret_cast<float *>(take(kMaxFresh * 4));
+    w.fval = take(kMaxFresh);
+    w.fpf = reinterpret_cast<float4 *>(take(kMaxFresh * 16));
+    w.sid = reinterpret_cast<uint32_t *>(take(kMaxFresh * 4));
+    w.sslot = reinterpret_cast<uint32_t *>(take(kMaxFresh * 4));
+    w.sdist = reinterpret_cast<float *>(take(kMaxFresh * 4));
+    w.shdr = reinterpret_cast<float2 *>(take(kMaxFresh * 8));
+    w.frontier = reinterpret_cast<uint32_t *>(take(kMaxBeam * 4));
+    return w;
+}
+
+__device__ __forceinline__ bool cand_less(float da, uint32_t ia, float db, uint32_t ib) {
+    return da < db || (da == db && ia < ib);
+}
+
+// Integer gate partial over one 32-dim chunk: sum of the query bytes whose MSB bit is set.
+__device__ __forceinline__ int gate_chunk(uint32_t w, const int (&xn)[8], int acc) {
+#pragma unroll
+    for (int g = 0; g < 8; ++g) acc = __dp4a(nibble_mask(w, 4 * g), xn[g], acc);
+    return acc;
+}
+
+// Integer traversal partial over one 32-dim chunk: sum of (code & 7) * x.
+__device__ __forceinline__ int trav_chunk(const uint4 c, const int (&xe)[4], const int (&xo)[4],
+                                          int acc) {
+    const uint32_t w[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        acc = __dp4a(static_cast<int>(w[k] & 0x07070707u), xe[k], acc);
+        acc = __dp4a(static_cast<int>((w[k] >> 4) & 0x07070707u), xo[k], acc);
+    }
+    return acc;
+}
+
+// Reduce-scatter of N per-lane partial sums across the warp (N = 32, 16, 8 or 4): on return
+// lane l holds the warp total of value (l & (N - 1)).
+template <int N>
+__device__ __forceinline__ int reduce_scatter(int (&p)[N], int lane) {
+    int v[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) v[i] = p[i];
+#pragma unroll
+    for (int half = N / 2; half >= 1; half >>= 1) {
+        const bool up = (lane & half) != 0;
+#pragma unroll
+        for (int i = 0; i < half; ++i) {
+            const int keep = up ? v[i + half] : v[i];
+            const int send = up ? v[i] : v[i + half];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, half);
+        }
+    }
+    int t = v[0];
+#pragma unroll
+    for (int o = N; o < 32; o <<= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    return t;
+}
+
+template <int D>
+struct QueryRegs {
+    int xn[Lay<D>::CPL][8];
+    int xe[Lay<D>::CPL][4];
+    int xo[Lay<D>::CPL][4];
+};
+
+template <int D>
+__device__ __forceinline__ void load_query(QueryRegs<D> &r, const int8_t *codes, int sub) {
+    using L = Lay<D>;
+#pragma unroll
+    for (int j = 0; j < L::CPL; ++j) {
+        const int c = sub + L::LPN * j;
+        const int4 *src = reinterpret_cast<const int4 *>(codes + 32 * c);
+        const int4 a = src[0], b = src[1];
+        const int w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int g = 0; g < 8; ++g) r.xn[j][g] = w[g];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            r.xe[j][k] = static_cast<int>(__byte_perm(w[2 * k], w[2 * k + 1], 0x6420));
+            r.xo[j][k] = static_cast<int>(__byte_perm(w[2 * k], w[2 * k + 1], 0x7531));
+        }
+    }
+}
+
+// ---- the per-query search ------------------------------------------------------------
+
+template <int D>
+__device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int lane,
+                           uint16_t *tags, uint32_t tag) {
+    using L = Lay<D>;
+    const DevIndex &ix = a.ix;
+    const int sub = lane % L::LPN;
+    const int grp = lane / L::LPN;
+    const float *rr = a.rr + static_cast<size_t>(q) * D;
+    const float4 sc = a.scal[q];
+    const float qn2 = sc.x, qn = sc.y, half_sum = sc.z, scale = sc.w;
+    const long long csum = a.csum[q];
+
+    int k = a.k_per_q ? a.k_per_q[q] : a.k_default;
+    int lval = a.l_per_q ? a.l_per_q[q] : a.l_default;
+    uint32_t *out_ids = a.ids_out + static_cast<size_t>(q) * a.k_stride;
+    float *out_d = a.dists_out + static_cast<size_t>(q) * a.k_stride;
+    unsigned long long st[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    enum { VIS, DC, HOPS, CHK, WPR, NPR, SAVED, MSBC, REMC };
+    if (k < 0) k = 0;
+    if (k > a.k_stride) k = a.k_stride;
+    if (lval < k) lval = k;
+    if (lval > a.l_cap) {
+        if (lane == 0) atomicOr(a.status, 4);
+        lval = a.l_cap;
+    }
+    for (int i = lane; i < a.k_stride; i += 32) {
+        out_ids[i] = 0xFFFFFFFFu;
+        out_d[i] = f_inf();
+    }
+    if (k == 0 || ix.n_total == 0) {
+        if (a.stats_out && lane == 0) a.stats_out[q] = qg_search_stats{};
+        return;
+    }
+
+    QueryRegs<D> qr;
+    load_query<D>(qr, a.codes + static_cast<size_t>(q) * D, sub);
+
+    int pn = 0;  // pool size (warp-uniform)
+    if (ix.n_base != 0) {
+        if (lane == 0) tags[0] = static_cast<uint16_t>(tag);
+        const float4 h = ix.hdr[0];
+        const float d0 = restore_distance_hw<D>(ix.codes, rr, h.x, h.y, half_sum, qn2, lane & 15);
+        if (lane == 0) {
+            s.pd[0] = d0;
+            s.pid[0] = 0;
+            s.plb[0] = kFltMax;
+        }
+        pn = 1;
+        st[VIS] += 1;
+        st[DC] += 1;
+        st[REMC] += 1;
+    }
+    __syncwarp();
+
+    const int beam = a.beam_width < 1 ? 1 : (a.beam_width > kMaxBeam ? kMaxBeam : a.beam_width);
+    int stall = 0;
+    int hops_done = 0;
+    bool failed = false;
+    for (;;) {
+        const float back_before = pn > 0 ? s.pd[pn - 1] : 0.0f;
+        // frontier: first `beam` unexpanded pool entries, marked expanded
+        int nf = 0;
+        for (int base = 0; base < pn && nf < beam; base += 32) {
+            const int i = base + lane;
+            const bool un = i < pn && !(s.pid[i] & kExpanded);
+            unsigned int m = __ballot_sync(0xffffffffu, un);
+            while (m && nf < beam) {
+                const int b = __ffs(m) - 1;
+                m &= m - 1;
+                if (lane == b) {
+                    s.frontier[nf] = s.pid[i] & kIdMask;
+                    s.pid[i] |= kExpanded;
+                }
+                ++nf;
+            }
+        }
+        __syncwarp();
+        if (nf == 0) break;
+        if (++hops_done > a.hop_cap) {
+            if (lane == 0) atomicOr(a.status, 2);
+            break;
+        }
+
+        for (int fi = 0; fi < nf; ++fi) {
+            const uint32_t node = s.frontier[fi];
+            const uint32_t deg = min(ix.degrees[node], ix.edge_stride);
+            const uint32_t *adj = ix.edges + static_cast<size_t>(node) * ix.edge_stride;
+            // ---- fresh neighbours in adjacency order (VisitedScratch::try_mark) ----
+            int F = 0;
+            bool oob = false;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int j = lane + 32 * h;
+                const bool valid = j < static_cast<int>(deg);
+                const uint32_t nb = valid ? adj[j] : 0u;
+                const bool bad = valid && nb >= ix.n_total;
+                const uint32_t key = (valid && !bad) ? nb : (0x80000000u | static_cast<uint32_t>(j));
+                const unsigned int same = __match_any_sync(0xffffffffu, key);
+                const bool leader = (__ffs(same) - 1) == lane;
+                bool fresh = false;
+                if (valid && !bad && leader) {
+                    if (tags[nb] != static_cast<uint16_t>(tag)) {
+                        tags[nb] = static_cast<uint16_t>(tag);
+                        fresh = true;
+                    }
+                }
+                if (__any_sync(0xffffffffu, bad)) oob = true;
+                const unsigned int fm = __ballot_sync(0xffffffffu, fresh);
+                if (fresh) s.fid[F + __popc(fm & ((1u << lane) - 1u))] = nb;
+                F += __popc(fm);
+                __syncwarp();
+            }
+            if (oob) {
+                failed = true;
+                break;
+            }
+            if (F == 0) continue;
+            st[VIS] += F;
+            st[MSBC] += F;
+
+            // ---- gate (paper-prune lower bound) for every fresh neighbour ----
+            for (int f = lane; f < F; f += 32) s.fpf[f] = ix.pf[s.fid[f]];
+            if constexpr (L::LPN == 32) {
+                constexpr int G = L::GG;
+                for (int gb = 0; gb < F; gb += G) {
+                    uint32_t w[G][L::CPL];
+#pragma unroll
+                    for (int g = 0; g < G; ++g) {
+                        const int f = gb + g < F ? gb + g : gb;
+                        const uint32_t *row = reinterpret_cast<const uint32_t *>(
+                            ix.msb + static_cast<size_t>(s.fid[f]) * (D / 8));
+#pragma unroll
+                        for (int j = 0; j < L::CPL; ++j) w[g][j] = __ldg(row + lane + 32 * j);
+                    }
+                    int p[G];
+#pragma unroll
+                    for (int g = 0; g < G; ++g) {
+                        int acc = 0;
+#pragma unroll
+                        for (int j = 0; j < L::CPL; ++j) acc = gate_chunk(w[g][j], qr.xn[j], acc);
+                        p[g] = acc;
+                    }
+                    const int tot = reduce_scatter<G>(p, lane);
+                    const int f = gb + lane;
+                    if (lane < G && f < F) {
+                        const GateOut go = finish_gate(tot, s.fpf[f], scale, csum, qn, qn2, a.eps);
+                        s.flb[f] = go.lower_bound;
+                        s.fsip[f] = go.short_ip;
+                        s.fval[f] = go.valid ? 1 : 0;
+                    }
+                }
+            } else {
+                constexpr int P = L::PG;
+                for (int fb = 0; fb < F; fb += P * L::NBP) {
+                    uint32_t w[P];
+#pragma unroll
+                    for (int pp = 0; pp < P; ++pp) {
+                        int f = fb + pp * L::NBP + grp;
+                        f = f < F ? f : fb;
+                        const uint32_t *row = reinterpret_cast<const uint32_t *>(
+                            ix.msb + static_cast<size_t>(s.fid[f]) * (D / 8));
+                        w[pp] = __ldg(row + sub);
+                    }
+#pragma unroll
+                    for (int pp = 0; pp < P; ++pp) {
+                        int acc = gate_chunk(w[pp], qr.xn[0], 0);
+#pragma unroll
+                        for (int o = 1; o < L::LPN; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                        const int f = fb + pp * L::NBP + grp;
+                        if (sub == 0 && f < F) {
+                            const GateOut go = finish_gate(acc, s.fpf[f], scale, csum, qn, qn2, a.eps);
+                            s.flb[f] = go.lower_bound;
+                            s.fsip[f] = go.short_ip;
+                            s.fval[f] = go.valid ? 1 : 0;
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+
+            // ---- first check against the pool tail (ours_diskann.rs:1708-1725) ----
+            int S = 0;
+            {
+                const bool full = pn >= lval;
+                const float tail = full ? s.pd[lval - 1] : kFltMax;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int f = lane + 32 * h;
+                    const bool in = f < F;
+                    const bool prune = in && full && s.fval[f] && s.flb[f] > tail;
+                    const bool keep = in && !prune;
+                    const unsigned int pm = __ballot_sync(0xffffffffu, prune);
+                    const unsigned int km = __ballot_sync(0xffffffffu, keep);
+                    if (keep) {
+                        const int at = S + __popc(km & ((1u << lane) - 1u));
+                        s.sid[at] = s.fid[f];
+                        s.sslot[at] = static_cast<uint32_t>(f);
+                    }
+                    st[CHK] += __popc(pm);
+                    st[WPR] += __popc(pm);
+                    st[SAVED] += __popc(pm);
+                    S += __popc(km);
+                }
+            }
+            __syncwarp();
+            if (S == 0) continue;
+
+            // ---- traversal distances of the survivors ----
+            for (int i = lane; i < S; i += 32) {
+                const float4 h = ix.hdr[s.sid[i]];
+                s.shdr[i] = make_float2(h.x, h.y);
+            }
+            bool any_full = false;
+            if constexpr (L::LPN == 32) {
+                constexpr int G = L::GT;
+                for (int gb = 0; gb < S; gb += G) {
+                    uint4 c[G][L::CPL];
+#pragma unroll
+                    for (int g = 0; g < G; ++g) {
+                        const int i = gb + g < S ? gb + g : gb;
+                        const uint4 *row = reinterpret_cast<const uint4 *>(
+                            ix.codes + static_cast<size_t>(s.sid[i]) * (D / 2));
+#pragma unroll
+                        for (int j = 0; j < L::CPL; ++j) c[g][j] = __ldg(row + lane + 32 * j);
+                    }
+                    int p[G];
+#pragma unroll
+                    for (int g = 0; g < G; ++g) {
+                        int acc = 0;
+#pragma unroll
+                        for (int j = 0; j < L::CPL; ++j) acc = trav_chunk(c[g][j], qr.xe[j], qr.xo[j], acc);
+                        p[g] = acc;
+                    }
+                    const int tot = reduce_scatter<G>(p, lane);
+                    const int i = gb + lane;
+                    if (lane < G && i < S) {
+                        const uint32_t slot = s.sslot[i];
+                        const float2 h = s.shdr[i];
+                        s.sdist[i] = finish_traversal(h.x, h.y, s.fsip[slot], tot, scale, csum, qn2);
+                    }
+                }
+            } else {
+                constexpr int P = L::PG;
+                for (int ib = 0; ib < S; ib += P * L::NBP) {
+                    uint4 c[P];
+#pragma unroll
+                    for (int pp = 0; pp < P; ++pp) {
+                        int i = ib + pp * L::NBP + grp;
+                        i = i < S ? i : ib;
+                        const uint4 *row = reinterpret_cast<const uint4 *>(
+                            ix.codes + static_cast<size_t>(s.sid[i]) * (D / 2));
+                        c[pp] = __ldg(row + sub);
+                    }
+#pragma unroll
+                    for (int pp = 0; pp < P; ++pp) {
+                        int acc = trav_chunk(c[pp], qr.xe[0], qr.xo[0], 0);
+#pragma unroll
+                        for (int o = 1; o < L::LPN; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                        const int i = ib + pp * L::NBP + grp;
+                        if (sub == 0 && i < S) {
+                            const uint32_t slot = s.sslot[i];
+                            const float2 h = s.shdr[i];
+                            s.sdist[i] = finish_traversal(h.x, h.y, s.fsip[slot], acc, scale, csum, qn2);
+                        }
+                    }
+                }
+            }
+            __syncwarp();
+            // survivors whose gate was invalid use the full FP32 restore (mode 0)
+            for (int i = 0; i < S; ++i) any_full |= s.fval[s.sslot[i]] == 0;
+            if (any_full) {
+                for (int i = 0; i < S; ++i) {
+                    if (s.fval[s.sslot[i]]) continue;
+                    const uint32_t id = s.sid[i];
+                    const float2 h = s.shdr[i];
+                    const float d = restore_distance_hw<D>(ix.codes + static_cast<size_t>(id) * (D / 2),
+                                                           rr, h.x, h.y, half_sum, qn2, lane & 15);
+                    if (lane == 0) s.sdist[i] = d;
+                    __syncwarp();
+                }
+            }
+            __syncwarp();
+
+            // ---- re-check and sorted insert in adjacency order (ours_diskann.rs:1944-1979) ----
+            for (int i = 0; i < S; ++i) {
+                const uint32_t slot = s.sslot[i];
+                const bool valid = s.fval[slot] != 0;
+                const float lb = s.flb[slot];
+                const float d = s.sdist[i];
+                const uint32_t id = s.sid[i];
+                const bool full = pn >= lval;
+                if (full && valid) {
+                    st[CHK] += 1;
+                    if (lb > s.pd[lval - 1]) {
+                        st[WPR] += 1;
+                        st[SAVED] += 1;
+                        continue;
+                    }
+                    st[NPR] += 1;
+                }
+                st[REMC] += 1;
+                st[DC] += 1;
+                // insert_candidate_sorted (ours_diskann.rs:1100-1126)
+                if (full && !cand_less(d, id, s.pd[lval - 1], s.pid[lval - 1] & kIdMask)) continue;
+                int pos = 0;
+                for (int base = 0; base < pn; base += 32) {
+                    const int e = base + lane;
+                    const bool lt = e < pn && cand_less(s.pd[e], s.pid[e] & kIdMask, d, id);
+                    const unsigned int m = __ballot_sync(0xffffffffu, lt);
+                    pos += __popc(m);
+                    if (m != 0xffffffffu) break;
+                }
+                const int newn = pn + 1 < lval ? pn + 1 : lval;
+                for (int top = newn - 1; top > pos; top -= 32) {
+                    const int e = top - lane;
+                    float vd = 0.0f, vl = 0.0f;
+                    uint32_t vi = 0;
+                    const bool mv = e > pos;
+                    if (mv) {
+                        vd = s.pd[e - 1];
+                        vi = s.pid[e - 1];
+                        vl = s.plb[e - 1];
+                    }
+                    __syncwarp();
+                    if (mv) {
+                        s.pd[e] = vd;
+                        s.pid[e] = vi;
+                        s.plb[e] = vl;
+                    }
+                    __syncwarp();
+                }
+                if (lane == 0) {
+                    s.pd[pos] = d;
+                    s.pid[pos] = id;
+                    s.plb[pos] = valid ? lb : kFltMax;
+                }
+                pn = newn;
+                __syncwarp();
+            }
+        }
+        if (failed) break;
+        st[HOPS] += nf;
+        if (a.kth_stop && pn >= k) {
+            const float kth = s.pd[k - 1];
+            float mlb = kFltMax;
+            for (int e = lane; e < pn; e += 32)
+                if (!(s.pid[e] & kExpanded)) mlb = fminf(mlb, s.plb[e]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) mlb = fminf(mlb, __shfl_xor_sync(0xffffffffu, mlb, o));
+            if (kth <= mlb) break;
+        }
+        if (a.early_stop_hops != 0 && pn >= lval) {
+            const float back_after = pn > 0 ? s.pd[pn - 1] : 0.0f;
+            stall = back_after >= back_before ? stall + 1 : 0;
+            if (stall >= a.early_stop_hops) break;
+        }
+    }
+
+    if (failed) {
+        if (lane == 0) atomicOr(a.status, 1);
+        if (a.stats_out && lane == 0) a.stats_out[q] = qg_search_stats{};
+        return;
+    }
+
+    // ---- rerank (ours_diskann.rs:1813-1902) ----
+    // candidates: the first min(#base entries, max(rerank, k)) pool entries with id < n_base,
+    // compacted in place (write index <= read index).
+    const int want = a.rerank > k ? a.rerank : k;
+    int m = 0;
+    for (int base = 0; base < pn && m < want; base += 32) {
+        const int e = base + lane;
+        uint32_t id = 0;
+        float d = 0.0f;
+        bool in = false;
+        if (e < pn) {
+            id = s.pid[e] & kIdMask;
+            d = s.pd[e];
+            in = id < ix.n_base;
+        }
+        const unsigned int bm = __ballot_sync(0xffffffffu, in);
+        const int at = m + __popc(bm & ((1u << lane) - 1u));
+        __syncwarp();
+        if (in && at < want) {
+            s.pid[at] = id;
+            s.pd[at] = d;
+        }
+        m += __popc(bm);
+        __syncwarp();
+    }
+    if (m > want) m = want;
+    // FP32 4-bit restore (mode 0), two records per pass (one per half-warp)
+    for (int base = 0; base < m; base += 2) {
+        const int e = base + (lane >> 4);
+        const int ee = e < m ? e : base;
+        const uint32_t id = s.pid[ee];
+        const float4 h = ix.hdr[id];
+        const float d = restore_distance_hw<D>(ix.codes + static_cast<size_t>(id) * (D / 2), rr,
+                                               h.x, h.y, half_sum, qn2, lane & 15);
+        if ((lane & 15) == 0 && e < m) s.pd[e] = d;
+    }
+    __syncwarp();
+    // residual correction, one record per lane
+    for (int e = lane; e < m; e += 32) {
+        const uint32_t id = s.pid[e];
+        float est, lo, hi;
+        residual_interval_thread<D>(ix.res_scales + static_cast<size_t>(id) * (D / 16),
+                                    ix.res_codes + static_cast<size_t>(id) * (D / 2), rr, s.pd[e],
+                                    qn, &est, &lo, &hi);
+        s.plb[e] = est;
+    }
+    __syncwarp();
+    // top-k by (estimate, id): rank of each candidate among all candidates
+    for (int e = lane; e < m; e += 32) {
+        const float me = s.plb[e];
+        const uint32_t mi = s.pid[e];
+        int rank = 0;
+        for (int o = 0; o < m; ++o) {
+            const float oe = s.plb[o];
+            const uint32_t oi = s.pid[o];
+            rank += (oe < me || (!(me < oe) && oi < mi)) ? 1 : 0;
+        }
+        if (rank < k) {
+            out_ids[rank] = mi;
+            out_d[rank] = me;
+        }
+    }
+    if (a.stats_out && lane == 0) {
+        qg_search_stats o;
+        o.visited_nodes = st[VIS];
+        o.distance_computations = st[DC];
+        o.hops = st[HOPS];
+        o.paper_checked = st[CHK];
+        o.paper_would_prune = st[WPR];
+        o.paper_not_pruned = st[NPR];
+        o.paper_full_saved = st[SAVED];
+        o.paper_msb_kernel_calls = st[MSBC];
+        o.paper_remaining_kernel_calls = st[REMC];
+        a.stats_out[q] = o;
+    }
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) search_kernel(SearchArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    const WarpSmem s = carve(smem + warp * warp_smem_bytes(a.l_cap), a.l_cap);
+    const int slot = blockIdx.x * wpb + warp;
+    uint16_t *tags = a.tags + static_cast<size_t>(slot) * a.ix.n_total;
+    for (;;) {
+        int q = 0;
+        if (lane == 0) q = static_cast<int>(atomicAdd(a.counter, 1u));
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= a.nq) break;
+        uint32_t e = a.epochs[slot] + 1;
+        if ((e & 0xFFFFu) == 0) {
+            // 16-bit tags wrapped: clear this slot's tags once every 65535 queries
+            for (size_t i = lane; i < a.ix.n_total; i += 32) tags[i] = 0;
+            __syncwarp();
+            e += 1;
+        }
+        if (lane == 0) a.epochs[slot] = e;
+        search_one<D>(a, s, q, lane, tags, e & 0xFFFFu);
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+size_t search_smem_per_warp(int code_dim, int l_cap) {
+    (void)code_dim;
+    return warp_smem_bytes(l_cap);
+}
+
+int search_supported_dim(int code_dim) {
+    return code_dim == 64 || code_dim == 128 || code_dim == 256 || code_dim == 512 ||
+           code_dim == 1024 || code_dim == 2048;
+}
+
+template <int D>
+static cudaError_t launch_d(const SearchArgs &a, int grid, int wpb, cudaStream_t stream) {
+    const size_t smem = warp_smem_bytes(a.l_cap) * static_cast<size_t>(wpb);
+    cudaError_t e = cudaFuncSetAttribute(search_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    search_kernel<D><<<grid, wpb * 32, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
+template <int D>
+static int blocks_per_sm_d(int l_cap, int wpb) {
+    const size_t smem = warp_smem_bytes(l_cap) * static_cast<size_t>(wpb);
+    if (cudaFuncSetAttribute(search_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem)) != cudaSuccess)
+        return 0;
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, search_kernel<D>, wpb * 32, smem) != cudaSuccess)
+        return 0;
+    return blocks;
+}
+
+int search_blocks_per_sm(int code_dim, int l_cap, int wpb) {
+    switch (code_dim) {
+        case 64: return blocks_per_sm_d<64>(l_cap, wpb);
+        case 128: return blocks_per_sm_d<128>(l_cap, wpb);
+        case 256: return blocks_per_sm_d<256>(l_cap, wpb);
+        case 512: return blocks_per_sm_d<512>(l_cap, wpb);
+        case 1024: return blocks_per_sm_d<1024>(l_cap, wpb);
+        case 2048: return blocks_per_sm_d<2048>(l_cap, wpb);
+        default: return 0;
+    }
+}
+
+cudaError_t launch_search(const SearchArgs &a, int grid, int wpb, cudaStream_t stream) {
+    switch (a.ix.code_dim) {
+        case 64: return launch_d<64>(a, grid, wpb, stream);
+        case 128: return launch_d<128>(a, grid, wpb, stream);
+        case 256: return launch_d<256>(a, grid, wpb, stream);
+        case 512: return launch_d<512>(a, grid, wpb, stream);
+        case 1024: return launch_d<1024>(a, grid, wpb, stream);
+        case 2048: return launch_d<2048>(a, grid, wpb, stream);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace qg

@@ -1,0 +1,139 @@
+"""Generates the golden fixtures under tests/golden/ from the REFERENCE ITSELF.
+
+Runs only on a host that has the reference tree: oracle/Makefile compiles the reference's
+own experiments/02_diskann_fair/native/rabitq_bridge.cpp (with the reference's flags,
+-O3 -march=native on x86-64) into oracle/_ref/libqg_ref.so. Every expected value below comes
+from that library: encode (rabitq_encode_full + copy_compact / copy_residual_record), the
+sidecar (rabitq_export_paper_sidecar), the INT8 prepared query (read from the reference's
+PreparedQuery), the batched gate / distance / residual kernels, the Vamana graph
+(rabitq_build_vamana_graph) and search results, where the Rust hot loop of
+ours_diskann.rs:1539-1986 (which cannot be built here) is driven over the reference's own
+bridge kernels (oracle/ref_probe.cpp).
+
+Inputs are regenerated from numpy seeds in the tests; a checksum of each input is stored
+to catch generator drift.  Usage:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import platform
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle_py  # noqa: E402
+sys.path.insert(0, HERE)
+from cases import c1_data, c2_data, c3_data, kernel_inputs  # noqa: E402
+
+FLAGS = "g++ -std=c++20 -O3 -march=native -fopenmp (experiments/02_diskann_fair/build.rs:22-36)"
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def kernel_case(name: str, dim: int, n: int, nq: int, seed: int, center_value: float | None):
+    """Kernel-level golden vectors for every query x every record."""
+    X, Q = kernel_inputs(dim, n, nq, seed)
+    center = (np.full(dim, center_value, np.float32) if center_value is not None
+              else X.mean(0).astype(np.float32))
+    ref = oracle_py.Reference(dim, center)
+    full = np.stack([ref.encode_full(x) for x in X])
+    compact, residual = ref.encode(X)
+    msb, factors = ref.sidecar(compact)
+    ids = np.arange(n, dtype=np.uint32)
+    out = dict(dim=dim, n=n, nq=nq, seed=seed, center=center, x_sha=sha(X), q_sha=sha(Q), full=full,
+               compact=compact, residual=residual, msb=msb, factors=factors)
+    rr, codes, scal, csum, gate, d2, d0, res, dsingle = [], [], [], [], [], [], [], [], []
+    for q in Q:
+        p = ref.prepare(q)
+        rr.append(p["rotated_residual"])
+        codes.append(p["codes"])
+        scal.append([p["query_norm_sqr"], p["query_norm"], p["half_sum"], p["scale"]])
+        csum.append(p["code_sum"])
+        g = ref.gate(ids, msb, factors, 1.9)
+        gate.append(g.view(np.uint8).reshape(n, -1))
+        d2.append(ref.distance(ids, np.full(n, 2, np.uint8), compact, g["short_ip"]))
+        dd0 = ref.distance(ids, np.zeros(n, np.uint8), compact, np.zeros(n, np.float32))
+        d0.append(dd0)
+        dsingle.append(np.array([ref.distance_single(compact[i]) for i in range(n)], np.float32))
+        res.append(ref.residual(ids, compact, residual, dd0).view(np.float32).reshape(n, 3))
+    out.update(rotated_residual=np.array(rr), codes=np.array(codes), scalars=np.array(scal, np.float32),
+               code_sum=np.array(csum, np.int64), gate=np.array(gate), dist_mode2=np.array(d2),
+               dist_mode0=np.array(d0), dist_single=np.array(dsingle), residual_iv=np.array(res))
+    sym = np.array([[ref.symmetric_distance(compact[i], compact[j]) for j in range(min(n, 16))]
+                    for i in range(min(n, 16))], np.float32)
+    out["symmetric"] = sym
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    print(name, "written")
+
+
+def search_case(name: str, data_fn, dim: int, n: int, nq: int, seed: int, M: int, l_build: int,
+                refine: int, cap: int, stop: int, batch: int, Ls, ks=(10,), extra=None):
+    X, Q = data_fn()
+    center = X.mean(0).astype(np.float32)  # N <= 100k: the reference centre is the f32 mean
+    ref = oracle_py.Reference(dim, center)
+    compact, residual = ref.encode(X)
+    deg, edges = ref.build_graph(compact, r=M, l_build=l_build, alpha=1.2, batch=batch, refine=refine,
+                                 cap=cap, stop_hops=stop)
+    msb, factors = ref.sidecar(compact)
+    index = dict(compact=compact, residual=residual, msb=msb, factors=factors, degrees=deg, edges=edges,
+                 total_points=n, base_points=n)
+    orc = oracle_py.Oracle(dim, center)
+    gt, gtd = orc.exact_knn(X, Q, 100)
+    out = dict(dim=dim, n=n, nq=nq, seed=seed, center=center, x_sha=sha(X), q_sha=sha(Q), compact=compact,
+               residual=residual, msb=msb, factors=factors, degrees=deg, edges=edges, gt=gt,
+               Ls=np.array(Ls), ks=np.array(ks))
+    for L in Ls:
+        for k in ks:
+            ids, dists, stats = ref.search(Q, index, k=k, L=L, eps=1.9, rerank=100)
+            out[f"ids_L{L}_k{k}"] = ids
+            out[f"dists_L{L}_k{k}"] = dists
+            out[f"stats_L{L}_k{k}"] = stats.view(np.uint64).reshape(nq, -1)
+            rec = np.mean([len(set(a[:10]) & set(b[:10])) / 10 for a, b in zip(ids, gt)]) if k >= 10 else -1
+            print(f"  {name} L={L} k={k} recall@10={rec:.4f}")
+    if extra:
+        extra(out, ref, Q, index)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **out)
+    print(name, "written")
+
+
+def c1_extras(out, ref, Q, index):
+    # beam width 2, kth stop, early stop, and k=1 / k=100 with L < k
+    for tag, kw in (("beam2", dict(beam=2, L=40, k=10)), ("kth", dict(kth_stop=True, L=40, k=10)),
+                    ("stall", dict(early_stop=2, L=40, k=10)), ("k100", dict(L=40, k=100)),
+                    ("k1", dict(L=20, k=1))):
+        ids, dists, stats = ref.search(Q, index, eps=1.9, rerank=100, **kw)
+        out[f"ids_{tag}"] = ids
+        out[f"dists_{tag}"] = dists
+        out[f"stats_{tag}"] = stats.view(np.uint64).reshape(len(Q), -1)
+
+
+def main():
+    oracle_py.build(ref=True)
+    if not oracle_py.reference_available():
+        raise SystemExit("the reference library could not be built")
+    kernel_case("kernels_d128", 128, 64, 8, seed=20260813, center_value=0.05)
+    kernel_case("kernels_d100", 100, 48, 4, seed=5, center_value=None)
+    kernel_case("kernels_d960", 960, 96, 4, seed=6, center_value=None)
+    kernel_case("kernels_d1536", 1536, 64, 3, seed=7, center_value=None)
+    search_case("search_c1", c1_data, 128, 2000, 50, 11, M=32, l_build=100, refine=1, cap=256, stop=2,
+                batch=256, Ls=(20, 40, 80), extra=c1_extras)
+    search_case("search_c2", c2_data, 960, 1500, 24, 21, M=32, l_build=64, refine=1, cap=256, stop=2,
+                batch=256, Ls=(40, 100))
+    search_case("search_c3", c3_data, 1536, 1000, 16, 31, M=32, l_build=64, refine=1, cap=256, stop=2,
+                batch=256, Ls=(40,))
+    with open(os.path.join(HERE, "PROVENANCE.txt"), "w") as f:
+        f.write(f"generated by tests/golden/make_golden.py on {platform.machine()} {platform.processor()}\n")
+        f.write(f"reference bridge compiled with: {FLAGS}\n")
+        f.write("search results: the restated Rust hot loop driven over the reference bridge kernels\n")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,67 @@
+"""The C-ABI library builds for sm_103a, loads without a GPU and exports every entry point of
+include/qgraph_gb300.h; the product package never reaches the oracle."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "qgraph_gb300.h")
+
+
+def header_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b((?:rabitq|qg)_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_reference_bridge_symbols():
+    names = header_functions()
+    assert len([n for n in names if n.startswith("rabitq_")]) == 37
+
+
+def test_library_builds_and_exports_every_symbol():
+    from quantization_graph_gb300 import build
+
+    lib = build.build()
+    out = subprocess.run(["nm", "-D", "--defined-only", lib], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r" T (\w+)$", out, flags=re.M))
+    missing = [n for n in header_functions() if n not in exported]
+    assert not missing, missing
+    handle = ctypes.CDLL(lib)  # loads without a GPU (no CUDA call at load time)
+    for n in header_functions():
+        getattr(handle, n)
+
+
+def test_python_bindings_cover_the_header():
+    from quantization_graph_gb300 import _native
+
+    assert sorted(_native.exported_symbols()) == header_functions()
+
+
+def test_library_targets_sm103a():
+    from quantization_graph_gb300 import build
+
+    assert "arch=compute_103a,code=sm_103a" in build.ARCH
+
+
+def test_package_never_imports_the_oracle():
+    pkg = os.path.join(ROOT, "quantization_graph_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        if "_build" in dirpath:
+            continue
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".cpp", ".h")):
+                src = open(os.path.join(dirpath, f)).read()
+                assert "oracle_py" not in src and "qg_oracle" not in src and "libqg_ref" not in src, f
+
+
+def test_record_layout_sizes(oracle):
+    # space_rabitq.h:2842-2868 with the formal bridge config (external residuals)
+    for dim, D, compact, residual, msb in ((128, 128, 81, 88, 16), (960, 1024, 529, 648, 128),
+                                           (1024, 1024, 529, 648, 128), (1536, 2048, 1041, 1288, 256)):
+        o = oracle.Oracle(dim, np.zeros(dim, np.float32))
+        assert (o.D, o.compact_bytes, o.residual_bytes, o.msb_bytes) == (D, compact, residual, msb)

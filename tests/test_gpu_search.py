@@ -1,0 +1,133 @@
+"""Persistent batched GPU search against the reference's search results (ids, distance bits
+and the nine OursPaperSearchStats counters, as verify_search_parity compares them,
+ours_diskann.rs:1988-2066) and against the oracle on edge cases."""
+import numpy as np
+import pytest
+
+from cases import SEARCH_CASES
+from conftest import golden_index, load_golden
+
+pytestmark = pytest.mark.gpu
+
+VARIANTS = {"beam2": dict(beam_width=2, l_value=40, k=10), "kth": dict(kth_stop=True, l_value=40, k=10),
+            "stall": dict(early_stop_hops=2, l_value=40, k=10), "k100": dict(l_value=40, k=100),
+            "k1": dict(l_value=20, k=1)}
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def make_index(torch, g, degrees=None, edges=None, total=None):
+    from quantization_graph_gb300.index import OursIndex
+    from quantization_graph_gb300.space import RabitqSpace
+
+    sp = RabitqSpace(int(g["dim"]), g["center"])
+    ix = OursIndex(sp, g["compact"], g["residual"], g["msb"], g["factors"],
+                   g["degrees"] if degrees is None else degrees, g["edges"] if edges is None else edges,
+                   base_points=int(g["n"]), total_points=total)
+    return sp, ix
+
+
+def stats_matrix(st):
+    return st.view(np.uint64).reshape(len(st), -1)
+
+
+@pytest.mark.parametrize("name", list(SEARCH_CASES))
+def test_search_matches_reference(cuda, name):
+    torch = cuda
+    g = load_golden(name)
+    _, Q = SEARCH_CASES[name]()
+    sp, ix = make_index(torch, g)
+    for L in g["Ls"]:
+        for k in g["ks"]:
+            r = ix.search(torch.from_numpy(Q).cuda(), k=int(k), l_value=int(L))
+            np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), g[f"ids_L{L}_k{k}"])
+            np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(g[f"dists_L{L}_k{k}"]))
+            np.testing.assert_array_equal(stats_matrix(r.stats), g[f"stats_L{L}_k{k}"])
+
+
+@pytest.mark.parametrize("tag", list(VARIANTS))
+def test_search_variants_match_reference(cuda, tag):
+    torch = cuda
+    g = load_golden("search_c1")
+    _, Q = SEARCH_CASES["search_c1"]()
+    sp, ix = make_index(torch, g)
+    r = ix.search(torch.from_numpy(Q).cuda(), **VARIANTS[tag])
+    np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), g[f"ids_{tag}"])
+    np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(g[f"dists_{tag}"]))
+    np.testing.assert_array_equal(stats_matrix(r.stats), g[f"stats_{tag}"])
+
+
+def test_uneven_per_query_k_and_l_match_oracle(cuda, oracle):
+    torch = cuda
+    g = load_golden("search_c1")
+    _, Q = SEARCH_CASES["search_c1"]()
+    sp, ix = make_index(torch, g)
+    rng = np.random.default_rng(5)
+    ks = rng.choice([1, 10, 100], size=len(Q)).astype(np.int32)
+    ls = rng.integers(5, 150, size=len(Q)).astype(np.int32)
+    r = ix.search(torch.from_numpy(Q).cuda(), k=100, l_value=150, k_per_query=torch.from_numpy(ks),
+                  l_per_query=torch.from_numpy(ls))
+    o = oracle.Oracle(128, g["center"])
+    gi = golden_index(g)
+    ids = r.ids.cpu().numpy().astype(np.uint32)
+    d = r.distances.cpu().numpy()
+    for i in range(len(Q)):
+        oi, od, os_ = o.search(Q[i:i + 1], gi, k=int(ks[i]), L=int(ls[i]))
+        np.testing.assert_array_equal(ids[i, :ks[i]], oi[0])
+        np.testing.assert_array_equal(bits(d[i, :ks[i]]), bits(od[0]))
+        np.testing.assert_array_equal(stats_matrix(r.stats[i:i + 1]), stats_matrix(os_))
+        assert (ids[i, ks[i]:] == 0xFFFFFFFF).all()
+
+
+def test_duplicates_frozen_point_and_short_lists(cuda, oracle):
+    """Adjacency with duplicate ids and a frozen start point appended last (adjacency [0])."""
+    torch = cuda
+    g = load_golden("search_c1")
+    _, Q = SEARCH_CASES["search_c1"]()
+    n = int(g["n"])
+    deg = g["degrees"].copy()
+    edges = g["edges"].copy()
+    for i in range(0, n, 7):
+        if deg[i] >= 3:
+            edges[i, 2] = edges[i, 0]   # duplicate neighbour inside one list
+    deg[::11] = np.minimum(deg[::11], 1)  # very short lists
+    deg = np.concatenate([deg, [1]]).astype(np.uint32)
+    edges = np.concatenate([edges, np.zeros((1, edges.shape[1]), np.uint32)])
+    sp, ix = make_index(torch, g, degrees=deg, edges=edges, total=n + 1)
+    r = ix.search(torch.from_numpy(Q).cuda(), k=10, l_value=40)
+    gi = golden_index(g)
+    gi.update(degrees=deg, edges=edges, total_points=n + 1)
+    oi, od, os_ = oracle.Oracle(128, g["center"]).search(Q, gi, k=10, L=40)
+    np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), oi)
+    np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(od))
+    np.testing.assert_array_equal(stats_matrix(r.stats), stats_matrix(os_))
+
+
+def test_out_of_range_neighbour_is_reported(cuda):
+    torch = cuda
+    g = load_golden("search_c1")
+    _, Q = SEARCH_CASES["search_c1"]()
+    edges = g["edges"].copy()
+    edges[0, 0] = 10 ** 6  # >= total points: the reference returns an error for the query
+    sp, ix = make_index(torch, g, edges=edges)
+    with pytest.raises(RuntimeError, match="QG_ERR_GRAPH"):
+        ix.search(torch.from_numpy(Q).cuda(), k=10, l_value=40)
+    # the index stays usable after the failed batch
+    sp2, ix2 = make_index(torch, g)
+    r = ix2.search(torch.from_numpy(Q[:4]).cuda(), k=10, l_value=40)
+    np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), g["ids_L40_k10"][:4])
+
+
+def test_empty_batch_and_repeated_calls(cuda):
+    torch = cuda
+    g = load_golden("search_c1")
+    _, Q = SEARCH_CASES["search_c1"]()
+    sp, ix = make_index(torch, g)
+    r0 = ix.search(torch.zeros((0, 128), device="cuda"), k=10, l_value=40)
+    assert r0.ids.shape == (0, 10)
+    # many batches through the same index exercise the visited-tag epochs
+    for _ in range(5):
+        r = ix.search(torch.from_numpy(Q).cuda(), k=10, l_value=40)
+        np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), g["ids_L40_k10"])

@@ -1,0 +1,119 @@
+"""The oracle (C++ restatement) against golden vectors produced by the reference itself.
+
+Everything here is bit-exact: codes, records, sidecars, INT8 query codes, every float of the
+gate / traversal / restore / residual kernels, and search ids, distances and counters.
+"""
+import numpy as np
+import pytest
+
+from cases import SEARCH_CASES, kernel_inputs
+from conftest import golden_index, load_golden, sha
+
+KERNEL_CASES = ["kernels_d128", "kernels_d100", "kernels_d960", "kernels_d1536"]
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+@pytest.mark.parametrize("name", KERNEL_CASES)
+def test_kernels_bit_exact(oracle, name):
+    g = load_golden(name)
+    dim, n, nq, seed = int(g["dim"]), int(g["n"]), int(g["nq"]), int(g["seed"])
+    X, Q = kernel_inputs(dim, n, nq, seed)
+    assert sha(X) == str(g["x_sha"]) and sha(Q) == str(g["q_sha"]), "input generator drifted"
+    o = oracle.Oracle(dim, g["center"])
+    full = np.stack([o.encode_full(x) for x in X])
+    np.testing.assert_array_equal(full, g["full"])
+    compact, residual = o.encode(X)
+    np.testing.assert_array_equal(compact, g["compact"])
+    np.testing.assert_array_equal(residual, g["residual"])
+    msb, factors = o.sidecar(g["compact"])
+    np.testing.assert_array_equal(msb, g["msb"])
+    np.testing.assert_array_equal(factors, g["factors"])
+    ids = np.arange(n, dtype=np.uint32)
+    for qi in range(nq):
+        p = o.prepare(Q[qi])
+        np.testing.assert_array_equal(bits(p["rotated_residual"]), bits(g["rotated_residual"][qi]))
+        np.testing.assert_array_equal(p["codes"], g["codes"][qi])
+        sc = np.array([p["query_norm_sqr"], p["query_norm"], p["half_sum"], p["scale"]], np.float32)
+        np.testing.assert_array_equal(bits(sc), bits(g["scalars"][qi]))
+        assert p["code_sum"] == int(g["code_sum"][qi])
+        est = o.gate(ids, g["msb"], g["factors"])
+        np.testing.assert_array_equal(est.view(np.uint8).reshape(n, -1)[:, :21], g["gate"][qi][:, :21])
+        sip = est["short_ip"]
+        d2 = o.distance(ids, np.full(n, 2, np.uint8), g["compact"], sip)
+        np.testing.assert_array_equal(bits(d2), bits(g["dist_mode2"][qi]))
+        d0 = o.distance(ids, np.zeros(n, np.uint8), g["compact"], np.zeros(n, np.float32))
+        np.testing.assert_array_equal(bits(d0), bits(g["dist_mode0"][qi]))
+        np.testing.assert_array_equal(bits(d0), bits(g["dist_single"][qi]))
+        iv = o.residual(ids, g["compact"], g["residual"], d0)
+        np.testing.assert_array_equal(bits(iv.view(np.float32).reshape(n, 3)), bits(g["residual_iv"][qi]))
+    m = g["symmetric"].shape[0]
+    sym = np.array([[o.symmetric_distance(g["compact"][i], g["compact"][j]) for j in range(m)] for i in range(m)],
+                   np.float32)
+    np.testing.assert_array_equal(bits(sym), bits(g["symmetric"]))
+
+
+@pytest.mark.parametrize("name", list(SEARCH_CASES))
+def test_search_loop_bit_exact(oracle, name):
+    g = load_golden(name)
+    X, Q = SEARCH_CASES[name]()
+    assert sha(X) == str(g["x_sha"]) and sha(Q) == str(g["q_sha"])
+    o = oracle.Oracle(int(g["dim"]), g["center"])
+    index = golden_index(g)
+    for L in g["Ls"]:
+        for k in g["ks"]:
+            ids, dists, stats = o.search(Q, index, k=int(k), L=int(L))
+            np.testing.assert_array_equal(ids, g[f"ids_L{L}_k{k}"])
+            np.testing.assert_array_equal(bits(dists), bits(g[f"dists_L{L}_k{k}"]))
+            np.testing.assert_array_equal(stats.view(np.uint64).reshape(len(Q), -1), g[f"stats_L{L}_k{k}"])
+
+
+VARIANTS = {"beam2": dict(beam=2, L=40, k=10), "kth": dict(kth_stop=True, L=40, k=10),
+            "stall": dict(early_stop=2, L=40, k=10), "k100": dict(L=40, k=100), "k1": dict(L=20, k=1)}
+
+
+@pytest.mark.parametrize("tag", list(VARIANTS))
+def test_search_variants_bit_exact(oracle, tag):
+    g = load_golden("search_c1")
+    _, Q = SEARCH_CASES["search_c1"]()
+    o = oracle.Oracle(128, g["center"])
+    ids, dists, stats = o.search(Q, golden_index(g), **VARIANTS[tag])
+    np.testing.assert_array_equal(ids, g[f"ids_{tag}"])
+    np.testing.assert_array_equal(bits(dists), bits(g[f"dists_{tag}"]))
+    np.testing.assert_array_equal(stats.view(np.uint64).reshape(len(Q), -1), g[f"stats_{tag}"])
+
+
+def test_golden_recall_is_sane():
+    g = load_golden("search_c1")
+    ids = g["ids_L40_k10"]
+    rec = np.mean([len(set(a) & set(b[:10])) / 10 for a, b in zip(ids, g["gt"])])
+    assert rec > 0.9
+
+
+def test_dither_seed_is_fnv1a(oracle):
+    q = np.linspace(-1, 1, 37).astype(np.float32)
+    o = oracle.Oracle(37, np.zeros(37, np.float32))
+    h = 1469598103934665603
+    for b in q.tobytes():
+        h ^= b
+        h = (h * 1099511628211) & (2 ** 64 - 1)
+    h ^= (0x9E3779B97F4A7C15 + ((h << 6) & (2 ** 64 - 1)) + (h >> 2)) & (2 ** 64 - 1)
+    assert o.dither_seed(q) == h
+    u = o.dither_draws(12345, 1000)
+    assert (u >= 0).all() and (u < 1).all()
+
+
+def test_reference_cross_check_random(oracle):
+    """When the reference library is present, compare on fresh random inputs too."""
+    if not oracle.reference_available():
+        pytest.skip("reference tree not present on this host")
+    rng = np.random.default_rng(99)
+    for dim in (64, 200, 1000):
+        X = (rng.standard_normal((40, dim)) * rng.uniform(0.1, 3, dim)).astype(np.float32)
+        c = X.mean(0).astype(np.float32)
+        o, r = oracle.Oracle(dim, c), oracle.Reference(dim, c)
+        np.testing.assert_array_equal(np.stack([o.encode_full(x) for x in X]), np.stack([r.encode_full(x) for x in X]))
+        po, pr = o.prepare(X[0] * 1.3), r.prepare(X[0] * 1.3)
+        np.testing.assert_array_equal(po["codes"], pr["codes"])
