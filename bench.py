@@ -1,0 +1,366 @@
+#!/usr/bin/env python
+"""Benchmark: QPS at recall@10 >= 0.95 of the Ours-DiskANN query path on one GB300.
+
+Workload (default): 1,000,000 base vectors x 1536-d, unit-norm anisotropic Gaussian
+(lambda_i ~ i^-0.8, seeded rotation), 10,000 queries drawn the same way, ExRaBitQ4 block16
+encoding on the GPU, degree-64 graph (this library's GPU builder: kNN-128 candidates, alpha
+1.2 robust prune, reverse edges), k = 10, INT8 query codec with the 1-bit paper-prune gate,
+residual4 top-100 rerank, fixed-L beam search with the smallest L from a sweep that reaches
+recall@10 >= 0.95 against an exact FP64 ground truth.
+
+One step = one batched search of all queries (one qg_search_batch: query preparation +
+persistent search kernel). `value` is device-timed with inputs resident in HBM; `e2e` adds the
+pinned host->device copy of the queries and the device->host copy of ids and distances.
+The index (~2.6 GB) exceeds the 129 MB L2, so no flush is needed between steps.
+
+--impl reference times the reference's search on the host cores instead (the CPU restatement
+of the reference, oracle/, all threads), on the same index and queries.
+Multi-GPU (torchrun): replicas only -- each rank searches its own copy; value sums ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--dim", type=int, default=1536)
+    ap.add_argument("--nq", type=int, default=10_000)
+    ap.add_argument("--M", type=int, default=64)
+    ap.add_argument("--k", type=int, default=10)
+    ap.add_argument("--target-recall", type=float, default=0.95)
+    ap.add_argument("--L", type=int, default=0, help="fixed L (0 = sweep)")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--skip-cpu", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def ground_truth(torch, base, queries, k):
+    """Exact top-k: FP32 GEMM shortlist of 64 per query, re-scored in FP64."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        bn = (base * base).sum(1)
+        short = []
+        for s in range(0, queries.shape[0], 1024):
+            q = queries[s:s + 1024]
+            d = torch.addmm(bn[None, :], q, base.T, beta=1.0, alpha=-2.0)
+            short.append(torch.topk(d, 64, dim=1, largest=False).indices)
+        short = torch.cat(short)
+        out = torch.empty((queries.shape[0], k), dtype=torch.int64, device=base.device)
+        for s in range(0, queries.shape[0], 1024):
+            cand = short[s:s + 1024]
+            diff = base[cand].double() - queries[s:s + 1024, None, :].double()
+            dd = (diff * diff).sum(-1)
+            order = torch.argsort(dd, dim=1, stable=True)[:, :k]
+            out[s:s + 1024] = torch.gather(cand, 1, order)
+        return out
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+def recall_at(ids, gt, k):
+    hit = (ids[:, :k, None] == gt[:, None, :k]).any(-1).sum().item()
+    return hit / (ids.shape[0] * k)
+
+
+def build_workload(torch, args, log):
+    from quantization_graph_gb300 import synthetic
+    from quantization_graph_gb300.graph_build import build_graph, reachable_fraction
+    from quantization_graph_gb300.index import OursIndex
+    from quantization_graph_gb300.space import RabitqSpace, train_global_center
+
+    t0 = time.time()
+    base = synthetic.anisotropic_torch(args.n, args.dim, 0.8, seed=1, normalize=True)
+    queries = synthetic.anisotropic_torch(args.nq, args.dim, 0.8, seed=2, normalize=True)
+    center = train_global_center(base)
+    space = RabitqSpace(args.dim, center)
+    torch.cuda.synchronize()
+    t1 = time.time()
+    compact, residual = space.encode(base)
+    torch.cuda.synchronize()
+    t_encode = time.time() - t1
+    msb, factors = space.export_paper_sidecar(compact)
+    t2 = time.time()
+    deg, edges = build_graph(space, base, compact, r=args.M, knn=2 * args.M, alpha=1.2, reverse=args.M)
+    torch.cuda.synchronize()
+    t_graph = time.time() - t2
+    reach = reachable_fraction(edges)
+    gt = ground_truth(torch, base, queries, args.k)
+    index = OursIndex(space, compact, residual, msb, factors, deg, edges)
+    log(f"setup: data {t1 - t0:.1f}s encode {t_encode:.2f}s graph {t_graph:.1f}s reachable {reach:.4f} "
+        f"index {index.device_bytes() / 1e9:.2f} GB")
+    return dict(base=base, queries=queries, space=space, index=index, gt=gt, compact=compact,
+                residual=residual, msb=msb, factors=factors, deg=deg, edges=edges, t_encode=t_encode,
+                t_graph=t_graph, reach=reach)
+
+
+def pick_l(torch, w, args, log):
+    if args.L:
+        r = w["index"].search(w["queries"], k=args.k, l_value=args.L, with_stats=False)
+        return args.L, recall_at(r.ids, w["gt"], args.k), {args.L: recall_at(r.ids, w["gt"], args.k)}
+    sweep = {}
+    chosen = None
+    for L in (10, 12, 14, 16, 20, 24, 28, 32, 40, 48, 56, 64, 80, 100, 128, 160, 200, 256, 320, 400):
+        if L < args.k:
+            continue
+        r = w["index"].search(w["queries"], k=args.k, l_value=L, with_stats=False)
+        rec = recall_at(r.ids, w["gt"], args.k)
+        sweep[L] = rec
+        log(f"  L={L} recall@{args.k}={rec:.4f}")
+        if rec >= args.target_recall:
+            chosen = L
+            break
+    if chosen is None:
+        chosen = max(sweep)
+    return chosen, sweep[chosen], sweep
+
+
+def algorithmic_bytes(stats, D, M, rerank, k):
+    """Bytes the search must read per query at their algorithmic size (device layout):
+    per hop 4 + 4*deg adjacency; per gated neighbour D/8 MSB + 16 factor bytes; per scored
+    survivor D/2 code + 16 header bytes; per reranked record 16 + D/2 + D/8 + D/2."""
+    s = stats
+    hops = s["hops"].astype(np.float64)
+    gated = s["paper_msb_kernel_calls"].astype(np.float64)
+    scored = s["paper_remaining_kernel_calls"].astype(np.float64)
+    rer = float(max(rerank, k))
+    per_q = hops * (4 + 4 * M) + gated * (D / 8 + 16) + scored * (D / 2 + 16) + rer * (16 + D / 2 + D / 8 + D / 2)
+    return float(per_q.sum())
+
+
+def cpu_baseline(w, args, L, log):
+    """Reference search restated on the CPU (oracle/), all host threads, bounded sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+
+    oracle_py.build()
+    o = oracle_py.Oracle(args.dim, w["space"].center)
+    index = dict(compact=w["compact"].cpu().numpy(), residual=w["residual"].cpu().numpy(),
+                 msb=w["msb"].cpu().numpy(), factors=w["factors"].cpu().numpy(),
+                 degrees=w["deg"].cpu().numpy().view(np.uint32), edges=w["edges"].cpu().numpy().view(np.uint32),
+                 total_points=args.n, base_points=args.n)
+    q = w["queries"].cpu().numpy()
+    threads = os.cpu_count() or 1
+    t = time.time()
+    o.search(q[:threads * 4], index, k=args.k, L=L, threads=threads)
+    per = (time.time() - t) / (threads * 4)
+    count = int(min(len(q), max(threads * 8, args.cpu_seconds / max(per, 1e-6))))
+    t = time.time()
+    ids, _, _ = o.search(q[:count], index, k=args.k, L=L, threads=threads)
+    el = time.time() - t
+    gt = w["gt"][:count].cpu().numpy()
+    rec = float(np.mean([len(set(a) & set(b)) / args.k for a, b in zip(ids, gt)]))
+    log(f"cpu oracle: {count} queries in {el:.2f}s on {threads} threads, recall {rec:.4f}")
+    return {"value": count / el, "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": f"{count} of {len(q)} queries at L={L}, k={args.k}, one query per thread"}, rec
+
+
+def main():
+    args = parse()
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference" and rank != 0:
+        return
+    if world > 1 and args.impl == "ours":
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    def log(msg):
+        if rank == 0:
+            print(msg, file=sys.stderr, flush=True)
+
+    from quantization_graph_gb300 import build as qbuild
+
+    qbuild.build()
+    w = build_workload(torch, args, log)
+    L, rec, sweep = pick_l(torch, w, args, log)
+    log(f"chosen L={L} recall={rec:.4f}")
+    workload = (f"{args.n} x {args.dim} unit-norm anisotropic (lambda_i ~ i^-0.8), M={args.M}, "
+                f"{args.nq} queries, k={args.k}, INT8 paper-prune gate, residual4 rerank 100, fixed-L beam L={L}")
+    config = {"workload": workload, "n": args.n, "dim": args.dim, "queries": args.nq, "M": args.M, "k": args.k,
+              "L": L, "recall@10": round(rec, 4), "graph": "GPU kNN-128 + alpha-1.2 prune + reverse edges",
+              "l2": "index larger than L2 (no flush needed)", "stop": "fixed-L (learned stop not built)"}
+    metric = "QPS@recall10>=0.95, 1M x 1536 4-bit, fixed-L beam, 1 GB300"
+    D = w["space"].code_dim
+
+    if args.impl == "reference":
+        cpu, cpu_rec = cpu_baseline(w, args, L, log)
+        line = {"impl": "reference", "metric": metric, "value": cpu["value"], "unit": "queries/s", "n_gpus": 1,
+                "steps": 1, "warmup": 0, "ms_per_step": 1000.0 * args.nq / cpu["value"], "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "int8/f32", "data": "synthetic",
+                "config": dict(config, recall_cpu=round(cpu_rec, 4)), "cpu_baseline": cpu,
+                "e2e": {"value": cpu["value"], "unit": "queries/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    index = w["index"]
+    q = w["queries"]
+    nq = q.shape[0]
+    ids = torch.empty((nq, args.k), dtype=torch.int32, device="cuda")
+    dists = torch.empty((nq, args.k), dtype=torch.float32, device="cuda")
+    stats = torch.empty((nq, 9), dtype=torch.int64, device="cuda")
+    index.search_into(q, ids, dists, k=args.k, l_value=L, stats_out=stats)
+    torch.cuda.synchronize()
+    st = stats.cpu().numpy().view(np.dtype([(f, "<u8") for f in
+                                            ("visited_nodes", "distance_computations", "hops", "paper_checked",
+                                             "paper_would_prune", "paper_not_pruned", "paper_full_saved",
+                                             "paper_msb_kernel_calls", "paper_remaining_kernel_calls")])).reshape(nq)
+    alg_bytes = algorithmic_bytes(st, D, args.M, 100, args.k)
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        index.search_into(q, ids, dists, k=args.k, l_value=L)
+    # prep-only timing, to split the step into its two kernels
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        w["space"].prepare(q)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    prep_ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for _ in range(args.steps):
+            index.search_into(q, ids, dists, k=args.k, l_value=L)
+        end.record(stream)
+        torch.cuda.synchronize()
+        step_ms = start.elapsed_time(end) / args.steps
+        # end to end through the public API with host buffers
+        hq = q.cpu().pin_memory()
+        hid = torch.empty((nq, args.k), dtype=torch.int32).pin_memory()
+        hd = torch.empty((nq, args.k), dtype=torch.float32).pin_memory()
+        dq = torch.empty_like(q)
+        torch.cuda.synchronize()
+        s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s2.record(stream)
+        for _ in range(args.steps):
+            dq.copy_(hq, non_blocking=True)
+            index.search_into(dq, ids, dists, k=args.k, l_value=L)
+            hid.copy_(ids, non_blocking=True)
+            hd.copy_(dists, non_blocking=True)
+        e2.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = s2.elapsed_time(e2) / args.steps
+    t = torch.tensor([step_ms, e2e_ms], device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    step_ms, e2e_ms = float(t[0]), float(t[1])
+    ok = bool((hid.to(torch.int64).cuda() == ids.to(torch.int64)).all())
+    value = world * nq / (step_ms / 1000.0)
+    e2e_value = world * nq / (e2e_ms / 1000.0)
+    search_ms = max(step_ms - prep_ms, 1e-6)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = alg_bytes / (search_ms / 1000.0) / 1e9
+    traffic = None
+    try:
+        prof = json.load(open(os.path.join(ROOT, "profiles", "search_kernel_traffic.json")))
+        traffic = prof.get("bytes_per_query", None)
+        if traffic is not None:
+            traffic = traffic * nq
+    except (OSError, ValueError):
+        pass
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        cpu, _ = cpu_baseline(w, args, L, log)
+    line = {"metric": metric, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int8/f32", "data": "synthetic", "config": config,
+            "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": int(nq * args.dim * 4),
+                    "d2h_bytes_per_step": int(nq * args.k * 8), "results_match_device": ok},
+            "gpu_launches": 2 * args.steps,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "search_kernel", "kernel_ms": search_ms, "prep_ms": prep_ms,
+                         "algorithmic_bytes_per_query": alg_bytes / nq,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"},
+            "clocks": clocks.summary(), "cpu_baseline": cpu,
+            "setup": {"encode_s": round(w["t_encode"], 3), "graph_s": round(w["t_graph"], 2),
+                      "reachable_from_0": round(w["reach"], 5), "l_sweep": {str(k): round(v, 4) for k, v in sweep.items()}}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -270,6 +270,15 @@ int qg_center_mean(const float *d_data, size_t stride, size_t dim, const uint32_
  * f32 data into compact and residual records (device). */
 int qg_encode_batch(const void *space, const float *d_raw, size_t n, uint8_t *d_compact,
                     uint8_t *d_residual, void *stream);
+/* GPU alpha robust prune for graph construction (this library's own builder; the reference
+ * prunes on the host, vamana_prune.h:42-156). For each of n nodes, scores its K candidate ids
+ * (device [n x K], UINT32_MAX = none; any order, duplicates allowed) with the symmetric 4-bit
+ * estimator, keeps at most R out-edges by occlusion with alpha 1.0 then `alpha`, and writes
+ * degrees [n] and edges [n x edge_stride] (UINT32_MAX padding). K <= 256, R <= edge_stride. */
+int qg_prune_candidates(const void *space, const uint8_t *d_compact, size_t compact_stride, size_t n,
+                        const uint32_t *d_candidates, size_t k, size_t r, float alpha,
+                        uint32_t *d_degrees, uint32_t *d_edges, size_t edge_stride, void *stream);
+
 /* GPU sidecar extraction (space_rabitq.h:4364-4392) from device compact records. */
 int qg_export_sidecar_device(const void *space, const uint8_t *d_compact, size_t n,
                              size_t compact_stride, uint8_t *d_msb, void *d_factors,

@@ -21,7 +21,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libqgraph_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["query_prep.cu", "batch_kernels.cu", "search.cu", "encode.cu"]
+CUDA_SOURCES = ["query_prep.cu", "batch_kernels.cu", "search.cu", "encode.cu", "graph_build.cu"]
 CXX_SOURCES = ["bridge.cpp"]
 
 

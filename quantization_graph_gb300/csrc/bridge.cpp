@@ -891,6 +891,21 @@ int qg_encode_batch(const void *space, const float *d_raw, size_t n, uint8_t *d_
     return QG_OK;
 }
 
+int qg_prune_candidates(const void *space, const uint8_t *d_compact, size_t compact_stride, size_t n,
+                        const uint32_t *d_candidates, size_t k, size_t r, float alpha,
+                        uint32_t *d_degrees, uint32_t *d_edges, size_t edge_stride, void *stream) {
+    const Space *s = as_space(space);
+    if (!s || (n && (!d_compact || !d_candidates || !d_degrees || !d_edges)) || k == 0 || k > 256 || r == 0 ||
+        r > edge_stride || n >= 0x7FFFFFFFu || compact_stride < s->compact_bytes)
+        return QG_ERR_INVALID;
+    if (!cuda_ok(launch_prune(static_cast<int>(s->code_dim), d_compact, compact_stride, static_cast<int>(n),
+                              d_candidates, static_cast<int>(k), static_cast<int>(r), alpha, d_degrees, d_edges,
+                              edge_stride, static_cast<cudaStream_t>(stream)),
+                 "prune kernel"))
+        return QG_ERR_CUDA;
+    return QG_OK;
+}
+
 int qg_export_sidecar_device(const void *space, const uint8_t *d_compact, size_t n,
                              size_t compact_stride, uint8_t *d_msb, void *d_factors, void *stream) {
     const Space *s = as_space(space);

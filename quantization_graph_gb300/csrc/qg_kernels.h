@@ -78,6 +78,9 @@ size_t search_smem_per_warp(int code_dim, int l_cap);
 int search_blocks_per_sm(int code_dim, int l_cap, int warps_per_block);
 int search_supported_dim(int code_dim);
 cudaError_t launch_encode(const EncodeArgs &a, cudaStream_t stream);
+cudaError_t launch_prune(int code_dim, const uint8_t *compact, size_t stride, int n, const uint32_t *cand,
+                         int K, int R, float alpha, uint32_t *degrees, uint32_t *edges, size_t edge_stride,
+                         cudaStream_t stream);
 cudaError_t launch_sidecar(const uint8_t *compact, size_t n, size_t stride, int code_dim,
                            uint8_t *msb, RabitqPaperFactors *factors, cudaStream_t stream);
 cudaError_t launch_repack(const uint8_t *compact, size_t compact_stride, const uint8_t *residual,

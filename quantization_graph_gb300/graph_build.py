@@ -1,0 +1,116 @@
+"""GPU graph construction for indexes the reference has not built (this library's own builder).
+
+The reference builds its Vamana graph on the host with the symmetric 4-bit estimator
+(rabitq_build_vamana_graph -> vamana_index.h:308-422; 3202 s at 64 threads for 1M x 960).
+This builder is not bit-identical to it. Steps:
+
+  1. exact-ish kNN candidates from the float vectors (TF32 GEMM through torch/cuBLAS, top-K),
+  2. alpha robust prune of the candidates to R out-edges on the GPU (qg_prune_candidates,
+     symmetric 4-bit distances, occlusion with alpha 1.0 then alpha),
+  3. reverse edges added as candidates and a second prune,
+  4. optional refinement rounds: every node is searched with the batched beam search and the
+     visited pool is pruned together with the current neighbours (the Vamana pass).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _native as N
+from .space import RabitqSpace, _cuda, _ptr, _stream
+
+NONE = -1  # UINT32_MAX viewed as int32
+
+
+def knn_candidates(data: torch.Tensor, k: int, chunk: int = 4096) -> torch.Tensor:
+    """[n, k] int32 nearest-neighbour ids (self excluded) by squared L2 (TF32 GEMM)."""
+    n = data.shape[0]
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = True
+    try:
+        norms = (data * data).sum(1)
+        out = torch.empty((n, k), dtype=torch.int32, device=data.device)
+        for s in range(0, n, chunk):
+            e = min(n, s + chunk)
+            d = torch.addmm(norms[None, :], data[s:e], data.T, beta=1.0, alpha=-2.0)
+            d += norms[s:e, None]
+            d[torch.arange(e - s, device=data.device), torch.arange(s, e, device=data.device)] = float("inf")
+            out[s:e] = torch.topk(d, k, dim=1, largest=False, sorted=True).indices.to(torch.int32)
+            del d
+        return out
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+def prune(space: RabitqSpace, compact: torch.Tensor, candidates: torch.Tensor, r: int, alpha: float,
+          edge_stride: int | None = None) -> tuple[torch.Tensor, torch.Tensor]:
+    lib = N.load()
+    n, k = candidates.shape
+    edge_stride = edge_stride or r
+    cand = _cuda(candidates, torch.int32)
+    deg = torch.empty(n, dtype=torch.int32, device="cuda")
+    edges = torch.empty((n, edge_stride), dtype=torch.int32, device="cuda")
+    N.check(lib.qg_prune_candidates(space.ptr, _ptr(compact), compact.shape[1], n, _ptr(cand), k, r, alpha,
+                                    _ptr(deg), _ptr(edges), edge_stride, _stream()), "qg_prune_candidates")
+    return deg, edges
+
+
+def reverse_candidates(edges: torch.Tensor, per_node: int) -> torch.Tensor:
+    """[n, per_node] reverse neighbours (sources of in-edges), NONE padded."""
+    n, r = edges.shape
+    valid = edges.flatten() != NONE
+    src = torch.arange(n, device=edges.device, dtype=torch.int64).repeat_interleave(r)[valid]
+    dst = edges.flatten()[valid].to(torch.int64)
+    order = torch.argsort(dst, stable=True)
+    dst, src = dst[order], src[order]
+    counts = torch.bincount(dst, minlength=n)
+    starts = torch.cumsum(counts, 0) - counts
+    rank = torch.arange(dst.numel(), device=edges.device) - starts[dst]
+    keep = rank < per_node
+    out = torch.full((n, per_node), NONE, dtype=torch.int32, device=edges.device)
+    out[dst[keep], rank[keep]] = src[keep].to(torch.int32)
+    return out
+
+
+def reachable_fraction(edges: torch.Tensor, start: int = 0, max_rounds: int = 10_000) -> float:
+    """Fraction of nodes reachable from `start` (breadth-first on the GPU)."""
+    n = edges.shape[0]
+    seen = torch.zeros(n, dtype=torch.bool, device=edges.device)
+    seen[start] = True
+    frontier = torch.tensor([start], device=edges.device, dtype=torch.int64)
+    for _ in range(max_rounds):
+        nb = edges[frontier].flatten()
+        nb = nb[nb != NONE].to(torch.int64)
+        nb = nb[~seen[nb]]
+        if nb.numel() == 0:
+            break
+        nb = torch.unique(nb)
+        seen[nb] = True
+        frontier = nb
+    return float(seen.float().mean())
+
+
+def build_graph(space: RabitqSpace, data: torch.Tensor, compact: torch.Tensor, r: int = 64,
+                knn: int = 128, alpha: float = 1.2, reverse: int = 64, refine_rounds: int = 0,
+                refine_l: int = 128, index_factory=None) -> tuple[torch.Tensor, torch.Tensor]:
+    """Returns (degrees [n] int32, edges [n, r] int32 with -1 padding) on the GPU."""
+    data = _cuda(data, torch.float32)
+    cand = knn_candidates(data, knn)
+    deg, edges = prune(space, compact, cand, r, alpha)
+    del cand
+    rev = reverse_candidates(edges, reverse)
+    deg, edges = prune(space, compact, torch.cat([edges, rev], dim=1), r, alpha)
+    del rev
+    for _ in range(refine_rounds):
+        ix = index_factory(deg, edges)
+        found = []
+        for s in range(0, data.shape[0], 65536):
+            res = ix.search(data[s:s + 65536], k=min(refine_l, 128), l_value=refine_l, with_stats=False)
+            found.append(res.ids.to(torch.int32))
+        visited = torch.cat(found)
+        visited[visited == -1] = NONE
+        rev = reverse_candidates(edges, reverse // 2)
+        cand = torch.cat([edges, visited[:, :max(1, 256 - r - reverse // 2)], rev], dim=1)
+        deg, edges = prune(space, compact, cand, r, alpha)
+    return deg, edges
