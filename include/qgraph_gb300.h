@@ -257,6 +257,13 @@ int qg_search_batch(qg_index *index, const float *d_queries, size_t nq,
                     const qg_search_params *params, const int *d_k, const int *d_l,
                     size_t k_stride, uint32_t *d_ids, float *d_dists, qg_search_stats *d_stats,
                     void *stream);
+/* qg_search_batch that also records, per query, the expanded nodes in hop order into
+ * d_expanded [nq x expanded_cap] (UINT32_MAX padding); the graph builder uses them as
+ * search-based prune candidates (the Vamana pass). */
+int qg_search_batch_ex(qg_index *index, const float *d_queries, size_t nq,
+                       const qg_search_params *params, const int *d_k, const int *d_l,
+                       size_t k_stride, uint32_t *d_ids, float *d_dists, qg_search_stats *d_stats,
+                       uint32_t *d_expanded, size_t expanded_cap, void *stream);
 /* Status word of the last qg_search_batch on this index (synchronises the stream). */
 int qg_search_status(qg_index *index, void *stream);
 

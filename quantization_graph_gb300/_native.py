@@ -89,6 +89,7 @@ _SIGS = {
     "qg_index_free": (None, [P]),
     "qg_index_device_bytes": (SZ, [P]),
     "qg_search_batch": (C.c_int, [P, P, SZ, P, P, P, SZ, P, P, P, P]),
+    "qg_search_batch_ex": (C.c_int, [P, P, SZ, P, P, P, SZ, P, P, P, P, SZ, P]),
     "qg_search_status": (C.c_int, [P, P]),
     "qg_center_mean": (C.c_int, [P, SZ, SZ, P, SZ, P, P]),
     "qg_encode_batch": (C.c_int, [P, P, SZ, P, P, P]),

@@ -1136,7 +1136,16 @@ int qg_search_batch(qg_index *index, const float *d_queries, size_t nq,
                     const qg_search_params *params, const int *d_k, const int *d_l,
                     size_t k_stride, uint32_t *d_ids, float *d_dists, qg_search_stats *d_stats,
                     void *stream) {
+    return qg_search_batch_ex(index, d_queries, nq, params, d_k, d_l, k_stride, d_ids, d_dists, d_stats,
+                              nullptr, 0, stream);
+}
+
+int qg_search_batch_ex(qg_index *index, const float *d_queries, size_t nq,
+                       const qg_search_params *params, const int *d_k, const int *d_l,
+                       size_t k_stride, uint32_t *d_ids, float *d_dists, qg_search_stats *d_stats,
+                       uint32_t *d_expanded, size_t expanded_cap, void *stream) {
     if (!index || !params || (nq && (!d_queries || !d_ids || !d_dists))) return QG_ERR_INVALID;
+    if (d_expanded && (expanded_cap == 0 || expanded_cap > 0x7FFFFFFF)) return QG_ERR_INVALID;
     if (nq > 0x7FFFFFFF) return QG_ERR_INVALID;
     const Space *s = index->space;
     const int k_max = d_k ? static_cast<int>(k_stride) : params->k;
@@ -1230,6 +1239,8 @@ int qg_search_batch(qg_index *index, const float *d_queries, size_t nq,
     a.counter = index->counter;
     a.status = index->status;
     a.hop_cap = static_cast<int>(std::min<size_t>(index->ix.n_total + 1, 0x7FFFFFFF));
+    a.expanded_out = d_expanded;
+    a.expanded_cap = static_cast<int>(expanded_cap);
     index->grid = grid;
     index->warps_per_block = wpb;
     if (!cuda_ok(launch_search(a, grid, wpb, st), "search kernel")) return QG_ERR_CUDA;

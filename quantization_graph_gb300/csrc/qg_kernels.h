@@ -52,6 +52,8 @@ struct SearchArgs {
     unsigned int *counter;
     int *status;
     int hop_cap;
+    uint32_t *expanded_out;  // optional [nq x expanded_cap]: expanded nodes in hop order
+    int expanded_cap;
 };
 
 struct EncodeArgs {

@@ -227,6 +227,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
     const int beam = a.beam_width < 1 ? 1 : (a.beam_width > kMaxBeam ? kMaxBeam : a.beam_width);
     int stall = 0;
     int hops_done = 0;
+    int n_expanded = 0;
     bool failed = false;
     for (;;) {
         const float back_before = pn > 0 ? s.pd[pn - 1] : 0.0f;
@@ -251,6 +252,12 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
         if (++hops_done > a.hop_cap) {
             if (lane == 0) atomicOr(a.status, 2);
             break;
+        }
+        if (a.expanded_out != nullptr) {
+            uint32_t *ex = a.expanded_out + static_cast<size_t>(q) * a.expanded_cap;
+            for (int fi = lane; fi < nf; fi += 32)
+                if (n_expanded + fi < a.expanded_cap) ex[n_expanded + fi] = s.frontier[fi];
+            n_expanded += nf;
         }
 
         for (int fi = 0; fi < nf; ++fi) {
@@ -528,6 +535,10 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
         }
     }
 
+    if (a.expanded_out != nullptr) {
+        uint32_t *ex = a.expanded_out + static_cast<size_t>(q) * a.expanded_cap;
+        for (int i = n_expanded + lane; i < a.expanded_cap; i += 32) ex[i] = 0xFFFFFFFFu;
+    }
     if (failed) {
         if (lane == 0) atomicOr(a.status, 1);
         if (a.stats_out && lane == 0) a.stats_out[q] = qg_search_stats{};

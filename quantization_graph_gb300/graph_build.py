@@ -93,24 +93,34 @@ def reachable_fraction(edges: torch.Tensor, start: int = 0, max_rounds: int = 10
 
 def build_graph(space: RabitqSpace, data: torch.Tensor, compact: torch.Tensor, r: int = 64,
                 knn: int = 128, alpha: float = 1.2, reverse: int = 64, refine_rounds: int = 0,
-                refine_l: int = 128, index_factory=None) -> tuple[torch.Tensor, torch.Tensor]:
-    """Returns (degrees [n] int32, edges [n, r] int32 with -1 padding) on the GPU."""
+                refine_l: int = 128, residual=None, msb=None, factors=None,
+                log=None) -> tuple[torch.Tensor, torch.Tensor]:
+    """Returns (degrees [n] int32, edges [n, r] int32 with -1 padding) on the GPU.
+
+    refine_rounds > 0 needs residual/msb/factors: each round searches every node from node 0
+    with list size refine_l, prunes the expanded nodes together with the current neighbours
+    (the Vamana pass, vamana_index.h:452-528) and adds reverse edges."""
+    from .index import OursIndex
+
     data = _cuda(data, torch.float32)
+    n = data.shape[0]
     cand = knn_candidates(data, knn)
     deg, edges = prune(space, compact, cand, r, alpha)
     del cand
     rev = reverse_candidates(edges, reverse)
     deg, edges = prune(space, compact, torch.cat([edges, rev], dim=1), r, alpha)
     del rev
-    for _ in range(refine_rounds):
-        ix = index_factory(deg, edges)
-        found = []
-        for s in range(0, data.shape[0], 65536):
-            res = ix.search(data[s:s + 65536], k=min(refine_l, 128), l_value=refine_l, with_stats=False)
-            found.append(res.ids.to(torch.int32))
-        visited = torch.cat(found)
-        visited[visited == -1] = NONE
-        rev = reverse_candidates(edges, reverse // 2)
-        cand = torch.cat([edges, visited[:, :max(1, 256 - r - reverse // 2)], rev], dim=1)
-        deg, edges = prune(space, compact, cand, r, alpha)
+    cap = 256 - r
+    for rnd in range(refine_rounds):
+        ix = OursIndex(space, compact, residual, msb, factors, deg, edges)
+        chunks = [ix.search_expanded(data[s:s + 131072], l_value=refine_l, cap=cap)
+                  for s in range(0, n, 131072)]
+        expanded = torch.cat(chunks)
+        del ix, chunks
+        deg, edges = prune(space, compact, torch.cat([edges, expanded], dim=1), r, alpha)
+        del expanded
+        rev = reverse_candidates(edges, reverse)
+        deg, edges = prune(space, compact, torch.cat([edges, rev], dim=1), r, alpha)
+        if log:
+            log(f"  graph refine round {rnd + 1} done")
     return deg, edges

@@ -81,6 +81,18 @@ class OursIndex:
                                          _ptr(k_per_query), _ptr(l_per_query), ids_out.shape[1], _ptr(ids_out),
                                          _ptr(dists_out), _ptr(stats_out), _stream()), "qg_search_batch")
 
+    def search_expanded(self, queries, l_value: int, cap: int, k: int = 1) -> torch.Tensor:
+        """[nq, cap] int32 ids of the nodes each query expanded, in hop order (-1 padding)."""
+        q = _cuda(queries, torch.float32)
+        nq = q.shape[0]
+        ids = torch.empty((nq, k), dtype=torch.int32, device="cuda")
+        dists = torch.empty((nq, k), dtype=torch.float32, device="cuda")
+        expanded = torch.empty((nq, cap), dtype=torch.int32, device="cuda")
+        params = N.SearchParams(k, l_value, 1, 1.9, 0, 0, 0)
+        N.check(self.lib.qg_search_batch_ex(self.handle, _ptr(q), nq, C.byref(params), None, None, k, _ptr(ids),
+                                            _ptr(dists), None, _ptr(expanded), cap, _stream()), "qg_search_batch_ex")
+        return expanded
+
     def search(self, queries, k: int = 10, l_value: int = 100, beam_width: int = 1,
                epsilon0: float = 1.9, rerank_candidates: int = 100, early_stop_hops: int = 0,
                kth_stop: bool = False, with_stats: bool = True, k_per_query=None,
