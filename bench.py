@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--L", type=int, default=0, help="fixed L (0 = sweep)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--refine", type=int, default=1, help="graph refinement rounds")
     return ap.parse_args()
 
 
@@ -147,12 +148,14 @@ def build_workload(torch, args, log):
     t_encode = time.time() - t1
     msb, factors = space.export_paper_sidecar(compact)
     t2 = time.time()
-    deg, edges = build_graph(space, base, compact, r=args.M, knn=2 * args.M, alpha=1.2, reverse=args.M)
+    deg, edges = build_graph(space, base, compact, r=args.M, knn=2 * args.M, alpha=1.2, reverse=args.M,
+                             refine_rounds=args.refine, refine_l=128, residual=residual, msb=msb, factors=factors)
     torch.cuda.synchronize()
     t_graph = time.time() - t2
     reach = reachable_fraction(edges)
     gt = ground_truth(torch, base, queries, args.k)
     index = OursIndex(space, compact, residual, msb, factors, deg, edges)
+    torch.cuda.empty_cache()
     log(f"setup: data {t1 - t0:.1f}s encode {t_encode:.2f}s graph {t_graph:.1f}s reachable {reach:.4f} "
         f"index {index.device_bytes() / 1e9:.2f} GB")
     return dict(base=base, queries=queries, space=space, index=index, gt=gt, compact=compact,
@@ -166,7 +169,7 @@ def pick_l(torch, w, args, log):
         return args.L, recall_at(r.ids, w["gt"], args.k), {args.L: recall_at(r.ids, w["gt"], args.k)}
     sweep = {}
     chosen = None
-    for L in (10, 12, 14, 16, 20, 24, 28, 32, 40, 48, 56, 64, 80, 100, 128, 160, 200, 256, 320, 400):
+    for L in (10, 16, 24, 32, 48, 64, 96, 128, 160, 200, 256, 320, 400, 480, 560, 640, 768, 896, 1024):
         if L < args.k:
             continue
         r = w["index"].search(w["queries"], k=args.k, l_value=L, with_stats=False)
@@ -248,7 +251,7 @@ def main():
     workload = (f"{args.n} x {args.dim} unit-norm anisotropic (lambda_i ~ i^-0.8), M={args.M}, "
                 f"{args.nq} queries, k={args.k}, INT8 paper-prune gate, residual4 rerank 100, fixed-L beam L={L}")
     config = {"workload": workload, "n": args.n, "dim": args.dim, "queries": args.nq, "M": args.M, "k": args.k,
-              "L": L, "recall@10": round(rec, 4), "graph": "GPU kNN-128 + alpha-1.2 prune + reverse edges",
+              "L": L, "recall@10": round(rec, 4), "graph": f"GPU kNN-{2 * args.M} + alpha-1.2 prune + reverse edges + {args.refine} search-based refinement round(s)",
               "l2": "index larger than L2 (no flush needed)", "stop": "fixed-L (learned stop not built)"}
     metric = "QPS@recall10>=0.95, 1M x 1536 4-bit, fixed-L beam, 1 GB300"
     D = w["space"].code_dim

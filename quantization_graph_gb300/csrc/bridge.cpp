@@ -1179,10 +1179,18 @@ int qg_search_batch_ex(qg_index *index, const float *d_queries, size_t nq,
     }
     // persistent grid: warps per block and resident blocks per SM from the occupancy of
     // this pool size; one visited-tag row per warp slot
-    const int wpb = 8;
+    // warps per block: the candidate with the most resident warps per SM (large pools need
+    // more shared memory per warp, where smaller blocks pack better)
+    int wpb = 8, per_sm = 0;
+    for (int cand : {8, 4, 2}) {
+        const int b = search_blocks_per_sm(static_cast<int>(s->code_dim), l_cap, cand);
+        if (b * cand > per_sm * wpb) {
+            wpb = cand;
+            per_sm = b;
+        }
+    }
     int sms = qg_device_sm_count();
     if (sms <= 0) sms = 1;
-    const int per_sm = search_blocks_per_sm(static_cast<int>(s->code_dim), l_cap, wpb);
     if (per_sm <= 0) {
         set_error("search kernel cannot be resident with this pool size");
         return QG_ERR_UNSUPPORTED;

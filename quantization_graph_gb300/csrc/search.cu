@@ -39,9 +39,9 @@ struct Lay {
     static constexpr int LPN = CH < 32 ? CH : 32;   // lanes per neighbour
     static constexpr int CPL = CH / LPN;            // 32-dim chunks per lane
     static constexpr int NBP = 32 / LPN;            // neighbours per pass
-    static constexpr int GG = 32 / CPL;             // gate group (LPN == 32)
-    static constexpr int GT = 8 / CPL;              // traversal group (LPN == 32)
-    static constexpr int PG = 8;                    // passes per batch (LPN < 32)
+    static constexpr int GG = 16 / CPL;             // gate group (LPN == 32)
+    static constexpr int GT = CPL == 1 ? 8 : 2;     // traversal group (LPN == 32)
+    static constexpr int PG = 4;                    // passes per batch (LPN < 32)
 };
 
 struct WarpSmem {
@@ -94,6 +94,34 @@ __device__ WarpSmem carve(unsigned char *base, int l_cap) {
     w.shdr = reinterpret_cast<float2 *>(take(kMaxFresh * 8));
     w.frontier = reinterpret_cast<uint32_t *>(take(kMaxBeam * 4));
     return w;
+}
+
+__device__ __forceinline__ void prefetch_l1(const void *p) {
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+// Prefetch `bytes` of `count` rows (row r at base + ids[r] * stride) with the warp's lanes,
+// one 128-byte line per lane-step.
+__device__ __forceinline__ void prefetch_rows_l1(const uint8_t *base, const uint32_t *ids, int count,
+                                                 size_t stride, int bytes, int lane) {
+    const int lines = (bytes + 127) >> 7;
+    for (int t = lane; t < count * lines; t += 32) {
+        const int r = t / lines, l = t - r * lines;
+        prefetch_l1(base + static_cast<size_t>(ids[r]) * stride + (l << 7));
+    }
+}
+
+__device__ __forceinline__ void prefetch_rows_l2(const uint8_t *base, const uint32_t *ids, int count,
+                                                 size_t stride, int bytes, int lane) {
+    const int lines = (bytes + 127) >> 7;
+    for (int t = lane; t < count * lines; t += 32) {
+        const int r = t / lines, l = t - r * lines;
+        prefetch_l2(base + static_cast<size_t>(ids[r]) * stride + (l << 7));
+    }
 }
 
 __device__ __forceinline__ bool cand_less(float da, uint32_t ia, float db, uint32_t ib) {
@@ -262,8 +290,15 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
 
         for (int fi = 0; fi < nf; ++fi) {
             const uint32_t node = s.frontier[fi];
-            const uint32_t deg = min(ix.degrees[node], ix.edge_stride);
+            // the degree and the whole adjacency row are loaded together (one round trip)
             const uint32_t *adj = ix.edges + static_cast<size_t>(node) * ix.edge_stride;
+            uint32_t row[2];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const uint32_t j = static_cast<uint32_t>(lane + 32 * h);
+                row[h] = j < ix.edge_stride ? __ldg(adj + j) : 0xFFFFFFFFu;
+            }
+            const uint32_t deg = min(__ldg(ix.degrees + node), ix.edge_stride);
             // ---- fresh neighbours in adjacency order (VisitedScratch::try_mark) ----
             int F = 0;
             bool oob = false;
@@ -271,7 +306,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             for (int h = 0; h < 2; ++h) {
                 const int j = lane + 32 * h;
                 const bool valid = j < static_cast<int>(deg);
-                const uint32_t nb = valid ? adj[j] : 0u;
+                const uint32_t nb = valid ? row[h] : 0u;
                 const bool bad = valid && nb >= ix.n_total;
                 const uint32_t key = (valid && !bad) ? nb : (0x80000000u | static_cast<uint32_t>(j));
                 const unsigned int same = __match_any_sync(0xffffffffu, key);
@@ -298,6 +333,9 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             st[MSBC] += F;
 
             // ---- gate (paper-prune lower bound) for every fresh neighbour ----
+            // all MSB rows and factor rows are requested at once, then consumed group by group
+            prefetch_rows_l1(ix.msb, s.fid, F, D / 8, D / 8, lane);
+            prefetch_rows_l1(reinterpret_cast<const uint8_t *>(ix.pf), s.fid, F, 16, 16, lane);
             for (int f = lane; f < F; f += 32) s.fpf[f] = ix.pf[s.fid[f]];
             if constexpr (L::LPN == 32) {
                 constexpr int G = L::GG;
@@ -385,6 +423,11 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             if (S == 0) continue;
 
             // ---- traversal distances of the survivors ----
+            prefetch_rows_l1(ix.codes, s.sid, S, D / 2, D / 2, lane);
+            prefetch_rows_l1(reinterpret_cast<const uint8_t *>(ix.hdr), s.sid, S, 16, 16, lane);
+            // survivors are the likeliest next expansions: warm L2 with their adjacency rows
+            prefetch_rows_l2(reinterpret_cast<const uint8_t *>(ix.edges), s.sid, S, ix.edge_stride * 4,
+                             static_cast<int>(ix.edge_stride * 4), lane);
             for (int i = lane; i < S; i += 32) {
                 const float4 h = ix.hdr[s.sid[i]];
                 s.shdr[i] = make_float2(h.x, h.y);
@@ -571,6 +614,9 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
         __syncwarp();
     }
     if (m > want) m = want;
+    prefetch_rows_l2(ix.codes, s.pid, m, D / 2, D / 2, lane);
+    prefetch_rows_l2(reinterpret_cast<const uint8_t *>(ix.res_scales), s.pid, m, D / 8, D / 8, lane);
+    prefetch_rows_l2(ix.res_codes, s.pid, m, D / 2, D / 2, lane);
     // FP32 4-bit restore (mode 0), two records per pass (one per half-warp)
     for (int base = 0; base < m; base += 2) {
         const int e = base + (lane >> 4);
@@ -623,7 +669,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
 }
 
 template <int D>
-__global__ void __launch_bounds__(256) search_kernel(SearchArgs a) {
+__global__ void __launch_bounds__(256, D >= 2048 ? 2 : 3) search_kernel(SearchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
