@@ -17,7 +17,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
-BUILD = os.path.join(PKG, "_build")
+BUILD = os.environ.get("QG_BUILD_DIR", os.path.join(PKG, "_build"))
 LIB = os.path.join(BUILD, "libqgraph_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -49,7 +49,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(INCLUDE, "qgraph_gb300.h"))
-    common = ["-std=c++17", "-O3", "-I", INCLUDE, "-I", CSRC]
+    common = ["-std=c++17", "-O3", "-I", INCLUDE, "-I", CSRC] + os.environ.get("QG_NVCC_DEFINES", "").split()
     jobs = []
     objs = []
     for src in CUDA_SOURCES:

@@ -668,8 +668,11 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
     }
 }
 
+#ifndef QG_SEARCH_MINBLOCKS_2048
+#define QG_SEARCH_MINBLOCKS_2048 2  // 128 registers: the 2048-dim query needs 32 of them
+#endif
 template <int D>
-__global__ void __launch_bounds__(256, D >= 2048 ? 2 : 3) search_kernel(SearchArgs a) {
+__global__ void __launch_bounds__(256, D >= 2048 ? QG_SEARCH_MINBLOCKS_2048 : 3) search_kernel(SearchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
