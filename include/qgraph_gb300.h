@@ -264,6 +264,23 @@ int qg_search_batch_ex(qg_index *index, const float *d_queries, size_t nq,
                        const qg_search_params *params, const int *d_k, const int *d_l,
                        size_t k_stride, uint32_t *d_ids, float *d_dists, qg_search_stats *d_stats,
                        uint32_t *d_expanded, size_t expanded_cap, void *stream);
+/* No counterpart in the reference. qg_search_batch for callers that cannot allocate device
+ * memory -- code running while a CUDA graph is captured, or a serving process whose device
+ * memory is fixed at start-up and may not call cudaMalloc on the request path. It allocates
+ * nothing: its scratch (prepared queries, visited tags, epochs, counter, status) is one
+ * file-scope device array of QG_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds
+ * until exit. The index must already exist; queries and outputs are the caller's. Limits: the
+ * prepared queries (nq x (5*D + 24) bytes) and at least one block of visited-tag rows
+ * (warps x n_total x 2 bytes) must fit the array, else QG_ERR_INVALID with the reason in
+ * qg_last_error(). All calls share the array: calls whose GPU work overlaps race, so serialise
+ * them. The first call on a device looks up the array's address (make it before any stream
+ * capture). Failed queries (bad neighbour ids) return UINT32_MAX ids; the status word is not
+ * read back (no synchronisation). */
+#define QG_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
+int qg_search_batch_noalloc(qg_index *index, const float *d_queries, size_t nq,
+                            const qg_search_params *params, const int *d_k, const int *d_l,
+                            size_t k_stride, uint32_t *d_ids, float *d_dists,
+                            qg_search_stats *d_stats, void *stream);
 /* Status word of the last qg_search_batch on this index (synchronises the stream). */
 int qg_search_status(qg_index *index, void *stream);
 

@@ -14,6 +14,7 @@ from . import build as _build
 LIB_PATH = _build.LIB
 
 QG_OK = 0
+QG_NOALLOC_SCRATCH_BYTES = 64 << 20  # include/qgraph_gb300.h
 STATUS_NAMES = {0: "QG_OK", 1: "QG_ERR_INVALID", 2: "QG_ERR_CUDA", 3: "QG_ERR_OOM", 4: "QG_ERR_GRAPH",
                 5: "QG_ERR_TIMEOUT", 6: "QG_ERR_UNSUPPORTED"}
 
@@ -90,6 +91,7 @@ _SIGS = {
     "qg_index_device_bytes": (SZ, [P]),
     "qg_search_batch": (C.c_int, [P, P, SZ, P, P, P, SZ, P, P, P, P]),
     "qg_search_batch_ex": (C.c_int, [P, P, SZ, P, P, P, SZ, P, P, P, P, SZ, P]),
+    "qg_search_batch_noalloc": (C.c_int, [P, P, SZ, P, P, P, SZ, P, P, P, P]),
     "qg_search_status": (C.c_int, [P, P]),
     "qg_center_mean": (C.c_int, [P, SZ, SZ, P, SZ, P, P]),
     "qg_encode_batch": (C.c_int, [P, P, SZ, P, P, P]),

@@ -281,6 +281,9 @@ void assemble_full(const Space *s, const uint8_t *compact, const uint8_t *residu
 }
 
 }  // namespace
+
+void record_error(const std::string &msg) { set_error(msg); }
+
 }  // namespace qg
 
 using namespace qg;

@@ -3,6 +3,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <string>
 
 #include <cuda_runtime.h>
 
@@ -69,6 +70,9 @@ struct EncodeArgs {
     size_t compact_bytes;
     size_t residual_bytes;
 };
+
+// Sets the message qg_last_error() returns on the calling thread.
+void record_error(const std::string &msg);
 
 cudaError_t launch_prepare(const PrepArgs &a, cudaStream_t stream);
 cudaError_t launch_center_setup(const float *center, const float *signs, int dim, int D,
