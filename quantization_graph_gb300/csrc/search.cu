@@ -129,9 +129,11 @@ __device__ __forceinline__ bool cand_less(float da, uint32_t ia, float db, uint3
 }
 
 // Integer gate partial over one 32-dim chunk: sum of the query bytes whose MSB bit is set.
-__device__ __forceinline__ int gate_chunk(uint32_t w, const int (&xn)[8], int acc) {
+// xg[k] holds the query bytes of dims k, 8+k, 16+k, 24+k, so (w >> k) & 0x01010101 is the
+// byte mask of exactly those four dims: one shift, one AND and one dp4a per four dims.
+__device__ __forceinline__ int gate_chunk(uint32_t w, const int (&xg)[8], int acc) {
 #pragma unroll
-    for (int g = 0; g < 8; ++g) acc = __dp4a(nibble_mask(w, 4 * g), xn[g], acc);
+    for (int k = 0; k < 8; ++k) acc = __dp4a(static_cast<int>((w >> k) & 0x01010101u), xg[k], acc);
     return acc;
 }
 
@@ -172,7 +174,7 @@ __device__ __forceinline__ int reduce_scatter(int (&p)[N], int lane) {
 
 template <int D>
 struct QueryRegs {
-    int xn[Lay<D>::CPL][8];
+    int xg[Lay<D>::CPL][8];
     int xe[Lay<D>::CPL][4];
     int xo[Lay<D>::CPL][4];
 };
@@ -187,7 +189,13 @@ __device__ __forceinline__ void load_query(QueryRegs<D> &r, const int8_t *codes,
         const int4 a = src[0], b = src[1];
         const int w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
 #pragma unroll
-        for (int g = 0; g < 8; ++g) r.xn[j][g] = w[g];
+        for (int k = 0; k < 8; ++k) {
+            // bytes (x[k], x[8+k], x[16+k], x[24+k]); x[4j+b] is byte b of w[j]
+            const uint32_t sel = static_cast<uint32_t>((k & 3) | (((k & 3) + 4) << 4));
+            const uint32_t lo = __byte_perm(w[k >> 2], w[2 + (k >> 2)], sel);
+            const uint32_t hi = __byte_perm(w[4 + (k >> 2)], w[6 + (k >> 2)], sel);
+            r.xg[j][k] = static_cast<int>(__byte_perm(lo, hi, 0x5410));
+        }
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             r.xe[j][k] = static_cast<int>(__byte_perm(w[2 * k], w[2 * k + 1], 0x6420));
@@ -299,6 +307,18 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                 row[h] = j < ix.edge_stride ? __ldg(adj + j) : 0xFFFFFFFFu;
             }
             const uint32_t deg = min(__ldg(ix.degrees + node), ix.edge_stride);
+            // speculative: the MSB and factor rows of every neighbour go to L2 while the
+            // visited tags are being read (about half of them turn out fresh)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const uint32_t nb = row[h];
+                if (lane + 32 * h < static_cast<int>(deg) && nb < ix.n_total) {
+                    const uint8_t *m = ix.msb + static_cast<size_t>(nb) * (D / 8);
+#pragma unroll
+                    for (int l = 0; l < (D / 8 + 127) / 128; ++l) prefetch_l2(m + 128 * l);
+                    prefetch_l2(ix.pf + nb);
+                }
+            }
             // ---- fresh neighbours in adjacency order (VisitedScratch::try_mark) ----
             int F = 0;
             bool oob = false;
@@ -354,7 +374,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                     for (int g = 0; g < G; ++g) {
                         int acc = 0;
 #pragma unroll
-                        for (int j = 0; j < L::CPL; ++j) acc = gate_chunk(w[g][j], qr.xn[j], acc);
+                        for (int j = 0; j < L::CPL; ++j) acc = gate_chunk(w[g][j], qr.xg[j], acc);
                         p[g] = acc;
                     }
                     const int tot = reduce_scatter<G>(p, lane);
@@ -380,7 +400,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                     }
 #pragma unroll
                     for (int pp = 0; pp < P; ++pp) {
-                        int acc = gate_chunk(w[pp], qr.xn[0], 0);
+                        int acc = gate_chunk(w[pp], qr.xg[0], 0);
 #pragma unroll
                         for (int o = 1; o < L::LPN; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
                         const int f = fb + pp * L::NBP + grp;
@@ -668,11 +688,11 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
     }
 }
 
-#ifndef QG_SEARCH_MINBLOCKS_2048
-#define QG_SEARCH_MINBLOCKS_2048 2  // 128 registers: the 2048-dim query needs 32 of them
+#ifndef QG_SEARCH_MINBLOCKS
+#define QG_SEARCH_MINBLOCKS 2  // 128 registers per thread; 80 (3 blocks) spills and measured slower
 #endif
 template <int D>
-__global__ void __launch_bounds__(256, D >= 2048 ? QG_SEARCH_MINBLOCKS_2048 : 3) search_kernel(SearchArgs a) {
+__global__ void __launch_bounds__(256, QG_SEARCH_MINBLOCKS) search_kernel(SearchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
