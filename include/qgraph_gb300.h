@@ -281,6 +281,49 @@ int qg_search_batch_noalloc(qg_index *index, const float *d_queries, size_t nq,
                             const qg_search_params *params, const int *d_k, const int *d_l,
                             size_t k_stride, uint32_t *d_ids, float *d_dists,
                             qg_search_stats *d_stats, void *stream);
+/* Learned early termination (no counterpart in the reference: its search stops at fixed L or
+ * by the kth / stall heuristics, ours_diskann.rs:1784-1809). A network 8 -> 64 -> 64 -> 1 with
+ * BF16 weights reads 8 search-state features every `every` hops; the query stops expanding when
+ * sigmoid(logit) > threshold (never before min_hops) and reranks its current pool. Weight layout:
+ * W1[64][8] b1[64] W2[64][64] b2[64] w3[64] b3 (QG_MLP_PARAMS values); d_norm = mean[8],
+ * inv_std[8] of the features. */
+#define QG_MLP_PARAMS 4353
+typedef struct qg_stop_model {
+    const uint16_t *d_weights;
+    const float *d_norm;
+    float threshold;
+    int every;
+    int min_hops;
+} qg_stop_model;
+
+/* Training traces: at every `every`-th hop, the 8 features and the label 1 when the first
+ * max(rerank, k) pool entries already contain all `truth_k` ids of d_truth (the final result of
+ * the full fixed-L search), else 0; at most `cap` rows per query, d_counts[q] rows written. */
+typedef struct qg_trace_request {
+    const uint32_t *d_truth;
+    int truth_k;
+    int every;
+    int cap;
+    float *d_features;
+    float *d_labels;
+    int *d_counts;
+} qg_trace_request;
+
+/* qg_search_batch with an optional stop model and/or trace request (either may be NULL). */
+int qg_search_batch_learned(qg_index *index, const float *d_queries, size_t nq,
+                            const qg_search_params *params, const int *d_k, const int *d_l,
+                            size_t k_stride, uint32_t *d_ids, float *d_dists,
+                            qg_search_stats *d_stats, const qg_stop_model *model,
+                            const qg_trace_request *trace, void *stream);
+/* Network training kernels: logits of n feature rows; BCE loss and its gradient w.r.t. the
+ * BF16 weights (FP32 accumulation; d_grad and d_loss are overwritten); one Adam step on the FP32
+ * master weights that also refreshes the BF16 copy (step counts from 1). */
+int qg_mlp_forward(const float *d_x, size_t n, const float *d_norm, const uint16_t *d_weights,
+                   float *d_logits, void *stream);
+int qg_mlp_backward(const float *d_x, const float *d_y, size_t n, const float *d_norm,
+                    const uint16_t *d_weights, float *d_grad, float *d_loss, void *stream);
+int qg_mlp_adam(float *d_master, uint16_t *d_weights, const float *d_grad, float *d_m, float *d_v,
+                float lr, float beta1, float beta2, float eps, int step, void *stream);
 /* Status word of the last qg_search_batch on this index (synchronises the stream). */
 int qg_search_status(qg_index *index, void *stream);
 

@@ -39,6 +39,20 @@ class DistanceInterval(C.Structure):
     _fields_ = [("estimate", C.c_float), ("lower_bound", C.c_float), ("upper_bound", C.c_float)]
 
 
+class StopModel(C.Structure):
+    """qg_stop_model"""
+    _fields_ = [("d_weights", C.c_void_p), ("d_norm", C.c_void_p), ("threshold", C.c_float), ("every", C.c_int),
+                ("min_hops", C.c_int)]
+
+
+class TraceRequest(C.Structure):
+    """qg_trace_request"""
+    _fields_ = [("d_truth", C.c_void_p), ("truth_k", C.c_int), ("every", C.c_int), ("cap", C.c_int),
+                ("d_features", C.c_void_p), ("d_labels", C.c_void_p), ("d_counts", C.c_void_p)]
+
+
+MLP_PARAMS = 4353
+
 STATS_FIELDS = ("visited_nodes", "distance_computations", "hops", "paper_checked", "paper_would_prune",
                 "paper_not_pruned", "paper_full_saved", "paper_msb_kernel_calls",
                 "paper_remaining_kernel_calls")
@@ -92,6 +106,10 @@ _SIGS = {
     "qg_search_batch": (C.c_int, [P, P, SZ, P, P, P, SZ, P, P, P, P]),
     "qg_search_batch_ex": (C.c_int, [P, P, SZ, P, P, P, SZ, P, P, P, P, SZ, P]),
     "qg_search_batch_noalloc": (C.c_int, [P, P, SZ, P, P, P, SZ, P, P, P, P]),
+    "qg_search_batch_learned": (C.c_int, [P, P, SZ, P, P, P, SZ, P, P, P, P, P, P]),
+    "qg_mlp_forward": (C.c_int, [P, SZ, P, P, P, P]),
+    "qg_mlp_backward": (C.c_int, [P, P, SZ, P, P, P, P, P]),
+    "qg_mlp_adam": (C.c_int, [P, P, P, P, P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, P]),
     "qg_search_status": (C.c_int, [P, P]),
     "qg_center_mean": (C.c_int, [P, SZ, SZ, P, SZ, P, P]),
     "qg_encode_batch": (C.c_int, [P, P, SZ, P, P, P]),

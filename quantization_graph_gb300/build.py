@@ -21,7 +21,7 @@ BUILD = os.environ.get("QG_BUILD_DIR", os.path.join(PKG, "_build"))
 LIB = os.path.join(BUILD, "libqgraph_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["query_prep.cu", "batch_kernels.cu", "search.cu", "encode.cu", "graph_build.cu",
+CUDA_SOURCES = ["query_prep.cu", "batch_kernels.cu", "search.cu", "encode.cu", "graph_build.cu", "mlp.cu",
                 "search_noalloc.cu"]
 CXX_SOURCES = ["bridge.cpp"]
 

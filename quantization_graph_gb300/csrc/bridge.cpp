@@ -1143,10 +1143,74 @@ int qg_search_batch(qg_index *index, const float *d_queries, size_t nq,
                               nullptr, 0, stream);
 }
 
+static int search_impl(qg_index *index, const float *d_queries, size_t nq, const qg_search_params *params,
+                       const int *d_k, const int *d_l, size_t k_stride, uint32_t *d_ids, float *d_dists,
+                       qg_search_stats *d_stats, uint32_t *d_expanded, size_t expanded_cap,
+                       const qg_stop_model *model, const qg_trace_request *trace, void *stream);
+
 int qg_search_batch_ex(qg_index *index, const float *d_queries, size_t nq,
                        const qg_search_params *params, const int *d_k, const int *d_l,
                        size_t k_stride, uint32_t *d_ids, float *d_dists, qg_search_stats *d_stats,
                        uint32_t *d_expanded, size_t expanded_cap, void *stream) {
+    return search_impl(index, d_queries, nq, params, d_k, d_l, k_stride, d_ids, d_dists, d_stats, d_expanded,
+                       expanded_cap, nullptr, nullptr, stream);
+}
+
+int qg_search_batch_learned(qg_index *index, const float *d_queries, size_t nq,
+                            const qg_search_params *params, const int *d_k, const int *d_l,
+                            size_t k_stride, uint32_t *d_ids, float *d_dists, qg_search_stats *d_stats,
+                            const qg_stop_model *model, const qg_trace_request *trace, void *stream) {
+    if (model && (!model->d_weights || !model->d_norm || model->every < 1 || !(model->threshold > 0.0f) ||
+                  !(model->threshold < 1.0f))) {
+        set_error("stop model needs weights, normalisation, every >= 1 and 0 < threshold < 1");
+        return QG_ERR_INVALID;
+    }
+    if (trace && (!trace->d_truth || trace->truth_k < 1 || trace->every < 1 || trace->cap < 1 ||
+                  !trace->d_features || !trace->d_labels || !trace->d_counts)) {
+        set_error("trace request needs truth ids, every >= 1, cap >= 1 and output buffers");
+        return QG_ERR_INVALID;
+    }
+    if (model && trace && model->every != trace->every) {
+        set_error("stop model and trace must use the same checkpoint interval");
+        return QG_ERR_INVALID;
+    }
+    return search_impl(index, d_queries, nq, params, d_k, d_l, k_stride, d_ids, d_dists, d_stats, nullptr, 0,
+                       model, trace, stream);
+}
+
+int qg_mlp_forward(const float *d_x, size_t n, const float *d_norm, const uint16_t *d_weights, float *d_logits,
+                   void *stream) {
+    if (n && (!d_x || !d_norm || !d_weights || !d_logits)) return QG_ERR_INVALID;
+    if (!cuda_ok(launch_mlp_forward(d_x, n, d_norm, d_weights, d_logits, static_cast<cudaStream_t>(stream)),
+                 "mlp forward"))
+        return QG_ERR_CUDA;
+    return QG_OK;
+}
+
+int qg_mlp_backward(const float *d_x, const float *d_y, size_t n, const float *d_norm, const uint16_t *d_weights,
+                    float *d_grad, float *d_loss, void *stream) {
+    if (!d_grad || !d_loss || (n && (!d_x || !d_y || !d_norm || !d_weights))) return QG_ERR_INVALID;
+    if (!cuda_ok(launch_mlp_backward(d_x, d_y, n, d_norm, d_weights, d_grad, d_loss,
+                                     static_cast<cudaStream_t>(stream)),
+                 "mlp backward"))
+        return QG_ERR_CUDA;
+    return QG_OK;
+}
+
+int qg_mlp_adam(float *d_master, uint16_t *d_weights, const float *d_grad, float *d_m, float *d_v, float lr,
+                float beta1, float beta2, float eps, int step, void *stream) {
+    if (!d_master || !d_weights || !d_grad || !d_m || !d_v || step < 1) return QG_ERR_INVALID;
+    if (!cuda_ok(launch_mlp_adam(d_master, d_weights, d_grad, d_m, d_v, lr, beta1, beta2, eps, step,
+                                 static_cast<cudaStream_t>(stream)),
+                 "mlp adam"))
+        return QG_ERR_CUDA;
+    return QG_OK;
+}
+
+static int search_impl(qg_index *index, const float *d_queries, size_t nq, const qg_search_params *params,
+                       const int *d_k, const int *d_l, size_t k_stride, uint32_t *d_ids, float *d_dists,
+                       qg_search_stats *d_stats, uint32_t *d_expanded, size_t expanded_cap,
+                       const qg_stop_model *model, const qg_trace_request *trace, void *stream) {
     if (!index || !params || (nq && (!d_queries || !d_ids || !d_dists))) return QG_ERR_INVALID;
     if (d_expanded && (expanded_cap == 0 || expanded_cap > 0x7FFFFFFF)) return QG_ERR_INVALID;
     if (nq > 0x7FFFFFFF) return QG_ERR_INVALID;
@@ -1252,6 +1316,24 @@ int qg_search_batch_ex(qg_index *index, const float *d_queries, size_t nq,
     a.hop_cap = static_cast<int>(std::min<size_t>(index->ix.n_total + 1, 0x7FFFFFFF));
     a.expanded_out = d_expanded;
     a.expanded_cap = static_cast<int>(expanded_cap);
+    a.stop_every = 1;
+    if (model) {
+        a.stop_w = model->d_weights;
+        a.stop_norm = model->d_norm;
+        a.stop_logit = std::log(model->threshold / (1.0f - model->threshold));
+        a.stop_every = model->every;
+        a.stop_min_hops = model->min_hops;
+    }
+    if (trace) {
+        a.trace_truth = trace->d_truth;
+        a.trace_truth_k = trace->truth_k;
+        a.trace_cap = trace->cap;
+        a.trace_feat = trace->d_features;
+        a.trace_label = trace->d_labels;
+        a.trace_count = trace->d_counts;
+        a.stop_every = trace->every;
+        if (!cuda_ok(cudaMemsetAsync(trace->d_counts, 0, nq * sizeof(int), st), "trace counts")) return QG_ERR_CUDA;
+    }
     index->grid = grid;
     index->warps_per_block = wpb;
     if (!cuda_ok(launch_search(a, grid, wpb, st), "search kernel")) return QG_ERR_CUDA;

@@ -55,6 +55,21 @@ struct SearchArgs {
     int hop_cap;
     uint32_t *expanded_out;  // optional [nq x expanded_cap]: expanded nodes in hop order
     int expanded_cap;
+    // learned early termination (optional): every stop_every hops the warp forms the 8 search-
+    // state features and evaluates the network; it stops when the logit exceeds stop_logit
+    const uint16_t *stop_w;
+    const float *stop_norm;
+    float stop_logit;
+    int stop_every;
+    int stop_min_hops;
+    // trace collection (optional): features at every stop_every-th hop with the label "the
+    // first max(rerank, k) pool entries already hold every id of trace_truth"
+    const uint32_t *trace_truth;  // [nq x trace_truth_k]
+    int trace_truth_k;
+    int trace_cap;
+    float *trace_feat;   // [nq x trace_cap x 8]
+    float *trace_label;  // [nq x trace_cap]
+    int *trace_count;    // [nq]
 };
 
 struct EncodeArgs {
@@ -84,6 +99,12 @@ size_t search_smem_per_warp(int code_dim, int l_cap);
 int search_blocks_per_sm(int code_dim, int l_cap, int warps_per_block);
 int search_supported_dim(int code_dim);
 cudaError_t launch_encode(const EncodeArgs &a, cudaStream_t stream);
+cudaError_t launch_mlp_forward(const float *X, size_t n, const float *norm, const uint16_t *w, float *logits,
+                               cudaStream_t stream);
+cudaError_t launch_mlp_backward(const float *X, const float *y, size_t n, const float *norm, const uint16_t *w,
+                                float *grad, float *loss, cudaStream_t stream);
+cudaError_t launch_mlp_adam(float *master, uint16_t *w, const float *grad, float *m, float *v, float lr,
+                            float beta1, float beta2, float eps, int step, cudaStream_t stream);
 cudaError_t launch_prune(int code_dim, const uint8_t *compact, size_t stride, int n, const uint32_t *cand,
                          int K, int R, float alpha, uint32_t *degrees, uint32_t *edges, size_t edge_stride,
                          cudaStream_t stream);

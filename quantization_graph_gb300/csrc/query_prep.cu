@@ -97,6 +97,8 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(PrepArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned long long *mt = reinterpret_cast<unsigned long long *>(smem_raw);  // [312]
     float *x = reinterpret_cast<float *>(mt + kMtN);                              // [D]
+    float *qs = x + a.code_dim;                                                   // [dim] raw query
+    float *cs = qs + a.dim;                                                       // [dim] centre
     __shared__ double s_rqn, s_dot;
     __shared__ float s_half, s_max;
     __shared__ int s_csum_part[4];
@@ -105,7 +107,14 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(PrepArgs a) {
     if (q >= a.nq) return;
     const int D = a.code_dim, dim = a.dim;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const float *raw = a.queries + static_cast<size_t>(q) * a.query_stride;
+    const float *gq = a.queries + static_cast<size_t>(q) * a.query_stride;
+    // stage the raw query and the centre once: the sequential chains below read shared memory
+    for (int i = threadIdx.x; i < dim; i += 128) {
+        qs[i] = gq[i];
+        cs[i] = a.center[i];
+    }
+    __syncthreads();
+    const float *raw = qs;
 
     if (warp == 0) {
         for (int i = lane; i < D; i += 32) x[i] = i < dim ? raw[i] * a.signs[i] : 0.0f;
@@ -127,7 +136,7 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(PrepArgs a) {
         for (int i = 0; i < dim; ++i) {
             const double v = static_cast<double>(raw[i]);
             rqn = __fma_rn(v, v, rqn);
-            dot = __fma_rn(v, static_cast<double>(a.center[i]), dot);
+            dot = __fma_rn(v, static_cast<double>(cs[i]), dot);
         }
         s_rqn = rqn;
         s_dot = dot;
@@ -218,7 +227,8 @@ __global__ void __launch_bounds__(128) center_setup_kernel(const float *center, 
 
 cudaError_t launch_prepare(const PrepArgs &a, cudaStream_t stream) {
     if (a.nq == 0) return cudaSuccess;
-    const size_t smem = kMtN * sizeof(unsigned long long) + static_cast<size_t>(a.code_dim) * sizeof(float);
+    const size_t smem = kMtN * sizeof(unsigned long long) +
+                        (static_cast<size_t>(a.code_dim) + 2 * static_cast<size_t>(a.dim)) * sizeof(float);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(prepare_queries_kernel,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -22,6 +22,7 @@
 // slot array of 16-bit epoch tags in global memory (no per-query clearing).
 #include <cstdint>
 
+#include "mlp.cuh"
 #include "qg_device.cuh"
 #include "qg_kernels.h"
 
@@ -172,6 +173,33 @@ __device__ __forceinline__ int reduce_scatter(int (&p)[N], int lane) {
     return t;
 }
 
+// The 8 search-state features of the learned stop (warp-uniform): hops / L; spread of the top
+// k relative to ||q - c||^2; improvement of the k-th distance over the last 3 hops; pool fill;
+// unexpanded fraction; position of the next expansion; its distance above the k-th; log ||q-c||^2.
+__device__ void search_features(const WarpSmem &s, int pn, int lval, int k, int hops, float qn2,
+                                const float (&kth_hist)[4], int lane, float (&f)[kMlpIn]) {
+    const float inv_q = 1.0f / (qn2 + 1e-6f);
+    const float inv_l = 1.0f / static_cast<float>(lval);
+    const int kk = k < pn ? k : pn;
+    const float d0 = s.pd[0], dk = s.pd[kk - 1];
+    int first = pn, count = 0;
+    for (int base = 0; base < pn; base += 32) {
+        const int e = base + lane;
+        const unsigned int m = __ballot_sync(0xffffffffu, e < pn && !(s.pid[e] & kExpanded));
+        if (m != 0u && first == pn) first = base + __ffs(m) - 1;
+        count += __popc(m);
+    }
+    const float dnext = first < pn ? s.pd[first] : dk;
+    f[0] = static_cast<float>(hops) * inv_l;
+    f[1] = (dk - d0) * inv_q;
+    f[2] = hops >= 4 ? (kth_hist[(hops + 1) & 3] - dk) * inv_q : 0.0f;
+    f[3] = static_cast<float>(pn) * inv_l;
+    f[4] = static_cast<float>(count) * inv_l;
+    f[5] = static_cast<float>(first) * inv_l;
+    f[6] = (dnext - dk) * inv_q;
+    f[7] = log1pf(qn2);
+}
+
 template <int D>
 struct QueryRegs {
     int xg[Lay<D>::CPL][8];
@@ -264,6 +292,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
     int stall = 0;
     int hops_done = 0;
     int n_expanded = 0;
+    float kth_hist[4] = {0.0f, 0.0f, 0.0f, 0.0f};  // k-th pool distance over the last 4 hops
     bool failed = false;
     for (;;) {
         const float back_before = pn > 0 ? s.pd[pn - 1] : 0.0f;
@@ -595,6 +624,51 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             const float back_after = pn > 0 ? s.pd[pn - 1] : 0.0f;
             stall = back_after >= back_before ? stall + 1 : 0;
             if (stall >= a.early_stop_hops) break;
+        }
+        // ---- learned early termination / trace rows (off unless requested) ----
+        if (a.stop_w != nullptr || a.trace_feat != nullptr) {
+            const float dk_now = s.pd[(k < pn ? k : pn) - 1];
+            kth_hist[hops_done & 3] = dk_now;
+            if (hops_done % a.stop_every == 0) {
+                float feat[kMlpIn];
+                search_features(s, pn, lval, k, hops_done, qn2, kth_hist, lane, feat);
+                if (a.trace_feat != nullptr) {
+                    int row = a.trace_count[q];
+                    if (row < a.trace_cap) {
+                        // label: every truth id already sits in the first max(rerank, k) entries
+                        const int want_r = a.rerank > k ? a.rerank : k;
+                        const int lim = want_r < pn ? want_r : pn;
+                        int found = 0;
+                        for (int t = 0; t < a.trace_truth_k; ++t) {
+                            const uint32_t tid = a.trace_truth[static_cast<size_t>(q) * a.trace_truth_k + t];
+                            bool hit = false;
+                            for (int base = 0; base < lim && !hit; base += 32) {
+                                const int e = base + lane;
+                                hit = __any_sync(0xffffffffu, e < lim && (s.pid[e] & kIdMask) == tid);
+                            }
+                            found += hit ? 1 : 0;
+                        }
+                        float mine = 0.0f;
+#pragma unroll
+                        for (int i = 0; i < kMlpIn; ++i) mine = lane == i ? feat[i] : mine;
+                        if (lane < kMlpIn)
+                            a.trace_feat[(static_cast<size_t>(q) * a.trace_cap + row) * kMlpIn + lane] = mine;
+                        if (lane == 0) {
+                            a.trace_label[static_cast<size_t>(q) * a.trace_cap + row] =
+                                found == a.trace_truth_k ? 1.0f : 0.0f;
+                            a.trace_count[q] = row + 1;
+                        }
+                        __syncwarp();
+                    }
+                }
+                if (a.stop_w != nullptr && hops_done >= a.stop_min_hops) {
+                    float f[kMlpIn];
+#pragma unroll
+                    for (int i = 0; i < kMlpIn; ++i) f[i] = (feat[i] - a.stop_norm[i]) * a.stop_norm[kMlpIn + i];
+                    const float z = mlp_forward_warp(f, a.stop_w, lane);
+                    if (z > a.stop_logit) break;
+                }
+            }
         }
     }
 

@@ -1,0 +1,94 @@
+"""Learned early termination: the network's forward, backward and Adam kernels against an FP64
+numpy restatement, trace collection, and what the trained stop gains over plain fixed-L search
+on a reference-built graph."""
+import numpy as np
+import pytest
+
+from cases import SEARCH_CASES
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def test_mlp_forward_backward_adam_match_fp64(cuda):
+    torch = cuda
+    import mlp_ref
+    from quantization_graph_gb300 import learned_stop as ls
+
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((257, 8)).astype(np.float32) * 3 + 1
+    y = (rng.random(257) < 0.4).astype(np.float32)
+    norm = np.concatenate([x.mean(0), 1 / x.std(0)]).astype(np.float32)
+    master = ls.init_weights(3)
+    w = ls.to_bf16_bits(master)
+    wb = mlp_ref.bf16_round(master.cpu().numpy())
+    np.testing.assert_array_equal(w.cpu().numpy().view(np.uint16).astype(np.uint32) << 16,
+                                  wb.astype(np.float32).view(np.uint32))
+    tn = torch.from_numpy(norm).cuda()
+    z = ls.forward(w, tn, torch.from_numpy(x)).cpu().numpy()
+    z_ref, _ = mlp_ref.forward(wb, norm.astype(np.float64), x)
+    np.testing.assert_allclose(z, z_ref, rtol=1e-4, atol=1e-4)
+    loss, grad = ls.loss_and_grad(w, tn, torch.from_numpy(x), torch.from_numpy(y))
+    l_ref, g_ref = mlp_ref.loss_and_grad(wb, norm.astype(np.float64), x, y)
+    assert abs(float(loss) - l_ref) < 1e-4 * max(1.0, abs(l_ref))
+    g = grad.cpu().numpy()
+    scale = np.abs(g_ref).max()
+    np.testing.assert_allclose(g, g_ref, rtol=1e-3, atol=1e-5 * scale)
+    # one Adam step
+    from quantization_graph_gb300 import _native as N
+    import ctypes as C
+
+    lib = N.load()
+    m = torch.zeros_like(master)
+    v = torch.zeros_like(master)
+    m0 = master.cpu().numpy().astype(np.float64)
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.qg_mlp_adam(C.c_void_p(master.data_ptr()), C.c_void_p(w.data_ptr()), C.c_void_p(grad.data_ptr()),
+                           C.c_void_p(m.data_ptr()), C.c_void_p(v.data_ptr()), 1e-2, 0.9, 0.999, 1e-8, 1,
+                           stream) == 0
+    want, _, _ = mlp_ref.adam(m0, g.astype(np.float64), 0, 0, 1e-2, 0.9, 0.999, 1e-8, 1)
+    np.testing.assert_allclose(master.cpu().numpy(), want, rtol=1e-5, atol=1e-6)
+
+
+def _index(torch):
+    from quantization_graph_gb300.index import OursIndex
+    from quantization_graph_gb300.space import RabitqSpace
+
+    g = load_golden("search_c1")
+    sp = RabitqSpace(128, g["center"])
+    return g, OursIndex(sp, g["compact"], g["residual"], g["msb"], g["factors"], g["degrees"], g["edges"])
+
+
+def test_learned_stop_saves_hops_at_equal_recall(cuda, oracle):
+    torch = cuda
+    from quantization_graph_gb300 import learned_stop as ls
+    from quantization_graph_gb300 import synthetic
+
+    g, ix = _index(torch)
+    X, _ = SEARCH_CASES["search_c1"]()
+    _, cent = synthetic.gmm(1, 128, components=64, sigma=0.3, seed=11)
+    train_q, _ = synthetic.gmm(3000, 128, sigma=0.3, seed=101, centres=cent)
+    test_q, _ = synthetic.gmm(1000, 128, sigma=0.3, seed=102, centres=cent)
+    L = 80
+    tq = torch.from_numpy(train_q).cuda()
+    truth = ix.search(tq, k=10, l_value=L, with_stats=False).ids.to(torch.int32)
+    feats, labels = ls.collect_traces(ix, tq, truth, k=10, l_value=L, every=2)
+    assert feats.shape[0] == labels.shape[0] > 10_000
+    assert 0.05 < float(labels.mean()) < 0.95
+    model = ls.train(feats, labels, epochs=6, batch=4096, every=2, min_hops=4)
+    o = oracle.Oracle(128, g["center"])
+    gt, _ = o.exact_knn(X, test_q, 10)
+    qq = torch.from_numpy(test_q).cuda()
+    plain = ix.search(qq, k=10, l_value=L)
+    rec_plain = np.mean([len(set(a) & set(b)) / 10 for a, b in zip(plain.ids.cpu().numpy(), gt)])
+    hops_plain = plain.stats["hops"].mean()
+    stats = torch.empty((len(test_q), 9), dtype=torch.int64, device="cuda")
+    best = None
+    for thr in (0.5, 0.7, 0.8, 0.9, 0.95, 0.98):
+        ids, _ = ls.search(ix, qq, model, thr, k=10, l_value=L, stats_out=stats)
+        rec = np.mean([len(set(a) & set(b)) / 10 for a, b in zip(ids.cpu().numpy(), gt)])
+        hops = stats[:, 2].double().mean().item()
+        if rec >= rec_plain - 0.002 and (best is None or hops < best[1]):
+            best = (thr, hops, rec)
+    assert best is not None, "no threshold kept recall within 0.002 of fixed-L"
+    assert best[1] <= 0.9 * hops_plain, (best, hops_plain, rec_plain)
