@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--refine", type=int, default=1, help="graph refinement rounds")
+    ap.add_argument("--no-learned", action="store_true", help="fixed-L only")
+    ap.add_argument("--train-queries", type=int, default=20_000)
+    ap.add_argument("--stop-every", type=int, default=4)
+    ap.add_argument("--stop-epochs", type=int, default=4)
     return ap.parse_args()
 
 
@@ -224,6 +228,68 @@ def cpu_baseline(w, args, L, log):
             "sample": f"{count} of {len(q)} queries at L={L}, k={args.k}, one query per thread"}, rec
 
 
+def device_ms(torch, fn, steps):
+    """Mean device time of `fn` over `steps` calls (CUDA events on the current stream)."""
+    stream = torch.cuda.current_stream()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record(stream)
+    for _ in range(steps):
+        fn()
+    end.record(stream)
+    torch.cuda.synchronize()
+    return start.elapsed_time(end) / steps
+
+
+def stats_struct(stats, nq):
+    names = ("visited_nodes", "distance_computations", "hops", "paper_checked", "paper_would_prune",
+             "paper_not_pruned", "paper_full_saved", "paper_msb_kernel_calls", "paper_remaining_kernel_calls")
+    return stats.cpu().numpy().view(np.dtype([(f, "<u8") for f in names])).reshape(nq)
+
+
+def learned_stop_select(torch, w, args, L_fixed, rec_fixed, log):
+    """Train the stop network on held-out queries and pick (L, threshold) with the highest QPS
+    whose recall is >= the target and within 0.002 of fixed-L at the same L."""
+    from quantization_graph_gb300 import learned_stop as ls
+    from quantization_graph_gb300 import synthetic
+
+    index, q, gt = w["index"], w["queries"], w["gt"]
+    cands = sorted({min(1024, max(args.k, int(round(L_fixed * f / 8.0)) * 8)) for f in (1.0, 1.25, 1.5, 2.0)})
+    L_train = max(cands)
+    t0 = time.time()
+    tq = synthetic.anisotropic_torch(args.train_queries, args.dim, 0.8, seed=3, normalize=True)
+    truth = index.search(tq, k=args.k, l_value=L_train, with_stats=False).ids.to(torch.int32)
+    feats, labels = ls.collect_traces(index, tq, truth, k=args.k, l_value=L_train, every=args.stop_every)
+    log(f"learned stop: {feats.shape[0]} trace rows from {args.train_queries} held-out queries at L={L_train}, "
+        f"positive {float(labels.mean()):.3f}")
+    model = ls.train(feats, labels, epochs=args.stop_epochs, every=args.stop_every, min_hops=2 * args.stop_every,
+                     log=log)
+    t_train = time.time() - t0
+    del tq, feats, labels, truth
+    ids = torch.empty((q.shape[0], args.k), dtype=torch.int32, device="cuda")
+    dists = torch.empty((q.shape[0], args.k), dtype=torch.float32, device="cuda")
+    table = []
+    best = None
+    for L in cands:
+        r = index.search(q, k=args.k, l_value=L, with_stats=False)
+        rec_l = recall_at(r.ids, gt, args.k)
+        fixed_ms = device_ms(torch, lambda: index.search_into(q, ids, dists, k=args.k, l_value=L), 2)
+        for thr in (0.5, 0.7, 0.8, 0.9, 0.95, 0.98, 0.99):
+            ls.search(index, q, model, thr, k=args.k, l_value=L, ids_out=ids, dists_out=dists)
+            rec = recall_at(ids.to(torch.int64), gt, args.k)
+            ms = device_ms(torch, lambda: ls.search(index, q, model, thr, k=args.k, l_value=L, ids_out=ids,
+                                                   dists_out=dists), 2)
+            row = {"L": L, "threshold": thr, "recall": round(rec, 4), "fixed_recall": round(rec_l, 4),
+                   "qps": round(q.shape[0] / ms * 1000.0, 1), "fixed_qps": round(q.shape[0] / fixed_ms * 1000.0, 1)}
+            table.append(row)
+            ok = rec >= args.target_recall and rec >= rec_l - 0.002
+            if ok and (best is None or ms < best[2]):
+                best = (L, thr, ms, rec, rec_l)
+        log(f"  L={L}: fixed recall {rec_l:.4f}; " + ", ".join(
+            f"t={r_['threshold']}: {r_['recall']:.4f}/{r_['qps']:.0f}" for r_ in table if r_["L"] == L))
+    return model, best, table, t_train
+
+
 def main():
     args = parse()
     import torch
@@ -243,25 +309,29 @@ def main():
             print(msg, file=sys.stderr, flush=True)
 
     from quantization_graph_gb300 import build as qbuild
+    from quantization_graph_gb300 import learned_stop as ls
 
     qbuild.build()
     w = build_workload(torch, args, log)
     L, rec, sweep = pick_l(torch, w, args, log)
-    log(f"chosen L={L} recall={rec:.4f}")
-    workload = (f"{args.n} x {args.dim} unit-norm anisotropic (lambda_i ~ i^-0.8), M={args.M}, "
-                f"{args.nq} queries, k={args.k}, INT8 paper-prune gate, residual4 rerank 100, fixed-L beam L={L}")
-    config = {"workload": workload, "n": args.n, "dim": args.dim, "queries": args.nq, "M": args.M, "k": args.k,
-              "L": L, "recall@10": round(rec, 4), "graph": f"GPU kNN-{2 * args.M} + alpha-1.2 prune + reverse edges + {args.refine} search-based refinement round(s)",
-              "l2": "index larger than L2 (no flush needed)", "stop": "fixed-L (learned stop not built)"}
-    metric = "QPS@recall10>=0.95, 1M x 1536 4-bit, fixed-L beam, 1 GB300"
+    log(f"fixed-L: L={L} recall={rec:.4f}")
+    metric = "QPS@recall10=0.95, 1M\u00d71536 4-bit, learned-stop vs fixed-L beam, 1 GB300"
+    config = {"workload": (f"{args.n} x {args.dim} unit-norm anisotropic (lambda_i ~ i^-0.8), M={args.M}, "
+                           f"{args.nq} queries, k={args.k}, INT8 paper-prune gate, residual4 rerank 100"),
+              "n": args.n, "dim": args.dim, "queries": args.nq, "M": args.M, "k": args.k,
+              "graph": f"GPU kNN-{2 * args.M} + alpha-1.2 prune + reverse edges + {args.refine} search-based refinement round(s)",
+              "l2": "index larger than L2 (no flush needed)",
+              "fixed_l": {"L": L, "recall@10": round(rec, 4)}}
     D = w["space"].code_dim
 
     if args.impl == "reference":
         cpu, cpu_rec = cpu_baseline(w, args, L, log)
+        config["fixed_l"]["recall_cpu"] = round(cpu_rec, 4)
         line = {"impl": "reference", "metric": metric, "value": cpu["value"], "unit": "queries/s", "n_gpus": 1,
                 "steps": 1, "warmup": 0, "ms_per_step": 1000.0 * args.nq / cpu["value"], "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "int8/f32", "data": "synthetic",
-                "config": dict(config, recall_cpu=round(cpu_rec, 4)), "cpu_baseline": cpu,
+                "config": dict(config, mode="fixed-L on the host cores (the reference search has no learned stop)"),
+                "cpu_baseline": cpu,
                 "e2e": {"value": cpu["value"], "unit": "queries/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
@@ -273,52 +343,61 @@ def main():
     ids = torch.empty((nq, args.k), dtype=torch.int32, device="cuda")
     dists = torch.empty((nq, args.k), dtype=torch.float32, device="cuda")
     stats = torch.empty((nq, 9), dtype=torch.int64, device="cuda")
-    index.search_into(q, ids, dists, k=args.k, l_value=L, stats_out=stats)
-    torch.cuda.synchronize()
-    st = stats.cpu().numpy().view(np.dtype([(f, "<u8") for f in
-                                            ("visited_nodes", "distance_computations", "hops", "paper_checked",
-                                             "paper_would_prune", "paper_not_pruned", "paper_full_saved",
-                                             "paper_msb_kernel_calls", "paper_remaining_kernel_calls")])).reshape(nq)
-    alg_bytes = algorithmic_bytes(st, D, args.M, 100, args.k)
-    stream = torch.cuda.current_stream()
+
+    # fixed-L: the fallback and the judge
     for _ in range(args.warmup):
         index.search_into(q, ids, dists, k=args.k, l_value=L)
-    # prep-only timing, to split the step into its two kernels
+    fixed_ms = device_ms(torch, lambda: index.search_into(q, ids, dists, k=args.k, l_value=L), args.steps)
+    config["fixed_l"]["qps"] = round(world * nq / fixed_ms * 1000.0, 1)
+
+    # learned stop
+    mode = {"kind": "fixed-L", "L": L, "threshold": None}
+    table, t_train, model = [], 0.0, None
+    if not args.no_learned:
+        model, best, table, t_train = learned_stop_select(torch, w, args, L, rec, log)
+        if best is not None:
+            mode = {"kind": "learned-stop", "L": best[0], "threshold": best[1]}
+            config["learned_stop"] = {"L": best[0], "threshold": best[1], "recall@10": round(best[3], 4),
+                                      "fixed_recall_same_L": round(best[4], 4), "train_s": round(t_train, 1),
+                                      "train_queries": args.train_queries, "checkpoint_every_hops": args.stop_every}
+        config["learned_stop_sweep"] = table
+
+    def step(qq):
+        if mode["kind"] == "learned-stop":
+            ls.search(index, qq, model, mode["threshold"], k=args.k, l_value=mode["L"], ids_out=ids, dists_out=dists)
+        else:
+            index.search_into(qq, ids, dists, k=args.k, l_value=mode["L"])
+
+    # counters of the chosen mode, for the algorithmic bytes
+    if mode["kind"] == "learned-stop":
+        ls.search(index, q, model, mode["threshold"], k=args.k, l_value=mode["L"], ids_out=ids, dists_out=dists,
+                  stats_out=stats)
+    else:
+        index.search_into(q, ids, dists, k=args.k, l_value=L, stats_out=stats)
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        w["space"].prepare(q)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    prep_ms = e0.elapsed_time(e1) / args.steps
+    final_recall = recall_at(ids.to(torch.int64), w["gt"], args.k)
+    alg_bytes = algorithmic_bytes(stats_struct(stats, nq), D, args.M, 100, args.k)
+    for _ in range(args.warmup):
+        step(q)
+    prep_ms = device_ms(torch, lambda: w["space"].prepare(q), args.steps)
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
-        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        start.record(stream)
-        for _ in range(args.steps):
-            index.search_into(q, ids, dists, k=args.k, l_value=L)
-        end.record(stream)
-        torch.cuda.synchronize()
-        step_ms = start.elapsed_time(end) / args.steps
+        step_ms = device_ms(torch, lambda: step(q), args.steps)
         # end to end through the public API with host buffers
         hq = q.cpu().pin_memory()
         hid = torch.empty((nq, args.k), dtype=torch.int32).pin_memory()
         hd = torch.empty((nq, args.k), dtype=torch.float32).pin_memory()
         dq = torch.empty_like(q)
-        torch.cuda.synchronize()
-        s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s2.record(stream)
-        for _ in range(args.steps):
+
+        def e2e_step():
             dq.copy_(hq, non_blocking=True)
-            index.search_into(dq, ids, dists, k=args.k, l_value=L)
+            step(dq)
             hid.copy_(ids, non_blocking=True)
             hd.copy_(dists, non_blocking=True)
-        e2.record(stream)
-        torch.cuda.synchronize()
-        e2e_ms = s2.elapsed_time(e2) / args.steps
+
+        e2e_ms = device_ms(torch, e2e_step, args.steps)
     t = torch.tensor([step_ms, e2e_ms], device="cuda")
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -337,14 +416,15 @@ def main():
     traffic = None
     try:
         prof = json.load(open(os.path.join(ROOT, "profiles", "search_kernel_traffic.json")))
-        traffic = prof.get("bytes_per_query", None)
-        if traffic is not None:
-            traffic = traffic * nq
+        ratio = prof.get("dram_over_algorithmic")
+        if ratio is not None:
+            traffic = ratio * alg_bytes
     except (OSError, ValueError):
         pass
     cpu = None
     if rank == 0 and not args.skip_cpu:
         cpu, _ = cpu_baseline(w, args, L, log)
+    config.update(mode=mode, **{"recall@10": round(final_recall, 4)})
     line = {"metric": metric, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int8/f32", "data": "synthetic", "config": config,
@@ -358,7 +438,8 @@ def main():
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"},
             "clocks": clocks.summary(), "cpu_baseline": cpu,
             "setup": {"encode_s": round(w["t_encode"], 3), "graph_s": round(w["t_graph"], 2),
-                      "reachable_from_0": round(w["reach"], 5), "l_sweep": {str(k): round(v, 4) for k, v in sweep.items()}}}
+                      "reachable_from_0": round(w["reach"], 5),
+                      "l_sweep": {str(k): round(v, 4) for k, v in sweep.items()}}}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

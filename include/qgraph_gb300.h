@@ -287,7 +287,7 @@ int qg_search_batch_noalloc(qg_index *index, const float *d_queries, size_t nq,
  * sigmoid(logit) > threshold (never before min_hops) and reranks its current pool. Weight layout:
  * W1[64][8] b1[64] W2[64][64] b2[64] w3[64] b3 (QG_MLP_PARAMS values); d_norm = mean[8],
  * inv_std[8] of the features. */
-#define QG_MLP_PARAMS 4353
+#define QG_MLP_PARAMS 4801
 typedef struct qg_stop_model {
     const uint16_t *d_weights;
     const float *d_norm;

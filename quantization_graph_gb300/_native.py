@@ -51,7 +51,7 @@ class TraceRequest(C.Structure):
                 ("d_features", C.c_void_p), ("d_labels", C.c_void_p), ("d_counts", C.c_void_p)]
 
 
-MLP_PARAMS = 4353
+MLP_PARAMS = 4801
 
 STATS_FIELDS = ("visited_nodes", "distance_computations", "hops", "paper_checked", "paper_would_prune",
                 "paper_not_pruned", "paper_full_saved", "paper_msb_kernel_calls",

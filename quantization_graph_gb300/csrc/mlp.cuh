@@ -21,7 +21,7 @@ constexpr int kMlpW2 = kMlpB1 + kMlpHidden;
 constexpr int kMlpB2 = kMlpW2 + kMlpHidden * kMlpHidden;
 constexpr int kMlpW3 = kMlpB2 + kMlpHidden;
 constexpr int kMlpB3 = kMlpW3 + kMlpHidden;
-constexpr int kMlpParams = kMlpB3 + 1;  // 4353
+constexpr int kMlpParams = kMlpB3 + 1;  // 4801
 
 __device__ __forceinline__ float mlp_w(const uint16_t *w, int i) {
     return __bfloat162float(__ushort_as_bfloat16(w[i]));

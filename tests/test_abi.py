@@ -65,3 +65,14 @@ def test_record_layout_sizes(oracle):
                                            (1024, 1024, 529, 648, 128), (1536, 2048, 1041, 1288, 256)):
         o = oracle.Oracle(dim, np.zeros(dim, np.float32))
         assert (o.D, o.compact_bytes, o.residual_bytes, o.msb_bytes) == (D, compact, residual, msb)
+
+
+def test_mlp_layout_constants_agree():
+    import mlp_ref
+    from quantization_graph_gb300 import _native
+
+    text = open(HEADER).read()
+    m = re.search(r"#define QG_MLP_PARAMS (\d+)", text)
+    assert int(m.group(1)) == mlp_ref.PARAMS == _native.MLP_PARAMS == 4801
+    m = re.search(r"#define QG_NOALLOC_SCRATCH_BYTES \(\(size_t\)(\d+) << (\d+)\)", text)
+    assert int(m.group(1)) << int(m.group(2)) == _native.QG_NOALLOC_SCRATCH_BYTES
