@@ -115,9 +115,7 @@ __global__ void __launch_bounds__(kWarps * 32) mlp_backward_kernel(const float *
         }
         if (v != 0.0f) atomicAdd(&grad[dst], v);
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) wloss += __shfl_xor_sync(0xffffffffu, wloss, o);
-    if (lane == 0) atomicAdd(loss, wloss * inv_n);
+    if (lane == 0) atomicAdd(loss, wloss * inv_n);  // the logit, hence wloss, is warp-uniform
 }
 
 __global__ void mlp_adam_kernel(float *master, uint16_t *w, const float *grad, float *m, float *v, int n,
