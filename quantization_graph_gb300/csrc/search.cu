@@ -474,9 +474,10 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             // ---- traversal distances of the survivors ----
             prefetch_rows_l1(ix.codes, s.sid, S, D / 2, D / 2, lane);
             prefetch_rows_l1(reinterpret_cast<const uint8_t *>(ix.hdr), s.sid, S, 16, 16, lane);
-            // survivors are the likeliest next expansions: warm L2 with their adjacency rows
-            prefetch_rows_l2(reinterpret_cast<const uint8_t *>(ix.edges), s.sid, S, ix.edge_stride * 4,
+            // survivors are the likeliest next expansions: bring their adjacency rows and degrees
+            prefetch_rows_l1(reinterpret_cast<const uint8_t *>(ix.edges), s.sid, S, ix.edge_stride * 4,
                              static_cast<int>(ix.edge_stride * 4), lane);
+            prefetch_rows_l1(reinterpret_cast<const uint8_t *>(ix.degrees), s.sid, S, 4, 4, lane);
             for (int i = lane; i < S; i += 32) {
                 const float4 h = ix.hdr[s.sid[i]];
                 s.shdr[i] = make_float2(h.x, h.y);
@@ -552,6 +553,20 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             }
             __syncwarp();
 
+            // the other candidate for the next expansion: the first unexpanded pool entry
+            for (int base = 0; base < pn; base += 32) {
+                const int e = base + lane;
+                const unsigned int m = __ballot_sync(0xffffffffu, e < pn && !(s.pid[e] & kExpanded));
+                if (m != 0u) {
+                    if (lane == __ffs(m) - 1) {
+                        const uint32_t u = s.pid[e] & kIdMask;
+                        const uint8_t *row = reinterpret_cast<const uint8_t *>(ix.edges + static_cast<size_t>(u) * ix.edge_stride);
+                        for (uint32_t off = 0; off < ix.edge_stride * 4; off += 128) prefetch_l1(row + off);
+                        prefetch_l1(ix.degrees + u);
+                    }
+                    break;
+                }
+            }
             // ---- re-check and sorted insert in adjacency order (ours_diskann.rs:1944-1979) ----
             for (int i = 0; i < S; ++i) {
                 const uint32_t slot = s.sslot[i];
