@@ -284,9 +284,9 @@ int qg_search_batch_noalloc(qg_index *index, const float *d_queries, size_t nq,
 /* Learned early termination (no counterpart in the reference: its search stops at fixed L or
  * by the kth / stall heuristics, ours_diskann.rs:1784-1809). A network 8 -> 64 -> 64 -> 1 with
  * BF16 weights reads 8 search-state features every `every` hops; the query stops expanding when
- * sigmoid(logit) > threshold (never before min_hops) and reranks its current pool. Weight layout:
- * W1[64][8] b1[64] W2[64][64] b2[64] w3[64] b3 (QG_MLP_PARAMS values); d_norm = mean[8],
- * inv_std[8] of the features. */
+ * sigmoid(logit) > threshold (never before min_hops) and reranks its current pool. Weight layout
+ * (matrices input-major, W[in][out]): W1[8][64] b1[64] W2[64][64] b2[64] w3[64] b3
+ * (QG_MLP_PARAMS values); d_norm = mean[8], inv_std[8] of the features. */
 #define QG_MLP_PARAMS 4801
 typedef struct qg_stop_model {
     const uint16_t *d_weights;
@@ -324,6 +324,20 @@ int qg_mlp_backward(const float *d_x, const float *d_y, size_t n, const float *d
                     const uint16_t *d_weights, float *d_grad, float *d_loss, void *stream);
 int qg_mlp_adam(float *d_master, uint16_t *d_weights, const float *d_grad, float *d_m, float *d_v,
                 float lr, float beta1, float beta2, float eps, int step, void *stream);
+/* Launch shape of the persistent search kernel: warps per block (2, 4 or 8) and an upper bound
+ * on resident blocks per SM; 0 restores the automatic choice. Used by the autotuner. */
+int qg_index_set_launch(qg_index *index, int warps_per_block, int blocks_per_sm);
+/* Allocate the prepared-query workspace for max_nq queries and the visited tags for the launch
+ * shape of pools up to max(max_l, max_k), so that qg_search_batch_graph never allocates. */
+int qg_index_reserve(qg_index *index, size_t max_nq, int max_l, int max_k);
+/* Capturable batched search for streams of uneven batches: the batch size is read on the device
+ * from d_nq (<= max_nq), so one captured CUDA graph serves every batch size; per-query k and L
+ * via d_k / d_l (params->k / l_value are their maxima). Never allocates: returns QG_ERR_INVALID
+ * if qg_index_reserve did not cover max_nq and the pool size. Optional learned-stop model. */
+int qg_search_batch_graph(qg_index *index, const float *d_queries, size_t max_nq, const int *d_nq,
+                          const qg_search_params *params, const int *d_k, const int *d_l,
+                          size_t k_stride, uint32_t *d_ids, float *d_dists, qg_search_stats *d_stats,
+                          const qg_stop_model *model, void *stream);
 /* Status word of the last qg_search_batch on this index (synchronises the stream). */
 int qg_search_status(qg_index *index, void *stream);
 

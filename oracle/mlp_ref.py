@@ -1,7 +1,8 @@
 """FP64 numpy restatement of the learned-stop network (test infrastructure only): the checker
 for the GPU forward / backward / Adam kernels (quantization_graph_gb300/csrc/mlp.cu).
 
-Packed layout: W1[64][8] b1[64] W2[64][64] b2[64] w3[64] b3. Inputs are standardised with
+Packed layout (weight matrices input-major): W1[8][64] b1[64] W2[64][64] b2[64] w3[64] b3,
+W[in][out]. Inputs are standardised with
 norm = (mean[8], inv_std[8]). Loss: mean binary cross-entropy with logits.
 """
 from __future__ import annotations
@@ -19,7 +20,8 @@ PARAMS = B3 + 1
 
 def unpack(w):
     w = np.asarray(w, np.float64)
-    return (w[W1:B1].reshape(H, IN), w[B1:W2], w[W2:B2].reshape(H, H), w[B2:W3], w[W3:B3], w[B3])
+    # returned as [out][in] matrices
+    return (w[W1:B1].reshape(IN, H).T, w[B1:W2], w[W2:B2].reshape(H, H).T, w[B2:W3], w[W3:B3], w[B3])
 
 
 def bf16_round(w32: np.ndarray) -> np.ndarray:
@@ -49,10 +51,10 @@ def loss_and_grad(w, norm, x, y):
     g[W3:B3] = h2.T @ dz
     d2 = (dz[:, None] * d[None, :]) * (h2 > 0)
     g[B2:W3] = d2.sum(0)
-    g[W2:B2] = (d2.T @ h1).ravel()
+    g[W2:B2] = (h1.T @ d2).ravel()
     d1 = (d2 @ c) * (h1 > 0)
     g[B1:W2] = d1.sum(0)
-    g[W1:B1] = (d1.T @ f).ravel()
+    g[W1:B1] = (f.T @ d1).ravel()
     return loss, g
 
 

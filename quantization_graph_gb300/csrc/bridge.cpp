@@ -1146,7 +1146,82 @@ int qg_search_batch(qg_index *index, const float *d_queries, size_t nq,
 static int search_impl(qg_index *index, const float *d_queries, size_t nq, const qg_search_params *params,
                        const int *d_k, const int *d_l, size_t k_stride, uint32_t *d_ids, float *d_dists,
                        qg_search_stats *d_stats, uint32_t *d_expanded, size_t expanded_cap,
-                       const qg_stop_model *model, const qg_trace_request *trace, void *stream);
+                       const qg_stop_model *model, const qg_trace_request *trace, void *stream,
+                       const int *d_nq = nullptr, bool allow_alloc = true);
+
+// Warps per block and resident blocks per SM for a pool of l_cap entries: the caller's override
+// (qg_index_set_launch) clamped to what is resident, else the candidate with the most resident
+// warps (large pools need more shared memory per warp, where smaller blocks pack better).
+static bool launch_geometry(const qg_index *index, int l_cap, int *wpb_out, int *per_sm_out) {
+    const int D = static_cast<int>(index->space->code_dim);
+    int wpb = 0, per_sm = 0;
+    if (index->launch_wpb > 0) {
+        wpb = index->launch_wpb;
+        per_sm = search_blocks_per_sm(D, l_cap, wpb);
+        if (index->launch_per_sm > 0 && index->launch_per_sm < per_sm) per_sm = index->launch_per_sm;
+    } else {
+        for (int cand : {8, 4, 2}) {
+            const int b = search_blocks_per_sm(D, l_cap, cand);
+            if (b * cand > per_sm * wpb) {
+                wpb = cand;
+                per_sm = b;
+            }
+        }
+    }
+    if (per_sm <= 0 || wpb <= 0) {
+        set_error("search kernel cannot be resident with this pool size and launch shape");
+        return false;
+    }
+    *wpb_out = wpb;
+    *per_sm_out = per_sm;
+    return true;
+}
+
+int qg_index_set_launch(qg_index *index, int warps_per_block, int blocks_per_sm) {
+    if (!index || warps_per_block < 0 || warps_per_block > 8 || blocks_per_sm < 0) return QG_ERR_INVALID;
+    index->launch_wpb = warps_per_block;
+    index->launch_per_sm = blocks_per_sm;
+    return QG_OK;
+}
+
+int qg_index_reserve(qg_index *index, size_t max_nq, int max_l, int max_k) {
+    if (!index || max_l < 1 || max_k < 1) return QG_ERR_INVALID;
+    // an ordinary search of an empty batch sizes the workspace and the visited tags
+    qg_search_params p{max_k, max_l, 1, 1.9f, 100, 0, 0};
+    const int rc = search_impl(index, nullptr, 0, &p, nullptr, nullptr, static_cast<size_t>(max_k), nullptr,
+                               nullptr, nullptr, nullptr, 0, nullptr, nullptr, nullptr);
+    if (rc != QG_OK) return rc;
+    if (index->q_capacity < max_nq) {
+        cudaFree(index->q.rr);
+        cudaFree(index->q.codes);
+        cudaFree(index->q.scal);
+        cudaFree(index->q.csum);
+        const Space *s = index->space;
+        index->q.rr = dev_alloc<float>(max_nq * s->code_dim);
+        index->q.codes = dev_alloc<int8_t>(max_nq * s->code_dim);
+        index->q.scal = dev_alloc<float4>(max_nq);
+        index->q.csum = dev_alloc<long long>(max_nq);
+        if (!index->q.rr || !index->q.codes || !index->q.scal || !index->q.csum) {
+            index->q_capacity = 0;
+            set_error("device allocation failed for prepared queries");
+            return QG_ERR_OOM;
+        }
+        index->q_capacity = max_nq;
+    }
+    return QG_OK;
+}
+
+int qg_search_batch_graph(qg_index *index, const float *d_queries, size_t max_nq, const int *d_nq,
+                          const qg_search_params *params, const int *d_k, const int *d_l, size_t k_stride,
+                          uint32_t *d_ids, float *d_dists, qg_search_stats *d_stats,
+                          const qg_stop_model *model, void *stream) {
+    if (!d_nq) return QG_ERR_INVALID;
+    if (model && (!model->d_weights || !model->d_norm || model->every < 1 || !(model->threshold > 0.0f) ||
+                  !(model->threshold < 1.0f)))
+        return QG_ERR_INVALID;
+    return search_impl(index, d_queries, max_nq, params, d_k, d_l, k_stride, d_ids, d_dists, d_stats, nullptr, 0,
+                       model, nullptr, stream, d_nq, false);
+}
 
 int qg_search_batch_ex(qg_index *index, const float *d_queries, size_t nq,
                        const qg_search_params *params, const int *d_k, const int *d_l,
@@ -1210,7 +1285,8 @@ int qg_mlp_adam(float *d_master, uint16_t *d_weights, const float *d_grad, float
 static int search_impl(qg_index *index, const float *d_queries, size_t nq, const qg_search_params *params,
                        const int *d_k, const int *d_l, size_t k_stride, uint32_t *d_ids, float *d_dists,
                        qg_search_stats *d_stats, uint32_t *d_expanded, size_t expanded_cap,
-                       const qg_stop_model *model, const qg_trace_request *trace, void *stream) {
+                       const qg_stop_model *model, const qg_trace_request *trace, void *stream,
+                       const int *d_nq, bool allow_alloc) {
     if (!index || !params || (nq && (!d_queries || !d_ids || !d_dists))) return QG_ERR_INVALID;
     if (d_expanded && (expanded_cap == 0 || expanded_cap > 0x7FFFFFFF)) return QG_ERR_INVALID;
     if (nq > 0x7FFFFFFF) return QG_ERR_INVALID;
@@ -1227,6 +1303,10 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // prepared-query workspace
+    if (index->q_capacity < nq && !allow_alloc) {
+        set_error("batch exceeds the reserved query capacity (qg_index_reserve)");
+        return QG_ERR_INVALID;
+    }
     if (index->q_capacity < nq) {
         cudaFree(index->q.rr);
         cudaFree(index->q.codes);
@@ -1248,22 +1328,16 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
     // this pool size; one visited-tag row per warp slot
     // warps per block: the candidate with the most resident warps per SM (large pools need
     // more shared memory per warp, where smaller blocks pack better)
-    int wpb = 8, per_sm = 0;
-    for (int cand : {8, 4, 2}) {
-        const int b = search_blocks_per_sm(static_cast<int>(s->code_dim), l_cap, cand);
-        if (b * cand > per_sm * wpb) {
-            wpb = cand;
-            per_sm = b;
-        }
-    }
+    int wpb = 0, per_sm = 0;
+    if (!launch_geometry(index, l_cap, &wpb, &per_sm)) return QG_ERR_UNSUPPORTED;
     int sms = qg_device_sm_count();
     if (sms <= 0) sms = 1;
-    if (per_sm <= 0) {
-        set_error("search kernel cannot be resident with this pool size");
-        return QG_ERR_UNSUPPORTED;
-    }
     const int grid = sms * per_sm;
     const int slots = grid * wpb;
+    if (index->slots < slots && !allow_alloc) {
+        set_error("launch needs more warp slots than reserved (qg_index_reserve)");
+        return QG_ERR_INVALID;
+    }
     if (index->slots < slots) {
         cudaFree(index->tags);
         cudaFree(index->epochs);
@@ -1281,10 +1355,12 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
         index->slots = slots;
     }
     if (nq == 0) return QG_OK;
-    int rc = qg_prepare_batch(s, d_queries, nq, index->q.rr, index->q.codes,
-                              reinterpret_cast<float *>(index->q.scal),
-                              reinterpret_cast<int64_t *>(index->q.csum), stream);
-    if (rc != QG_OK) return rc;
+    {
+        PrepArgs pa{d_queries, s->dim, static_cast<int>(nq), static_cast<int>(s->dim),
+                    static_cast<int>(s->code_dim), s->d_signs, s->d_center, s->d_rotated_center,
+                    s->d_center_norm, index->q.rr, index->q.codes, index->q.scal, index->q.csum, d_nq};
+        if (!cuda_ok(launch_prepare(pa, st), "prepare kernel")) return QG_ERR_CUDA;
+    }
     if (!cuda_ok(cudaMemsetAsync(index->counter, 0, 4, st), "counter reset") ||
         !cuda_ok(cudaMemsetAsync(index->status, 0, 4, st), "status reset"))
         return QG_ERR_CUDA;
@@ -1314,6 +1390,7 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
     a.counter = index->counter;
     a.status = index->status;
     a.hop_cap = static_cast<int>(std::min<size_t>(index->ix.n_total + 1, 0x7FFFFFFF));
+    a.nq_dev = d_nq;
     a.expanded_out = d_expanded;
     a.expanded_cap = static_cast<int>(expanded_cap);
     a.stop_every = 1;

@@ -8,9 +8,9 @@
 //
 // forward:  one warp per sample (the same warp-cooperative pass the search kernel runs).
 // backward: one warp per strided set of samples; each lane owns hidden units l and l+32, so its
-//           gradient rows are private; rows are kept in per-warp shared memory in transposed
-//           order (conflict-free), summed over the block's warps and added to the global
-//           gradient with one atomicAdd per parameter per block.
+//           gradient columns are private; they are kept in per-warp shared memory (input-major,
+//           so lanes write consecutive words), summed over the block's warps and added to the
+//           global gradient with one atomicAdd per parameter per block.
 // adam:     one thread per parameter; refreshes the BF16 copy.
 #include <cstdint>
 
@@ -40,8 +40,8 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(const float *X, size_t
     if (lane == 0) logits[s] = z;
 }
 
-// per-warp gradient layout in shared memory (transposed where lanes index the fast dim)
-//   gW1t[8][64]  gb1[64]  gW2t[64][64] (i-major: gW2t[i][j] = dL/dW2[j][i])  gb2[64]  gw3[64]  gb3
+// per-warp gradients in shared memory, in the parameter layout itself: the weight matrices are
+// input-major, so lane j (output unit j) writes consecutive words
 __global__ void __launch_bounds__(kWarps * 32) mlp_backward_kernel(const float *X, const float *y, size_t n,
                                                                    const float *norm, const uint16_t *w,
                                                                    float *grad, float *loss) {
@@ -75,7 +75,7 @@ __global__ void __launch_bounds__(kWarps * 32) mlp_backward_kernel(const float *
         d2s[warp][lane] = d2a;
         d2s[warp][lane + 32] = d2b;
         __syncwarp();
-        // layer 2: dW2[j][i] = d2[j] * h1[i]; stored transposed so lane j writes consecutive words
+        // layer 2: dW2[i][j] = h1[i] * d2[j]
         for (int i = 0; i < kMlpHidden; ++i) {
             const float hi = h1s[warp][i];
             gw[kMlpW2 + i * kMlpHidden + lane] += d2a * hi;
@@ -85,8 +85,8 @@ __global__ void __launch_bounds__(kWarps * 32) mlp_backward_kernel(const float *
         float dh[2] = {0.0f, 0.0f};
         for (int j = 0; j < kMlpHidden; ++j) {
             const float dj = d2s[warp][j];
-            dh[0] = __fmaf_rn(dj, mlp_w(w, kMlpW2 + j * kMlpHidden + lane), dh[0]);
-            dh[1] = __fmaf_rn(dj, mlp_w(w, kMlpW2 + j * kMlpHidden + lane + 32), dh[1]);
+            dh[0] = __fmaf_rn(dj, mlp_w(w, kMlpW2 + lane * kMlpHidden + j), dh[0]);
+            dh[1] = __fmaf_rn(dj, mlp_w(w, kMlpW2 + (lane + 32) * kMlpHidden + j), dh[1]);
         }
         const float d1a = h1a > 0.0f ? dh[0] : 0.0f;
         const float d1b = h1b > 0.0f ? dh[1] : 0.0f;
@@ -101,19 +101,11 @@ __global__ void __launch_bounds__(kWarps * 32) mlp_backward_kernel(const float *
         __syncwarp();
     }
     __syncthreads();
-    // sum the warps, undo the transposes, one atomicAdd per parameter per block
+    // sum the warps, one atomicAdd per parameter per block
     for (int p = threadIdx.x; p < kMlpParams; p += blockDim.x) {
         float v = 0.0f;
         for (int k = 0; k < kWarps; ++k) v += g[k][p];
-        int dst = p;
-        if (p >= kMlpW1 && p < kMlpB1) {  // stored [c][j] -> W1[j][c]
-            const int c = (p - kMlpW1) / kMlpHidden, j = (p - kMlpW1) % kMlpHidden;
-            dst = kMlpW1 + j * kMlpIn + c;
-        } else if (p >= kMlpW2 && p < kMlpB2) {  // stored [i][j] -> W2[j][i]
-            const int i = (p - kMlpW2) / kMlpHidden, j = (p - kMlpW2) % kMlpHidden;
-            dst = kMlpW2 + j * kMlpHidden + i;
-        }
-        if (v != 0.0f) atomicAdd(&grad[dst], v);
+        if (v != 0.0f) atomicAdd(&grad[p], v);
     }
     if (lane == 0) atomicAdd(loss, wloss * inv_n);  // the logit, hence wloss, is warp-uniform
 }

@@ -2,8 +2,9 @@
 // warp-cooperative forward pass shared by the search kernel and the training kernels.
 //
 // 8 standardised search-state features -> 64 -> 64 -> 1 (ReLU hidden layers, one logit).
-// Packed parameters (BF16 in device memory):
-//   W1[64][8] | b1[64] | W2[64][64] | b2[64] | w3[64] | b3
+// Packed parameters (BF16 in device memory), weight matrices input-major so that the lanes of a
+// warp, which own consecutive output units, read consecutive words:
+//   W1[8][64] | b1[64] | W2[64][64] | b2[64] | w3[64] | b3      (Wk[in][out])
 // Standardisation block (FP32): mean[8] | inv_std[8].
 #pragma once
 
@@ -39,15 +40,15 @@ __device__ __forceinline__ float mlp_forward_warp(const float (&f)[kMlpIn], cons
         const int j = lane + 32 * u;
         float acc = mlp_w(w, kMlpB1 + j);
 #pragma unroll
-        for (int i = 0; i < kMlpIn; ++i) acc = __fmaf_rn(mlp_w(w, kMlpW1 + j * kMlpIn + i), f[i], acc);
+        for (int i = 0; i < kMlpIn; ++i) acc = __fmaf_rn(mlp_w(w, kMlpW1 + i * kMlpHidden + j), f[i], acc);
         a1[u] = fmaxf(acc, 0.0f);
     }
     float acc2[2] = {mlp_w(w, kMlpB2 + lane), mlp_w(w, kMlpB2 + lane + 32)};
 #pragma unroll 8
     for (int i = 0; i < kMlpHidden; ++i) {
         const float hi = __shfl_sync(0xffffffffu, a1[i >> 5], i & 31);
-        acc2[0] = __fmaf_rn(mlp_w(w, kMlpW2 + lane * kMlpHidden + i), hi, acc2[0]);
-        acc2[1] = __fmaf_rn(mlp_w(w, kMlpW2 + (lane + 32) * kMlpHidden + i), hi, acc2[1]);
+        acc2[0] = __fmaf_rn(mlp_w(w, kMlpW2 + i * kMlpHidden + lane), hi, acc2[0]);
+        acc2[1] = __fmaf_rn(mlp_w(w, kMlpW2 + i * kMlpHidden + lane + 32), hi, acc2[1]);
     }
     const float a2a = fmaxf(acc2[0], 0.0f), a2b = fmaxf(acc2[1], 0.0f);
     float out = __fmaf_rn(mlp_w(w, kMlpW3 + lane), a2a, mlp_w(w, kMlpW3 + lane + 32) * a2b);

@@ -25,6 +25,7 @@ struct PrepArgs {
     int8_t *codes;
     float4 *scal;
     long long *csum;
+    const int *nq_dev;  // optional: the batch size read on the device (CUDA-graph replay)
 };
 
 struct SearchArgs {
@@ -70,6 +71,7 @@ struct SearchArgs {
     float *trace_feat;   // [nq x trace_cap x 8]
     float *trace_label;  // [nq x trace_cap]
     int *trace_count;    // [nq]
+    const int *nq_dev;   // optional: the batch size read on the device (CUDA-graph replay)
 };
 
 struct EncodeArgs {

@@ -81,5 +81,7 @@ struct qg_index {
     qg::DevQueries q;
     size_t q_capacity = 0;
     size_t device_bytes = 0;
+    int launch_wpb = 0;      // qg_index_set_launch override (0 = automatic)
+    int launch_per_sm = 0;
     std::vector<void *> owned;
 };

@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(PrepArgs a) {
     __shared__ int s_csum_part[4];
 
     const int q = blockIdx.x;
-    if (q >= a.nq) return;
+    if (q >= a.nq || (a.nq_dev != nullptr && q >= *a.nq_dev)) return;
     const int D = a.code_dim, dim = a.dim;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const float *gq = a.queries + static_cast<size_t>(q) * a.query_stride;

@@ -174,10 +174,11 @@ __device__ __forceinline__ int reduce_scatter(int (&p)[N], int lane) {
 }
 
 // The 8 search-state features of the learned stop (warp-uniform): hops / L; spread of the top
-// k relative to ||q - c||^2; improvement of the k-th distance over the last 3 hops; pool fill;
-// unexpanded fraction; position of the next expansion; its distance above the k-th; log ||q-c||^2.
+// k relative to ||q - c||^2; hops since the top k last changed / L; hops since the first
+// max(rerank, k) entries last changed / L; unexpanded fraction; position of the next expansion;
+// its distance above the k-th; log ||q - c||^2.
 __device__ void search_features(const WarpSmem &s, int pn, int lval, int k, int hops, float qn2,
-                                const float (&kth_hist)[4], int lane, float (&f)[kMlpIn]) {
+                                int last_topk, int last_topr, int lane, float (&f)[kMlpIn]) {
     const float inv_q = 1.0f / (qn2 + 1e-6f);
     const float inv_l = 1.0f / static_cast<float>(lval);
     const int kk = k < pn ? k : pn;
@@ -192,8 +193,8 @@ __device__ void search_features(const WarpSmem &s, int pn, int lval, int k, int 
     const float dnext = first < pn ? s.pd[first] : dk;
     f[0] = static_cast<float>(hops) * inv_l;
     f[1] = (dk - d0) * inv_q;
-    f[2] = hops >= 4 ? (kth_hist[(hops + 1) & 3] - dk) * inv_q : 0.0f;
-    f[3] = static_cast<float>(pn) * inv_l;
+    f[2] = static_cast<float>(hops - last_topk) * inv_l;
+    f[3] = static_cast<float>(hops - last_topr) * inv_l;
     f[4] = static_cast<float>(count) * inv_l;
     f[5] = static_cast<float>(first) * inv_l;
     f[6] = (dnext - dk) * inv_q;
@@ -292,7 +293,8 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
     int stall = 0;
     int hops_done = 0;
     int n_expanded = 0;
-    float kth_hist[4] = {0.0f, 0.0f, 0.0f, 0.0f};  // k-th pool distance over the last 4 hops
+    int last_topk = 0, last_topr = 0;  // last hop that inserted into the top k / top max(rerank, k)
+    const int want_r_all = a.rerank > k ? a.rerank : k;
     bool failed = false;
     for (;;) {
         const float back_before = pn > 0 ? s.pd[pn - 1] : 0.0f;
@@ -474,10 +476,9 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             // ---- traversal distances of the survivors ----
             prefetch_rows_l1(ix.codes, s.sid, S, D / 2, D / 2, lane);
             prefetch_rows_l1(reinterpret_cast<const uint8_t *>(ix.hdr), s.sid, S, 16, 16, lane);
-            // survivors are the likeliest next expansions: bring their adjacency rows and degrees
-            prefetch_rows_l1(reinterpret_cast<const uint8_t *>(ix.edges), s.sid, S, ix.edge_stride * 4,
+            // survivors are the likeliest next expansions: warm L2 with their adjacency rows
+            prefetch_rows_l2(reinterpret_cast<const uint8_t *>(ix.edges), s.sid, S, ix.edge_stride * 4,
                              static_cast<int>(ix.edge_stride * 4), lane);
-            prefetch_rows_l1(reinterpret_cast<const uint8_t *>(ix.degrees), s.sid, S, 4, 4, lane);
             for (int i = lane; i < S; i += 32) {
                 const float4 h = ix.hdr[s.sid[i]];
                 s.shdr[i] = make_float2(h.x, h.y);
@@ -553,20 +554,6 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             }
             __syncwarp();
 
-            // the other candidate for the next expansion: the first unexpanded pool entry
-            for (int base = 0; base < pn; base += 32) {
-                const int e = base + lane;
-                const unsigned int m = __ballot_sync(0xffffffffu, e < pn && !(s.pid[e] & kExpanded));
-                if (m != 0u) {
-                    if (lane == __ffs(m) - 1) {
-                        const uint32_t u = s.pid[e] & kIdMask;
-                        const uint8_t *row = reinterpret_cast<const uint8_t *>(ix.edges + static_cast<size_t>(u) * ix.edge_stride);
-                        for (uint32_t off = 0; off < ix.edge_stride * 4; off += 128) prefetch_l1(row + off);
-                        prefetch_l1(ix.degrees + u);
-                    }
-                    break;
-                }
-            }
             // ---- re-check and sorted insert in adjacency order (ours_diskann.rs:1944-1979) ----
             for (int i = 0; i < S; ++i) {
                 const uint32_t slot = s.sslot[i];
@@ -620,6 +607,8 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                     s.pid[pos] = id;
                     s.plb[pos] = valid ? lb : kFltMax;
                 }
+                if (pos < k) last_topk = hops_done;
+                if (pos < want_r_all) last_topr = hops_done;
                 pn = newn;
                 __syncwarp();
             }
@@ -642,11 +631,9 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
         }
         // ---- learned early termination / trace rows (off unless requested) ----
         if (a.stop_w != nullptr || a.trace_feat != nullptr) {
-            const float dk_now = s.pd[(k < pn ? k : pn) - 1];
-            kth_hist[hops_done & 3] = dk_now;
             if (hops_done % a.stop_every == 0) {
                 float feat[kMlpIn];
-                search_features(s, pn, lval, k, hops_done, qn2, kth_hist, lane, feat);
+                search_features(s, pn, lval, k, hops_done, qn2, last_topk, last_topr, lane, feat);
                 if (a.trace_feat != nullptr) {
                     int row = a.trace_count[q];
                     if (row < a.trace_cap) {
@@ -788,11 +775,12 @@ __global__ void __launch_bounds__(256, QG_SEARCH_MINBLOCKS) search_kernel(Search
     const WarpSmem s = carve(smem + warp * warp_smem_bytes(a.l_cap), a.l_cap);
     const int slot = blockIdx.x * wpb + warp;
     uint16_t *tags = a.tags + static_cast<size_t>(slot) * a.ix.n_total;
+    const int nq = a.nq_dev != nullptr ? min(a.nq, *a.nq_dev) : a.nq;
     for (;;) {
         int q = 0;
         if (lane == 0) q = static_cast<int>(atomicAdd(a.counter, 1u));
         q = __shfl_sync(0xffffffffu, q, 0);
-        if (q >= a.nq) break;
+        if (q >= nq) break;
         uint32_t e = a.epochs[slot] + 1;
         if ((e & 0xFFFFu) == 0) {
             // 16-bit tags wrapped: clear this slot's tags once every 65535 queries

@@ -1,9 +1,9 @@
 """Learned early termination for the batched search (no counterpart in the reference).
 
 A network 8 -> 64 -> 64 -> 1 (BF16 weights, FP32 accumulation) reads the search state every
-`every` hops inside the search kernel: hops / L, the spread of the current top-k, the
-improvement of the k-th distance over the last 3 hops, pool fill, unexpanded fraction,
-position and distance of the next expansion, log ||q - c||^2. When sigmoid(logit) exceeds a
+`every` hops inside the search kernel: hops / L, the spread of the current top-k, hops since
+the top k last changed / L, hops since the first max(rerank, k) pool entries last changed / L,
+unexpanded fraction, position and distance of the next expansion, log ||q - c||^2. When sigmoid(logit) exceeds a
 threshold the query stops expanding and reranks its pool. Plain fixed-L search stays the
 fallback and the judge: training labels come from it (a checkpoint is positive when the first
 max(rerank, k) pool entries already hold every id the full fixed-L search returns), and every

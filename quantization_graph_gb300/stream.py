@@ -1,0 +1,114 @@
+"""Serving uneven query batches with one captured CUDA graph, and the launch-shape autotuner.
+
+GraphSearcher captures qg_search_batch_graph once (query preparation + the persistent search
+kernel, plus the two counter resets) for the largest batch; every later batch -- any size up to
+the maximum, any mix of per-query k and L -- only copies its queries, k, L and batch size into
+the captured buffers and replays the graph. The kernels read the batch size on the device, so
+nothing is re-captured and nothing is allocated per batch.
+
+autotune() times the persistent kernel's launch shapes (warps per block, resident blocks per
+SM) on a sample of the workload and keeps the fastest on the index.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import time
+
+import torch
+
+from . import _native as N
+from .space import _cuda, _ptr
+
+
+def autotune(index, queries: torch.Tensor, k: int, l_value: int, shapes=None, repeats: int = 3, log=None):
+    """Pick (warps_per_block, blocks_per_sm) for this index and pool size; returns the timings."""
+    lib = N.load()
+    shapes = shapes or [(8, 0), (4, 0), (2, 0), (8, 1), (4, 2), (4, 1)]
+    q = _cuda(queries, torch.float32)
+    ids = torch.empty((q.shape[0], k), dtype=torch.int32, device="cuda")
+    dists = torch.empty((q.shape[0], k), dtype=torch.float32, device="cuda")
+    results = []
+    for wpb, per_sm in shapes:
+        N.check(lib.qg_index_set_launch(index.handle, wpb, per_sm), "qg_index_set_launch")
+        index.search_into(q, ids, dists, k=k, l_value=l_value)
+        torch.cuda.synchronize()
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record()
+        for _ in range(repeats):
+            index.search_into(q, ids, dists, k=k, l_value=l_value)
+        end.record()
+        torch.cuda.synchronize()
+        results.append(((wpb, per_sm), start.elapsed_time(end) / repeats))
+        if log:
+            log(f"  launch {wpb} warps/block, <= {per_sm or 'max'} blocks/SM: {results[-1][1]:.3f} ms")
+    best = min(results, key=lambda r: r[1])[0]
+    N.check(lib.qg_index_set_launch(index.handle, best[0], best[1]), "qg_index_set_launch")
+    return best, results
+
+
+class GraphSearcher:
+    def __init__(self, index, dim: int, max_batch: int, max_k: int, max_l: int, model=None,
+                 threshold: float | None = None, rerank: int = 100):
+        self.lib = N.load()
+        self.index = index
+        self.max_batch, self.max_k, self.max_l = max_batch, max_k, max_l
+        N.check(self.lib.qg_index_reserve(index.handle, max_batch, max_l, max_k), "qg_index_reserve")
+        self.q = torch.zeros((max_batch, dim), dtype=torch.float32, device="cuda")
+        self.k = torch.full((max_batch,), max_k, dtype=torch.int32, device="cuda")
+        self.l = torch.full((max_batch,), max_l, dtype=torch.int32, device="cuda")
+        self.nq = torch.zeros(1, dtype=torch.int32, device="cuda")
+        self.ids = torch.empty((max_batch, max_k), dtype=torch.int32, device="cuda")
+        self.dists = torch.empty((max_batch, max_k), dtype=torch.float32, device="cuda")
+        self.params = N.SearchParams(max_k, max_l, 1, 1.9, rerank, 0, 0)
+        self.model = model.struct(threshold) if model is not None else None
+        self.stream = torch.cuda.Stream()
+        self.graph = torch.cuda.CUDAGraph()
+        # one uncaptured call settles every lazy set-up, then the capture
+        with torch.cuda.stream(self.stream):
+            self.nq.fill_(1)
+            self._launch()
+        torch.cuda.synchronize()
+        with torch.cuda.graph(self.graph, stream=self.stream):
+            self._launch()
+        torch.cuda.synchronize()
+
+    def _launch(self):
+        st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        model = C.byref(self.model) if self.model is not None else None
+        N.check(self.lib.qg_search_batch_graph(self.index.handle, _ptr(self.q), self.max_batch, _ptr(self.nq),
+                                               C.byref(self.params), _ptr(self.k), _ptr(self.l), self.max_k,
+                                               _ptr(self.ids), _ptr(self.dists), None, model, st),
+                "qg_search_batch_graph")
+
+    def search(self, queries: torch.Tensor, k: torch.Tensor, l_value: torch.Tensor):
+        """Replay the graph for one batch; returns views of the result buffers (valid until the
+        next call) after the batch completes on the searcher's stream."""
+        n = queries.shape[0]
+        if n > self.max_batch:
+            raise ValueError("batch larger than the captured maximum")
+        self.stream.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(self.stream):
+            self.q[:n].copy_(queries, non_blocking=True)
+            self.k[:n].copy_(k, non_blocking=True)
+            self.l[:n].copy_(l_value, non_blocking=True)
+            self.nq.fill_(n)  # the size travels as a kernel argument: no host buffer to race on
+            self.graph.replay()
+        return self.ids[:n], self.dists[:n]
+
+    def synchronize(self):
+        self.stream.synchronize()
+
+
+def serve(searcher: GraphSearcher, batches, log=None):
+    """Run a list of (queries, k, L) batches back to back; returns per-batch latencies (ms, host
+    wall clock from submission to completion) and the total elapsed seconds."""
+    lat = []
+    outs = []
+    t_all = time.perf_counter()
+    for qb, kb, lb in batches:
+        t0 = time.perf_counter()
+        ids, dists = searcher.search(qb, kb, lb)
+        searcher.synchronize()
+        lat.append((time.perf_counter() - t0) * 1000.0)
+        outs.append(ids.clone())
+    return lat, time.perf_counter() - t_all, outs

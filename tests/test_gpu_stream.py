@@ -1,0 +1,54 @@
+"""One captured CUDA graph serving uneven batches (sizes 1..max, per-query k and L) returns exactly
+what the ordinary search returns; the launch-shape autotuner keeps results unchanged."""
+import numpy as np
+import pytest
+
+from cases import SEARCH_CASES
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _index(torch):
+    from quantization_graph_gb300.index import OursIndex
+    from quantization_graph_gb300.space import RabitqSpace
+
+    g = load_golden("search_c1")
+    sp = RabitqSpace(128, g["center"])
+    return g, OursIndex(sp, g["compact"], g["residual"], g["msb"], g["factors"], g["degrees"], g["edges"])
+
+
+def test_graph_replay_matches_plain_search_on_uneven_batches(cuda):
+    torch = cuda
+    from quantization_graph_gb300.stream import GraphSearcher
+
+    g, ix = _index(torch)
+    _, Q = SEARCH_CASES["search_c1"]()
+    rng = np.random.default_rng(7)
+    allq = np.concatenate([Q] * 4)
+    gs = GraphSearcher(ix, 128, max_batch=64, max_k=100, max_l=160)
+    start = 0
+    for size in (1, 64, 7, 33, 2, 64, 13):
+        qb = allq[start:start + size]
+        start += size
+        kb = rng.choice([1, 10, 100], size=size).astype(np.int32)
+        lb = rng.integers(10, 160, size=size).astype(np.int32)
+        ids, dists = gs.search(torch.from_numpy(qb).cuda(), torch.from_numpy(kb).cuda(), torch.from_numpy(lb).cuda())
+        gs.synchronize()
+        ref = ix.search(torch.from_numpy(qb).cuda(), k=100, l_value=160, k_per_query=torch.from_numpy(kb),
+                        l_per_query=torch.from_numpy(lb), with_stats=False)
+        np.testing.assert_array_equal(ids.cpu().numpy().astype(np.uint32), ref.ids.cpu().numpy().astype(np.uint32))
+        np.testing.assert_array_equal(dists.cpu().numpy().view(np.uint32), ref.distances.cpu().numpy().view(np.uint32))
+
+
+def test_autotuner_keeps_results(cuda):
+    torch = cuda
+    from quantization_graph_gb300.stream import autotune
+
+    g, ix = _index(torch)
+    _, Q = SEARCH_CASES["search_c1"]()
+    q = torch.from_numpy(Q).cuda()
+    best, results = autotune(ix, q, k=10, l_value=40, repeats=1)
+    assert best in [r[0] for r in results]
+    r = ix.search(q, k=10, l_value=40)
+    np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), g["ids_L40_k10"])
