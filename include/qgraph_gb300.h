@@ -369,6 +369,13 @@ int qg_export_sidecar_device(const void *space, const uint8_t *d_compact, size_t
  * query_norm, half_sum_residual, int8_scale}, code sums [nq] int64. */
 int qg_prepare_batch(const void *space, const float *d_queries, size_t nq, float *d_rotated,
                      int8_t *d_codes, float *d_scalars, int64_t *d_code_sum, void *stream);
+/* Kernel-level check of the INT8 dither decision used by qg_prepare_batch (no reference
+ * counterpart; it restates the expression of space_rabitq.h:3625-3643): out[i] =
+ * floor(double(x[i]) / double(scale[i]) + u) with u = double(draws[i]) * 2^-64 clamped below 1,
+ * before the [-128, 127] clamp; undecided[i] (optional) = 1 where the FP32 decision fell back
+ * to double arithmetic. */
+int qg_dither_floor_pairs(const float *d_x, const float *d_scale, const uint64_t *d_draws, size_t n,
+                          int32_t *d_out, uint8_t *d_undecided, void *stream);
 /* Kernel-level entry points over (query, id) pairs, for parity tests and tools: prepared
  * query arrays as produced by qg_prepare_batch; pair i uses query qidx[i] and record ids[i].
  * Records/sidecars in the reference host layouts, but in device memory. */

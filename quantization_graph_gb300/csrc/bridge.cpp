@@ -936,6 +936,17 @@ int qg_prepare_batch(const void *space, const float *d_queries, size_t nq, float
     return QG_OK;
 }
 
+int qg_dither_floor_pairs(const float *d_x, const float *d_scale, const uint64_t *d_draws, size_t n,
+                          int32_t *d_out, uint8_t *d_undecided, void *stream) {
+    if (n && (!d_x || !d_scale || !d_draws || !d_out)) return QG_ERR_INVALID;
+    if (!cuda_ok(launch_dither_pairs(d_x, d_scale, reinterpret_cast<const unsigned long long *>(d_draws), n,
+                                     reinterpret_cast<int *>(d_out), d_undecided,
+                                     static_cast<cudaStream_t>(stream)),
+                 "dither kernel"))
+        return QG_ERR_CUDA;
+    return QG_OK;
+}
+
 int qg_gate_pairs(const void *space, const int8_t *d_codes, const float *d_scalars,
                   const int64_t *d_code_sum, const uint32_t *d_qidx, const uint32_t *d_ids,
                   size_t count, const uint8_t *d_msb, size_t msb_stride, const void *d_factors,

@@ -92,6 +92,8 @@ struct EncodeArgs {
 void record_error(const std::string &msg);
 
 cudaError_t launch_prepare(const PrepArgs &a, cudaStream_t stream);
+cudaError_t launch_dither_pairs(const float *x, const float *scale, const unsigned long long *draws, size_t n,
+                                int *out, uint8_t *undecided, cudaStream_t stream);
 cudaError_t launch_center_setup(const float *center, const float *signs, int dim, int D,
                                 float *rotated, float *norm_out, cudaStream_t stream);
 cudaError_t launch_center_mean(const float *data, size_t stride, int dim, const uint32_t *rows,

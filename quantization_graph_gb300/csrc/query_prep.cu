@@ -1,12 +1,14 @@
 // query_prep.cu -- batched INT8 query preparation (RaBitQSpace::prepare_query with the Int8
 // codec: initializePreparedQuery + buildCentroidQuery, space_rabitq.h:3429-3706).
 //
-// One 128-thread CTA per query. The three long sequential chains of the reference run in
-// separate warps so they overlap: warp 0 rotates the query (random-sign Hadamard transform
-// in shared memory, the reference's butterfly order) and reduces max|q'|; warp 1 lane 0
-// accumulates ||q||^2 and <q, c> as FMA chains in double; warp 2 lane 0 hashes the raw
-// query bytes (FNV-1a) and seeds MT19937-64; warp 3 lane 0 forms the pairwise half sum.
-// The dither stream is then produced by the whole CTA (parallel MT19937-64 twist).
+// One 128-thread CTA per query; the warps work side by side: warp 0 rotates the query
+// (random-sign Hadamard transform in shared memory, the reference's butterfly order) and
+// reduces max|q'|; warp 1 forms ||q - c||^2 exactly from 128-bit fixed-point sums (the
+// reference's double FMA chains run only when a rigorous bound cannot decide the float);
+// warp 2 lane 0 hashes the raw query bytes (FNV-1a, the one long sequential chain) and seeds
+// MT19937-64; warp 3 lane 0 forms the pairwise half sum. The dither stream is then produced by
+// the whole CTA (parallel MT19937-64 twist) and the INT8 codes are decided in FP32 with an
+// exact margin test, double arithmetic only for draws within 2^-36 of an integer.
 #include <cstdint>
 
 #include "qg_device.cuh"
@@ -81,10 +83,11 @@ __device__ void mt_twist(unsigned long long *mt) {
 // In-place random-sign Hadamard transform of one D-vector in shared memory by one warp,
 // butterfly order of RaBitQSpace::hadamard (space_rabitq.h:944-988).
 __device__ void fht_warp(float *x, int D, int lane) {
-    for (int step = 1; step < D; step <<= 1) {
+    for (int ls = 0; (1 << ls) < D; ++ls) {
+        const int step = 1 << ls;
         for (int b = lane; b < D / 2; b += 32) {
-            const int block = b / step, i = b - block * step;
-            const int ia = block * 2 * step + i, ib = ia + step;
+            const int i = b & (step - 1);
+            const int ia = ((b >> ls) << (ls + 1)) + i, ib = ia + step;
             const float a = x[ia], c = x[ib];
             x[ia] = a + c;
             x[ib] = a - c;
@@ -93,26 +96,178 @@ __device__ void fht_warp(float *x, int D, int lane) {
     }
 }
 
+namespace {
+
+// ---- ||q - c||^2 without FP64 ---------------------------------------------------------
+// The reference forms ||q||^2 and <q, c> as sequential FMA chains in double (each q_i * q_i
+// and q_i * c_i is exact in double, so every step is one rounding of acc + p_i), then
+// qn2 = max(0, float((rqn + ||c||^2) - 2 dot)) in double. FP64 is a narrow pipe on this
+// part, so the chains are not run: the exact real sums A = sum q_i^2 and B = sum q_i c_i are
+// formed warp-parallel in 128-bit fixed point, and the rounding error of the reference's
+// sequential evaluation is bounded (Higham, Accuracy and Stability of Numerical Algorithms,
+// 2nd ed., sec. 4.2: |fl(sum) - sum| <= u * sum_i |partial_i|, u = 2^-53):
+//   |t2 - X| <= 2^-53 (n + 2) (A + ||c||^2 + 2 sum|q_i c_i|),  X = A + ||c||^2 - 2B.
+// If every value within that bound of X rounds to the same float, that float is the
+// reference's qn2; otherwise (about once in 10^5 queries) the caller runs the double chains.
+
+struct FloatParts {
+    long long m;  // signed integer significand, |m| < 2^24
+    int e;        // value = m * 2^e
+    bool finite;
+};
+
+__device__ __forceinline__ FloatParts split_float(float f) {
+    const uint32_t b = __float_as_uint(f);
+    const int ex = static_cast<int>((b >> 23) & 0xFFu);
+    long long m = static_cast<long long>(b & 0x7FFFFFu);
+    int e = -149;
+    if (ex != 0) {
+        m |= 0x800000;
+        e = ex - 150;
+    }
+    if (b >> 31) m = -m;
+    return {m, e, ex != 0xFF};
+}
+
+// |v| (< 2^49) * 2^sh as a 128-bit fixed-point value; shifts below the grid truncate.
+__device__ __forceinline__ unsigned __int128 to_grid(unsigned long long v, int sh) {
+    if (sh >= 0) return static_cast<unsigned __int128>(v) << sh;
+    if (sh <= -64) return 0;
+    return static_cast<unsigned __int128>(v >> (-sh));
+}
+
+__device__ __forceinline__ __int128 shfl_xor_i128(__int128 v, int o) {
+    const unsigned __int128 u = static_cast<unsigned __int128>(v);
+    uint32_t w[4] = {static_cast<uint32_t>(u), static_cast<uint32_t>(u >> 32), static_cast<uint32_t>(u >> 64),
+                     static_cast<uint32_t>(u >> 96)};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) w[i] = __shfl_xor_sync(0xffffffffu, w[i], o);
+    const unsigned __int128 r = static_cast<unsigned __int128>(w[0]) |
+                                (static_cast<unsigned __int128>(w[1]) << 32) |
+                                (static_cast<unsigned __int128>(w[2]) << 64) |
+                                (static_cast<unsigned __int128>(w[3]) << 96);
+    return static_cast<__int128>(r);
+}
+
+__device__ __forceinline__ int msb_u128(unsigned __int128 v) {
+    const unsigned long long hi = static_cast<unsigned long long>(v >> 64);
+    if (hi != 0) return 127 - __clzll(static_cast<long long>(hi));
+    const unsigned long long lo = static_cast<unsigned long long>(v);
+    return lo ? 63 - __clzll(static_cast<long long>(lo)) : -1;
+}
+
+// One warp. Returns true and the reference's qn2 in *out when the bound decides it.
+__device__ bool exact_qn2_warp(const float *q, const float *c, int dim, float cn, int lane, float *out) {
+    constexpr int kNone = -100000;
+    int emax = kNone;
+    bool finite = true;
+    for (int i = lane; i < dim; i += 32) {
+        const FloatParts a = split_float(q[i]), b = split_float(c[i]);
+        finite = finite && a.finite && b.finite;
+        if (a.m != 0) {
+            emax = max(emax, 2 * a.e + 48);
+            if (b.m != 0) emax = max(emax, a.e + b.e + 49);
+        }
+    }
+    const FloatParts pc = split_float(cn);
+    finite = finite && pc.finite;
+    if (pc.m != 0) emax = max(emax, pc.e + 24);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+    if (!__all_sync(0xffffffffu, finite) || emax == kNone) return false;
+    const int G = emax - 100;  // grid: every term and sum below 2^112 in grid units
+    __int128 A = 0, B = 0, Babs = 0;
+    for (int i = lane; i < dim; i += 32) {
+        const FloatParts a = split_float(q[i]), b = split_float(c[i]);
+        const unsigned long long aa = static_cast<unsigned long long>(a.m * a.m);
+        A += static_cast<__int128>(to_grid(aa, 2 * a.e - G));
+        const long long pb = a.m * b.m;
+        const __int128 t = static_cast<__int128>(to_grid(static_cast<unsigned long long>(pb < 0 ? -pb : pb),
+                                                         a.e + b.e - G));
+        B += pb < 0 ? -t : t;
+        Babs += t;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        A += shfl_xor_i128(A, o);
+        B += shfl_xor_i128(B, o);
+        Babs += shfl_xor_i128(Babs, o);
+    }
+    const __int128 C = static_cast<__int128>(to_grid(static_cast<unsigned long long>(pc.m < 0 ? -pc.m : pc.m),
+                                                     pc.e - G)) * (pc.m < 0 ? -1 : 1);
+    const __int128 X = A + C - 2 * B;
+    const __int128 S = A + (C < 0 ? -C : C) + 2 * Babs;
+    // bound in grid units: 2x the rounding bound, plus one unit per truncated term
+    const __int128 base = (S >> 52) + 1;
+    const __int128 n5 = static_cast<__int128>(dim + 5);
+    const __int128 E = base * n5 + ((base * n5) >> 6) + 3 * static_cast<__int128>(dim) + 4;
+    const __int128 lo = X - E, hi = X + E;
+    if (lo <= 0) return false;
+    const int mb = msb_u128(static_cast<unsigned __int128>(lo));
+    if (mb != msb_u128(static_cast<unsigned __int128>(hi))) return false;
+    const int sh = mb - 23;  // float significand = bits [sh, mb]
+    if (sh < 1) return false;
+    const __int128 half = static_cast<__int128>(1) << (sh - 1);
+    const __int128 j = (X + half) >> sh;
+    if (!(lo > (2 * j - 1) * half && hi < (2 * j + 1) * half)) return false;
+    const int fe = sh + G;  // the float is j * 2^fe, j in [2^23, 2^24]
+    if (fe + 23 < -126 || fe + 24 > 127) return false;
+    const uint32_t jj = static_cast<uint32_t>(static_cast<long long>(j));
+    *out = jj == (1u << 24) ? __uint_as_float(static_cast<uint32_t>(fe + 24 + 127) << 23)
+                            : __uint_as_float((static_cast<uint32_t>(fe + 23 + 127) << 23) | (jj - (1u << 23)));
+    return true;
+}
+
+// ---- INT8 dither without FP64 ---------------------------------------------------------
+// Reference: v = floor(double(x) / double(scale) + u), u = RN53(K) * 2^-64 clamped below 1
+// (K = the tempered MT19937-64 draw). Here s1 + tail approximates x/scale + K 2^-64 to
+// within 2^-38.5 (remainder of the float quotient by FMA, a TwoSum of the quotient and the
+// top 24 bits of K, the next 24 bits of K), and the reference's T to within 2^-44.9 of the
+// same real number; the floor is decided unless T lies within 2^-36 of an integer, in which
+// case `undecided` is set and the caller evaluates the double expression.
+__device__ __forceinline__ int dither_floor(float x, float scale, unsigned long long K, bool &undecided) {
+    const float y = __fdiv_rn(x, scale);
+    const float r = __fmaf_rn(-y, scale, x);  // exact: x - y * scale
+    const float c = __fdiv_rn(r, scale);
+    const float uh = __uint2float_rn(static_cast<unsigned>(K >> 40)) * 0x1p-24f;
+    const float ul = __uint2float_rn(static_cast<unsigned>((K >> 16) & 0xFFFFFFu)) * 0x1p-48f;
+    const float s1 = __fadd_rn(y, uh);  // TwoSum(y, uh) = s1 + e1 exactly
+    const float bv = __fsub_rn(s1, y);
+    const float e1 = __fadd_rn(__fsub_rn(y, __fsub_rn(s1, bv)), __fsub_rn(uh, bv));
+    const float tail = __fadd_rn(__fadd_rn(e1, c), ul);
+    const float n = floorf(s1);
+    const float d0 = __fsub_rn(s1, n);
+    constexpr float kEps = 0x1p-36f;
+    int v = static_cast<int>(n);
+    if (d0 < 0.5f) {  // only the lower boundary n is reachable; s1 - n is exact here
+        const float g = __fadd_rn(d0, tail);
+        if (g < -kEps) v -= 1;
+        else if (!(g > kEps)) undecided = true;
+    } else {  // only n + 1 is reachable; s1 - (n + 1) is exact here
+        const float g = __fadd_rn(__fsub_rn(s1, n + 1.0f), tail);
+        if (g > kEps) v += 1;
+        else if (!(g < -kEps)) undecided = true;
+    }
+    return v;
+}
+
+}  // namespace
+
 __global__ void __launch_bounds__(128) prepare_queries_kernel(PrepArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     unsigned long long *mt = reinterpret_cast<unsigned long long *>(smem_raw);  // [312]
     float *x = reinterpret_cast<float *>(mt + kMtN);                              // [D]
     float *qs = x + a.code_dim;                                                   // [dim] raw query
-    float *cs = qs + a.dim;                                                       // [dim] centre
-    __shared__ double s_rqn, s_dot;
-    __shared__ float s_half, s_max;
-    __shared__ int s_csum_part[4];
+    __shared__ float s_half, s_max, s_qn2;
+    __shared__ int s_csum_part[4], s_need_chain;
 
     const int q = blockIdx.x;
     if (q >= a.nq || (a.nq_dev != nullptr && q >= *a.nq_dev)) return;
     const int D = a.code_dim, dim = a.dim;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const float *gq = a.queries + static_cast<size_t>(q) * a.query_stride;
-    // stage the raw query and the centre once: the sequential chains below read shared memory
-    for (int i = threadIdx.x; i < dim; i += 128) {
-        qs[i] = gq[i];
-        cs[i] = a.center[i];
-    }
+    // stage the raw query once: the FNV chain below reads it byte by byte
+    for (int i = threadIdx.x; i < dim; i += 128) qs[i] = gq[i];
     __syncthreads();
     const float *raw = qs;
 
@@ -130,16 +285,14 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(PrepArgs a) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
         if (lane == 0) s_max = m;
-    } else if (warp == 1 && lane == 0) {
-        // ||q||^2 and <q, c> (space_rabitq.h:3688-3693, 3444-3450), FMA chains in double.
-        double rqn = 0.0, dot = 0.0;
-        for (int i = 0; i < dim; ++i) {
-            const double v = static_cast<double>(raw[i]);
-            rqn = __fma_rn(v, v, rqn);
-            dot = __fma_rn(v, static_cast<double>(cs[i]), dot);
+    } else if (warp == 1) {
+        // ||q - c||^2 (space_rabitq.h:3688-3693, 3444-3450)
+        float v = 0.0f;
+        const bool ok = exact_qn2_warp(raw, a.center, dim, a.center_norm_sqr[0], lane, &v);
+        if (lane == 0) {
+            s_qn2 = v;
+            s_need_chain = ok ? 0 : 1;
         }
-        s_rqn = rqn;
-        s_dot = dot;
     } else if (warp == 2 && lane == 0) {
         // FNV-1a over the raw query bytes, centroid-id mix (space_rabitq.h:3568-3580), then
         // the MT19937-64 seeding recurrence.
@@ -164,13 +317,23 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(PrepArgs a) {
         float half = 0.0f;
         for (int p = 0; p < D / 2; ++p) half += x[2 * p] + x[2 * p + 1];
         s_half = half;
+    } else if (warp == 1 && lane == 0 && s_need_chain) {
+        // the bound did not decide qn2: the reference's double FMA chains, in order
+        double rqn = 0.0, dot = 0.0;
+        for (int i = 0; i < dim; ++i) {
+            const double v = static_cast<double>(raw[i]);
+            rqn = __fma_rn(v, v, rqn);
+            dot = __fma_rn(v, static_cast<double>(a.center[i]), dot);
+        }
+        s_qn2 = fmaxf(0.0f, static_cast<float>(rqn + static_cast<double>(a.center_norm_sqr[0]) - 2.0 * dot));
     }
     __syncthreads();
 
-    const float qn2 = fmaxf(0.0f, static_cast<float>(s_rqn + static_cast<double>(a.center_norm_sqr[0]) -
-                                                      2.0 * s_dot));
+    const float qn2 = s_qn2;
     const float max_abs = s_max;
     const float scale = max_abs > 0.0f ? max_abs / 128.0f : 1.0f;
+    // below this the quotient's FMA remainder may underflow: take the double expression
+    const bool fast = scale >= 0x1p-100f;
     int csum = 0;
     int8_t *codes = a.codes + static_cast<size_t>(q) * D;
     if (max_abs > 0.0f) {
@@ -182,8 +345,13 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(PrepArgs a) {
                 const int j = base + p;
                 if (j < draws && (j & 1) == 0) {
                     const int i = j >> 1;
-                    const double u = canonical_u01(mt_temper(mt[p]));
-                    int v = static_cast<int>(floor(static_cast<double>(x[i]) / static_cast<double>(scale) + u));
+                    const unsigned long long K = mt_temper(mt[p]);
+                    bool undecided = !fast;
+                    int v = fast ? dither_floor(x[i], scale, K, undecided) : 0;
+                    if (undecided) {
+                        const double u = canonical_u01(K);
+                        v = static_cast<int>(floor(static_cast<double>(x[i]) / static_cast<double>(scale) + u));
+                    }
                     v = max(-128, min(127, v));
                     codes[i] = static_cast<int8_t>(v);
                     csum += v;
@@ -228,7 +396,7 @@ __global__ void __launch_bounds__(128) center_setup_kernel(const float *center, 
 cudaError_t launch_prepare(const PrepArgs &a, cudaStream_t stream) {
     if (a.nq == 0) return cudaSuccess;
     const size_t smem = kMtN * sizeof(unsigned long long) +
-                        (static_cast<size_t>(a.code_dim) + 2 * static_cast<size_t>(a.dim)) * sizeof(float);
+                        (static_cast<size_t>(a.code_dim) + static_cast<size_t>(a.dim)) * sizeof(float);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(prepare_queries_kernel,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -236,6 +404,28 @@ cudaError_t launch_prepare(const PrepArgs &a, cudaStream_t stream) {
         if (e != cudaSuccess) return e;
     }
     prepare_queries_kernel<<<a.nq, 128, smem, stream>>>(a);
+    return cudaGetLastError();
+}
+
+// Kernel-level check of the dither decision: out[i] = floor(double(x) / double(scale) + u(K))
+// (before the INT8 clamp), undecided[i] = 1 where the double expression had to be evaluated.
+__global__ void dither_pairs_kernel(const float *x, const float *scale, const unsigned long long *draws, size_t n,
+                                    int *out, uint8_t *undecided) {
+    const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float s = scale[i];
+    bool und = !(s >= 0x1p-100f);
+    int v = und ? 0 : dither_floor(x[i], s, draws[i], und);
+    if (und) v = static_cast<int>(floor(static_cast<double>(x[i]) / static_cast<double>(s) + canonical_u01(draws[i])));
+    out[i] = v;
+    if (undecided) undecided[i] = und ? 1 : 0;
+}
+
+cudaError_t launch_dither_pairs(const float *x, const float *scale, const unsigned long long *draws, size_t n,
+                                int *out, uint8_t *undecided, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    dither_pairs_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(x, scale, draws, n, out,
+                                                                                     undecided);
     return cudaGetLastError();
 }
 

@@ -104,3 +104,86 @@ def test_center_mean_matches_sequential_f32(cuda):
         acc = (acc + row).astype(np.float32)
     want = (acc * (np.float32(1.0) / np.float32(5000))).astype(np.float32)
     np.testing.assert_array_equal(bits(got), bits(want))
+
+
+def test_dither_decision_near_integer_boundaries(cuda):
+    """The FP32 dither decision equals floor(double(x)/double(scale) + u) exactly, including
+    draws placed on and within a few ulps of integer boundaries (where it must fall back)."""
+    torch = cuda
+    import ctypes as C
+
+    from quantization_graph_gb300 import _native as N
+
+    rng = np.random.default_rng(11)
+    m = 20000
+    scale = rng.uniform(0.001, 4.0, m).astype(np.float32)
+    K = rng.integers(0, 2**64 - 1, m, dtype=np.uint64, endpoint=True)
+    K[:50] = np.arange(50, dtype=np.uint64)                # u ~ 0
+    K[50:100] = np.uint64(2**64 - 1) - np.arange(50, dtype=np.uint64)  # u rounds to 1: clamped
+    u = np.minimum(K.astype(np.float64) * 2.0 ** -64, 1.0 - 2.0 ** -53)
+    target = rng.integers(-128, 129, m).astype(np.float64)
+    x0 = ((target - u) * scale.astype(np.float64)).astype(np.float32)
+    step = rng.integers(-3, 4, m)
+    x = x0.copy()
+    for s in (-3, -2, -1, 1, 2, 3):
+        sel = step == s
+        x[sel] = np.nextafter(x0[sel], np.float32(np.sign(s) * np.inf), dtype=np.float32)
+        for _ in range(abs(s) - 1):
+            x[sel] = np.nextafter(x[sel], np.float32(np.sign(s) * np.inf), dtype=np.float32)
+    # exact hits: x / scale an integer, u ~ 0 or clamped just below 1
+    scale[:100] = np.float32(0.5)
+    x[:50] = (target[:50] * 0.5).astype(np.float32)
+    x[50:100] = ((target[50:100] - 1.0) * 0.5).astype(np.float32)
+    # and plain random draws
+    xr = rng.uniform(-130, 130, m).astype(np.float32) * scale
+    X = np.concatenate([x, xr]).astype(np.float32)
+    S = np.concatenate([scale, scale])
+    KK = np.concatenate([K, K[::-1]])
+    want = np.floor(X.astype(np.float64) / S.astype(np.float64) +
+                    np.minimum(KK.astype(np.float64) * 2.0 ** -64, 1.0 - 2.0 ** -53)).astype(np.int64)
+    dx, ds = torch.from_numpy(X).cuda(), torch.from_numpy(S).cuda()
+    dk = torch.from_numpy(KK.view(np.int64)).cuda()
+    out = torch.empty(len(X), dtype=torch.int32, device="cuda")
+    und = torch.empty(len(X), dtype=torch.uint8, device="cuda")
+    lib = N.load()
+    N.check(lib.qg_dither_floor_pairs(C.c_void_p(dx.data_ptr()), C.c_void_p(ds.data_ptr()),
+                                      C.c_void_p(dk.data_ptr()), len(X), C.c_void_p(out.data_ptr()),
+                                      C.c_void_p(und.data_ptr()), None), "qg_dither_floor_pairs")
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy().astype(np.int64), want)
+    u8 = und.cpu().numpy()
+    assert u8[:m].sum() > 0, "boundary cases must reach the double fallback"
+    assert u8[m:].sum() <= 2, "random draws should be decided in FP32"
+
+
+def test_prepare_query_norm_fallbacks(cuda, oracle):
+    """||q - c||^2 in the exact fixed-point path and its double-chain fallback: a float tie,
+    a denormal result, a query on the centre, and wide dynamic ranges."""
+    torch = cuda
+    dim = 96
+    c = np.zeros(dim, np.float32)
+    rng = np.random.default_rng(5)
+    Q = np.zeros((8, dim), np.float32)
+    Q[0, 0] = np.float32(1.0 + 2.0 ** -12)      # q0^2 = 1 + 2^-11 + 2^-24: a float tie
+    Q[1, 5] = np.float32(1e-20)                   # ||q||^2 below the float normal range
+    Q[2] = rng.standard_normal(dim) * np.float32(1e-12)
+    Q[3] = (rng.standard_normal(dim) * np.exp(rng.uniform(-30, 30, dim))).astype(np.float32)
+    Q[4] = rng.standard_normal(dim) * np.float32(1e15)
+    Q[5, ::2] = 1.0
+    Q[5, 1::2] = -1.0
+    Q[6] = rng.standard_normal(dim)
+    o = oracle.Oracle(dim, c)
+    sp = _space(torch, dim, c)
+    p = sp.prepare(torch.from_numpy(Q).cuda())
+    c2 = (rng.standard_normal(dim)).astype(np.float32)
+    Q2 = np.stack([c2, c2 + np.float32(1e-6), -c2, c2 * np.float32(3.0)]).astype(np.float32)
+    o2 = oracle.Oracle(dim, c2)
+    sp2 = _space(torch, dim, c2)
+    p2 = sp2.prepare(torch.from_numpy(Q2).cuda())
+    for pp, oo, QQ in ((p, o, Q), (p2, o2, Q2)):
+        for i in range(len(QQ)):
+            po = oo.prepare(QQ[i])
+            sc = pp["scalars"][i].cpu().numpy()
+            np.testing.assert_array_equal(bits(sc), bits(np.array([po["query_norm_sqr"], po["query_norm"],
+                                                                   po["half_sum"], po["scale"]], np.float32)))
+            np.testing.assert_array_equal(pp["codes"][i].cpu().numpy(), po["codes"])
