@@ -70,7 +70,9 @@ __device__ __forceinline__ float restore_distance_hw(const uint8_t *__restrict__
     return out;
 }
 
-// finishQuantizedTraversalDistance (space_rabitq.h:4342-4358); every product is exact.
+// finishQuantizedTraversalDistance (space_rabitq.h:4342-4358); every product is exact. The
+// search calls it for all survivors of a hop in one warp-wide pass, so the double latency is
+// paid once per hop rather than once per group of survivors.
 __device__ __forceinline__ float finish_traversal(float norm_sqr, float long_scale, float short_ip,
                                                   int64_t remaining_dot, float scale,
                                                   int64_t code_sum, float qn2) {

@@ -506,11 +506,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                     }
                     const int tot = reduce_scatter<G>(p, lane);
                     const int i = gb + lane;
-                    if (lane < G && i < S) {
-                        const uint32_t slot = s.sslot[i];
-                        const float2 h = s.shdr[i];
-                        s.sdist[i] = finish_traversal(h.x, h.y, s.fsip[slot], tot, scale, csum, qn2);
-                    }
+                    if (lane < G && i < S) s.sdist[i] = __int_as_float(tot);  // finished below
                 }
             } else {
                 constexpr int P = L::PG;
@@ -530,13 +526,16 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
 #pragma unroll
                         for (int o = 1; o < L::LPN; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
                         const int i = ib + pp * L::NBP + grp;
-                        if (sub == 0 && i < S) {
-                            const uint32_t slot = s.sslot[i];
-                            const float2 h = s.shdr[i];
-                            s.sdist[i] = finish_traversal(h.x, h.y, s.fsip[slot], acc, scale, csum, qn2);
-                        }
+                        if (sub == 0 && i < S) s.sdist[i] = __int_as_float(acc);  // finished below
                     }
                 }
+            }
+            __syncwarp();
+            // finish every survivor at once, one lane each (finishQuantizedTraversalDistance)
+            for (int i = lane; i < S; i += 32) {
+                const float2 h = s.shdr[i];
+                s.sdist[i] = finish_traversal(h.x, h.y, s.fsip[s.sslot[i]], __float_as_int(s.sdist[i]), scale,
+                                              csum, qn2);
             }
             __syncwarp();
             // survivors whose gate was invalid use the full FP32 restore (mode 0)

@@ -187,3 +187,4 @@ def test_prepare_query_norm_fallbacks(cuda, oracle):
             np.testing.assert_array_equal(bits(sc), bits(np.array([po["query_norm_sqr"], po["query_norm"],
                                                                    po["half_sum"], po["scale"]], np.float32)))
             np.testing.assert_array_equal(pp["codes"][i].cpu().numpy(), po["codes"])
+
