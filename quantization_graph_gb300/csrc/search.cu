@@ -34,13 +34,16 @@ constexpr uint32_t kIdMask = 0x7FFFFFFFu;
 constexpr int kMaxFresh = 64;   // fresh neighbours per expanded node (max degree)
 constexpr int kMaxBeam = 8;
 
+#ifndef QG_GATE_GROUP
+#define QG_GATE_GROUP 16  // 32-dim MSB chunks in flight per lane in the gate (neighbours x chunks)
+#endif
 template <int D>
 struct Lay {
     static constexpr int CH = D / 32;
     static constexpr int LPN = CH < 32 ? CH : 32;   // lanes per neighbour
     static constexpr int CPL = CH / LPN;            // 32-dim chunks per lane
     static constexpr int NBP = 32 / LPN;            // neighbours per pass
-    static constexpr int GG = 16 / CPL;             // gate group (LPN == 32)
+    static constexpr int GG = QG_GATE_GROUP / CPL;  // gate group (LPN == 32)
     static constexpr int GT = CPL == 1 ? 8 : 2;     // traversal group (LPN == 32)
     static constexpr int PG = 4;                    // passes per batch (LPN < 32)
 };
@@ -251,8 +254,13 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
     int lval = a.l_per_q ? a.l_per_q[q] : a.l_default;
     uint32_t *out_ids = a.ids_out + static_cast<size_t>(q) * a.k_stride;
     float *out_d = a.dists_out + static_cast<size_t>(q) * a.k_stride;
-    unsigned long long st[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    // OursPaperSearchStats counters, distributed: counter c lives in lane c (two registers
+    // per lane instead of eighteen)
     enum { VIS, DC, HOPS, CHK, WPR, NPR, SAVED, MSBC, REMC };
+    unsigned long long stc = 0;
+    auto bump = [&](unsigned int counters, unsigned long long v) {
+        if ((counters >> lane) & 1u) stc += v;
+    };
     if (k < 0) k = 0;
     if (k > a.k_stride) k = a.k_stride;
     if (lval < k) lval = k;
@@ -283,9 +291,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             s.plb[0] = kFltMax;
         }
         pn = 1;
-        st[VIS] += 1;
-        st[DC] += 1;
-        st[REMC] += 1;
+        bump((1u << VIS) | (1u << DC) | (1u << REMC), 1);
     }
     __syncwarp();
 
@@ -380,8 +386,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                 break;
             }
             if (F == 0) continue;
-            st[VIS] += F;
-            st[MSBC] += F;
+            bump((1u << VIS) | (1u << MSBC), static_cast<unsigned>(F));
 
             // ---- gate (paper-prune lower bound) for every fresh neighbour ----
             // all MSB rows and factor rows are requested at once, then consumed group by group
@@ -464,9 +469,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                         s.sid[at] = s.fid[f];
                         s.sslot[at] = static_cast<uint32_t>(f);
                     }
-                    st[CHK] += __popc(pm);
-                    st[WPR] += __popc(pm);
-                    st[SAVED] += __popc(pm);
+                    bump((1u << CHK) | (1u << WPR) | (1u << SAVED), static_cast<unsigned>(__popc(pm)));
                     S += __popc(km);
                 }
             }
@@ -562,16 +565,13 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                 const uint32_t id = s.sid[i];
                 const bool full = pn >= lval;
                 if (full && valid) {
-                    st[CHK] += 1;
                     if (lb > s.pd[lval - 1]) {
-                        st[WPR] += 1;
-                        st[SAVED] += 1;
+                        bump((1u << CHK) | (1u << WPR) | (1u << SAVED), 1);
                         continue;
                     }
-                    st[NPR] += 1;
+                    bump((1u << CHK) | (1u << NPR), 1);
                 }
-                st[REMC] += 1;
-                st[DC] += 1;
+                bump((1u << REMC) | (1u << DC), 1);
                 // insert_candidate_sorted (ours_diskann.rs:1100-1126)
                 if (full && !cand_less(d, id, s.pd[lval - 1], s.pid[lval - 1] & kIdMask)) continue;
                 int pos = 0;
@@ -613,7 +613,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             }
         }
         if (failed) break;
-        st[HOPS] += nf;
+        bump(1u << HOPS, static_cast<unsigned>(nf));
         if (a.kth_stop && pn >= k) {
             const float kth = s.pd[k - 1];
             float mlb = kFltMax;
@@ -748,26 +748,20 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             out_d[rank] = me;
         }
     }
-    if (a.stats_out && lane == 0) {
-        qg_search_stats o;
-        o.visited_nodes = st[VIS];
-        o.distance_computations = st[DC];
-        o.hops = st[HOPS];
-        o.paper_checked = st[CHK];
-        o.paper_would_prune = st[WPR];
-        o.paper_not_pruned = st[NPR];
-        o.paper_full_saved = st[SAVED];
-        o.paper_msb_kernel_calls = st[MSBC];
-        o.paper_remaining_kernel_calls = st[REMC];
-        a.stats_out[q] = o;
+    if (a.stats_out && lane < 9) {
+        static_assert(sizeof(qg_search_stats) == 9 * sizeof(unsigned long long), "stats layout");
+        reinterpret_cast<unsigned long long *>(a.stats_out + q)[lane] = stc;
     }
 }
 
 #ifndef QG_SEARCH_MINBLOCKS
 #define QG_SEARCH_MINBLOCKS 2  // 128 registers per thread; 80 (3 blocks) spills and measured slower
 #endif
+#ifndef QG_SEARCH_THREADS
+#define QG_SEARCH_THREADS 256
+#endif
 template <int D>
-__global__ void __launch_bounds__(256, QG_SEARCH_MINBLOCKS) search_kernel(SearchArgs a) {
+__global__ void __launch_bounds__(QG_SEARCH_THREADS, QG_SEARCH_MINBLOCKS) search_kernel(SearchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
