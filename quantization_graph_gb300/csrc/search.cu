@@ -34,6 +34,12 @@ constexpr uint32_t kIdMask = 0x7FFFFFFFu;
 constexpr int kMaxFresh = 64;   // fresh neighbours per expanded node (max degree)
 constexpr int kMaxBeam = 8;
 
+#ifndef QG_GATE_PREFETCH
+#define QG_GATE_PREFETCH 0  // 0: every fresh MSB row to L1 at once; 1: one gate group ahead
+#endif
+#ifndef QG_TRAV_PREFETCH
+#define QG_TRAV_PREFETCH 0  // 0: every survivor code row to L1 at once; 1: L2, L1 one group ahead; 2: L2
+#endif
 #ifndef QG_GATE_GROUP
 #define QG_GATE_GROUP 16  // 32-dim MSB chunks in flight per lane in the gate (neighbours x chunks)
 #endif
@@ -390,7 +396,14 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
 
             // ---- gate (paper-prune lower bound) for every fresh neighbour ----
             // all MSB rows and factor rows are requested at once, then consumed group by group
+#if QG_GATE_PREFETCH == 0
             prefetch_rows_l1(ix.msb, s.fid, F, D / 8, D / 8, lane);
+#else
+            if constexpr (L::LPN == 32)
+                prefetch_rows_l1(ix.msb, s.fid, F < L::GG ? F : L::GG, D / 8, D / 8, lane);
+            else
+                prefetch_rows_l1(ix.msb, s.fid, F, D / 8, D / 8, lane);
+#endif
             prefetch_rows_l1(reinterpret_cast<const uint8_t *>(ix.pf), s.fid, F, 16, 16, lane);
             for (int f = lane; f < F; f += 32) s.fpf[f] = ix.pf[s.fid[f]];
             if constexpr (L::LPN == 32) {
@@ -405,6 +418,11 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
 #pragma unroll
                         for (int j = 0; j < L::CPL; ++j) w[g][j] = __ldg(row + lane + 32 * j);
                     }
+#if QG_GATE_PREFETCH == 1
+                    if (gb + G < F)
+                        prefetch_rows_l1(ix.msb, s.fid + gb + G, F - gb - G < G ? F - gb - G : G, D / 8, D / 8,
+                                         lane);
+#endif
                     int p[G];
 #pragma unroll
                     for (int g = 0; g < G; ++g) {
@@ -477,7 +495,14 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             if (S == 0) continue;
 
             // ---- traversal distances of the survivors ----
+#if QG_TRAV_PREFETCH == 0
             prefetch_rows_l1(ix.codes, s.sid, S, D / 2, D / 2, lane);
+#else
+            prefetch_rows_l2(ix.codes, s.sid, S, D / 2, D / 2, lane);
+#if QG_TRAV_PREFETCH == 1
+            if constexpr (L::LPN == 32) prefetch_rows_l1(ix.codes, s.sid, S < L::GT ? S : L::GT, D / 2, D / 2, lane);
+#endif
+#endif
             prefetch_rows_l1(reinterpret_cast<const uint8_t *>(ix.hdr), s.sid, S, 16, 16, lane);
             // survivors are the likeliest next expansions: warm L2 with their adjacency rows
             prefetch_rows_l2(reinterpret_cast<const uint8_t *>(ix.edges), s.sid, S, ix.edge_stride * 4,
@@ -499,6 +524,11 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
 #pragma unroll
                         for (int j = 0; j < L::CPL; ++j) c[g][j] = __ldg(row + lane + 32 * j);
                     }
+#if QG_TRAV_PREFETCH == 1
+                    if (gb + G < S)
+                        prefetch_rows_l1(ix.codes, s.sid + gb + G, S - gb - G < G ? S - gb - G : G, D / 2, D / 2,
+                                         lane);
+#endif
                     int p[G];
 #pragma unroll
                     for (int g = 0; g < G; ++g) {
