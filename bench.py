@@ -53,6 +53,12 @@ def parse():
     ap.add_argument("--train-queries", type=int, default=20_000)
     ap.add_argument("--stop-every", type=int, default=4)
     ap.add_argument("--stop-epochs", type=int, default=4)
+    ap.add_argument("--workload", default="dbpedia1536", choices=["dbpedia1536", "stream"],
+                    help="stream: uneven batched stream over a 120k x 1024 clustered index")
+    ap.add_argument("--stream-n", type=int, default=120_000)
+    ap.add_argument("--stream-queries", type=int, default=200_000)
+    ap.add_argument("--stream-threshold", type=float, default=0.0,
+                    help="learned-stop threshold for the stream (0 = fixed per-query L)")
     return ap.parse_args()
 
 
@@ -449,5 +455,121 @@ def main():
         dist.destroy_process_group()
 
 
+def run_stream(args, log):
+    """Uneven batched stream: 200k queries over a 120k x 1024 clustered unit-norm index (16
+    clusters, lambda_i ~ i^-1.0 within each), batch sizes log-uniform in [1, 4096], per-query
+    k in {1, 10, 100} and L uniform in [20, 400]; every batch is one replay of the captured
+    CUDA graph (GraphSearcher) with the autotuned launch shape. Reports QPS over the whole
+    stream and p50/p99 batch latency, measured end to end from pinned host buffers (queries,
+    k and L copied in, ids copied out, per batch)."""
+    import torch
+
+    from quantization_graph_gb300 import learned_stop as ls
+    from quantization_graph_gb300 import synthetic
+    from quantization_graph_gb300.graph_build import build_graph, reachable_fraction
+    from quantization_graph_gb300.index import OursIndex
+    from quantization_graph_gb300.space import RabitqSpace, train_global_center
+    from quantization_graph_gb300.stream import GraphSearcher, autotune
+
+    dim, n, nq_total = 1024, args.stream_n, args.stream_queries
+    t0 = time.time()
+    base = synthetic.clustered_torch(n, dim, 16, 1.0, seed=1)
+    queries = synthetic.clustered_torch(nq_total, dim, 16, 1.0, seed=2)
+    space = RabitqSpace(dim, train_global_center(base))
+    compact, residual = space.encode(base)
+    msb, factors = space.export_paper_sidecar(compact)
+    deg, edges = build_graph(space, base, compact, r=args.M, knn=2 * args.M, alpha=1.2, reverse=args.M,
+                             refine_rounds=args.refine, refine_l=128, residual=residual, msb=msb, factors=factors)
+    index = OursIndex(space, compact, residual, msb, factors, deg, edges)
+    gt = ground_truth(torch, base, queries, 10)
+    torch.cuda.synchronize()
+    t_setup = time.time() - t0
+    log(f"stream setup {t_setup:.1f}s, reachable {reachable_fraction(edges):.4f}")
+
+    rng = np.random.default_rng(5)
+    sizes = []
+    left = nq_total
+    while left > 0:
+        b = int(np.exp(rng.uniform(0.0, np.log(4097.0))))
+        b = max(1, min(b, 4096, left))
+        sizes.append(b)
+        left -= b
+    kq = rng.choice(np.array([1, 10, 100], np.int32), size=nq_total)
+    lq = rng.integers(20, 401, size=nq_total).astype(np.int32)
+
+    best, tune = autotune(index, queries[:4096], k=10, l_value=200, log=log)
+    model, thr = None, None
+    if args.stream_threshold > 0:
+        tq = synthetic.clustered_torch(20000, dim, 16, 1.0, seed=3)
+        truth = index.search(tq, k=10, l_value=400, with_stats=False).ids.to(torch.int32)
+        feats, labels = ls.collect_traces(index, tq, truth, k=10, l_value=400, every=args.stop_every)
+        model = ls.train(feats, labels, epochs=args.stop_epochs, every=args.stop_every,
+                         min_hops=2 * args.stop_every, log=log)
+        thr = args.stream_threshold
+    gs = GraphSearcher(index, dim, max_batch=4096, max_k=100, max_l=400, model=model, threshold=thr)
+    hq = queries.cpu().pin_memory()
+    hk = torch.from_numpy(kq).pin_memory()
+    hl = torch.from_numpy(lq).pin_memory()
+    out = torch.empty((nq_total, 100), dtype=torch.int32).pin_memory()
+
+    def run():
+        lat = []
+        start = 0
+        t_all = time.perf_counter()
+        for b in sizes:
+            tb = time.perf_counter()
+            with torch.cuda.stream(gs.stream):
+                dq = hq[start:start + b].to("cuda", non_blocking=True)
+                dk = hk[start:start + b].to("cuda", non_blocking=True)
+                dl = hl[start:start + b].to("cuda", non_blocking=True)
+            ids, _ = gs.search(dq, dk, dl)
+            with torch.cuda.stream(gs.stream):
+                out[start:start + b].copy_(ids, non_blocking=True)
+            gs.synchronize()
+            lat.append((time.perf_counter() - tb) * 1000.0)
+            start += b
+        return lat, time.perf_counter() - t_all
+
+    run()  # warm-up pass over the whole stream
+    with ClockSampler(0) as clocks:
+        lat, elapsed = run()
+    ids_all = out.to(torch.int64)
+    k10 = torch.from_numpy(kq >= 10)
+    gtc = gt.cpu()
+    hit = (ids_all[k10][:, :10, None] == gtc[k10][:, None, :10]).any(-1).sum().item()
+    rec10 = hit / (int(k10.sum()) * 10)
+    k1 = torch.from_numpy(kq == 1)
+    rec1 = (ids_all[k1][:, 0] == gtc[k1][:, 0]).float().mean().item()
+    lat_a = np.array(lat)
+    line = {"metric": "QPS, uneven batched stream, 120k\u00d71024 clustered 4-bit, 1 GB300",
+            "value": nq_total / elapsed, "unit": "queries/s", "n_gpus": 1, "steps": len(sizes), "warmup": len(sizes),
+            "ms_per_step": float(lat_a.mean()), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int8/f32", "data": "synthetic",
+            "config": {"workload": (f"{n} x {dim} unit-norm 16-cluster mixture (lambda_i ~ i^-1.0), M={args.M}, "
+                                    f"{nq_total} queries in {len(sizes)} batches (log-uniform 1..4096), "
+                                    "k in {1,10,100}, L ~ U[20,400]"),
+                       "launch": {"warps_per_block": best[0], "blocks_per_sm": best[1] or "max",
+                                  "tuned": [[list(s_), round(ms, 3)] for s_, ms in tune]},
+                       "learned_stop_threshold": thr,
+                       "recall@10 (k>=10 queries)": round(rec10, 4), "recall@1 (k=1 queries)": round(rec1, 4),
+                       "batch_latency_ms": {"p50": float(np.percentile(lat_a, 50)),
+                                            "p99": float(np.percentile(lat_a, 99)),
+                                            "max": float(lat_a.max())},
+                       "timing": "host wall clock per batch: pinned H2D of queries/k/L, graph replay, D2H of ids"},
+            "e2e": {"value": nq_total / elapsed, "unit": "queries/s",
+                    "h2d_bytes_per_step": int(nq_total * (dim * 4 + 8) / len(sizes)),
+                    "d2h_bytes_per_step": int(nq_total * 400 / len(sizes))},
+            "gpu_launches": 2 * len(sizes), "clocks": clocks.summary(),
+            "setup": {"seconds": round(t_setup, 1)}}
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
-    main()
+    _args = parse()
+    if _args.workload == "stream":
+        from quantization_graph_gb300 import build as _qb
+
+        _qb.build()
+        run_stream(_args, lambda m: print(m, file=sys.stderr, flush=True))
+    else:
+        main()
