@@ -497,6 +497,8 @@ def run_stream(args, log):
     kq = rng.choice(np.array([1, 10, 100], np.int32), size=nq_total)
     lq = rng.integers(20, 401, size=nq_total).astype(np.int32)
 
+    chk = index.search(queries[:4096], k=10, l_value=200, with_stats=False)
+    log(f"plain search, 4096 queries, L=200: recall@10 {recall_at(chk.ids, gt[:4096], 10):.4f}")
     best, tune = autotune(index, queries[:4096], k=10, l_value=200, log=log)
     model, thr = None, None
     if args.stream_threshold > 0:
@@ -545,7 +547,7 @@ def run_stream(args, log):
             "value": nq_total / elapsed, "unit": "queries/s", "n_gpus": 1, "steps": len(sizes), "warmup": len(sizes),
             "ms_per_step": float(lat_a.mean()), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int8/f32", "data": "synthetic",
-            "config": {"workload": (f"{n} x {dim} unit-norm 16-cluster mixture (lambda_i ~ i^-1.0), M={args.M}, "
+            "config": {"workload": (f"{n} x {dim} unit-norm 16-cluster mixture (lambda_i ~ i^-1.0, centre spread = within-cluster spread), M={args.M}, "
                                     f"{nq_total} queries in {len(sizes)} batches (log-uniform 1..4096), "
                                     "k in {1,10,100}, L ~ U[20,400]"),
                        "launch": {"warps_per_block": best[0], "blocks_per_sm": best[1] or "max",

@@ -5,6 +5,8 @@ The reference builds its Vamana graph on the host with the symmetric 4-bit estim
 This builder is not bit-identical to it. Steps:
 
   1. exact-ish kNN candidates from the float vectors (TF32 GEMM through torch/cuBLAS, top-K),
+     plus a few seeded random nodes per row (long-range candidates: on clustered data they are
+     what the prune keeps as links between clusters, as Vamana's random initial graph does),
   2. alpha robust prune of the candidates to R out-edges on the GPU (qg_prune_candidates,
      symmetric 4-bit distances, occlusion with alpha 1.0 then alpha),
   3. reverse edges added as candidates and a second prune,
@@ -94,7 +96,7 @@ def reachable_fraction(edges: torch.Tensor, start: int = 0, max_rounds: int = 10
 def build_graph(space: RabitqSpace, data: torch.Tensor, compact: torch.Tensor, r: int = 64,
                 knn: int = 128, alpha: float = 1.2, reverse: int = 64, refine_rounds: int = 0,
                 refine_l: int = 128, residual=None, msb=None, factors=None,
-                log=None) -> tuple[torch.Tensor, torch.Tensor]:
+                log=None, random_candidates: int = 16, seed: int = 0) -> tuple[torch.Tensor, torch.Tensor]:
     """Returns (degrees [n] int32, edges [n, r] int32 with -1 padding) on the GPU.
 
     refine_rounds > 0 needs residual/msb/factors: each round searches every node from node 0
@@ -105,6 +107,11 @@ def build_graph(space: RabitqSpace, data: torch.Tensor, compact: torch.Tensor, r
     data = _cuda(data, torch.float32)
     n = data.shape[0]
     cand = knn_candidates(data, knn)
+    if random_candidates > 0:
+        g = torch.Generator(device=data.device)
+        g.manual_seed(seed)
+        rnd = torch.randint(0, n, (n, random_candidates), generator=g, device=data.device, dtype=torch.int32)
+        cand = torch.cat([cand, rnd], dim=1)
     deg, edges = prune(space, compact, cand, r, alpha)
     del cand
     rev = reverse_candidates(edges, reverse)

@@ -6,9 +6,9 @@ distributions of the workloads the reference is measured on (DBpedia-1M 1536-d, 
   anisotropic  -- x ~ N(0, Q diag(lambda) Q^T), lambda_i proportional to i^-alpha, Q a seeded
                   random orthogonal matrix; optional |x| (960-d workload) or L2 normalisation
                   (1536-d workload)
-  clustered    -- mixture of anisotropic Gaussians: centres N(0, I), within cluster c
-                  N(0, Q_c diag(lambda) Q_c^T) with its own rotation, then L2-normalised
-                  (1024-d streaming workload)
+  clustered    -- mixture of anisotropic Gaussians: centres N(0, (sum(lambda)/d) I) (between-
+                  and within-cluster variance equal), within cluster c N(0, Q_c diag(lambda)
+                  Q_c^T) with its own rotation, then L2-normalised (1024-d streaming workload)
 
 numpy versions are bit-reproducible on every host (used by fixtures and tests); the torch
 versions generate large sets directly on the GPU for the benchmark.
@@ -75,15 +75,19 @@ def anisotropic_torch(n: int, dim: int, alpha: float, seed: int, rotation_seed: 
 
 def clustered_torch(n: int, dim: int, clusters: int, alpha: float, seed: int, structure_seed: int = 17,
                     device: str = "cuda", chunk: int = 131_072):
-    """Unit-norm rows of a `clusters`-component mixture; cluster c has centre N(0, I) and
-    covariance Q_c diag(i^-alpha) Q_c^T. The centres and rotations depend on `structure_seed`
-    only, so base and query sets drawn with different `seed` share the mixture."""
+    """Unit-norm rows of a `clusters`-component mixture; cluster c has covariance
+    Q_c diag(i^-alpha) Q_c^T and centre N(0, (sum_i i^-alpha / dim) I), so the spread of the
+    centres equals the spread inside a cluster. The centres and rotations depend on
+    `structure_seed` only, so base and query sets drawn with different `seed` share the
+    mixture."""
     import torch
 
     g = torch.Generator(device=device)
     g.manual_seed(structure_seed)
+    lam64 = torch.arange(1, dim + 1, device=device, dtype=torch.float64).pow(-alpha)
     centres = torch.randn((clusters, dim), generator=g, device=device, dtype=torch.float32)
-    lam = torch.arange(1, dim + 1, device=device, dtype=torch.float64).pow(-alpha).sqrt().to(torch.float32)
+    centres *= float((lam64.sum() / dim).sqrt())
+    lam = lam64.sqrt().to(torch.float32)
     mats = []
     for c in range(clusters):
         a = torch.randn((dim, dim), generator=g, device=device, dtype=torch.float32)
