@@ -376,6 +376,13 @@ int qg_prepare_batch(const void *space, const float *d_queries, size_t nq, float
  * to double arithmetic. */
 int qg_dither_floor_pairs(const float *d_x, const float *d_scale, const uint64_t *d_draws, size_t n,
                           int32_t *d_out, uint8_t *d_undecided, void *stream);
+/* Kernel-level check of the residual-code rounding used by the GPU encoder (no reference
+ * counterpart; the expression of residualMseOptimalScale and the residual codes,
+ * space_rabitq.h:748-786, 5936-5983): out[i] = clamp(round(double(x[i]) / double(s[i])), -7, 7)
+ * (half away from zero); undecided[i] (optional) = 1 where the FP32 decision fell back to
+ * double arithmetic. */
+int qg_round_quotient_pairs(const float *d_x, const float *d_s, size_t n, int32_t *d_out, uint8_t *d_undecided,
+                            void *stream);
 /* Kernel-level entry points over (query, id) pairs, for parity tests and tools: prepared
  * query arrays as produced by qg_prepare_batch; pair i uses query qidx[i] and record ids[i].
  * Records/sidecars in the reference host layouts, but in device memory. */

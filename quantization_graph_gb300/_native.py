@@ -120,6 +120,7 @@ _SIGS = {
     "qg_prune_candidates": (C.c_int, [P, P, SZ, SZ, P, SZ, SZ, C.c_float, P, P, SZ, P]),
     "qg_prepare_batch": (C.c_int, [P, P, SZ, P, P, P, P, P]),
     "qg_dither_floor_pairs": (C.c_int, [P, P, P, SZ, P, P, P]),
+    "qg_round_quotient_pairs": (C.c_int, [P, P, SZ, P, P, P]),
     "qg_gate_pairs": (C.c_int, [P, P, P, P, P, P, SZ, P, SZ, P, SZ, C.c_float, P, P]),
     "qg_distance_pairs": (C.c_int, [P, P, P, P, P, P, P, P, SZ, P, SZ, P, P, P]),
     "qg_residual_pairs": (C.c_int, [P, P, P, P, P, SZ, P, SZ, P, P, P]),

@@ -947,6 +947,16 @@ int qg_dither_floor_pairs(const float *d_x, const float *d_scale, const uint64_t
     return QG_OK;
 }
 
+int qg_round_quotient_pairs(const float *d_x, const float *d_s, size_t n, int32_t *d_out, uint8_t *d_undecided,
+                            void *stream) {
+    if (n && (!d_x || !d_s || !d_out)) return QG_ERR_INVALID;
+    if (!cuda_ok(launch_round_quotient_pairs(d_x, d_s, n, reinterpret_cast<int *>(d_out), d_undecided,
+                                             static_cast<cudaStream_t>(stream)),
+                 "round quotient kernel"))
+        return QG_ERR_CUDA;
+    return QG_OK;
+}
+
 int qg_gate_pairs(const void *space, const int8_t *d_codes, const float *d_scalars,
                   const int64_t *d_code_sum, const uint32_t *d_qidx, const uint32_t *d_ids,
                   size_t count, const uint8_t *d_msb, size_t msb_stride, const void *d_factors,
@@ -1163,16 +1173,16 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
 // Warps per block and resident blocks per SM for a pool of l_cap entries: the caller's override
 // (qg_index_set_launch) clamped to what is resident, else the candidate with the most resident
 // warps (large pools need more shared memory per warp, where smaller blocks pack better).
-static bool launch_geometry(const qg_index *index, int l_cap, int *wpb_out, int *per_sm_out) {
+static bool launch_geometry(const qg_index *index, int l_cap, bool stop_model, int *wpb_out, int *per_sm_out) {
     const int D = static_cast<int>(index->space->code_dim);
     int wpb = 0, per_sm = 0;
     if (index->launch_wpb > 0) {
         wpb = index->launch_wpb;
-        per_sm = search_blocks_per_sm(D, l_cap, wpb);
+        per_sm = search_blocks_per_sm(D, l_cap, wpb, stop_model);
         if (index->launch_per_sm > 0 && index->launch_per_sm < per_sm) per_sm = index->launch_per_sm;
     } else {
         for (int cand : {8, 4, 2}) {
-            const int b = search_blocks_per_sm(D, l_cap, cand);
+            const int b = search_blocks_per_sm(D, l_cap, cand, stop_model);
             if (b * cand > per_sm * wpb) {
                 wpb = cand;
                 per_sm = b;
@@ -1340,7 +1350,7 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
     // warps per block: the candidate with the most resident warps per SM (large pools need
     // more shared memory per warp, where smaller blocks pack better)
     int wpb = 0, per_sm = 0;
-    if (!launch_geometry(index, l_cap, &wpb, &per_sm)) return QG_ERR_UNSUPPORTED;
+    if (!launch_geometry(index, l_cap, model != nullptr, &wpb, &per_sm)) return QG_ERR_UNSUPPORTED;
     int sms = qg_device_sm_count();
     if (sms <= 0) sms = 1;
     const int grid = sms * per_sm;

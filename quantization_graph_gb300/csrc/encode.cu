@@ -14,6 +14,7 @@
 // order, and a 7-way merge by (t, i) replays the heap's pop sequence exactly.
 #include <cstdint>
 
+#include "exact_fp.cuh"
 #include "qg_device.cuh"
 #include "qg_kernels.h"
 
@@ -48,8 +49,8 @@ __device__ __forceinline__ int round_away(double v) {  // std::round: half away 
     return static_cast<int>(round(v));
 }
 
-// residualMseOptimalScale, 4-bit (space_rabitq.h:748-786)
-__device__ float mse_scale16(const float *e) {
+// residualMseOptimalScale, 4-bit (space_rabitq.h:748-786), in double as the reference does.
+__device__ float mse_scale16_f64(const float *e) {
     float m = 0.0f;
     for (int i = 0; i < 16; ++i) m = fmaxf(m, fabsf(e[i]));
     if (m <= 0.0f) return 0.0f;
@@ -72,6 +73,89 @@ __device__ float mse_scale16(const float *e) {
         scale = next;
     }
     return scale;
+}
+
+// The same scale without FP64. Each q = round(e / scale) is decided in FP32
+// (round_away_quotient); n = sum e_i q_i is summed exactly in integers on the grid of the
+// smallest term, which equals the reference's double sum whenever every partial sum fits 53
+// bits there (the products e_i q_i are exact in double); next = float(n / d) is rounded from
+// the exact quotient (128-bit division by the integer d) through 53 and then 24 bits. Returns
+// false when any of those conditions fails; the caller then takes mse_scale16_f64.
+__device__ bool mse_scale16_exact(const float *e, float *out) {
+    float m = 0.0f;
+    for (int i = 0; i < 16; ++i) m = fmaxf(m, fabsf(e[i]));
+    if (m <= 0.0f) {
+        *out = 0.0f;
+        return true;
+    }
+    float scale = m / 7.0f;
+    if (scale == 0.0f || !isfinite(scale)) {
+        *out = scale;
+        return true;
+    }
+    for (int iter = 0; iter < 8; ++iter) {
+        if (!(scale >= 0x1p-100f)) return false;
+        int d = 0, G = 1 << 30;
+        int qv[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            bool und = false;
+            int q = round_away_quotient(e[i], scale, und);
+            if (und) q = max(-7, min(7, round_away(static_cast<double>(e[i]) / static_cast<double>(scale))));
+            qv[i] = q;
+            d += q * q;
+            if (q != 0 && e[i] != 0.0f) G = min(G, split_float(e[i]).e);
+        }
+        if (d <= 0) break;
+        __int128 N = 0;
+        if (G != (1 << 30)) {
+            for (int i = 0; i < 16; ++i) {
+                if (qv[i] == 0 || e[i] == 0.0f) continue;
+                const FloatParts p = split_float(e[i]);
+                const int sh = p.e - G;
+                if (sh > 60) return false;
+                N += static_cast<__int128>(p.m * qv[i]) << sh;
+                const __int128 a = N < 0 ? -N : N;
+                if (a >= (static_cast<__int128>(1) << 53)) return false;  // a partial sum may have rounded
+            }
+        }
+        if (N == 0) break;  // next = 0: the reference stops
+        bool ok = true;
+        const unsigned long long mag = static_cast<unsigned long long>(N < 0 ? -N : N);
+        const float next = float_via_double(N < 0, div_shift64_sticky(mag, static_cast<uint32_t>(d)), G - 65, ok);
+        if (!ok) return false;
+        if (next <= 0.0f || !isfinite(next)) break;
+        if (fabsf(next - scale) <= 1e-6f * fmaxf(1.0f, scale)) {
+            scale = next;
+            break;
+        }
+        scale = next;
+    }
+    *out = scale;
+    return true;
+}
+
+// float(double(rn) * double(r) - 0.5 * double(long_scale) * (code - 7.5)) (space_rabitq.h:5927-5935)
+// from the two exact products held in integers; falls back to the double expression when the
+// operands' exponents are too far apart for the 128-bit grid or the float is not normal.
+__device__ __forceinline__ float quant_error(float rn, float r, float long_scale, int code) {
+    const FloatParts a = split_float(rn), b = split_float(r), c = split_float(long_scale);
+    const long long tv = a.m * b.m;                       // * 2^(a.e + b.e), |tv| < 2^48
+    const long long x4 = c.m * static_cast<long long>(2 * code - 15);  // * 2^(c.e - 2), |x4| < 2^29
+    const int et = a.e + b.e, ex = c.e - 2;
+    const int G = min(et, ex);
+    bool ok = a.finite && b.finite && c.finite && et - G <= 70 && ex - G <= 90;
+    float out = 0.0f;
+    if (ok) {
+        const __int128 v = (static_cast<__int128>(tv) << (et - G)) - (static_cast<__int128>(x4) << (ex - G));
+        out = float_via_double(v < 0, static_cast<unsigned __int128>(v < 0 ? -v : v), G, ok);
+    }
+    if (!ok) {
+        const double tvd = static_cast<double>(rn) * static_cast<double>(r);
+        const double x4d = 0.5 * static_cast<double>(long_scale) * (static_cast<double>(code) - 7.5);
+        out = static_cast<float>(tvd - x4d);
+    }
+    return out;
 }
 
 __device__ void bitonic_sort_warp(unsigned long long *k, int n, int lane) {
@@ -103,6 +187,167 @@ __device__ void fht_warp_local(float *x, int D, int lane) {
         }
         __syncwarp();
     }
+}
+
+// The largest float not above the double 1e-5: a > 1e-5 (double) <=> a > kEpsBelowF.
+constexpr float kEpsBelowF = 9.99999974737875e-06f;
+
+// floor(RN53(t * a + 1e-5)) for t = th + tl (t a double split into two floats, a >= 0) in FP32:
+// ph + pl = th * a exactly, the rest is below 2^-16 and positive, so only the boundary above
+// can be crossed; decided unless the value lies within 2^-36 of it (`undecided`).
+__device__ __forceinline__ int floor_fma_eps(float th, float tl, float a, bool &undecided) {
+    const float ph = __fmul_rn(th, a);
+    const float pl = __fmaf_rn(th, a, -ph);
+    const float tail = __fadd_rn(__fadd_rn(__fadd_rn(pl, __fmul_rn(tl, a)), kEpsBelowF), 2.5262124e-13f);
+    const float n = floorf(ph);
+    const float d0 = __fsub_rn(ph, n);  // exact
+    int v = static_cast<int>(n);
+    if (d0 >= 0.5f) {
+        const float g = __fadd_rn(__fsub_rn(d0, 1.0f), tail);  // d0 - 1 exact for d0 >= 0.5
+        if (g > 0x1p-36f) v += 1;
+        else if (!(g < -0x1p-36f)) undecided = true;
+    } else if (!(tail > 0.0f)) {
+        undecided = true;  // cannot happen for a >= 0; keeps the decision honest
+    }
+    return v;
+}
+
+// sign of c1 / a1 - c2 / a2 for integers 1 <= c <= 17 and positive normal floats a, exactly:
+// the sign of c1 a2 - c2 a1, compared on the significands.
+__device__ __forceinline__ int ratio_cmp(int c1, float a1, int c2, float a2) {
+    const FloatParts p1 = split_float(a1), p2 = split_float(a2);
+    long long l = c1 * p2.m, r = c2 * p1.m;  // < 2^29
+    const int d = p2.e - p1.e;                 // l * 2^d against r
+    if (d > 30) return 1;
+    if (d < -30) return -1;
+    if (d > 0) l <<= d;
+    else r <<= -d;
+    return l < r ? -1 : (l > r ? 1 : 0);
+}
+
+// Truncation of a positive normal double to float (relative error below 2^-23), by bits.
+__device__ __forceinline__ float approx_float(double x) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+    const int ex = static_cast<int>((b >> 52) & 0x7FF) - 1023 + 127;
+    if (ex <= 0) return 0.0f;
+    if (ex >= 255) return __int_as_float(0x7f800000);
+    return __uint_as_float((static_cast<uint32_t>(ex) << 23) | static_cast<uint32_t>((b >> 29) & 0x7FFFFFu));
+}
+
+// fastQuantizeAbs's search over the rescale factor t (space_rabitq.h:867-942), lane 0: the
+// (t, i) events of the seven levels in heap order (t = level / |v_i|, ties by i), running
+// num and sqr_den, t at the first maximum of num / sqrt(sqr_den). Event order and the t_end
+// cut are decided by exact ratio comparisons (distinct level / |v| ratios differ by far more
+// than a double's rounding, so they order as their doubles do); num stays a double sum; the
+// maximum is screened in FP32 (error below 2^-21 relative) and only the events within 2^-19 of
+// the running FP32 maximum are evaluated in double at the end. If more than kCand events are
+// in that band at once, the whole search runs again in double as the reference does.
+__device__ double code_search_lane0(const unsigned long long *keys, const float *ru, const unsigned char *c0,
+                                    int D, float mx) {
+    long long sd4 = D;  // 4 * sqr_den
+    double num = 0.0;
+    for (int i = 0; i < D; ++i) {
+        const int c = c0[i];
+        sd4 += 4LL * (c * c + c);
+        num += (c + 0.5) * static_cast<double>(fabsf(ru[i]));
+    }
+    const long long sd4_0 = sd4;
+    const double num_0 = num;
+    int ptr[8], head[8];
+    auto advance = [&](int c) {
+        while (ptr[c] < D) {
+            const int i = static_cast<int>(keys[ptr[c]] & 0xFFFFFFFFu);
+            const float ai = fabsf(ru[i]);
+            const int ci = c0[i];
+            if (ai > kEpsBelowF && c > ci && (c == ci + 1 || ratio_cmp(c, ai, 17, mx) < 0)) {
+                head[c] = i;
+                return;
+            }
+            ++ptr[c];
+        }
+        head[c] = -1;
+    };
+    auto earlier = [&](int c, int b) {  // event of level c before that of level b
+        const int r = ratio_cmp(c, fabsf(ru[head[c]]), b, fabsf(ru[head[b]]));
+        return r < 0 || (r == 0 && head[c] < head[b]);
+    };
+    constexpr int kCand = 24;
+    double cn[kCand];
+    int cs[kCand], clev[kCand], cid[kCand];
+    float cf[kCand];
+    int nc = 0;
+    bool overflow = false;
+    float maxf = 0.0f;
+    for (int c = 1; c <= 7; ++c) {
+        ptr[c] = 0;
+        advance(c);
+    }
+    for (;;) {
+        int bc = -1;
+        for (int c = 1; c <= 7; ++c)
+            if (head[c] >= 0 && (bc < 0 || earlier(c, bc))) bc = c;
+        if (bc < 0) break;
+        const int id = head[bc];
+        sd4 += 8LL * bc;
+        num += static_cast<double>(fabsf(ru[id]));
+        const float ipf = __fdiv_rn(approx_float(num), sqrtf(__ll2float_rn(sd4) * 0.25f));
+        if (ipf > maxf) {
+            maxf = ipf;
+            int w = 0;  // drop candidates that fell out of the band
+            for (int k = 0; k < nc; ++k)
+                if (cf[k] >= maxf * (1.0f - 0x1p-19f)) {
+                    cn[w] = cn[k]; cs[w] = cs[k]; clev[w] = clev[k]; cid[w] = cid[k]; cf[w] = cf[k];
+                    ++w;
+                }
+            nc = w;
+        }
+        if (ipf >= maxf * (1.0f - 0x1p-19f)) {
+            if (nc < kCand) {
+                cn[nc] = num; cs[nc] = static_cast<int>(sd4); clev[nc] = bc; cid[nc] = id; cf[nc] = ipf;
+                ++nc;
+            } else {
+                overflow = true;
+            }
+        }
+        ++ptr[bc];
+        advance(bc);
+    }
+    double best_t = 0.0, max_ip = 0.0;
+    if (!overflow) {
+        for (int k = 0; k < nc; ++k) {
+            if (!(cf[k] >= maxf * (1.0f - 0x1p-19f))) continue;
+            const double ip = cn[k] / sqrt(static_cast<double>(cs[k]) * 0.25);
+            if (ip > max_ip) {
+                max_ip = ip;
+                best_t = static_cast<double>(clev[k]) / static_cast<double>(fabsf(ru[cid[k]]));
+            }
+        }
+        return best_t;
+    }
+    // the reference's loop in double, from the same start
+    sd4 = sd4_0;
+    num = num_0;
+    for (int c = 1; c <= 7; ++c) {
+        ptr[c] = 0;
+        advance(c);
+    }
+    for (;;) {
+        int bc = -1;
+        for (int c = 1; c <= 7; ++c)
+            if (head[c] >= 0 && (bc < 0 || earlier(c, bc))) bc = c;
+        if (bc < 0) break;
+        const int id = head[bc];
+        sd4 += 8LL * bc;
+        num += static_cast<double>(fabsf(ru[id]));
+        const double ip = num / sqrt(static_cast<double>(sd4) * 0.25);
+        if (ip > max_ip) {
+            max_ip = ip;
+            best_t = static_cast<double>(bc) / static_cast<double>(fabsf(ru[id]));
+        }
+        ++ptr[bc];
+        advance(bc);
+    }
+    return best_t;
 }
 
 __device__ __forceinline__ void put_f32(uint8_t *dst, float v) {
@@ -155,82 +400,38 @@ __global__ void __launch_bounds__(32) encode_kernel(EncodeArgs a) {
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     const double max_o = static_cast<double>(mx);
     float ip_norm = 1.0f;
-    if (max_o <= kEps) {
+    if (!(mx > kEpsBelowF)) {  // max_o <= kEps
         for (int i = lane; i < D; i += 32) c0[i] = 0;
     } else {
-        const double t_start = 2.0 / max_o;
-        const double t_end = 17.0 / max_o;
-        for (int i = lane; i < D; i += 32) {
-            const float ai = fabsf(ru[i]);
-            int c = static_cast<int>(__fma_rn(t_start, static_cast<double>(ai), kEps));
-            c0[i] = static_cast<unsigned char>(min(c, 7));
-            keys[i] = (static_cast<unsigned long long>(0xFFFFFFFFu - __float_as_uint(ai)) << 32) |
-                      static_cast<unsigned int>(i);
+        const double t_start = 2.0 / max_o;  // t_end = 17 / max_o is applied as an exact ratio test
+        {
+            const float th = __double2float_rn(t_start);
+            const float tl = __double2float_rn(t_start - static_cast<double>(th));
+            for (int i = lane; i < D; i += 32) {
+                const float ai = fabsf(ru[i]);
+                bool und = false;
+                int c = floor_fma_eps(th, tl, ai, und);
+                if (und) c = static_cast<int>(__fma_rn(t_start, static_cast<double>(ai), kEps));
+                c0[i] = static_cast<unsigned char>(min(c, 7));
+                keys[i] = (static_cast<unsigned long long>(0xFFFFFFFFu - __float_as_uint(ai)) << 32) |
+                          static_cast<unsigned int>(i);
+            }
         }
         __syncwarp();
         bitonic_sort_warp(keys, D, lane);
-        if (lane == 0) {
-            double sqr_den = static_cast<double>(D) * 0.25;
-            double num = 0.0;
-            for (int i = 0; i < D; ++i) {
-                const int c = c0[i];
-                sqr_den += static_cast<double>(c * c + c);
-                num += (c + 0.5) * static_cast<double>(fabsf(ru[i]));
-            }
-            // 7-way merge over levels c = 1..7 of the (t, i) events
-            int ptr[8];
-            double head_t[8];
-            int head_i[8];
-            auto advance = [&](int c) {
-                while (ptr[c] < D) {
-                    const unsigned int i = static_cast<unsigned int>(keys[ptr[c]] & 0xFFFFFFFFu);
-                    const float ai = fabsf(ru[i]);
-                    const int ci = c0[i];
-                    if (static_cast<double>(ai) > kEps && c > ci) {
-                        const double t = static_cast<double>(c) / static_cast<double>(ai);
-                        if (c == ci + 1 || t < t_end) {
-                            head_t[c] = t;
-                            head_i[c] = static_cast<int>(i);
-                            return;
-                        }
-                    }
-                    ++ptr[c];
-                }
-                head_i[c] = -1;
-            };
-            for (int c = 1; c <= 7; ++c) {
-                ptr[c] = 0;
-                advance(c);
-            }
-            double best_t = 0.0, max_ip = 0.0;
-            for (;;) {
-                int bc = -1;
-                for (int c = 1; c <= 7; ++c) {
-                    if (head_i[c] < 0) continue;
-                    if (bc < 0 || head_t[c] < head_t[bc] ||
-                        (head_t[c] == head_t[bc] && head_i[c] < head_i[bc]))
-                        bc = c;
-                }
-                if (bc < 0) break;
-                const double t = head_t[bc];
-                const int id = head_i[bc];
-                sqr_den += 2.0 * static_cast<double>(bc);
-                num += static_cast<double>(fabsf(ru[id]));
-                const double ip = num / sqrt(sqr_den);
-                if (ip > max_ip) {
-                    max_ip = ip;
-                    best_t = t;
-                }
-                ++ptr[bc];
-                advance(bc);
-            }
-            s_best_t = best_t;
-        }
+        if (lane == 0) s_best_t = code_search_lane0(keys, ru, c0, D, mx);
         __syncwarp();
         const double best_t = s_best_t;
-        for (int i = lane; i < D; i += 32) {
-            const int c = static_cast<int>(__fma_rn(best_t, static_cast<double>(fabsf(ru[i])), kEps));
-            c0[i] = static_cast<unsigned char>(min(c, 7));
+        {
+            const float th = __double2float_rn(best_t);
+            const float tl = __double2float_rn(best_t - static_cast<double>(th));
+            for (int i = lane; i < D; i += 32) {
+                const float ai = fabsf(ru[i]);
+                bool und = false;
+                int c = floor_fma_eps(th, tl, ai, und);
+                if (und) c = static_cast<int>(__fma_rn(best_t, static_cast<double>(ai), kEps));
+                c0[i] = static_cast<unsigned char>(min(c, 7));
+            }
         }
         __syncwarp();
         if (lane == 0) {
@@ -287,14 +488,13 @@ __global__ void __launch_bounds__(32) encode_kernel(EncodeArgs a) {
     // quantisation error of the 4-bit code (:5927-5935); products are exact
     for (int i = lane; i < D; i += 32) {
         const int code = ru[i] > 0.0f ? 8 + c0[i] : 7 - c0[i];
-        const double tv = static_cast<double>(rn) * static_cast<double>(ru[i]);
-        const double x4 = 0.5 * static_cast<double>(long_scale) * (static_cast<double>(code) - 7.5);
-        qerr[i] = static_cast<float>(tv - x4);
+        qerr[i] = quant_error(rn, ru[i], long_scale, code);
     }
     __syncwarp();
     // per-block MSE scale, fp16 store/reload, residual codes (:5936-5983)
     for (int b = lane; b < D / 16; b += 32) {
-        const float sc = mse_scale16(qerr + 16 * b);
+        float sc;
+        if (!mse_scale16_exact(qerr + 16 * b, &sc)) sc = mse_scale16_f64(qerr + 16 * b);
         const uint16_t h = float_to_half_ref(sc);
         rp[8 + 2 * b] = static_cast<uint8_t>(h & 0xFF);
         rp[9 + 2 * b] = static_cast<uint8_t>(h >> 8);
@@ -302,8 +502,11 @@ __global__ void __launch_bounds__(32) encode_kernel(EncodeArgs a) {
         s_sc[b] = stored;
         for (int i = 16 * b; i < 16 * b + 16; ++i) {
             int q = 0;
-            if (stored != 0.0f && isfinite(stored))
-                q = max(-7, min(7, round_away(static_cast<double>(qerr[i]) / static_cast<double>(stored))));
+            if (stored != 0.0f && isfinite(stored)) {
+                bool und = !(stored >= 0x1p-100f) || !isfinite(qerr[i]);
+                if (!und) q = round_away_quotient(qerr[i], stored, und);
+                if (und) q = max(-7, min(7, round_away(static_cast<double>(qerr[i]) / static_cast<double>(stored))));
+            }
             rcode[i] = static_cast<signed char>(q);
         }
     }

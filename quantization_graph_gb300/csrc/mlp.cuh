@@ -63,4 +63,65 @@ __device__ __forceinline__ float mlp_forward_warp(const float (&f)[kMlpIn], cons
     return out + mlp_w(w, kMlpB3);
 }
 
+// Shared-memory copy for the search kernel (one per block, staged once): every word packs
+// the BF16 pair (unit j, unit j+32) that lane j reads together, so a layer step is one 32-bit
+// shared load per lane. Words: W1 [8][32] | b1 [32] | W2 [64][32] | b2 [32] | w3 [32] | b3.
+constexpr int kMlpSmemW1 = 0;
+constexpr int kMlpSmemB1 = kMlpSmemW1 + kMlpIn * 32;
+constexpr int kMlpSmemW2 = kMlpSmemB1 + 32;
+constexpr int kMlpSmemB2 = kMlpSmemW2 + kMlpHidden * 32;
+constexpr int kMlpSmemW3 = kMlpSmemB2 + 32;
+constexpr int kMlpSmemB3 = kMlpSmemW3 + 32;
+constexpr int kMlpSmemWords = kMlpSmemB3 + 1;
+constexpr int kMlpSmemBytes = ((kMlpSmemWords * 4 + 15) / 16) * 16;
+
+__device__ __forceinline__ uint32_t mlp_pair(const uint16_t *w, int base, int j) {
+    return static_cast<uint32_t>(w[base + j]) | (static_cast<uint32_t>(w[base + j + 32]) << 16);
+}
+
+// All threads of the block call it; the caller synchronises before use.
+__device__ __forceinline__ void mlp_stage_smem(const uint16_t *w, uint32_t *s, int tid, int nthreads) {
+    for (int t = tid; t < kMlpSmemWords; t += nthreads) {
+        uint32_t v;
+        if (t < kMlpSmemB1) v = mlp_pair(w, kMlpW1 + (t >> 5) * kMlpHidden, t & 31);
+        else if (t < kMlpSmemW2) v = mlp_pair(w, kMlpB1, t - kMlpSmemB1);
+        else if (t < kMlpSmemB2) v = mlp_pair(w, kMlpW2 + ((t - kMlpSmemW2) >> 5) * kMlpHidden, (t - kMlpSmemW2) & 31);
+        else if (t < kMlpSmemW3) v = mlp_pair(w, kMlpB2, t - kMlpSmemB2);
+        else if (t < kMlpSmemB3) v = mlp_pair(w, kMlpW3, t - kMlpSmemW3);
+        else v = w[kMlpB3];
+        s[t] = v;
+    }
+}
+
+__device__ __forceinline__ float bf16_lo(uint32_t v) { return __uint_as_float(v << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t v) { return __uint_as_float(v & 0xFFFF0000u); }
+
+// mlp_forward_warp over the shared-memory copy: the same operations in the same order.
+__device__ __forceinline__ float mlp_forward_warp_smem(const float (&f)[kMlpIn], const uint32_t *s, int lane) {
+    const uint32_t bb1 = s[kMlpSmemB1 + lane];
+    float acc0 = bf16_lo(bb1), acc1 = bf16_hi(bb1);
+#pragma unroll
+    for (int i = 0; i < kMlpIn; ++i) {
+        const uint32_t ww = s[kMlpSmemW1 + i * 32 + lane];
+        acc0 = __fmaf_rn(bf16_lo(ww), f[i], acc0);
+        acc1 = __fmaf_rn(bf16_hi(ww), f[i], acc1);
+    }
+    const float a1[2] = {fmaxf(acc0, 0.0f), fmaxf(acc1, 0.0f)};
+    const uint32_t bb2 = s[kMlpSmemB2 + lane];
+    float acc2[2] = {bf16_lo(bb2), bf16_hi(bb2)};
+#pragma unroll 8
+    for (int i = 0; i < kMlpHidden; ++i) {
+        const float hi = __shfl_sync(0xffffffffu, a1[i >> 5], i & 31);
+        const uint32_t ww = s[kMlpSmemW2 + i * 32 + lane];
+        acc2[0] = __fmaf_rn(bf16_lo(ww), hi, acc2[0]);
+        acc2[1] = __fmaf_rn(bf16_hi(ww), hi, acc2[1]);
+    }
+    const float a2a = fmaxf(acc2[0], 0.0f), a2b = fmaxf(acc2[1], 0.0f);
+    const uint32_t w3 = s[kMlpSmemW3 + lane];
+    float out = __fmaf_rn(bf16_lo(w3), a2a, bf16_hi(w3) * a2b);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) out += __shfl_xor_sync(0xffffffffu, out, o);
+    return out + bf16_lo(s[kMlpSmemB3]);
+}
+
 }  // namespace qg

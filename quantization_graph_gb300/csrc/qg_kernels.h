@@ -92,6 +92,8 @@ struct EncodeArgs {
 void record_error(const std::string &msg);
 
 cudaError_t launch_prepare(const PrepArgs &a, cudaStream_t stream);
+cudaError_t launch_round_quotient_pairs(const float *x, const float *s, size_t n, int *out, uint8_t *undecided,
+                                        cudaStream_t stream);
 cudaError_t launch_dither_pairs(const float *x, const float *scale, const unsigned long long *draws, size_t n,
                                 int *out, uint8_t *undecided, cudaStream_t stream);
 cudaError_t launch_center_setup(const float *center, const float *signs, int dim, int D,
@@ -100,7 +102,10 @@ cudaError_t launch_center_mean(const float *data, size_t stride, int dim, const 
                                size_t count, float *out, cudaStream_t stream);
 cudaError_t launch_search(const SearchArgs &a, int grid, int warps_per_block, cudaStream_t stream);
 size_t search_smem_per_warp(int code_dim, int l_cap);
-int search_blocks_per_sm(int code_dim, int l_cap, int warps_per_block);
+// Resident blocks per SM and dynamic shared memory of one search block; a stop model adds
+// the staged network weights to every block.
+int search_blocks_per_sm(int code_dim, int l_cap, int warps_per_block, bool stop_model = false);
+size_t search_block_smem(int l_cap, int warps_per_block, bool stop_model);
 int search_supported_dim(int code_dim);
 cudaError_t launch_encode(const EncodeArgs &a, cudaStream_t stream);
 cudaError_t launch_mlp_forward(const float *X, size_t n, const float *norm, const uint16_t *w, float *logits,

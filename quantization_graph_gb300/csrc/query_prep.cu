@@ -11,6 +11,7 @@
 // exact margin test, double arithmetic only for draws within 2^-36 of an integer.
 #include <cstdint>
 
+#include "exact_fp.cuh"
 #include "qg_device.cuh"
 #include "qg_kernels.h"
 
@@ -109,52 +110,6 @@ namespace {
 //   |t2 - X| <= 2^-53 (n + 2) (A + ||c||^2 + 2 sum|q_i c_i|),  X = A + ||c||^2 - 2B.
 // If every value within that bound of X rounds to the same float, that float is the
 // reference's qn2; otherwise (about once in 10^5 queries) the caller runs the double chains.
-
-struct FloatParts {
-    long long m;  // signed integer significand, |m| < 2^24
-    int e;        // value = m * 2^e
-    bool finite;
-};
-
-__device__ __forceinline__ FloatParts split_float(float f) {
-    const uint32_t b = __float_as_uint(f);
-    const int ex = static_cast<int>((b >> 23) & 0xFFu);
-    long long m = static_cast<long long>(b & 0x7FFFFFu);
-    int e = -149;
-    if (ex != 0) {
-        m |= 0x800000;
-        e = ex - 150;
-    }
-    if (b >> 31) m = -m;
-    return {m, e, ex != 0xFF};
-}
-
-// |v| (< 2^49) * 2^sh as a 128-bit fixed-point value; shifts below the grid truncate.
-__device__ __forceinline__ unsigned __int128 to_grid(unsigned long long v, int sh) {
-    if (sh >= 0) return static_cast<unsigned __int128>(v) << sh;
-    if (sh <= -64) return 0;
-    return static_cast<unsigned __int128>(v >> (-sh));
-}
-
-__device__ __forceinline__ __int128 shfl_xor_i128(__int128 v, int o) {
-    const unsigned __int128 u = static_cast<unsigned __int128>(v);
-    uint32_t w[4] = {static_cast<uint32_t>(u), static_cast<uint32_t>(u >> 32), static_cast<uint32_t>(u >> 64),
-                     static_cast<uint32_t>(u >> 96)};
-#pragma unroll
-    for (int i = 0; i < 4; ++i) w[i] = __shfl_xor_sync(0xffffffffu, w[i], o);
-    const unsigned __int128 r = static_cast<unsigned __int128>(w[0]) |
-                                (static_cast<unsigned __int128>(w[1]) << 32) |
-                                (static_cast<unsigned __int128>(w[2]) << 64) |
-                                (static_cast<unsigned __int128>(w[3]) << 96);
-    return static_cast<__int128>(r);
-}
-
-__device__ __forceinline__ int msb_u128(unsigned __int128 v) {
-    const unsigned long long hi = static_cast<unsigned long long>(v >> 64);
-    if (hi != 0) return 127 - __clzll(static_cast<long long>(hi));
-    const unsigned long long lo = static_cast<unsigned long long>(v);
-    return lo ? 63 - __clzll(static_cast<long long>(lo)) : -1;
-}
 
 // One warp. Returns true and the reference's qn2 in *out when the bound decides it.
 __device__ bool exact_qn2_warp(const float *q, const float *c, int dim, float cn, int lane, float *out) {
@@ -419,6 +374,25 @@ __global__ void dither_pairs_kernel(const float *x, const float *scale, const un
     if (und) v = static_cast<int>(floor(static_cast<double>(x[i]) / static_cast<double>(s) + canonical_u01(draws[i])));
     out[i] = v;
     if (undecided) undecided[i] = und ? 1 : 0;
+}
+
+// Kernel-level check of the residual-code rounding of the encoder: out[i] =
+// clamp(round(double(x) / double(s)), -7, 7), undecided[i] = 1 where the FP32 decision fell back.
+__global__ void round_quotient_kernel(const float *x, const float *s, size_t n, int *out, uint8_t *undecided) {
+    const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    bool und = !(s[i] >= 0x1p-100f) || !isfinite(x[i]);
+    int q = und ? 0 : round_away_quotient(x[i], s[i], und);
+    if (und) q = max(-7, min(7, static_cast<int>(round(static_cast<double>(x[i]) / static_cast<double>(s[i])))));
+    out[i] = q;
+    if (undecided) undecided[i] = und ? 1 : 0;
+}
+
+cudaError_t launch_round_quotient_pairs(const float *x, const float *s, size_t n, int *out, uint8_t *undecided,
+                                        cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    round_quotient_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, stream>>>(x, s, n, out, undecided);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_dither_pairs(const float *x, const float *scale, const unsigned long long *draws, size_t n,

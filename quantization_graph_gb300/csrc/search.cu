@@ -246,7 +246,7 @@ __device__ __forceinline__ void load_query(QueryRegs<D> &r, const int8_t *codes,
 
 template <int D>
 __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int lane,
-                           uint16_t *tags, uint32_t tag) {
+                           uint16_t *tags, uint32_t tag, const uint32_t *stop_smem) {
     using L = Lay<D>;
     const DevIndex &ix = a.ix;
     const int sub = lane % L::LPN;
@@ -696,7 +696,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                     float f[kMlpIn];
 #pragma unroll
                     for (int i = 0; i < kMlpIn; ++i) f[i] = (feat[i] - a.stop_norm[i]) * a.stop_norm[kMlpIn + i];
-                    const float z = mlp_forward_warp(f, a.stop_w, lane);
+                    const float z = mlp_forward_warp_smem(f, stop_smem, lane);
                     if (z > a.stop_logit) break;
                 }
             }
@@ -795,7 +795,14 @@ __global__ void __launch_bounds__(QG_SEARCH_THREADS, QG_SEARCH_MINBLOCKS) search
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
-    const WarpSmem s = carve(smem + warp * warp_smem_bytes(a.l_cap), a.l_cap);
+    // the stop network's weights (when a model is given) precede the per-warp regions
+    const size_t wsm = a.stop_w != nullptr ? kMlpSmemBytes : 0;
+    const uint32_t *stop_smem = reinterpret_cast<const uint32_t *>(smem);
+    if (a.stop_w != nullptr) {
+        mlp_stage_smem(a.stop_w, reinterpret_cast<uint32_t *>(smem), threadIdx.x, blockDim.x);
+        __syncthreads();
+    }
+    const WarpSmem s = carve(smem + wsm + warp * warp_smem_bytes(a.l_cap), a.l_cap);
     const int slot = blockIdx.x * wpb + warp;
     uint16_t *tags = a.tags + static_cast<size_t>(slot) * a.ix.n_total;
     const int nq = a.nq_dev != nullptr ? min(a.nq, *a.nq_dev) : a.nq;
@@ -812,7 +819,7 @@ __global__ void __launch_bounds__(QG_SEARCH_THREADS, QG_SEARCH_MINBLOCKS) search
             e += 1;
         }
         if (lane == 0) a.epochs[slot] = e;
-        search_one<D>(a, s, q, lane, tags, e & 0xFFFFu);
+        search_one<D>(a, s, q, lane, tags, e & 0xFFFFu, stop_smem);
         __syncwarp();
     }
 }
@@ -831,7 +838,7 @@ int search_supported_dim(int code_dim) {
 
 template <int D>
 static cudaError_t launch_d(const SearchArgs &a, int grid, int wpb, cudaStream_t stream) {
-    const size_t smem = warp_smem_bytes(a.l_cap) * static_cast<size_t>(wpb);
+    const size_t smem = search_block_smem(a.l_cap, wpb, a.stop_w != nullptr);
     cudaError_t e = cudaFuncSetAttribute(search_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
@@ -839,9 +846,13 @@ static cudaError_t launch_d(const SearchArgs &a, int grid, int wpb, cudaStream_t
     return cudaGetLastError();
 }
 
+size_t search_block_smem(int l_cap, int wpb, bool stop_model) {
+    return warp_smem_bytes(l_cap) * static_cast<size_t>(wpb) + (stop_model ? kMlpSmemBytes : 0);
+}
+
 template <int D>
-static int blocks_per_sm_d(int l_cap, int wpb) {
-    const size_t smem = warp_smem_bytes(l_cap) * static_cast<size_t>(wpb);
+static int blocks_per_sm_d(int l_cap, int wpb, bool stop_model) {
+    const size_t smem = search_block_smem(l_cap, wpb, stop_model);
     if (cudaFuncSetAttribute(search_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(smem)) != cudaSuccess)
         return 0;
@@ -851,14 +862,14 @@ static int blocks_per_sm_d(int l_cap, int wpb) {
     return blocks;
 }
 
-int search_blocks_per_sm(int code_dim, int l_cap, int wpb) {
+int search_blocks_per_sm(int code_dim, int l_cap, int wpb, bool stop_model) {
     switch (code_dim) {
-        case 64: return blocks_per_sm_d<64>(l_cap, wpb);
-        case 128: return blocks_per_sm_d<128>(l_cap, wpb);
-        case 256: return blocks_per_sm_d<256>(l_cap, wpb);
-        case 512: return blocks_per_sm_d<512>(l_cap, wpb);
-        case 1024: return blocks_per_sm_d<1024>(l_cap, wpb);
-        case 2048: return blocks_per_sm_d<2048>(l_cap, wpb);
+        case 64: return blocks_per_sm_d<64>(l_cap, wpb, stop_model);
+        case 128: return blocks_per_sm_d<128>(l_cap, wpb, stop_model);
+        case 256: return blocks_per_sm_d<256>(l_cap, wpb, stop_model);
+        case 512: return blocks_per_sm_d<512>(l_cap, wpb, stop_model);
+        case 1024: return blocks_per_sm_d<1024>(l_cap, wpb, stop_model);
+        case 2048: return blocks_per_sm_d<2048>(l_cap, wpb, stop_model);
         default: return 0;
     }
 }

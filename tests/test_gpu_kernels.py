@@ -188,3 +188,45 @@ def test_prepare_query_norm_fallbacks(cuda, oracle):
                                                                    po["half_sum"], po["scale"]], np.float32)))
             np.testing.assert_array_equal(pp["codes"][i].cpu().numpy(), po["codes"])
 
+
+
+def test_round_quotient_decision_near_half_integers(cuda):
+    """The encoder's FP32 rounding of x / s equals clamp(round(double(x)/double(s)), -7, 7),
+    including quotients on and a few ulps around half-integers (where it must fall back)."""
+    torch = cuda
+    import ctypes as C
+
+    from quantization_graph_gb300 import _native as N
+
+    rng = np.random.default_rng(12)
+    m = 20000
+    s = rng.uniform(1e-4, 2.0, m).astype(np.float32)
+    half = rng.integers(-8, 8, m) + 0.5
+    x0 = (half * s.astype(np.float64)).astype(np.float32)
+    x = x0.copy()
+    step = rng.integers(-3, 4, m)
+    for k in (-3, -2, -1, 1, 2, 3):
+        sel = step == k
+        for _ in range(abs(k)):
+            x[sel] = np.nextafter(x[sel], np.float32(np.sign(k) * np.inf), dtype=np.float32)
+    s[:200] = np.float32(0.25)                      # exact half-integers: ties away from zero
+    x[:200] = (half[:200] * 0.25).astype(np.float32)
+    xr = (rng.standard_normal(m) * 4).astype(np.float32) * s
+    X = np.concatenate([x, xr]).astype(np.float32)
+    S = np.concatenate([s, s])
+    q = X.astype(np.float64) / S.astype(np.float64)
+    aq = np.abs(q)
+    fl = np.floor(aq)
+    want = np.clip(np.sign(q) * (fl + (aq - fl >= 0.5)), -7, 7).astype(np.int64)  # C round(), exactly
+    dx, ds = torch.from_numpy(X).cuda(), torch.from_numpy(S).cuda()
+    out = torch.empty(len(X), dtype=torch.int32, device="cuda")
+    und = torch.empty(len(X), dtype=torch.uint8, device="cuda")
+    lib = N.load()
+    N.check(lib.qg_round_quotient_pairs(C.c_void_p(dx.data_ptr()), C.c_void_p(ds.data_ptr()), len(X),
+                                        C.c_void_p(out.data_ptr()), C.c_void_p(und.data_ptr()), None),
+            "qg_round_quotient_pairs")
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out.cpu().numpy().astype(np.int64), want)
+    u8 = und.cpu().numpy()
+    assert u8[:200].sum() > 0
+    assert u8[m:].sum() <= 2

@@ -92,3 +92,58 @@ def test_learned_stop_saves_hops_at_equal_recall(cuda, oracle):
             best = (thr, hops, rec)
     assert best is not None, "no threshold kept recall within 0.002 of fixed-L"
     assert best[1] <= 0.9 * hops_plain, (best, hops_plain, rec_plain)
+
+
+def test_in_kernel_stop_matches_standalone_forward(cuda):
+    """The search kernel's stop decision (network staged in shared memory) equals the standalone
+    forward kernel applied to the trace of the same search: each query stops at the first
+    checkpoint whose logit exceeds the threshold, else runs to the end."""
+    torch = cuda
+    from quantization_graph_gb300 import learned_stop as ls
+    from quantization_graph_gb300 import synthetic
+
+    g, ix = _index(torch)
+    _, cent = synthetic.gmm(1, 128, components=64, sigma=0.3, seed=11)
+    train_q, _ = synthetic.gmm(1500, 128, sigma=0.3, seed=201, centres=cent)
+    test_q, _ = synthetic.gmm(400, 128, sigma=0.3, seed=202, centres=cent)
+    L, every, min_hops, thr = 80, 2, 4, 0.8
+    tq = torch.from_numpy(train_q).cuda()
+    truth = ix.search(tq, k=10, l_value=L, with_stats=False).ids.to(torch.int32)
+    feats, labels = ls.collect_traces(ix, tq, truth, k=10, l_value=L, every=every)
+    model = ls.train(feats, labels, epochs=2, batch=4096, every=every, min_hops=min_hops)
+    qq = torch.from_numpy(test_q).cuda()
+    truth_te = ix.search(qq, k=10, l_value=L, with_stats=False).ids.to(torch.int32)
+    # per-checkpoint rows of the plain search, query by query
+    import ctypes as C
+
+    from quantization_graph_gb300 import _native as N
+    from quantization_graph_gb300.space import _ptr, _stream
+
+    nq, cap = len(test_q), (4 * L) // every + 8
+    feat = torch.empty((nq, cap, 8), dtype=torch.float32, device="cuda")
+    lab = torch.empty((nq, cap), dtype=torch.float32, device="cuda")
+    cnt = torch.empty(nq, dtype=torch.int32, device="cuda")
+    ids = torch.empty((nq, 10), dtype=torch.int32, device="cuda")
+    dists = torch.empty((nq, 10), dtype=torch.float32, device="cuda")
+    stats = torch.empty((nq, 9), dtype=torch.int64, device="cuda")
+    params = N.SearchParams(10, L, 1, 1.9, 100, 0, 0)
+    treq = N.TraceRequest(truth_te.data_ptr(), 10, every, cap, feat.data_ptr(), lab.data_ptr(), cnt.data_ptr())
+    lib = N.load()
+    N.check(lib.qg_search_batch_learned(ix.handle, _ptr(qq), nq, C.byref(params), None, None, 10, _ptr(ids),
+                                        _ptr(dists), _ptr(stats), None, C.byref(treq), _stream()), "trace")
+    full_hops = stats[:, 2].cpu().numpy()
+    logits = ls.forward(model.weights, model.norm, feat.reshape(-1, 8)).reshape(nq, cap).cpu().numpy()
+    cnt = cnt.cpu().numpy()
+    z_thr = np.log(np.float32(thr) / (np.float32(1.0) - np.float32(thr)))
+    want = full_hops.copy()
+    for q in range(nq):
+        for r in range(cnt[q]):
+            h = (r + 1) * every
+            if h >= min_hops and logits[q, r] > z_thr:
+                want[q] = h
+                break
+    stats2 = torch.empty((nq, 9), dtype=torch.int64, device="cuda")
+    ls.search(ix, qq, model, thr, k=10, l_value=L, stats_out=stats2)
+    got = stats2[:, 2].cpu().numpy()
+    assert (want < full_hops).sum() > 20, "the threshold should stop some queries early"
+    np.testing.assert_array_equal(got, want)
