@@ -306,13 +306,15 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
     int hops_done = 0;
     int n_expanded = 0;
     int last_topk = 0, last_topr = 0;  // last hop that inserted into the top k / top max(rerank, k)
+    int fu = 0;                        // every pool entry before fu is expanded
     const int want_r_all = a.rerank > k ? a.rerank : k;
     bool failed = false;
     for (;;) {
         const float back_before = pn > 0 ? s.pd[pn - 1] : 0.0f;
-        // frontier: first `beam` unexpanded pool entries, marked expanded
+        // frontier: first `beam` unexpanded pool entries, marked expanded; entries before fu are
+        // all expanded (fu moves past each frontier and back to any insert before it)
         int nf = 0;
-        for (int base = 0; base < pn && nf < beam; base += 32) {
+        for (int base = fu & ~31; base < pn && nf < beam; base += 32) {
             const int i = base + lane;
             const bool un = i < pn && !(s.pid[i] & kExpanded);
             unsigned int m = __ballot_sync(0xffffffffu, un);
@@ -324,6 +326,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                     s.pid[i] |= kExpanded;
                 }
                 ++nf;
+                fu = base + b + 1;
             }
         }
         __syncwarp();
@@ -604,13 +607,36 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                 bump((1u << REMC) | (1u << DC), 1);
                 // insert_candidate_sorted (ours_diskann.rs:1100-1126)
                 if (full && !cand_less(d, id, s.pd[lval - 1], s.pid[lval - 1] & kIdMask)) continue;
+                // rank in the sorted pool: small pools by a scan that stops at the first
+                // 32-entry chunk not entirely below the candidate; large pools by two ballots per
+                // 1024 entries (the chunk, from the chunks' last entries; then the entry)
                 int pos = 0;
-                for (int base = 0; base < pn; base += 32) {
-                    const int e = base + lane;
-                    const bool lt = e < pn && cand_less(s.pd[e], s.pid[e] & kIdMask, d, id);
-                    const unsigned int m = __ballot_sync(0xffffffffu, lt);
-                    pos += __popc(m);
-                    if (m != 0xffffffffu) break;
+                if (pn <= 256) {
+                    for (int base = 0; base < pn; base += 32) {
+                        const int e = base + lane;
+                        const bool lt = e < pn && cand_less(s.pd[e], s.pid[e] & kIdMask, d, id);
+                        const unsigned int m = __ballot_sync(0xffffffffu, lt);
+                        pos += __popc(m);
+                        if (m != 0xffffffffu) break;
+                    }
+                } else for (int sb = 0; sb < pn; sb += 1024) {
+                    const int last = sb + 32 * lane + 31;
+                    const int probe = last < pn ? last : pn - 1;
+                    const bool clt = sb + 32 * lane < pn && cand_less(s.pd[probe], s.pid[probe] & kIdMask, d, id);
+                    const unsigned int cm = __ballot_sync(0xffffffffu, clt);
+                    const int chunk = __popc(cm);  // chunks entirely before the candidate
+                    const int base = sb + 32 * chunk;
+                    if (base >= pn) {  // after every entry of the pool
+                        pos = pn;
+                        break;
+                    }
+                    if (chunk < 32) {
+                        const int e = base + lane;
+                        const bool lt = e < pn && cand_less(s.pd[e], s.pid[e] & kIdMask, d, id);
+                        pos = base + __popc(__ballot_sync(0xffffffffu, lt));
+                        break;
+                    }
+                    pos = sb + 1024;
                 }
                 const int newn = pn + 1 < lval ? pn + 1 : lval;
                 for (int top = newn - 1; top > pos; top -= 32) {
@@ -638,6 +664,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                 }
                 if (pos < k) last_topk = hops_done;
                 if (pos < want_r_all) last_topr = hops_done;
+                if (pos < fu) fu = pos;
                 pn = newn;
                 __syncwarp();
             }
