@@ -502,10 +502,19 @@ def run_stream(args, log):
     best, tune = autotune(index, queries[:4096], k=10, l_value=200, log=log)
     model, thr = None, None
     if args.stream_threshold > 0:
-        tq = synthetic.clustered_torch(20000, dim, 16, 1.0, seed=3)
-        truth = index.search(tq, k=10, l_value=400, with_stats=False).ids.to(torch.int32)
-        feats, labels = ls.collect_traces(index, tq, truth, k=10, l_value=400, every=args.stop_every)
-        model = ls.train(feats, labels, epochs=args.stop_epochs, every=args.stop_every,
+        # traces of the plain search over the stream's own mix of k and L (held-out queries)
+        tq = synthetic.clustered_torch(24000, dim, 16, 1.0, seed=3)
+        feats, labels, j = [], [], 0
+        for kk in (1, 10, 100):
+            for ll in (50, 100, 200, 400):
+                sub = tq[j:j + 2000]
+                j += 2000
+                lv = max(ll, kk)
+                truth = index.search(sub, k=kk, l_value=lv, with_stats=False).ids.to(torch.int32)
+                f, lab = ls.collect_traces(index, sub, truth, k=kk, l_value=lv, every=args.stop_every)
+                feats.append(f)
+                labels.append(lab)
+        model = ls.train(torch.cat(feats), torch.cat(labels), epochs=args.stop_epochs, every=args.stop_every,
                          min_hops=2 * args.stop_every, log=log)
         thr = args.stream_threshold
     gs = GraphSearcher(index, dim, max_batch=4096, max_k=100, max_l=400, model=model, threshold=thr)
