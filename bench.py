@@ -49,8 +49,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--refine", type=int, default=1, help="graph refinement rounds")
-    ap.add_argument("--knn", type=int, default=0, help="kNN candidates per node for the graph (0 = 2M)")
-    ap.add_argument("--refine-l", type=int, default=128, help="search list size of the refinement rounds")
+    ap.add_argument("--knn", type=int, default=240, help="kNN candidates per node for the graph")
+    ap.add_argument("--refine-l", type=int, default=256, help="search list size of the refinement rounds")
     ap.add_argument("--no-learned", action="store_true", help="fixed-L only")
     ap.add_argument("--train-queries", type=int, default=20_000)
     ap.add_argument("--stop-every", type=int, default=4)
@@ -194,6 +194,17 @@ def pick_l(torch, w, args, log):
             break
     if chosen is None:
         chosen = max(sweep)
+    else:
+        # refine between the last L below the target and the first above it, in steps of 16
+        below = max([l_ for l_ in sweep if l_ < chosen] or [chosen])
+        for L in range(below + 16, chosen, 16):
+            r = w["index"].search(w["queries"], k=args.k, l_value=L, with_stats=False)
+            rec = recall_at(r.ids, w["gt"], args.k)
+            sweep[L] = rec
+            log(f"  L={L} recall@{args.k}={rec:.4f}")
+            if rec >= args.target_recall:
+                chosen = L
+                break
     return chosen, sweep[chosen], sweep
 
 
