@@ -221,8 +221,10 @@ def algorithmic_bytes(stats, D, M, rerank, k):
     return float(per_q.sum())
 
 
-def cpu_baseline(w, args, L, log):
-    """Reference search restated on the CPU (oracle/), all host threads, bounded sample."""
+def cpu_baseline(w, args, L, log, steps=1, warmup=0):
+    """Reference search restated on the CPU (oracle/), all host threads, bounded sample: `warmup`
+    untimed rounds of one query per thread, then `steps` timed slices of a sample of about
+    --cpu-seconds of work."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py
 
@@ -237,14 +239,23 @@ def cpu_baseline(w, args, L, log):
     t = time.time()
     o.search(q[:threads * 4], index, k=args.k, L=L, threads=threads)
     per = (time.time() - t) / (threads * 4)
+    for i in range(warmup):
+        o.search(q[i * threads:(i + 1) * threads], index, k=args.k, L=L, threads=threads)
     count = int(min(len(q), max(threads * 8, args.cpu_seconds / max(per, 1e-6))))
-    t = time.time()
-    ids, _, _ = o.search(q[:count], index, k=args.k, L=L, threads=threads)
-    el = time.time() - t
+    steps = max(1, min(steps, count // threads))
+    bounds = np.linspace(0, count, steps + 1).astype(int)
+    el = 0.0
+    parts = []
+    for a_, b_ in zip(bounds[:-1], bounds[1:]):
+        t = time.time()
+        part, _, _ = o.search(q[a_:b_], index, k=args.k, L=L, threads=threads)
+        el += time.time() - t
+        parts.append(part)
+    ids = np.concatenate(parts)
     gt = w["gt"][:count].cpu().numpy()
     rec = float(np.mean([len(set(a) & set(b)) / args.k for a, b in zip(ids, gt)]))
     log(f"cpu oracle: {count} queries in {el:.2f}s on {threads} threads, recall {rec:.4f}")
-    return {"value": count / el, "unit": "queries/s", "cores": threads, "kind": "port",
+    return {"value": count / el, "unit": "queries/s", "cores": threads, "kind": "port", "steps": steps,
             "sample": f"{count} of {len(q)} queries at L={L}, k={args.k}, one query per thread"}, rec
 
 
@@ -346,10 +357,11 @@ def main():
     D = w["space"].code_dim
 
     if args.impl == "reference":
-        cpu, cpu_rec = cpu_baseline(w, args, L, log)
+        cpu, cpu_rec = cpu_baseline(w, args, L, log, steps=args.steps, warmup=args.warmup)
         config["fixed_l"]["recall_cpu"] = round(cpu_rec, 4)
         line = {"impl": "reference", "metric": metric, "value": cpu["value"], "unit": "queries/s", "n_gpus": 1,
-                "steps": 1, "warmup": 0, "ms_per_step": 1000.0 * args.nq / cpu["value"], "higher_is_better": True,
+                "steps": cpu["steps"], "warmup": args.warmup, "ms_per_step": 1000.0 * args.nq / cpu["value"],
+                "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "int8/f32", "data": "synthetic",
                 "config": dict(config, mode="fixed-L on the host cores (the reference search has no learned stop)"),
                 "cpu_baseline": cpu,
