@@ -55,8 +55,9 @@ def parse():
     ap.add_argument("--train-queries", type=int, default=20_000)
     ap.add_argument("--stop-every", type=int, default=4)
     ap.add_argument("--stop-epochs", type=int, default=4)
-    ap.add_argument("--workload", default="dbpedia1536", choices=["dbpedia1536", "stream"],
-                    help="stream: uneven batched stream over a 120k x 1024 clustered index")
+    ap.add_argument("--workload", default="dbpedia1536", choices=["dbpedia1536", "gist960", "stream"],
+                    help="gist960: 1M x 960 |x| with lambda_i ~ i^-1.2; stream: uneven batched stream over "
+                         "a 120k x 1024 clustered index")
     ap.add_argument("--stream-n", type=int, default=120_000)
     ap.add_argument("--stream-queries", type=int, default=200_000)
     ap.add_argument("--stream-thresholds", default="0.9,0.95,0.98",
@@ -149,8 +150,12 @@ def build_workload(torch, args, log):
     from quantization_graph_gb300.space import RabitqSpace, train_global_center
 
     t0 = time.time()
-    base = synthetic.anisotropic_torch(args.n, args.dim, 0.8, seed=1, normalize=True)
-    queries = synthetic.anisotropic_torch(args.nq, args.dim, 0.8, seed=2, normalize=True)
+    if args.workload == "gist960":  # |x|, x ~ N(0, Q diag(i^-1.2) Q^T)
+        base = synthetic.anisotropic_torch(args.n, args.dim, 1.2, seed=1, absolute=True)
+        queries = synthetic.anisotropic_torch(args.nq, args.dim, 1.2, seed=2, absolute=True)
+    else:
+        base = synthetic.anisotropic_torch(args.n, args.dim, 0.8, seed=1, normalize=True)
+        queries = synthetic.anisotropic_torch(args.nq, args.dim, 0.8, seed=2, normalize=True)
     center = train_global_center(base)
     space = RabitqSpace(args.dim, center)
     torch.cuda.synchronize()
@@ -323,6 +328,8 @@ def learned_stop_select(torch, w, args, L_fixed, rec_fixed, log):
 
 def main():
     args = parse()
+    if args.workload == "gist960" and args.dim == 1536:
+        args.dim = 960
     import torch
     import torch.distributed as dist
 
@@ -347,7 +354,11 @@ def main():
     L, rec, sweep = pick_l(torch, w, args, log)
     log(f"fixed-L: L={L} recall={rec:.4f}")
     metric = "QPS@recall10=0.95, 1M\u00d71536 4-bit, learned-stop vs fixed-L beam, 1 GB300"
-    config = {"workload": (f"{args.n} x {args.dim} unit-norm anisotropic (lambda_i ~ i^-0.8), M={args.M}, "
+    data_desc = f"{args.n} x {args.dim} unit-norm anisotropic (lambda_i ~ i^-0.8)"
+    if args.workload == "gist960":
+        metric = "QPS@recall10=0.95, 1M\u00d7960 4-bit, fixed-L beam, 1 GB300"
+        data_desc = f"{args.n} x {args.dim} |x|, x ~ N(0, Q diag(i^-1.2) Q^T)"
+    config = {"workload": (f"{data_desc}, M={args.M}, "
                            f"{args.nq} queries, k={args.k}, INT8 paper-prune gate, residual4 rerank 100"),
               "n": args.n, "dim": args.dim, "queries": args.nq, "M": args.M, "k": args.k,
               "graph": (f"GPU kNN-{args.knn or 2 * args.M} + 16 random + alpha-1.2 prune + reverse edges + "
