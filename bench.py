@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--refine-l", type=int, default=256, help="search list size of the refinement rounds")
     ap.add_argument("--no-learned", action="store_true", help="fixed-L only")
     ap.add_argument("--train-queries", type=int, default=20_000)
-    ap.add_argument("--stop-every", type=int, default=4)
+    ap.add_argument("--stop-every", type=int, default=8)
     ap.add_argument("--stop-epochs", type=int, default=4)
     ap.add_argument("--workload", default="dbpedia1536", choices=["dbpedia1536", "gist960", "stream"],
                     help="gist960: 1M x 960 |x| with lambda_i ~ i^-1.2; stream: uneven batched stream over "
