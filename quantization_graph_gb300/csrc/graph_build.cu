@@ -3,8 +3,8 @@
 // the reference graph bit for bit).
 //
 // prune_kernel: one warp per node. Candidate ids (any order, duplicates and padding allowed)
-// are scored with the reference's symmetric 4-bit estimator (distanceBetweenEncoded,
-// space_rabitq.h:2634-2683, the distance the reference builder uses), sorted by
+// are scored with the symmetric 4-bit estimator (distanceBetweenEncoded,
+// space_rabitq.h:2634-2683, the distance the reference builder uses; here in FP32), sorted by
 // (distance, id), de-duplicated, and reduced to at most R out-edges by alpha robust pruning
 // with the occlusion-factor schedule alpha = 1.0 then alpha (the "alpha ramp" of
 // robust_prune_4bit, vamana_prune.h:42-156): candidate j is occluded once a kept neighbour i
@@ -28,28 +28,32 @@ __device__ __forceinline__ float ld_f32u(const uint8_t *p) {
     return __uint_as_float(v);
 }
 
+// Per-record factors of the symmetric estimator: norm_sqr, ||r|| = sqrt(norm_sqr) and
+// ip_norm = long_scale / (2 ||r||), computed once per record (FP32: this builder's graph is its
+// own, and the FP64 pipe is narrow on this part).
 struct CodeRef {
     float norm_sqr;
-    float long_scale;
-    int nibble_sum;
+    float rn;
+    float ipn;  // NaN when the record is degenerate (zero norm or bad long_scale)
 };
 
-// symmetric estimator from the unsigned nibble dot (space_rabitq.h:2634-2683)
-__device__ float symmetric_from_dot(const CodeRef &a, const CodeRef &b, int dot_ab, int D) {
-    const double ln = sqrt(fmax(0.0, static_cast<double>(a.norm_sqr)));
-    const double rn = sqrt(fmax(0.0, static_cast<double>(b.norm_sqr)));
-    if (!(ln > 0.0) || !(rn > 0.0) || !(a.long_scale > 0.0f) || !(b.long_scale > 0.0f) ||
-        !isfinite(a.long_scale) || !isfinite(b.long_scale))
-        return static_cast<float>(static_cast<double>(a.norm_sqr) + static_cast<double>(b.norm_sqr));
-    const long long centred = 4LL * dot_ab - 30LL * (a.nibble_sum + b.nibble_sum) + 225LL * D;
-    const double code_ip = 0.25 * static_cast<double>(centred);
-    const double lip = static_cast<double>(a.long_scale) / (2.0 * ln);
-    const double rip = static_cast<double>(b.long_scale) / (2.0 * rn);
-    double u = code_ip * lip * rip;
-    if (!isfinite(u)) u = 0.0;
-    u = fmax(-1.0, fmin(1.0, u));
-    return static_cast<float>(static_cast<double>(a.norm_sqr) + static_cast<double>(b.norm_sqr) -
-                              2.0 * (ln * rn * u));
+__device__ __forceinline__ CodeRef code_ref(const uint8_t *rec) {
+    const float ns = ld_f32u(rec), ls = ld_f32u(rec + 4);
+    const float rn = sqrtf(fmaxf(0.0f, ns));
+    const bool ok = rn > 0.0f && ls > 0.0f && isfinite(ls);
+    return CodeRef{ns, rn, ok ? ls / (2.0f * rn) : __int_as_float(0x7fc00000)};
+}
+
+// symmetric estimator (distanceBetweenEncoded, space_rabitq.h:2634-2683) from the unsigned
+// nibble dot: u = clamp(code_ip * ipn_a * ipn_b, +-1), d = n_a + n_b - 2 ||r_a|| ||r_b|| u
+__device__ __forceinline__ float symmetric_from_dot(const CodeRef &a, const CodeRef &b, int dot_ab, int sum_a,
+                                                    int sum_b, int D) {
+    if (!(a.ipn == a.ipn) || !(b.ipn == b.ipn)) return a.norm_sqr + b.norm_sqr;
+    const int centred = 4 * dot_ab - 30 * (sum_a + sum_b) + 225 * D;  // |centred| <= 225 D
+    float u = (0.25f * static_cast<float>(centred)) * a.ipn * b.ipn;
+    if (!isfinite(u)) u = 0.0f;
+    u = fmaxf(-1.0f, fminf(1.0f, u));
+    return a.norm_sqr + b.norm_sqr - 2.0f * (a.rn * b.rn * u);
 }
 
 template <int D>
@@ -126,7 +130,8 @@ __global__ void __launch_bounds__(128) prune_kernel(const uint8_t *compact, size
     const uint8_t *prec = compact + static_cast<size_t>(p) * stride;
     uint32_t pw[PER];
     load_code_words<D>(prec, pw, lane);
-    CodeRef pref{ld_f32u(prec), ld_f32u(prec + 4), warp_sum(nibble_sum_words<D>(pw))};
+    const CodeRef pref = code_ref(prec);
+    const int psum = warp_sum(nibble_sum_words<D>(pw));
 
     int KP = 1;
     while (KP < K) KP <<= 1;
@@ -145,8 +150,7 @@ __global__ void __launch_bounds__(128) prune_kernel(const uint8_t *compact, size
         const int dot = warp_sum(nibble_dot_words<D>(pw, cw));
         const int s = warp_sum(nibble_sum_words<D>(cw));
         if (lane == 0) {
-            CodeRef cref{ld_f32u(crec), ld_f32u(crec + 4), s};
-            dd[i] = symmetric_from_dot(pref, cref, dot, D);
+            dd[i] = symmetric_from_dot(pref, code_ref(crec), dot, psum, s, D);
             nsum[i] = s;
         }
     }
@@ -196,7 +200,7 @@ __global__ void __launch_bounds__(128) prune_kernel(const uint8_t *compact, size
             const uint8_t *irec = compact + static_cast<size_t>(ids[i]) * stride;
             uint32_t iw[PER];
             load_code_words<D>(irec, iw, lane);
-            CodeRef iref{ld_f32u(irec), ld_f32u(irec + 4), nsum[i]};
+            const CodeRef iref = code_ref(irec);
             for (int j = i + 1; j < KP; ++j) {
                 if (state[j] != 0 || occ[j] > alpha) continue;
                 const uint8_t *jrec = compact + static_cast<size_t>(ids[j]) * stride;
@@ -204,8 +208,7 @@ __global__ void __launch_bounds__(128) prune_kernel(const uint8_t *compact, size
                 load_code_words<D>(jrec, jw, lane);
                 const int dot = warp_sum(nibble_dot_words<D>(iw, jw));
                 if (lane == 0) {
-                    CodeRef jref{ld_f32u(jrec), ld_f32u(jrec + 4), nsum[j]};
-                    const float dij = symmetric_from_dot(iref, jref, dot, D);
+                    const float dij = symmetric_from_dot(iref, code_ref(jrec), dot, nsum[i], nsum[j], D);
                     const float ratio = dij > 0.0f ? dd[j] / dij : kFltMax;
                     occ[j] = fmaxf(occ[j], ratio);
                 }
