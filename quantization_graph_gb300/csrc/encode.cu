@@ -234,14 +234,50 @@ __device__ __forceinline__ float approx_float(double x) {
     return __uint_as_float((static_cast<uint32_t>(ex) << 23) | static_cast<uint32_t>((b >> 29) & 0x7FFFFFu));
 }
 
+// Heads of the seven level lists of fastQuantizeAbs's events: the next admissible dim of each
+// level in |v| order. Dim i is an event of level c when |v_i| > 1e-5, c > c0_i and
+// (c = c0_i + 1 or c / |v_i| < 17 / max|v|).
+struct LevelHead {
+    int ptr;
+    int id;   // -1 when the level is exhausted
+    float a;  // |v_id|
+    float t;  // RN24(c / a): orders heads unless two are equal
+};
+
+__device__ __forceinline__ void advance_level(LevelHead &h, int c, const unsigned long long *keys, const float *ru,
+                                              const unsigned char *c0, int D, float mx) {
+    while (h.ptr < D) {
+        const int i = static_cast<int>(keys[h.ptr] & 0xFFFFFFFFu);
+        const float ai = fabsf(ru[i]);
+        const int ci = c0[i];
+        if (ai > kEpsBelowF && c > ci && (c == ci + 1 || ratio_cmp(c, ai, 17, mx) < 0)) {
+            h.id = i;
+            h.a = ai;
+            h.t = __fdiv_rn(static_cast<float>(c), ai);
+            return;
+        }
+        ++h.ptr;
+    }
+    h.id = -1;
+}
+
+// event (c, h) before event (b, g): t ascending, ties by dim index; the float ratios decide
+// unless equal (rounding is monotone), then the exact comparison
+__device__ __forceinline__ bool event_before(int c, const LevelHead &h, int b, const LevelHead &g) {
+    if (h.t != g.t) return h.t < g.t;
+    const int r = ratio_cmp(c, h.a, b, g.a);
+    return r < 0 || (r == 0 && h.id < g.id);
+}
+
 // fastQuantizeAbs's search over the rescale factor t (space_rabitq.h:867-942), lane 0: the
 // (t, i) events of the seven levels in heap order (t = level / |v_i|, ties by i), running
-// num and sqr_den, t at the first maximum of num / sqrt(sqr_den). Event order and the t_end
-// cut are decided by exact ratio comparisons (distinct level / |v| ratios differ by far more
-// than a double's rounding, so they order as their doubles do); num stays a double sum; the
-// maximum is screened in FP32 (error below 2^-21 relative) and only the events within 2^-19 of
-// the running FP32 maximum are evaluated in double at the end. If more than kCand events are
-// in that band at once, the whole search runs again in double as the reference does.
+// num and sqr_den, t at the first maximum of ip = num / sqrt(sqr_den). Event order and the t_end
+// cut are decided by ratio comparisons (distinct level / |v| ratios differ by far more than a
+// double's rounding, so they order as their doubles do); num stays a double sum. The maximum is
+// screened in FP32 on squares, (ip_k / ip_best)^2 = num_k^2 sqr_den_best / (num_best^2 sqr_den_k)
+// (within 2^-20 of the float products): an event clearly above the running best (by more than
+// 2^-17) becomes the best, one clearly below is skipped, and only events inside that band are
+// compared exactly, in double, with the best (whose exact ip is computed once).
 __device__ double code_search_lane0(const unsigned long long *keys, const float *ru, const unsigned char *c0,
                                     int D, float mx) {
     long long sd4 = D;  // 4 * sqr_den
@@ -251,103 +287,70 @@ __device__ double code_search_lane0(const unsigned long long *keys, const float 
         sd4 += 4LL * (c * c + c);
         num += (c + 0.5) * static_cast<double>(fabsf(ru[i]));
     }
-    const long long sd4_0 = sd4;
-    const double num_0 = num;
-    int ptr[8], head[8];
-    auto advance = [&](int c) {
-        while (ptr[c] < D) {
-            const int i = static_cast<int>(keys[ptr[c]] & 0xFFFFFFFFu);
-            const float ai = fabsf(ru[i]);
-            const int ci = c0[i];
-            if (ai > kEpsBelowF && c > ci && (c == ci + 1 || ratio_cmp(c, ai, 17, mx) < 0)) {
-                head[c] = i;
-                return;
-            }
-            ++ptr[c];
-        }
-        head[c] = -1;
-    };
-    auto earlier = [&](int c, int b) {  // event of level c before that of level b
-        const int r = ratio_cmp(c, fabsf(ru[head[c]]), b, fabsf(ru[head[b]]));
-        return r < 0 || (r == 0 && head[c] < head[b]);
-    };
-    constexpr int kCand = 24;
-    double cn[kCand];
-    int cs[kCand], clev[kCand], cid[kCand];
-    float cf[kCand];
-    int nc = 0;
-    bool overflow = false;
-    float maxf = 0.0f;
+    LevelHead hd[8];
+#pragma unroll
     for (int c = 1; c <= 7; ++c) {
-        ptr[c] = 0;
-        advance(c);
+        hd[c].ptr = 0;
+        advance_level(hd[c], c, keys, ru, c0, D, mx);
     }
+    // the best so far: its ip is > 0 for every event, the reference starts from max_ip = 0
+    bool have = false, best_exact = false;
+    float best_n2 = 0.0f, best_sdf = 1.0f;  // num^2 and 4 sqr_den of the best, in float
+    double best_num = 0.0, best_ip = 0.0;
+    long long best_sd4 = 0;
+    int best_c = 0;
+    float best_a = 1.0f;
+    constexpr float kHi = 1.0f + 0x1p-17f, kLo = 1.0f - 0x1p-17f;
     for (;;) {
-        int bc = -1;
+        int bc = 0;
+        LevelHead cur{0, -1, 0.0f, 0.0f};
+#pragma unroll
         for (int c = 1; c <= 7; ++c)
-            if (head[c] >= 0 && (bc < 0 || earlier(c, bc))) bc = c;
-        if (bc < 0) break;
-        const int id = head[bc];
-        sd4 += 8LL * bc;
-        num += static_cast<double>(fabsf(ru[id]));
-        const float ipf = __fdiv_rn(approx_float(num), sqrtf(__ll2float_rn(sd4) * 0.25f));
-        if (ipf > maxf) {
-            maxf = ipf;
-            int w = 0;  // drop candidates that fell out of the band
-            for (int k = 0; k < nc; ++k)
-                if (cf[k] >= maxf * (1.0f - 0x1p-19f)) {
-                    cn[w] = cn[k]; cs[w] = cs[k]; clev[w] = clev[k]; cid[w] = cid[k]; cf[w] = cf[k];
-                    ++w;
-                }
-            nc = w;
-        }
-        if (ipf >= maxf * (1.0f - 0x1p-19f)) {
-            if (nc < kCand) {
-                cn[nc] = num; cs[nc] = static_cast<int>(sd4); clev[nc] = bc; cid[nc] = id; cf[nc] = ipf;
-                ++nc;
-            } else {
-                overflow = true;
+            if (hd[c].id >= 0 && (bc == 0 || event_before(c, hd[c], bc, cur))) {
+                bc = c;
+                cur = hd[c];
             }
-        }
-        ++ptr[bc];
-        advance(bc);
-    }
-    double best_t = 0.0, max_ip = 0.0;
-    if (!overflow) {
-        for (int k = 0; k < nc; ++k) {
-            if (!(cf[k] >= maxf * (1.0f - 0x1p-19f))) continue;
-            const double ip = cn[k] / sqrt(static_cast<double>(cs[k]) * 0.25);
-            if (ip > max_ip) {
-                max_ip = ip;
-                best_t = static_cast<double>(clev[k]) / static_cast<double>(fabsf(ru[cid[k]]));
-            }
-        }
-        return best_t;
-    }
-    // the reference's loop in double, from the same start
-    sd4 = sd4_0;
-    num = num_0;
-    for (int c = 1; c <= 7; ++c) {
-        ptr[c] = 0;
-        advance(c);
-    }
-    for (;;) {
-        int bc = -1;
+        if (bc == 0) break;
+#pragma unroll
         for (int c = 1; c <= 7; ++c)
-            if (head[c] >= 0 && (bc < 0 || earlier(c, bc))) bc = c;
-        if (bc < 0) break;
-        const int id = head[bc];
+            if (c == bc) {
+                ++hd[c].ptr;
+                advance_level(hd[c], c, keys, ru, c0, D, mx);
+            }
         sd4 += 8LL * bc;
-        num += static_cast<double>(fabsf(ru[id]));
-        const double ip = num / sqrt(static_cast<double>(sd4) * 0.25);
-        if (ip > max_ip) {
-            max_ip = ip;
-            best_t = static_cast<double>(bc) / static_cast<double>(fabsf(ru[id]));
+        num += static_cast<double>(cur.a);
+        const float nf = approx_float(num);
+        const float n2 = nf * nf, sdf = __ll2float_rn(sd4);  // sd4 < 2^24: exact
+        const float lhs = n2 * best_sdf, rhs = best_n2 * sdf;
+        bool take;
+        double ip = 0.0;
+        bool exact = false;
+        if (!have || lhs > rhs * kHi) {
+            take = true;
+        } else if (lhs < rhs * kLo) {
+            take = false;
+        } else {
+            if (!best_exact) {
+                best_ip = best_num / sqrt(static_cast<double>(best_sd4) * 0.25);
+                best_exact = true;
+            }
+            ip = num / sqrt(static_cast<double>(sd4) * 0.25);
+            exact = true;
+            take = ip > best_ip;
         }
-        ++ptr[bc];
-        advance(bc);
+        if (take) {
+            have = true;
+            best_n2 = n2;
+            best_sdf = sdf;
+            best_num = num;
+            best_sd4 = sd4;
+            best_c = bc;
+            best_a = cur.a;
+            best_exact = exact;
+            best_ip = ip;
+        }
     }
-    return best_t;
+    return have ? static_cast<double>(best_c) / static_cast<double>(best_a) : 0.0;
 }
 
 __device__ __forceinline__ void put_f32(uint8_t *dst, float v) {
