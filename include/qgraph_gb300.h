@@ -85,9 +85,10 @@ bool rabitq_encode_full(const void *space, const float *raw, void *encoded_out);
 bool rabitq_copy_compact(const void *space, const void *full_encoded, void *compact_out);
 /* rabitq_bridge.cpp:214-222 */
 bool rabitq_copy_residual_record(const void *space, const void *full_encoded, void *residual_out);
-/* rabitq_bridge.cpp:224-303. Builds a graph on the GPU with this library's own builder
- * (exact-kNN candidates + alpha robust prune + reverse edges); it does NOT reproduce the
- * reference's symmetric-4-bit Vamana graph. Load reference graphs unchanged instead. */
+/* rabitq_bridge.cpp:224-303. Not built: returns false (qg_last_error says why). Graphs come
+ * from the reference, loaded unchanged, or from this library's own GPU builder
+ * (quantization_graph_gb300.graph_build, qg_prune_candidates), which works from the float
+ * vectors and does not reproduce the reference's graph. */
 bool rabitq_build_vamana_graph(void *space, const void *compact_records_in, size_t record_count,
                                size_t compact_stride, size_t r, size_t l_build, float alpha,
                                size_t beam_width, size_t batch_size, size_t refine_passes,
