@@ -21,6 +21,9 @@
 // warp-parallel rank + shift of the pool in shared memory. The visited set is a per-warp-
 // slot array of 16-bit epoch tags in global memory (no per-query clearing).
 #include <cstdint>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "mlp.cuh"
 #include "qg_device.cuh"
@@ -943,7 +946,7 @@ static int blocks_per_sm_d(int l_cap, int wpb, bool stop_model) {
     return blocks;
 }
 
-int search_blocks_per_sm(int code_dim, int l_cap, int wpb, bool stop_model) {
+static int blocks_per_sm_uncached(int code_dim, int l_cap, int wpb, bool stop_model) {
     switch (code_dim) {
         case 64: return blocks_per_sm_d<64>(l_cap, wpb, stop_model);
         case 128: return blocks_per_sm_d<128>(l_cap, wpb, stop_model);
@@ -953,6 +956,25 @@ int search_blocks_per_sm(int code_dim, int l_cap, int wpb, bool stop_model) {
         case 2048: return blocks_per_sm_d<2048>(l_cap, wpb, stop_model);
         default: return 0;
     }
+}
+
+// Occupancy queries cost host time on every call; their answers depend only on the device and
+// the launch parameters, so they are kept.
+int search_blocks_per_sm(int code_dim, int l_cap, int wpb, bool stop_model) {
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, int, int, bool>, int> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    const auto key = std::make_tuple(dev, code_dim, l_cap, wpb, stop_model);
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        const auto it = cache.find(key);
+        if (it != cache.end()) return it->second;
+    }
+    const int b = blocks_per_sm_uncached(code_dim, l_cap, wpb, stop_model);
+    std::lock_guard<std::mutex> lock(mu);
+    cache[key] = b;
+    return b;
 }
 
 cudaError_t launch_search(const SearchArgs &a, int grid, int wpb, cudaStream_t stream) {
