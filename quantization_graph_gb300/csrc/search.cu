@@ -46,6 +46,9 @@ constexpr int kMaxBeam = 8;
 #ifndef QG_GATE_ASYNC
 #define QG_GATE_ASYNC 0  // 1: gate MSB rows staged in shared memory by cp.async, two groups in flight
 #endif
+#ifndef QG_TRAV_GROUP_WIDE
+#define QG_TRAV_GROUP_WIDE 2  // code rows in flight per traversal group for D = 2048
+#endif
 #ifndef QG_GATE_GROUP
 #define QG_GATE_GROUP 16  // 32-dim MSB chunks in flight per lane in the gate (neighbours x chunks)
 #endif
@@ -56,7 +59,7 @@ struct Lay {
     static constexpr int CPL = CH / LPN;            // 32-dim chunks per lane
     static constexpr int NBP = 32 / LPN;            // neighbours per pass
     static constexpr int GG = QG_GATE_GROUP / CPL;  // gate group (LPN == 32)
-    static constexpr int GT = CPL == 1 ? 8 : 2;     // traversal group (LPN == 32)
+    static constexpr int GT = CPL == 1 ? 8 : QG_TRAV_GROUP_WIDE;  // traversal group (LPN == 32)
     static constexpr int PG = 4;                    // passes per batch (LPN < 32)
 };
 
