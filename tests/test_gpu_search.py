@@ -131,3 +131,35 @@ def test_empty_batch_and_repeated_calls(cuda):
     for _ in range(5):
         r = ix.search(torch.from_numpy(Q).cuda(), k=10, l_value=40)
         np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), g["ids_L40_k10"])
+
+
+@pytest.mark.parametrize("dim", [40, 200, 400, 700])
+def test_other_code_dims_match_oracle(cuda, oracle, dim):
+    """The search kernel instantiations for D = 64, 256, 512 and 1024 against the oracle, on
+    this library's own encode and graph (ids, distance bits, counters)."""
+    torch = cuda
+    from quantization_graph_gb300.graph_build import build_graph
+    from quantization_graph_gb300.index import OursIndex
+    from quantization_graph_gb300.space import RabitqSpace
+
+    rng = np.random.default_rng(dim)
+    X = (rng.standard_normal((1500, dim)) * rng.uniform(0.2, 2.0, dim)).astype(np.float32)
+    Q = (rng.standard_normal((20, dim)) * rng.uniform(0.2, 2.0, dim)).astype(np.float32)
+    c = X.mean(0).astype(np.float32)
+    sp = RabitqSpace(dim, c)
+    xd = torch.from_numpy(X).cuda()
+    compact, residual = sp.encode(xd)
+    msb, factors = sp.export_paper_sidecar(compact)
+    deg, edges = build_graph(sp, xd, compact, r=32, knn=64, alpha=1.2, reverse=32, refine_rounds=1, refine_l=64,
+                             residual=residual, msb=msb, factors=factors)
+    ix = OursIndex(sp, compact, residual, msb, factors, deg, edges)
+    gi = dict(compact=compact.cpu().numpy(), residual=residual.cpu().numpy(), msb=msb.cpu().numpy(),
+              factors=factors.cpu().numpy(), degrees=deg.cpu().numpy().view(np.uint32),
+              edges=edges.cpu().numpy().view(np.uint32), total_points=1500, base_points=1500)
+    o = oracle.Oracle(dim, c)
+    for L, k in ((32, 10), (120, 100)):
+        r = ix.search(torch.from_numpy(Q).cuda(), k=k, l_value=L)
+        oi, od, os_ = o.search(Q, gi, k=k, L=L)
+        np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), oi)
+        np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(od))
+        np.testing.assert_array_equal(stats_matrix(r.stats), stats_matrix(os_))
