@@ -130,6 +130,18 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+#ifndef QG_STREAM_ROWS
+#define QG_STREAM_ROWS 0  // 1: gate and code rows read with the evict-first hint (each is read once)
+#endif
+template <typename T>
+__device__ __forceinline__ T row_load(const T *p) {
+#if QG_STREAM_ROWS
+    return __ldcs(p);
+#else
+    return __ldg(p);
+#endif
+}
+
 __device__ __forceinline__ void prefetch_l1(const void *p) {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
@@ -475,7 +487,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                         const uint32_t *row = reinterpret_cast<const uint32_t *>(
                             ix.msb + static_cast<size_t>(s.fid[f]) * (D / 8));
 #pragma unroll
-                        for (int j = 0; j < L::CPL; ++j) w[g][j] = __ldg(row + lane + 32 * j);
+                        for (int j = 0; j < L::CPL; ++j) w[g][j] = row_load(row + lane + 32 * j);
                     }
 #endif
 #if QG_GATE_PREFETCH == 1
@@ -585,7 +597,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                         const uint4 *row = reinterpret_cast<const uint4 *>(
                             ix.codes + static_cast<size_t>(s.sid[i]) * (D / 2));
 #pragma unroll
-                        for (int j = 0; j < L::CPL; ++j) c[g][j] = __ldg(row + lane + 32 * j);
+                        for (int j = 0; j < L::CPL; ++j) c[g][j] = row_load(row + lane + 32 * j);
                     }
 #if QG_TRAV_PREFETCH == 1
                     if (gb + G < S)
