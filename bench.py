@@ -293,7 +293,11 @@ def learned_stop_select(torch, w, args, L_fixed, rec_fixed, log):
     cands = sorted({min(1024, max(args.k, int(round(L_fixed * f / 8.0)) * 8)) for f in (1.0, 1.25, 1.5, 2.0)})
     L_train = max(cands)
     t0 = time.time()
-    tq = synthetic.anisotropic_torch(args.train_queries, args.dim, 0.8, seed=3, normalize=True)
+    # held-out queries from the base distribution of the workload
+    if args.workload == "gist960":
+        tq = synthetic.anisotropic_torch(args.train_queries, args.dim, 1.2, seed=3, absolute=True)
+    else:
+        tq = synthetic.anisotropic_torch(args.train_queries, args.dim, 0.8, seed=3, normalize=True)
     truth = index.search(tq, k=args.k, l_value=L_train, with_stats=False).ids.to(torch.int32)
     feats, labels = ls.collect_traces(index, tq, truth, k=args.k, l_value=L_train, every=args.stop_every)
     log(f"learned stop: {feats.shape[0]} trace rows from {args.train_queries} held-out queries at L={L_train}, "
