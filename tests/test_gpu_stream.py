@@ -52,3 +52,30 @@ def test_autotuner_keeps_results(cuda):
     assert best in [r[0] for r in results]
     r = ix.search(q, k=10, l_value=40)
     np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), g["ids_L40_k10"])
+
+
+def test_graph_replay_with_learned_stop_matches_direct_call(cuda):
+    """The captured graph with a stop model returns what the direct learned-stop call returns."""
+    torch = cuda
+    from quantization_graph_gb300 import learned_stop as ls
+    from quantization_graph_gb300 import synthetic
+    from quantization_graph_gb300.stream import GraphSearcher
+
+    g, ix = _index(torch)
+    _, cent = synthetic.gmm(1, 128, components=64, sigma=0.3, seed=11)
+    tq, _ = synthetic.gmm(800, 128, sigma=0.3, seed=301, centres=cent)
+    tq = torch.from_numpy(tq).cuda()
+    truth = ix.search(tq, k=10, l_value=80, with_stats=False).ids.to(torch.int32)
+    feats, labels = ls.collect_traces(ix, tq, truth, k=10, l_value=80, every=4)
+    model = ls.train(feats, labels, epochs=2, batch=4096, every=4, min_hops=8)
+    _, Q = SEARCH_CASES["search_c1"]()
+    q = torch.from_numpy(Q).cuda()
+    gs = GraphSearcher(ix, 128, max_batch=64, max_k=10, max_l=80, model=model, threshold=0.8)
+    n = q.shape[0]
+    ids, dists = gs.search(q, torch.full((n,), 10, dtype=torch.int32, device="cuda"),
+                           torch.full((n,), 80, dtype=torch.int32, device="cuda"))
+    gs.synchronize()
+    ref_ids, ref_d = ls.search(ix, q, model, 0.8, k=10, l_value=80)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(ids.cpu().numpy(), ref_ids.cpu().numpy())
+    np.testing.assert_array_equal(dists.cpu().numpy().view(np.uint32), ref_d.cpu().numpy().view(np.uint32))
