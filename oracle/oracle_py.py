@@ -199,6 +199,24 @@ class Oracle:
         return _search(self.lib.qgo_search_batch, [self.space], queries, index, k, L, eps,
                        rerank, beam, early_stop, kth_stop, threads)
 
+    def build_graph(self, compact, r=32, l_build=100, alpha=1.2, beam=1, batch=4096, refine=1,
+                    cap=256, stop_hops=2, threads=0):
+        """The restated Vamana build; same arguments as Reference.build_graph.
+        Returns (degrees, edges [n, r], distances evaluated)."""
+        compact = np.ascontiguousarray(compact)
+        n = compact.shape[0]
+        degrees = np.zeros(n, np.uint32)
+        edges = np.zeros((n, r), np.uint32)
+        evals = C.c_uint64(0)
+        rc = self.lib.qgo_build_vamana(
+            self.space, _p(compact), C.c_size_t(n), C.c_size_t(compact.shape[1]), C.c_size_t(r),
+            C.c_size_t(l_build), C.c_float(alpha), C.c_size_t(beam), C.c_size_t(batch), C.c_size_t(refine),
+            C.c_size_t(cap), C.c_size_t(stop_hops), _p(degrees), _p(edges), C.c_size_t(r), C.byref(evals),
+            C.c_int(threads))
+        if rc != 0:
+            raise RuntimeError("oracle graph build failed")
+        return degrees, edges, int(evals.value)
+
     def exact_knn(self, base, queries, k, threads=0):
         base = np.ascontiguousarray(base, np.float32)
         queries = np.ascontiguousarray(queries, np.float32)
@@ -368,6 +386,7 @@ class Reference:
             C.c_size_t(r), _p(msb), _p(factors), C.byref(msb_stride), C.byref(fbytes), C.byref(evals))
         if not ok:
             raise RuntimeError("reference graph build failed")
+        self.last_build_evals = int(evals.value)
         return degrees, edges
 
     def search(self, queries, index, k=10, L=40, eps=1.9, rerank=100, beam=1, early_stop=0,

@@ -1097,3 +1097,297 @@ extern "C" void qgo_exact_knn(const float *base, size_t n, const float *queries,
     }
     (void)threads;
 }
+
+// ---- Vamana graph build over the symmetric 4-bit estimator --------------------------
+// Restates VamanaIndex::buildGraphFromLoadedPayloads (vamana_index.h:452-528),
+// refineGraphSymmetric (:328-422), addBackedgesGroupedAndPrune / addBackedgeGroupAndPrune
+// (:995-1117), capBuildPrunePool (:201-211), search_vamana (vamana_search.h:98-198) and
+// robust_prune_4bit (vamana_prune.h:42-156), as rabitq_build_vamana_graph
+// (rabitq_bridge.cpp:224-303) drives them. The build is deterministic: searches of one batch
+// read the graph as it was when the batch started, back-edge groups write disjoint sources.
+namespace {
+
+struct BuildCand {
+    float d;
+    uint32_t id;
+    bool expanded;
+};
+
+inline bool build_less(const BuildCand &a, const BuildCand &b) {
+    return a.d != b.d ? a.d < b.d : a.id < b.id;
+}
+
+struct BuildState {
+    const qgo_space *space;
+    const uint8_t *compact;
+    size_t stride;
+    size_t r, l_build, beam, cap, stop_hops;
+    float alpha;
+    std::vector<std::vector<uint32_t>> graph;
+    uint64_t evals = 0;  // distances evaluated, counted like distance_evaluations_
+
+    float dist(uint32_t lhs, uint32_t rhs) const {
+        return qgo_symmetric_distance(space, compact + lhs * stride, compact + rhs * stride);
+    }
+};
+
+struct BuildScratch {
+    std::vector<uint32_t> tags;
+    uint32_t epoch = 0;
+    std::vector<BuildCand> pool;
+    uint64_t evals = 0;
+};
+
+// search_vamana: beam search from node 0 over nodes [0, node_count); returns false on an
+// out-of-range neighbour (the reference throws there).
+bool build_search(const BuildState &st, uint32_t query, size_t node_count, BuildScratch &sc) {
+    if (sc.tags.size() < node_count) sc.tags.resize(node_count, 0);
+    if (++sc.epoch == 0) {
+        std::fill(sc.tags.begin(), sc.tags.end(), 0);
+        sc.epoch = 1;
+    }
+    auto &pool = sc.pool;
+    pool.clear();
+    pool.push_back({st.dist(query, 0), 0, false});
+    sc.evals += 1;
+    sc.tags[0] = sc.epoch;
+    std::vector<uint32_t> frontier;
+    size_t stall = 0;
+    for (;;) {
+        const float back_before = pool.back().d;
+        frontier.clear();
+        for (auto &c : pool) {
+            if (!c.expanded) {
+                c.expanded = true;
+                frontier.push_back(c.id);
+                if (frontier.size() == st.beam) break;
+            }
+        }
+        if (frontier.empty()) break;
+        for (uint32_t node : frontier) {
+            for (uint32_t nb : st.graph[node]) {
+                if (nb >= node_count) return false;
+                if (sc.tags[nb] == sc.epoch) continue;
+                sc.tags[nb] = sc.epoch;
+                const BuildCand c{st.dist(query, nb), nb, false};
+                sc.evals += 1;
+                // insert_candidate_sorted (vamana_search.h:79-96)
+                if (pool.size() >= st.l_build && !build_less(c, pool.back())) continue;
+                pool.insert(std::lower_bound(pool.begin(), pool.end(), c, build_less), c);
+                if (pool.size() > st.l_build) pool.resize(st.l_build);
+            }
+        }
+        if (st.stop_hops != 0 && pool.size() >= st.l_build) {
+            stall = pool.back().d >= back_before ? stall + 1 : 0;
+            if (stall >= st.stop_hops) break;
+        }
+    }
+    return true;
+}
+
+void cap_pool(const BuildState &st, std::vector<BuildCand> &pool) {
+    if (st.cap == 0 || pool.size() <= st.cap) return;
+    std::partial_sort(pool.begin(), pool.begin() + static_cast<long>(st.cap), pool.end(), build_less);
+    pool.resize(st.cap);
+}
+
+// robust_prune_4bit: alpha ramp 1 -> alpha in steps of x min(alpha, 1.2); pair distances
+// (candidate, selected) evaluated lazily and memoised, as the reference does.
+std::vector<uint32_t> robust_prune(const BuildState &st, uint32_t source, std::vector<BuildCand> cands,
+                                   uint64_t &evals) {
+    std::sort(cands.begin(), cands.end(), build_less);
+    std::vector<BuildCand> uniq;
+    uniq.reserve(cands.size());
+    for (const auto &c : cands) {
+        if (c.id == source) continue;
+        bool dup = false;
+        for (const auto &u : uniq) {
+            if (u.id == c.id) {
+                dup = true;
+                break;
+            }
+        }
+        if (!dup) uniq.push_back(c);
+    }
+    const size_t degree = st.r;
+    std::vector<uint32_t> selected;
+    std::vector<uint8_t> disabled(uniq.size(), 0);
+    std::vector<float> memo(uniq.size() * degree, -1.0f);
+    float cur = 1.0f;
+    const float step = std::min(st.alpha, 1.2f);
+    while (selected.size() < degree) {
+        bool promoted = false;
+        for (size_t i = 0; i < uniq.size() && selected.size() < degree; ++i) {
+            if (disabled[i]) continue;
+            bool occluded = false;
+            for (size_t k = 0; k < selected.size(); ++k) {
+                float &m = memo[i * degree + k];
+                if (m < 0.0f) {
+                    m = st.dist(uniq[i].id, selected[k]);
+                    evals += 1;
+                }
+                if (cur * m <= uniq[i].d) {
+                    occluded = true;
+                    break;
+                }
+            }
+            if (occluded) continue;
+            selected.push_back(uniq[i].id);
+            disabled[i] = 1;
+            promoted = true;
+        }
+        if (cur == st.alpha) break;
+        const float next = std::min(st.alpha, cur * step);
+        if (next == cur) break;
+        cur = next;
+        if (!promoted && selected.size() >= degree) break;
+    }
+    return selected;
+}
+
+// addBackedgesGroupedAndPrune: pairs (source, target) grouped by source; each source takes
+// its sorted, de-duplicated targets and is re-pruned when it grows past R.
+void add_backedges(BuildState &st, std::vector<std::pair<uint32_t, uint32_t>> &pairs, int threads) {
+    if (pairs.empty()) return;
+    std::sort(pairs.begin(), pairs.end());
+    std::vector<size_t> starts{0};
+    for (size_t i = 1; i < pairs.size(); ++i)
+        if (pairs[i].first != pairs[i - 1].first) starts.push_back(i);
+    starts.push_back(pairs.size());
+    uint64_t evals = 0;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 32) num_threads(threads) reduction(+ : evals)
+#endif
+    for (long long g = 0; g < static_cast<long long>(starts.size()) - 1; ++g) {
+        const uint32_t source = pairs[starts[g]].first;
+        std::vector<uint32_t> targets;
+        for (size_t i = starts[g]; i < starts[g + 1]; ++i)
+            if (pairs[i].second != source) targets.push_back(pairs[i].second);
+        if (targets.empty()) continue;
+        std::sort(targets.begin(), targets.end());
+        targets.erase(std::unique(targets.begin(), targets.end()), targets.end());
+        auto &nb = st.graph[source];
+        size_t added = 0;
+        for (uint32_t t : targets) {
+            if (std::find(nb.begin(), nb.end(), t) == nb.end()) {
+                nb.push_back(t);
+                ++added;
+            }
+        }
+        if (added == 0 || nb.size() <= st.r) continue;
+        std::vector<BuildCand> pool;
+        for (uint32_t c : nb) {
+            if (c == source) continue;
+            pool.push_back({st.dist(source, c), c, false});
+            evals += 1;
+        }
+        nb = robust_prune(st, source, std::move(pool), evals);
+    }
+    (void)threads;
+    st.evals += evals;
+}
+
+}  // namespace
+
+extern "C" int qgo_build_vamana(const qgo_space *space, const uint8_t *compact, size_t n, size_t stride,
+                                size_t r, size_t l_build, float alpha, size_t beam, size_t batch,
+                                size_t refine, size_t cap, size_t stop_hops, uint32_t *degrees,
+                                uint32_t *edges, size_t edge_stride, uint64_t *evals_out, int threads) {
+    if (space == nullptr || (compact == nullptr && n != 0) || degrees == nullptr || edges == nullptr ||
+        edge_stride < r || r == 0 || l_build == 0 || beam == 0 || !(alpha >= 1.0f) || !std::isfinite(alpha))
+        return -1;
+#ifdef _OPENMP
+    if (threads <= 0) threads = omp_get_max_threads();
+#endif
+    if (batch == 0) batch = 1;
+    BuildState st{space, compact, stride, r, l_build, beam, cap, stop_hops, alpha, {}, 0};
+    st.graph.assign(n, {});
+    bool ok = true;
+    // bulk insertion in batches (vamana_index.h:452-528)
+    for (size_t begin = 1; begin < n && ok; begin += batch) {
+        const size_t end = std::min(n, begin + batch);
+        std::vector<std::vector<uint32_t>> lists(end - begin);
+        uint64_t evals = 0;
+        bool bad = false;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(threads) reduction(+ : evals) reduction(|| : bad)
+#endif
+        {
+            BuildScratch sc;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 32)
+#endif
+            for (long long off = 0; off < static_cast<long long>(end - begin); ++off) {
+                const uint32_t id = static_cast<uint32_t>(begin + static_cast<size_t>(off));
+                if (!build_search(st, id, begin, sc)) {
+                    bad = true;
+                    continue;
+                }
+                std::vector<BuildCand> pool = sc.pool;
+                cap_pool(st, pool);
+                lists[static_cast<size_t>(off)] = robust_prune(st, id, std::move(pool), evals);
+            }
+            evals += sc.evals;
+        }
+        st.evals += evals;
+        if (bad) {
+            ok = false;
+            break;
+        }
+        std::vector<std::pair<uint32_t, uint32_t>> pairs;
+        for (size_t off = 0; off < lists.size(); ++off) {
+            const uint32_t id = static_cast<uint32_t>(begin + off);
+            st.graph[id] = std::move(lists[off]);
+            for (uint32_t nb : st.graph[id]) pairs.emplace_back(nb, id);
+        }
+        add_backedges(st, pairs, threads);
+    }
+    // refinement passes over the whole graph (vamana_index.h:328-422)
+    for (size_t pass = 0; pass < refine && ok && n > 1; ++pass) {
+        std::vector<std::vector<uint32_t>> refined(n);
+        uint64_t evals = 0;
+        bool bad = false;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(threads) reduction(+ : evals) reduction(|| : bad)
+#endif
+        {
+            BuildScratch sc;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 32)
+#endif
+            for (long long sid = 0; sid < static_cast<long long>(n); ++sid) {
+                const uint32_t id = static_cast<uint32_t>(sid);
+                if (!build_search(st, id, n, sc)) {
+                    bad = true;
+                    continue;
+                }
+                std::vector<BuildCand> pool = sc.pool;
+                cap_pool(st, pool);
+                for (uint32_t x : st.graph[id]) {
+                    pool.push_back({st.dist(id, x), x, false});
+                    evals += 1;
+                }
+                refined[id] = robust_prune(st, id, std::move(pool), evals);
+            }
+            evals += sc.evals;
+        }
+        st.evals += evals;
+        if (bad) {
+            ok = false;
+            break;
+        }
+        st.graph.swap(refined);
+        std::vector<std::pair<uint32_t, uint32_t>> pairs;
+        for (size_t id = 0; id < n; ++id)
+            for (uint32_t nb : st.graph[id]) pairs.emplace_back(nb, static_cast<uint32_t>(id));
+        add_backedges(st, pairs, threads);
+    }
+    if (!ok) return -1;
+    for (size_t id = 0; id < n; ++id) {
+        if (st.graph[id].size() > edge_stride) return -1;
+        degrees[id] = static_cast<uint32_t>(st.graph[id].size());
+        std::copy(st.graph[id].begin(), st.graph[id].end(), edges + id * edge_stride);
+    }
+    if (evals_out != nullptr) *evals_out = st.evals;
+    return 0;
+}

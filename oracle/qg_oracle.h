@@ -151,6 +151,16 @@ int qgo_search_one_with(const qgo_kernel_table *kt, const float *query,
                         size_t base_points, uint32_t *ids_out, float *dists_out,
                         qgo_search_stats *stats_out);
 
+/* ---- Vamana graph build (rabitq_build_vamana_graph, rabitq_bridge.cpp:224-303) ----
+ * Bulk insertion in batches from node 0, refinement passes, grouped back-edges, all over the
+ * symmetric 4-bit estimator. edges: `edge_stride` slots per node, degrees[i] valid. evals_out
+ * (may be NULL) counts the distances evaluated, like VamanaIndex::distance_evaluations().
+ * Returns 0 on success, -1 on bad arguments or an out-of-range neighbour. */
+int qgo_build_vamana(const qgo_space *space, const uint8_t *compact, size_t n, size_t stride,
+                     size_t r, size_t l_build, float alpha, size_t beam, size_t batch,
+                     size_t refine, size_t cap, size_t stop_hops, uint32_t *degrees,
+                     uint32_t *edges, size_t edge_stride, uint64_t *evals_out, int threads);
+
 /* ---- exact ground truth (FP64 brute force, query_coarse_codec_test.cpp:29-36 style) ---- */
 void qgo_exact_knn(const float *base, size_t n, const float *queries, size_t nq, size_t dim,
                    size_t k, uint32_t *ids_out, double *dists_out, int threads);

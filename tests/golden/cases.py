@@ -35,3 +35,22 @@ def c3_data(n=1000, nq=16):
 
 
 SEARCH_CASES = {"search_c1": c1_data, "search_c2": c2_data, "search_c3": c3_data}
+
+
+# rabitq_build_vamana_graph arguments of the graphs stored in the search fixtures (alpha 1.2,
+# beam 1) and of the extra build variants (build_variants.npz) over the same records.
+SEARCH_GRAPH_ARGS = {
+    "search_c1": dict(r=32, l_build=100, alpha=1.2, beam=1, batch=256, refine=1, cap=256, stop_hops=2),
+    "search_c2": dict(r=32, l_build=64, alpha=1.2, beam=1, batch=256, refine=1, cap=256, stop_hops=2),
+    "search_c3": dict(r=32, l_build=64, alpha=1.2, beam=1, batch=256, refine=1, cap=256, stop_hops=2),
+}
+BUILD_VARIANTS = {
+    "beam2_alpha13_cap48": dict(src="search_c1", r=32, l_build=64, alpha=1.3, beam=2, batch=300, refine=0,
+                                cap=48, stop_hops=0),
+    "alpha1_r16_refine2": dict(src="search_c1", r=16, l_build=40, alpha=1.0, beam=1, batch=1000, refine=2,
+                               cap=0, stop_hops=3),
+    "alpha2_batch1": dict(src="search_c1", r=8, l_build=24, alpha=2.0, beam=3, batch=1, refine=1, cap=16,
+                          stop_hops=1),
+    "d960_r24": dict(src="search_c2", r=24, l_build=48, alpha=1.2, beam=1, batch=4096, refine=1, cap=32,
+                     stop_hops=2),
+}

@@ -11,7 +11,7 @@ ours_diskann.rs:1539-1986 (which cannot be built here) is driven over the refere
 bridge kernels (oracle/ref_probe.cpp).
 
 Inputs are regenerated from numpy seeds in the tests; a checksum of each input is stored
-to catch generator drift.  Usage:  python tests/golden/make_golden.py
+to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants]
 """
 from __future__ import annotations
 
@@ -29,7 +29,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 import oracle_py  # noqa: E402
 sys.path.insert(0, HERE)
-from cases import c1_data, c2_data, c3_data, kernel_inputs  # noqa: E402
+from cases import BUILD_VARIANTS, c1_data, c2_data, c3_data, kernel_inputs  # noqa: E402
 
 FLAGS = "g++ -std=c++20 -O3 -march=native -fopenmp (experiments/02_diskann_fair/build.rs:22-36)"
 
@@ -115,20 +115,41 @@ def c1_extras(out, ref, Q, index):
         out[f"stats_{tag}"] = stats.view(np.uint64).reshape(len(Q), -1)
 
 
+def build_variants():
+    """Graphs of the reference's own rabitq_build_vamana_graph for argument sets other than the
+    formal one, over the records already stored in the search fixtures."""
+    out = {}
+    for name, kw in BUILD_VARIANTS.items():
+        kw = dict(kw)
+        g = np.load(os.path.join(HERE, kw.pop("src") + ".npz"))
+        ref = oracle_py.Reference(int(g["dim"]), g["center"])
+        deg, edges = ref.build_graph(g["compact"], **kw)
+        out[f"{name}_degrees"] = deg
+        out[f"{name}_edges"] = edges
+        out[f"{name}_evals"] = np.array(ref.last_build_evals, np.uint64)
+        print(name, "mean degree", deg.mean(), "evals", ref.last_build_evals)
+    np.savez_compressed(os.path.join(HERE, "build_variants.npz"), **out)
+
+
 def main():
     oracle_py.build(ref=True)
     if not oracle_py.reference_available():
         raise SystemExit("the reference library could not be built")
+    if sys.argv[1:] == ["build_variants"]:
+        build_variants()
+        return
     kernel_case("kernels_d128", 128, 64, 8, seed=20260813, center_value=0.05)
     kernel_case("kernels_d100", 100, 48, 4, seed=5, center_value=None)
     kernel_case("kernels_d960", 960, 96, 4, seed=6, center_value=None)
     kernel_case("kernels_d1536", 1536, 64, 3, seed=7, center_value=None)
+    # graph arguments: cases.SEARCH_GRAPH_ARGS
     search_case("search_c1", c1_data, 128, 2000, 50, 11, M=32, l_build=100, refine=1, cap=256, stop=2,
                 batch=256, Ls=(20, 40, 80), extra=c1_extras)
     search_case("search_c2", c2_data, 960, 1500, 24, 21, M=32, l_build=64, refine=1, cap=256, stop=2,
                 batch=256, Ls=(40, 100))
     search_case("search_c3", c3_data, 1536, 1000, 16, 31, M=32, l_build=64, refine=1, cap=256, stop=2,
                 batch=256, Ls=(40,))
+    build_variants()
     with open(os.path.join(HERE, "PROVENANCE.txt"), "w") as f:
         f.write(f"generated by tests/golden/make_golden.py on {platform.machine()} {platform.processor()}\n")
         f.write(f"reference bridge compiled with: {FLAGS}\n")

@@ -117,3 +117,37 @@ def test_reference_cross_check_random(oracle):
         np.testing.assert_array_equal(np.stack([o.encode_full(x) for x in X]), np.stack([r.encode_full(x) for x in X]))
         po, pr = o.prepare(X[0] * 1.3), r.prepare(X[0] * 1.3)
         np.testing.assert_array_equal(po["codes"], pr["codes"])
+
+
+def _graph_equal(deg, edges, gdeg, gedges):
+    np.testing.assert_array_equal(deg, gdeg)
+    for i in range(len(deg)):
+        np.testing.assert_array_equal(edges[i, :deg[i]], gedges[i, :gdeg[i]])
+
+
+@pytest.mark.parametrize("name", list(SEARCH_CASES))
+def test_vamana_build_matches_reference_graph(oracle, name):
+    """The restated build reproduces the graph the reference's rabitq_build_vamana_graph made
+    for the search fixtures (formal arguments: alpha 1.2, refine 1, cap 256, stop 2)."""
+    from cases import SEARCH_GRAPH_ARGS
+
+    g = load_golden(name)
+    o = oracle.Oracle(int(g["dim"]), g["center"])
+    deg, edges, _ = o.build_graph(g["compact"], **SEARCH_GRAPH_ARGS[name])
+    _graph_equal(deg, edges, g["degrees"], g["edges"])
+
+
+def test_vamana_build_variants_match_reference(oracle):
+    """Other argument sets (beam 2-3, alpha 1.0 / 1.3 / 2.0, caps below L, no cap, several
+    refinement passes, batch 1, 960-d) against the reference's own graphs, including the
+    reference's distance-evaluation count."""
+    from cases import BUILD_VARIANTS
+
+    v = load_golden("build_variants")
+    for name, kw in BUILD_VARIANTS.items():
+        kw = dict(kw)
+        g = load_golden(kw.pop("src"))
+        o = oracle.Oracle(int(g["dim"]), g["center"])
+        deg, edges, evals = o.build_graph(g["compact"], **kw)
+        _graph_equal(deg, edges, v[f"{name}_degrees"], v[f"{name}_edges"])
+        assert evals == int(v[f"{name}_evals"]), name
