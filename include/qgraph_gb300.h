@@ -85,10 +85,12 @@ bool rabitq_encode_full(const void *space, const float *raw, void *encoded_out);
 bool rabitq_copy_compact(const void *space, const void *full_encoded, void *compact_out);
 /* rabitq_bridge.cpp:214-222 */
 bool rabitq_copy_residual_record(const void *space, const void *full_encoded, void *residual_out);
-/* rabitq_bridge.cpp:224-303. Not built: returns false (qg_last_error says why). Graphs come
- * from the reference, loaded unchanged, or from this library's own GPU builder
- * (quantization_graph_gb300.graph_build, qg_prune_candidates), which works from the float
- * vectors and does not reproduce the reference's graph. */
+/* rabitq_bridge.cpp:224-303: the reference's Vamana build (bulk insertion in batches,
+ * refinement passes, grouped back-edges, robust_prune_4bit over the symmetric 4-bit estimator),
+ * run on the GPU; the same graph as the reference for the same arguments. Host buffers; also
+ * exports the paper sidecar like the reference. distance_evaluations_out counts the distances
+ * this implementation evaluated (its prune evaluates them eagerly, so the count differs from
+ * the reference's lazy count). Returns false on bad arguments, R > 64 or beam * R > 1024. */
 bool rabitq_build_vamana_graph(void *space, const void *compact_records_in, size_t record_count,
                                size_t compact_stride, size_t r, size_t l_build, float alpha,
                                size_t beam_width, size_t batch_size, size_t refine_passes,
@@ -360,6 +362,15 @@ int qg_encode_batch(const void *space, const float *d_raw, size_t n, uint8_t *d_
 int qg_prune_candidates(const void *space, const uint8_t *d_compact, size_t compact_stride, size_t n,
                         const uint32_t *d_candidates, size_t k, size_t r, float alpha,
                         uint32_t *d_degrees, uint32_t *d_edges, size_t edge_stride, void *stream);
+
+/* rabitq_build_vamana_graph over device compact records: degrees [n] and edges
+ * [n x edge_stride] (device, zero past each degree); *distance_evaluations (host, may be NULL)
+ * as above. Synchronises `stream`. */
+int qg_build_vamana_device(const void *space, const uint8_t *d_compact, size_t n, size_t compact_stride,
+                           size_t r, size_t l_build, float alpha, size_t beam_width, size_t batch_size,
+                           size_t refine_passes, size_t prune_candidate_cap, size_t build_early_stop_hops,
+                           uint32_t *d_degrees, uint32_t *d_edges, size_t edge_stride,
+                           uint64_t *distance_evaluations, void *stream);
 
 /* GPU sidecar extraction (space_rabitq.h:4364-4392) from device compact records. */
 int qg_export_sidecar_device(const void *space, const uint8_t *d_compact, size_t n,

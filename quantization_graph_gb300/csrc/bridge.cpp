@@ -500,28 +500,46 @@ bool rabitq_build_vamana_graph(void *space, const void *compact_records_in, size
                                uint8_t *paper_msb_out, void *paper_factors_out,
                                size_t *paper_msb_stride_out, size_t *paper_factor_bytes_out,
                                uint64_t *distance_evaluations_out) {
-    (void)space;
-    (void)compact_records_in;
-    (void)record_count;
-    (void)compact_stride;
-    (void)r;
-    (void)l_build;
-    (void)alpha;
-    (void)beam_width;
-    (void)batch_size;
-    (void)refine_passes;
-    (void)prune_candidate_cap;
-    (void)build_early_stop_hops;
-    (void)degrees_out;
-    (void)edges_out;
-    (void)edge_stride;
-    (void)paper_msb_out;
-    (void)paper_factors_out;
-    (void)paper_msb_stride_out;
-    (void)paper_factor_bytes_out;
-    (void)distance_evaluations_out;
-    set_error("graph build from compact records is not built; load a reference graph");
-    return false;
+    try {
+        const Space *s = as_space(space);
+        if (!s || (!compact_records_in && record_count != 0) || !degrees_out || !edges_out || edge_stride < r ||
+            !paper_msb_out || !paper_factors_out || !paper_msb_stride_out || !paper_factor_bytes_out ||
+            compact_stride < s->compact_bytes)
+            return false;
+        Carve c;
+        const size_t o_c = c.take(record_count * compact_stride), o_d = c.take(record_count * 4),
+                     o_e = c.take(record_count * edge_stride * 4);
+        if (!t_stage.reserve(c.off)) return false;
+        uint8_t *d = static_cast<uint8_t *>(t_stage.d);
+        cudaStream_t st = t_stage.stream;
+        if (record_count && !cuda_ok(cudaMemcpyAsync(d + o_c, compact_records_in, record_count * compact_stride,
+                                                     cudaMemcpyHostToDevice, st),
+                                     "build upload"))
+            return false;
+        uint64_t evals = 0;
+        if (qg_build_vamana_device(s, d + o_c, record_count, compact_stride, r, l_build, alpha, beam_width,
+                                   batch_size, refine_passes, prune_candidate_cap, build_early_stop_hops,
+                                   reinterpret_cast<uint32_t *>(d + o_d), reinterpret_cast<uint32_t *>(d + o_e),
+                                   edge_stride, &evals, st) != QG_OK)
+            return false;
+        if (record_count &&
+            (!cuda_ok(cudaMemcpyAsync(degrees_out, d + o_d, record_count * 4, cudaMemcpyDeviceToHost, st),
+                      "build download") ||
+             !cuda_ok(cudaMemcpyAsync(edges_out, d + o_e, record_count * edge_stride * 4, cudaMemcpyDeviceToHost,
+                                      st),
+                      "build download") ||
+             !cuda_ok(cudaStreamSynchronize(st), "build sync")))
+            return false;
+        if (!rabitq_export_paper_sidecar(space, compact_records_in, record_count, compact_stride, paper_msb_out,
+                                         paper_factors_out))
+            return false;
+        *paper_msb_stride_out = s->msb_bytes;
+        *paper_factor_bytes_out = 20;
+        if (distance_evaluations_out) *distance_evaluations_out = evals;
+        return true;
+    } catch (...) {
+        return false;
+    }
 }
 
 bool rabitq_export_paper_sidecar(const void *space, const void *compact_records_in,
@@ -906,6 +924,33 @@ int qg_prune_candidates(const void *space, const uint8_t *d_compact, size_t comp
                               edge_stride, static_cast<cudaStream_t>(stream)),
                  "prune kernel"))
         return QG_ERR_CUDA;
+    return QG_OK;
+}
+
+int qg_build_vamana_device(const void *space, const uint8_t *d_compact, size_t n, size_t compact_stride,
+                           size_t r, size_t l_build, float alpha, size_t beam_width, size_t batch_size,
+                           size_t refine_passes, size_t prune_candidate_cap, size_t build_early_stop_hops,
+                           uint32_t *d_degrees, uint32_t *d_edges, size_t edge_stride,
+                           uint64_t *distance_evaluations, void *stream) {
+    const Space *s = as_space(space);
+    if (!s || (n && (!d_compact || !d_degrees || !d_edges)) || compact_stride < s->compact_bytes || r == 0 ||
+        r > 64 || edge_stride < r || l_build == 0 || beam_width == 0 || beam_width * r > 1024 ||
+        !(alpha >= 1.0f) || !std::isfinite(alpha) || n >= 0x7FFFFFFFu) {
+        set_error("vamana build: invalid arguments (R <= 64, beam * R <= 1024, alpha >= 1)");
+        return QG_ERR_INVALID;
+    }
+    VbBuildParams p{r, l_build, alpha, beam_width, batch_size, refine_passes, prune_candidate_cap,
+                    build_early_stop_hops};
+    unsigned long long ev = 0;
+    const cudaError_t e = launch_vamana_build(static_cast<int>(s->code_dim), d_compact, n, compact_stride, p,
+                                              d_degrees, d_edges, edge_stride, &ev,
+                                              static_cast<cudaStream_t>(stream));
+    if (e == cudaErrorInvalidValue) {
+        set_error("vamana build: a neighbour outside the graph or unsupported arguments");
+        return QG_ERR_INVALID;
+    }
+    if (!cuda_ok(e, "vamana build")) return QG_ERR_CUDA;
+    if (distance_evaluations) *distance_evaluations = ev;
     return QG_OK;
 }
 

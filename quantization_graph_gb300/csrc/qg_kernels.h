@@ -143,4 +143,23 @@ cudaError_t launch_residual_pairs(int code_dim, const float *rr, const float4 *s
 cudaError_t launch_symmetric_pairs(int code_dim, const uint8_t *lhs, const uint8_t *rhs,
                                    size_t count, size_t stride, float *out, cudaStream_t stream);
 
+// rabitq_build_vamana_graph arguments (rabitq_bridge.cpp:224-303)
+struct VbBuildParams {
+    size_t r;
+    size_t l_build;
+    float alpha;
+    size_t beam;
+    size_t batch;
+    size_t refine;
+    size_t cap;
+    size_t stop_hops;
+};
+// The reference's Vamana build (vamana_index.h:452-528, 328-422, 995-1117) over n device compact
+// records; writes degrees [n] and edges [n x edge_stride] (device; zero past each degree).
+// evals_out (host, may be null) receives the number of distances this implementation evaluated.
+// Synchronises `stream`. r <= 64, beam * r <= 1024.
+cudaError_t launch_vamana_build(int code_dim, const uint8_t *d_compact, size_t n, size_t stride,
+                                const VbBuildParams &p, uint32_t *d_degrees, uint32_t *d_edges, size_t edge_stride,
+                                unsigned long long *evals_out, cudaStream_t stream);
+
 }  // namespace qg

@@ -1,8 +1,12 @@
-"""GPU graph construction for indexes the reference has not built (this library's own builder).
+"""GPU graph construction.
 
-The reference builds its Vamana graph on the host with the symmetric 4-bit estimator
-(rabitq_build_vamana_graph -> vamana_index.h:308-422; 3202 s at 64 threads for 1M x 960).
-This builder is not bit-identical to it. Steps:
+build_vamana() is the reference's own build (rabitq_build_vamana_graph, rabitq_bridge.cpp:224-303:
+bulk insertion in batches, refinement passes, grouped back-edges, robust_prune_4bit over the
+symmetric 4-bit estimator) run on the GPU; it yields the reference's graph for the same
+arguments (the reference spends 3202 s at 64 threads on it for 1M x 960).
+
+build_graph() is this library's own faster builder, which does not reproduce the reference's
+graph. Steps:
 
   1. exact-ish kNN candidates from the float vectors (TF32 GEMM through torch/cuBLAS, top-K),
      plus a few seeded random nodes per row (long-range candidates: on clustered data they are
@@ -43,6 +47,26 @@ def knn_candidates(data: torch.Tensor, k: int, chunk: int = 4096) -> torch.Tenso
         return out
     finally:
         torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+def build_vamana(space: RabitqSpace, compact: torch.Tensor, r: int = 64, l_build: int = 400, alpha: float = 1.2,
+                 beam: int = 1, batch: int = 4096, refine: int = 1, cap: int = 256, stop_hops: int = 2,
+                 edge_stride: int | None = None) -> tuple[torch.Tensor, torch.Tensor, int]:
+    """rabitq_build_vamana_graph over device compact records [n, compact_bytes] (uint8).
+    Defaults are the formal run's (max degree 64, build beam 400, alpha 1.2, build beam width 1,
+    batch 4096, refine 1, prune cap 256, early stop 2). Returns (degrees int32 [n], edges int32
+    [n, edge_stride], zero past each degree, distances evaluated)."""
+    lib = N.load()
+    compact = _cuda(compact, torch.uint8)
+    n = compact.shape[0]
+    edge_stride = edge_stride or r
+    deg = torch.empty(n, dtype=torch.int32, device="cuda")
+    edges = torch.empty((n, edge_stride), dtype=torch.int32, device="cuda")
+    evals = C.c_uint64(0)
+    N.check(lib.qg_build_vamana_device(space.ptr, _ptr(compact), n, compact.shape[1], r, l_build, alpha, beam, batch,
+                                       refine, cap, stop_hops, _ptr(deg), _ptr(edges), edge_stride,
+                                       C.byref(evals), _stream()), "qg_build_vamana_device")
+    return deg, edges, int(evals.value)
 
 
 def prune(space: RabitqSpace, compact: torch.Tensor, candidates: torch.Tensor, r: int, alpha: float,
