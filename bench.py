@@ -3,8 +3,10 @@
 
 Workload (default): 1,000,000 base vectors x 1536-d, unit-norm anisotropic Gaussian
 (lambda_i ~ i^-0.8, seeded rotation), 10,000 queries drawn the same way, ExRaBitQ4 block16
-encoding on the GPU, degree-64 graph (this library's GPU builder: kNN-128 candidates, alpha
-1.2 robust prune, reverse edges), k = 10, INT8 query codec with the 1-bit paper-prune gate,
+encoding on the GPU, degree-64 graph built by the reference's Vamana algorithm on the GPU
+(rabitq_build_vamana_graph with the formal arguments: L_build 400, alpha 1.2, batch 4096, refine
+1, prune cap 256, early stop 2; the same graph the reference builds; --graph own selects this
+library's faster kNN + prune builder), k = 10, INT8 query codec with the 1-bit paper-prune gate,
 residual4 top-100 rerank, fixed-L beam search with the smallest L from a sweep that reaches
 recall@10 >= 0.95 against an exact FP64 ground truth.
 
@@ -48,6 +50,10 @@ def parse():
     ap.add_argument("--L", type=int, default=0, help="fixed L (0 = sweep)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--graph", default="reference", choices=["reference", "own"],
+                    help="reference: the reference's Vamana build (rabitq_build_vamana_graph) on the GPU with the "
+                         "formal arguments; own: this library's kNN + prune builder")
+    ap.add_argument("--l-build", type=int, default=400, help="build search list size (--graph reference)")
     ap.add_argument("--refine", type=int, default=1, help="graph refinement rounds")
     ap.add_argument("--knn", type=int, default=240, help="kNN candidates per node for the graph")
     ap.add_argument("--refine-l", type=int, default=256, help="search list size of the refinement rounds")
@@ -143,9 +149,18 @@ def recall_at(ids, gt, k):
     return hit / (ids.shape[0] * k)
 
 
+def graph_desc(args) -> str:
+    if args.graph == "reference":
+        return (f"the reference's Vamana build (rabitq_build_vamana_graph) on the GPU, identical graph: R={args.M}, "
+                f"L_build={args.l_build}, alpha 1.2, beam 1, batch 4096, refine {args.refine}, prune cap 256, "
+                f"early stop 2")
+    return (f"GPU kNN-{args.knn or 2 * args.M} + 16 random + alpha-1.2 prune + reverse edges + "
+            f"{args.refine} search-based refinement round(s) at L={args.refine_l}")
+
+
 def build_workload(torch, args, log):
     from quantization_graph_gb300 import synthetic
-    from quantization_graph_gb300.graph_build import build_graph, reachable_fraction
+    from quantization_graph_gb300.graph_build import build_graph, build_vamana, reachable_fraction
     from quantization_graph_gb300.index import OursIndex
     from quantization_graph_gb300.space import RabitqSpace, train_global_center
 
@@ -165,9 +180,14 @@ def build_workload(torch, args, log):
     t_encode = time.time() - t1
     msb, factors = space.export_paper_sidecar(compact)
     t2 = time.time()
-    deg, edges = build_graph(space, base, compact, r=args.M, knn=args.knn or 2 * args.M, alpha=1.2, reverse=args.M,
-                             refine_rounds=args.refine, refine_l=args.refine_l, residual=residual, msb=msb,
-                             factors=factors)
+    if args.graph == "reference":  # max degree M, build beam 400, alpha 1.2, beam 1, batch 4096, refine 1,
+        # prune cap 256, early stop 2 (scripts/local_runs/build_agnews_dbpedia_prereqs.sh, diskann_runner.rs:286-296)
+        deg, edges, _ = build_vamana(space, compact, r=args.M, l_build=args.l_build, alpha=1.2, beam=1, batch=4096,
+                                     refine=args.refine, cap=256, stop_hops=2)
+    else:
+        deg, edges = build_graph(space, base, compact, r=args.M, knn=args.knn or 2 * args.M, alpha=1.2,
+                                 reverse=args.M, refine_rounds=args.refine, refine_l=args.refine_l, residual=residual,
+                                 msb=msb, factors=factors)
     torch.cuda.synchronize()
     t_graph = time.time() - t2
     reach = reachable_fraction(edges)
@@ -365,8 +385,7 @@ def main():
     config = {"workload": (f"{data_desc}, M={args.M}, "
                            f"{args.nq} queries, k={args.k}, INT8 paper-prune gate, residual4 rerank 100"),
               "n": args.n, "dim": args.dim, "queries": args.nq, "M": args.M, "k": args.k,
-              "graph": (f"GPU kNN-{args.knn or 2 * args.M} + 16 random + alpha-1.2 prune + reverse edges + "
-                        f"{args.refine} search-based refinement round(s) at L={args.refine_l}"),
+              "graph": graph_desc(args),
               "l2": "index larger than L2 (no flush needed)",
               "fixed_l": {"L": L, "recall@10": round(rec, 4)}}
     D = w["space"].code_dim
@@ -488,7 +507,7 @@ def main():
                          "algorithmic_bytes_per_query": alg_bytes / nq,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback"},
             "clocks": clocks.summary(), "cpu_baseline": cpu,
-            "setup": {"encode_s": round(w["t_encode"], 3), "graph_s": round(w["t_graph"], 2),
+            "setup": {"encode_s": round(w["t_encode"], 3), "graph_s": round(w["t_graph"], 2), "graph": args.graph,
                       "reachable_from_0": round(w["reach"], 5),
                       "l_sweep": {str(k): round(v, 4) for k, v in sweep.items()}}}
     if rank == 0:
@@ -508,7 +527,7 @@ def run_stream(args, log):
 
     from quantization_graph_gb300 import learned_stop as ls
     from quantization_graph_gb300 import synthetic
-    from quantization_graph_gb300.graph_build import build_graph, reachable_fraction
+    from quantization_graph_gb300.graph_build import build_graph, build_vamana, reachable_fraction
     from quantization_graph_gb300.index import OursIndex
     from quantization_graph_gb300.space import RabitqSpace, train_global_center
     from quantization_graph_gb300.stream import GraphSearcher, autotune
@@ -520,8 +539,12 @@ def run_stream(args, log):
     space = RabitqSpace(dim, train_global_center(base))
     compact, residual = space.encode(base)
     msb, factors = space.export_paper_sidecar(compact)
-    deg, edges = build_graph(space, base, compact, r=args.M, knn=2 * args.M, alpha=1.2, reverse=args.M,
-                             refine_rounds=args.refine, refine_l=128, residual=residual, msb=msb, factors=factors)
+    if args.graph == "reference":
+        deg, edges, _ = build_vamana(space, compact, r=args.M, l_build=args.l_build, alpha=1.2, beam=1, batch=4096,
+                                     refine=args.refine, cap=256, stop_hops=2)
+    else:
+        deg, edges = build_graph(space, base, compact, r=args.M, knn=2 * args.M, alpha=1.2, reverse=args.M,
+                                 refine_rounds=args.refine, refine_l=128, residual=residual, msb=msb, factors=factors)
     index = OursIndex(space, compact, residual, msb, factors, deg, edges)
     gt = ground_truth(torch, base, queries, 10)
     torch.cuda.synchronize()

@@ -27,7 +27,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -1004,32 +1007,62 @@ struct Builder {
         return h ? cudaErrorInvalidValue : cudaSuccess;
     }
 
+    // QG_VB_TRACE=1 prints the time of each stage (search, prune, back-edges) of the bulk and
+    // refinement phases to stderr; it synchronises around every stage.
+    bool trace = false;
+    double t_stage[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    template <typename F>
+    cudaError_t timed(int phase, int stage, F f) {
+        if (!trace) return f();
+        VB_TRY(cudaStreamSynchronize(st));
+        const auto t0 = std::chrono::steady_clock::now();
+        VB_TRY(f());
+        VB_TRY(cudaStreamSynchronize(st));
+        t_stage[phase][stage] += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return cudaSuccess;
+    }
+
     cudaError_t run() {
+        const char *tr = std::getenv("QG_VB_TRACE");
+        trace = tr && tr[0] == '1';
         // bulk insertion (vamana_index.h:452-528)
         const size_t batch = std::max<size_t>(p.batch, 1);
         for (size_t begin = 1; begin < n; begin += batch) {
             const size_t end = std::min(n, begin + batch);
             for (size_t c0 = begin; c0 < end; c0 += chunk) {
                 const uint32_t cnt_c = static_cast<uint32_t>(std::min(chunk, end - c0));
-                VB_TRY(search(static_cast<uint32_t>(c0), cnt_c, static_cast<uint32_t>(begin)));
-                VB_TRY(prune_pools(static_cast<uint32_t>(c0), cnt_c, false));
+                VB_TRY(timed(0, 0, [&] {
+                    return search(static_cast<uint32_t>(c0), cnt_c, static_cast<uint32_t>(begin));
+                }));
+                VB_TRY(timed(0, 1, [&] { return prune_pools(static_cast<uint32_t>(c0), cnt_c, false); }));
             }
-            VB_TRY(backedges(static_cast<uint32_t>(begin), static_cast<uint32_t>(end - begin),
-                             static_cast<uint32_t>(end)));
+            VB_TRY(timed(0, 2, [&] {
+                return backedges(static_cast<uint32_t>(begin), static_cast<uint32_t>(end - begin),
+                                 static_cast<uint32_t>(end));
+            }));
             VB_TRY(check_error());
         }
         // refinement passes (vamana_index.h:328-422)
         for (size_t pass = 0; pass < p.refine && n > 1; ++pass) {
             for (size_t c0 = 0; c0 < n; c0 += chunk) {
                 const uint32_t cnt_c = static_cast<uint32_t>(std::min(chunk, n - c0));
-                VB_TRY(search(static_cast<uint32_t>(c0), cnt_c, static_cast<uint32_t>(n)));
-                VB_TRY(prune_pools(static_cast<uint32_t>(c0), cnt_c, true));
+                VB_TRY(timed(1, 0, [&] {
+                    return search(static_cast<uint32_t>(c0), cnt_c, static_cast<uint32_t>(n));
+                }));
+                VB_TRY(timed(1, 1, [&] { return prune_pools(static_cast<uint32_t>(c0), cnt_c, true); }));
             }
             std::swap(adj, adj2);
             std::swap(deg, deg2);
-            VB_TRY(backedges(0, static_cast<uint32_t>(n), static_cast<uint32_t>(n)));
+            VB_TRY(timed(1, 2, [&] {
+                return backedges(0, static_cast<uint32_t>(n), static_cast<uint32_t>(n));
+            }));
             VB_TRY(check_error());
         }
+        if (trace)
+            std::fprintf(stderr,
+                         "vamana build: bulk search %.3f s prune %.3f s back-edges %.3f s | refine search %.3f s "
+                         "prune %.3f s back-edges %.3f s\n",
+                         t_stage[0][0], t_stage[0][1], t_stage[0][2], t_stage[1][0], t_stage[1][1], t_stage[1][2]);
         return cudaSuccess;
     }
 };
