@@ -24,6 +24,7 @@
 //     the neighbour lists, are the reference's; the number of distances evaluated is not.
 //   * back-edges: pairs are bucketed by source with a count / scan / scatter instead of a sort;
 //     each group sorts its (distinct) targets itself.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -35,6 +36,7 @@
 #include <vector>
 
 #include "qg_kernels.h"
+#include "sym_ff.cuh"
 
 namespace qg {
 namespace {
@@ -43,17 +45,9 @@ constexpr uint32_t kNoNode = 0xFFFFFFFFu;
 constexpr unsigned long long kKeyMax = ~0ull;
 constexpr int kWarpsPerBlock = 4;
 
-// Per-record factors of the symmetric estimator (space_rabitq.h:2691-2704): norm,
-// ip_norm = long_scale / (2 norm), validity of the record for the estimator.
-struct __align__(16) VbAux {
-    double rn;
-    double rip;
-    float n2;
-    int32_t nsum;  // sum of the 4-bit codes, for the centred product
-    int32_t valid;
-    int32_t pad;
-};
-static_assert(sizeof(VbAux) == 32, "VbAux is 32 bytes");
+// Per-record factors of the symmetric estimator (sym_ff.cuh): norm, ip_norm, their float
+// pairs, norm_sqr, code sum, validity.
+using VbAux = SymFactors;
 
 // (distance, id) as one ordered 64-bit key: the float mapped to an unsigned order, -0 folded
 // onto +0 (candidate_less compares floats, so the two are equal there and the id decides),
@@ -88,19 +82,12 @@ __device__ __forceinline__ uint32_t nib_dot4(uint4 a, uint4 b, uint32_t acc) {
 }
 
 // symmetricBuildDistanceFromPrepared with lhs the prepared side: the centred code product
-// sum (2a-15)(2b-15) = 4 ab - 30 a - 30 b + 225, then the double-precision estimator in the
-// reference's operation order.
+// sum (2a-15)(2b-15) = 4 ab - 30 a - 30 b + 225 from the plain nibble product ab, then the
+// estimator; float-float with a proven margin, double precision near rounding boundaries.
 template <int D>
 __device__ __forceinline__ float sym_distance(const VbAux &l, const VbAux &r, uint32_t ab) {
-    if (!l.valid || !r.valid) return __double2float_rn(__dadd_rn(static_cast<double>(l.n2), static_cast<double>(r.n2)));
     const int s = 4 * static_cast<int>(ab) - 30 * (l.nsum + r.nsum) + 225 * D;
-    const double code_ip = 0.25 * static_cast<double>(s);
-    double u = __dmul_rn(__dmul_rn(code_ip, l.rip), r.rip);
-    if (!isfinite(u)) u = 0.0;
-    u = fmax(-1.0, fmin(1.0, u));
-    const double rip = __dmul_rn(__dmul_rn(l.rn, r.rn), u);
-    return __double2float_rn(
-        __dsub_rn(__dadd_rn(static_cast<double>(l.n2), static_cast<double>(r.n2)), __dmul_rn(2.0, rip)));
+    return sym_distance_exact(l, r, s);
 }
 
 // Lanes split into groups of G; a group scores one candidate, each lane a fixed set of 16-byte
@@ -197,14 +184,7 @@ __global__ void vb_prepare_kernel(const uint8_t *compact, size_t n, size_t strid
         float n2, ls;
         memcpy(&n2, rec, 4);
         memcpy(&ls, rec + 4, 4);
-        VbAux a;
-        a.rn = sqrt(fmax(0.0, static_cast<double>(n2)));
-        a.valid = (a.rn > 0.0 && ls > 0.0f && isfinite(ls)) ? 1 : 0;
-        a.rip = a.valid ? static_cast<double>(ls) / (2.0 * a.rn) : 0.0;
-        a.n2 = n2;
-        a.nsum = static_cast<int32_t>(sum);
-        a.pad = 0;
-        aux[row] = a;
+        aux[row] = sym_factors(n2, ls, static_cast<int32_t>(sum));
     }
 }
 
@@ -667,7 +647,9 @@ __global__ void vb_scan_apply_kernel(const uint32_t *in, size_t n, const uint32_
 // and never the source), append those not yet neighbours. A list still within R is written
 // back; a longer one records its length in need[] for the pruning pass.
 __global__ void vb_group_append_kernel(uint32_t *adj, uint32_t *deg, uint32_t r, uint32_t nc, const uint32_t *offs,
-                                       const uint32_t *tgt, uint32_t *tgt_sorted, uint32_t *need) {
+                                       const uint32_t *tgt, uint32_t *tgt_sorted, uint32_t *need, uint32_t pmax,
+                                       uint32_t pmax_big, uint32_t *glist, uint32_t *gcount, uint32_t *glist_big,
+                                       uint32_t *gcount_big) {
     const int lane = threadIdx.x & 31;
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
     for (uint32_t s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); s < nc; s += warps) {
@@ -705,9 +687,261 @@ __global__ void vb_group_append_kernel(uint32_t *adj, uint32_t *deg, uint32_t r,
         if (dg + added <= r) {
             if (lane == 0) deg[s] = dg + added;
         } else if (lane == 0) {
-            need[s] = dg + added;
+            if (dg + added <= pmax) glist[atomicAdd(gcount, 1u)] = s;  // any order: sources are independent
+            else if (dg + added <= pmax_big) glist_big[atomicAdd(gcount_big, 1u)] = s;
+            else need[s] = dg + added;
         }
     }
+}
+
+// Rebuilds a source's candidate list for a re-prune: its current neighbours, then its sorted
+// targets that are not among them (the order addBackedgeGroupAndPrune appends them in). One
+// warp; returns the count.
+__device__ uint32_t vb_merged_list(const uint32_t *row, uint32_t dg, const uint32_t *targets, uint32_t t,
+                                   uint32_t *ids) {
+    const int lane = threadIdx.x & 31;
+    for (uint32_t i = lane; i < dg; i += 32) ids[i] = row[i];
+    const uint32_t n0 = lane < dg ? row[lane] : kNoNode, n1 = lane + 32 < dg ? row[lane + 32] : kNoNode;
+    uint32_t added = 0;
+    for (uint32_t base = 0; base < t; base += 32) {
+        const uint32_t i = base + lane;
+        const uint32_t v = i < t ? targets[i] : kNoNode;
+        bool present = v == kNoNode;
+        for (uint32_t j = 0; j < dg; ++j) {
+            const uint32_t nb = j < 32 ? __shfl_sync(0xffffffffu, n0, j) : __shfl_sync(0xffffffffu, n1, j - 32);
+            present |= nb == v;
+        }
+        const unsigned mk = __ballot_sync(0xffffffffu, !present);
+        if (!present) ids[dg + added + __popc(mk & lanemask_lt())] = v;
+        added += __popc(mk);
+    }
+    __syncwarp();
+    return dg + added;
+}
+
+// Group pass 2a: re-prune of one source per CTA with every candidate code in shared memory.
+// All pairwise centred code products (and those with the source) are computed first, in
+// parallel, as an integer Gram matrix; the selection then runs on one warp and finishes each
+// distance it needs in double precision from the cached product, lhs = the candidate being
+// checked, rhs = the selected neighbour, as robust_prune_4bit does.
+// kPmax candidates per CTA: the small configuration fits two or three CTAs per SM, the big one
+// (lists grown by many back-edges at once, early in the build) one CTA of eight warps per SM.
+template <int D, bool kBig>
+struct GramCfg {
+    static constexpr int kPmax = kBig ? 150 : (D >= 2048 ? 79 : (D >= 1024 ? 95 : 127));
+    static constexpr int kThreads = 256;
+    static constexpr int kSlots = kPmax + 1;                // + the source
+    static constexpr int kRows = (kSlots + 15) / 16 * 16;   // MMA row blocks of 16
+    static constexpr int kCodeBytes = D / 2;
+    static constexpr int kStride = kCodeBytes + 16;         // padded: rows start in different banks
+    // the codes, then (after the Gram) the distance matrix, share the first region
+    static constexpr size_t kCodesBytes = static_cast<size_t>(kRows) * kStride;
+    static constexpr size_t kDmatBytes = static_cast<size_t>(kSlots) * kSlots * 4;
+    static constexpr size_t kOffLut = ((kCodesBytes > kDmatBytes ? kCodesBytes : kDmatBytes) + 15) & ~static_cast<size_t>(15);
+    static constexpr size_t kOffAux = kOffLut + 256 * 4;
+    static constexpr size_t kOffGram = kOffAux + static_cast<size_t>(kSlots) * sizeof(VbAux);
+    static constexpr size_t kGramWords = static_cast<size_t>(kSlots) * (kSlots - 1) / 2;
+    static constexpr size_t kOffKeys = kOffGram + ((kGramWords * 4 + 15) & ~static_cast<size_t>(15));
+    static constexpr size_t kOffOrder = kOffKeys + kPmax * 8;
+    static constexpr size_t kOffMind = kOffOrder + kPmax * 4;
+    static constexpr size_t kOffIds = kOffMind + kPmax * 4;
+    static constexpr size_t kOffState = kOffIds + kPmax * 4;
+    static constexpr size_t kOffMisc = (kOffState + kPmax + 15) & ~static_cast<size_t>(15);
+    static constexpr size_t kBytes = kOffMisc + 16;
+};
+
+// D = A B + C, m16n8k16, bf16 inputs, f32 accumulate (row-major A, column-major B).
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                               uint32_t b0, uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t tri_index(uint32_t i, uint32_t j) {  // i != j
+    const uint32_t lo = min(i, j), hi = max(i, j);
+    return hi * (hi - 1) / 2 + lo;
+}
+
+struct VbGramArgs {
+    const uint4 *codes;
+    const VbAux *aux;
+    uint32_t *adj;
+    uint32_t *deg;
+    uint32_t r;
+    const uint32_t *offs;
+    const uint32_t *tgt_sorted;
+    const uint32_t *glist;
+    const uint32_t *gcount;
+    PruneCfg cfg;
+    unsigned int *work;
+    unsigned long long *evals;
+};
+
+template <int D, bool kBig>
+__global__ void __launch_bounds__(GramCfg<D, kBig>::kThreads) vb_group_gram_kernel(VbGramArgs a) {
+    using Cfg = GramCfg<D, kBig>;
+    extern __shared__ __align__(16) unsigned char gsm[];
+    uint32_t *lut = reinterpret_cast<uint32_t *>(gsm + Cfg::kOffLut);
+    VbAux *saux = reinterpret_cast<VbAux *>(gsm + Cfg::kOffAux);
+    uint32_t *gram = reinterpret_cast<uint32_t *>(gsm + Cfg::kOffGram);
+    unsigned long long *keys = reinterpret_cast<unsigned long long *>(gsm + Cfg::kOffKeys);
+    uint32_t *order = reinterpret_cast<uint32_t *>(gsm + Cfg::kOffOrder);
+    float *mind = reinterpret_cast<float *>(gsm + Cfg::kOffMind);
+    uint32_t *ids = reinterpret_cast<uint32_t *>(gsm + Cfg::kOffIds);
+    uint8_t *state = gsm + Cfg::kOffState;
+    uint32_t *misc = reinterpret_cast<uint32_t *>(gsm + Cfg::kOffMisc);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int kChunks = D / 32;
+    constexpr int kG = Geo<D>::kG, kPer = Geo<D>::kPer, kCands = Geo<D>::kCands;
+    const int grp = lane / kG, g = lane % kG;
+    const uint32_t total = *a.gcount;
+    unsigned long long evals = 0;
+    for (int b = tid; b < 256; b += blockDim.x) {  // byte -> (bf16(2 lo - 15), bf16(2 hi - 15))
+        const __nv_bfloat162 v = __floats2bfloat162_rn(static_cast<float>(2 * (b & 15) - 15),
+                                                       static_cast<float>(2 * (b >> 4) - 15));
+        lut[b] = *reinterpret_cast<const uint32_t *>(&v);
+    }
+    for (;;) {
+        if (tid == 0) misc[0] = atomicAdd(a.work, 1u);
+        __syncthreads();
+        const uint32_t item = misc[0];
+        if (item >= total) break;
+        const uint32_t s = a.glist[item];
+        uint32_t *row = a.adj + static_cast<size_t>(s) * a.r;
+        if (warp == 0) {
+            const uint32_t b = a.offs[s];
+            const uint32_t m = vb_merged_list(row, a.deg[s], a.tgt_sorted + b, a.offs[s + 1] - b, ids);
+            if (lane == 0) misc[1] = m;
+        }
+        __syncthreads();
+        const uint32_t m = misc[1];  // <= kPmax (the append pass routes larger lists elsewhere)
+        // stage codes and factors: slots 0..m-1 the candidates, slot m the source
+        // asynchronous copies: every chunk in flight at once, no register round trip
+        for (uint32_t x = tid; x < (m + 1) * kChunks; x += blockDim.x) {
+            const uint32_t slot = x / kChunks, c = x % kChunks;
+            const uint32_t node = slot < m ? ids[slot] : s;
+            const uint32_t dst = static_cast<uint32_t>(__cvta_generic_to_shared(gsm + slot * Cfg::kStride + c * 16));
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(dst),
+                         "l"(a.codes + static_cast<size_t>(node) * kChunks + c)
+                         : "memory");
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        for (uint32_t slot = tid; slot <= m; slot += blockDim.x) saux[slot] = a.aux[slot < m ? ids[slot] : s];
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        __syncthreads();
+        // Gram of slots 0..m on the tensor cores: the centred codes 2a - 15 are integers of at most
+        // 15 in magnitude, exact in bf16, and every partial sum of their products (at most
+        // 225 D < 2^24) is exact in the f32 accumulator, so the products come out exact. Tiles of
+        // 16 x 16 on and above the diagonal; fragments built from the packed nibbles through the
+        // byte -> bf16 pair table. Rows past m hold stale codes and are never stored.
+        {
+            const int Q = static_cast<int>((m + 1 + 15) / 16);
+            const int ntiles = Q * (Q + 1) / 2;
+            const int gq = lane >> 2, tq = lane & 3;
+            for (int ti = warp; ti < ntiles; ti += static_cast<int>(blockDim.x >> 5)) {
+                int q = 0, rem = ti;
+                while (rem >= Q - q) {
+                    rem -= Q - q;
+                    ++q;
+                }
+                const int c = q + rem;
+                const uint8_t *ra0 = gsm + (16 * q + gq) * Cfg::kStride + tq;
+                const uint8_t *ra1 = ra0 + 8 * Cfg::kStride;
+                const uint8_t *rb0 = gsm + (16 * c + gq) * Cfg::kStride + tq;
+                const uint8_t *rb1 = rb0 + 8 * Cfg::kStride;
+                float acc0[4] = {0.f, 0.f, 0.f, 0.f}, acc1[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
+                for (int ks = 0; ks < D / 16; ++ks) {
+                    const int o = ks * 8;
+                    const uint32_t a0 = lut[ra0[o]], a1 = lut[ra1[o]], a2 = lut[ra0[o + 4]], a3 = lut[ra1[o + 4]];
+                    const uint32_t b00 = lut[rb0[o]], b01 = lut[rb0[o + 4]];
+                    const uint32_t b10 = lut[rb1[o]], b11 = lut[rb1[o + 4]];
+                    mma_bf16_16816(acc0, a0, a1, a2, a3, b00, b01);
+                    mma_bf16_16816(acc1, a0, a1, a2, a3, b10, b11);
+                }
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    const float v = k < 4 ? acc0[k] : acc1[k - 4];
+                    const uint32_t i = 16 * q + gq + ((k & 2) ? 8 : 0);
+                    const uint32_t j = 16 * c + ((k & 4) ? 8 : 0) + 2 * tq + (k & 1);
+                    if (i < j && j <= m) gram[j * (j - 1) / 2 + i] = static_cast<uint32_t>(__float2int_rn(v));
+                }
+            }
+        }
+        __syncthreads();
+        // every distance the selection can need, in parallel: dmat[i][j] = d(lhs i, rhs j) over
+        // slots 0..m (row m = the source), written over the codes (no longer needed)
+        float *dmat = reinterpret_cast<float *>(gsm);
+        const uint32_t w = m + 1;
+#pragma unroll 2
+        for (uint32_t x = tid; x < w * w; x += blockDim.x) {
+            const uint32_t i = x / w, j = x % w;
+            if (i == j || j == m) continue;
+            dmat[x] = sym_distance_exact(saux[i], saux[j], static_cast<int32_t>(gram[tri_index(i, j)]));
+        }
+        __syncthreads();
+        evals += (m * m) / blockDim.x + (tid < (m * m) % blockDim.x ? 1 : 0);
+        for (uint32_t i = tid; i < m; i += blockDim.x) keys[i] = make_key(dmat[m * w + i], ids[i]);
+        __syncthreads();
+        for (uint32_t i = tid; i < m; i += blockDim.x) {
+            const unsigned long long k = keys[i];
+            uint32_t rank = 0;
+            for (uint32_t j = 0; j < m; ++j) rank += keys[j] < k;  // ids distinct: no ties
+            order[rank] = i;
+            mind[rank] = __int_as_float(0x7fc00000);
+            state[rank] = 0;
+        }
+        __syncthreads();
+        // selection: every warp scans the same shared state and finds the same candidate; the
+        // updates of the live candidates are spread over the block
+        {
+            const float a_lo = a.cfg.alphas[0], a_hi = a.cfg.alphas[a.cfg.npass - 1];
+            uint32_t nsel = 0;
+            for (int p = 0; p < a.cfg.npass && nsel < a.r; ++p) {
+                const float alpha = a.cfg.alphas[p];
+                uint32_t i = 0;
+                while (nsel < a.r) {
+                    int found = -1;
+                    for (uint32_t base = i; base < m; base += 32) {
+                        const uint32_t x = base + lane;
+                        bool ok = false;
+                        if (x < m && state[x] == 0) ok = !(alpha * mind[x] <= key_dist(keys[order[x]]));
+                        const unsigned mk = __ballot_sync(0xffffffffu, ok);
+                        if (mk) {
+                            found = static_cast<int>(base) + __ffs(mk) - 1;
+                            break;
+                        }
+                    }
+                    __syncthreads();  // every warp has scanned before anything changes
+                    if (found < 0) break;
+                    const uint32_t fslot = order[found];
+                    if (tid == 0) {
+                        row[nsel] = ids[fslot];
+                        state[found] = 1;
+                    }
+                    ++nsel;
+                    if (nsel == a.r) break;
+                    for (uint32_t x = tid; x < m; x += blockDim.x) {
+                        if (x == static_cast<uint32_t>(found) || state[x] != 0) continue;
+                        const uint32_t cs = order[x];
+                        const float nm = fminf(mind[x], dmat[cs * w + fslot]);
+                        mind[x] = nm;
+                        const float dist = key_dist(keys[cs]);
+                        if (a_hi * nm <= dist && a_lo * nm <= dist) state[x] = 2;
+                    }
+                    __syncthreads();
+                    i = static_cast<uint32_t>(found) + 1;
+                }
+            }
+            if (tid == 0) a.deg[s] = nsel;
+        }
+        __syncthreads();
+    }
+    for (int o = 16; o > 0; o >>= 1) evals += __shfl_xor_sync(0xffffffffu, evals, o);
+    if (lane == 0 && evals) atomicAdd(a.evals, evals);
 }
 
 // Group pass 2: sources whose list grew past R: candidates = old neighbours then the appended
@@ -842,7 +1076,8 @@ struct Builder {
     uint8_t *pws_state = nullptr;
     uint32_t *pool_n = nullptr;
     uint32_t *cnt = nullptr, *fill = nullptr, *offs = nullptr, *tgt = nullptr, *tgt_sorted = nullptr, *need = nullptr,
-             *noffs = nullptr, *bsum = nullptr;
+             *noffs = nullptr, *bsum = nullptr, *glist = nullptr, *gcount = nullptr, *glist_big = nullptr;
+    int gram_grid = 0, gram_big_grid = 0;
     unsigned int *work = nullptr;
     unsigned long long *evals = nullptr;
     int *error = nullptr;
@@ -860,6 +1095,27 @@ struct Builder {
     uint32_t fresh_cap = 0;
 
     Builder(const VbBuildParams &params, size_t count, cudaStream_t stream) : p(params), n(count), st(stream) {}
+
+    template <bool kBig>
+    static cudaError_t gram_grid_for(int sm_count, int &grid) {
+        int per_sm = 0;
+        VB_TRY(cudaFuncSetAttribute(vb_group_gram_kernel<D, kBig>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(GramCfg<D, kBig>::kBytes)));
+        VB_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, vb_group_gram_kernel<D, kBig>,
+                                                             GramCfg<D, kBig>::kThreads, GramCfg<D, kBig>::kBytes));
+        if (per_sm <= 0) return cudaErrorInvalidConfiguration;
+        grid = sm_count * per_sm;
+        return cudaSuccess;
+    }
+
+    template <bool kBig>
+    cudaError_t launch_gram(const uint32_t *list, const uint32_t *count, int grid) {
+        VB_TRY(cudaMemsetAsync(work, 0, sizeof(unsigned int), st));
+        VbGramArgs ga{codes, aux, adj, deg, static_cast<uint32_t>(p.r), offs, tgt_sorted, list, count,
+                      PruneCfg{alphas, npass, static_cast<uint32_t>(p.r)}, work, evals};
+        vb_group_gram_kernel<D, kBig><<<grid, GramCfg<D, kBig>::kThreads, GramCfg<D, kBig>::kBytes, st>>>(ga);
+        return cudaGetLastError();
+    }
 
     cudaError_t scan(const uint32_t *in, size_t len, uint32_t *out) {
         const int nb = static_cast<int>((len + kScanBlock - 1) / kScanBlock);
@@ -928,6 +1184,11 @@ struct Builder {
         pairs_cap = std::max(std::min(std::max<size_t>(p.batch, 1), n), p.refine ? n : 0) * p.r;
         tgt = mem.get<uint32_t>(pairs_cap);
         tgt_sorted = mem.get<uint32_t>(pairs_cap);
+        glist = mem.get<uint32_t>(n);
+        glist_big = mem.get<uint32_t>(n);
+        gcount = mem.get<uint32_t>(2);
+        VB_TRY(gram_grid_for<false>(sm_count, gram_grid));
+        VB_TRY(gram_grid_for<true>(sm_count, gram_big_grid));
         work = mem.get<unsigned int>(1);
         evals = mem.get<unsigned long long>(1);
         error = mem.get<int>(1);
@@ -969,17 +1230,31 @@ struct Builder {
         const size_t slots = static_cast<size_t>(count) * p.r;
         if (slots == 0) return cudaSuccess;
         const unsigned eg = static_cast<unsigned>((slots + 255) / 256);
-        VB_TRY(cudaMemsetAsync(cnt, 0, nc * sizeof(uint32_t), st));
-        VB_TRY(cudaMemsetAsync(fill, 0, nc * sizeof(uint32_t), st));
-        vb_count_kernel<<<eg, 256, 0, st>>>(adj, deg, static_cast<uint32_t>(p.r), first, count, cnt);
-        VB_TRY(scan(cnt, nc, offs));
-        vb_scatter_kernel<<<eg, 256, 0, st>>>(adj, deg, static_cast<uint32_t>(p.r), first, count, offs, fill, tgt);
-        vb_group_append_kernel<<<group_grid, 256, 0, st>>>(adj, deg, static_cast<uint32_t>(p.r), nc, offs, tgt,
-                                                           tgt_sorted, need);
-        VB_TRY(scan(need, nc, noffs));
+        VB_TRY(sub(0, [&] {
+            VB_TRY(cudaMemsetAsync(cnt, 0, nc * sizeof(uint32_t), st));
+            VB_TRY(cudaMemsetAsync(fill, 0, nc * sizeof(uint32_t), st));
+            vb_count_kernel<<<eg, 256, 0, st>>>(adj, deg, static_cast<uint32_t>(p.r), first, count, cnt);
+            return cudaGetLastError();
+        }));
+        VB_TRY(sub(1, [&] { return scan(cnt, nc, offs); }));
+        VB_TRY(sub(2, [&] {
+            vb_scatter_kernel<<<eg, 256, 0, st>>>(adj, deg, static_cast<uint32_t>(p.r), first, count, offs, fill,
+                                                  tgt);
+            VB_TRY(cudaMemsetAsync(gcount, 0, 2 * sizeof(uint32_t), st));
+            vb_group_append_kernel<<<group_grid, 256, 0, st>>>(adj, deg, static_cast<uint32_t>(p.r), nc, offs, tgt,
+                                                               tgt_sorted, need, GramCfg<D, false>::kPmax,
+                                                               GramCfg<D, true>::kPmax, glist, gcount, glist_big,
+                                                               gcount + 1);
+            return cudaGetLastError();
+        }));
+        VB_TRY(sub(3, [&] { return launch_gram<false>(glist, gcount, gram_grid); }));
+        VB_TRY(sub(4, [&] { return launch_gram<true>(glist_big, gcount + 1, gram_big_grid); }));
         uint32_t total = 0;
-        VB_TRY(cudaMemcpyAsync(&total, noffs + nc, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-        VB_TRY(cudaStreamSynchronize(st));
+        VB_TRY(sub(5, [&] {
+            VB_TRY(scan(need, nc, noffs));
+            VB_TRY(cudaMemcpyAsync(&total, noffs + nc, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+            return cudaStreamSynchronize(st);
+        }));
         if (total == 0) return cudaSuccess;
         if (total > gws_cap) {
             mem.release(gws_keys);
@@ -996,8 +1271,10 @@ struct Builder {
         VbGroupPruneArgs a{codes, aux, adj, deg, static_cast<uint32_t>(p.r), nc, offs, tgt_sorted, need, noffs,
                            PruneCfg{alphas, npass, static_cast<uint32_t>(p.r)}, gws_keys, gws_mind, gws_state,
                            gws_ids, evals};
-        vb_group_prune_kernel<D><<<group_grid, kWarpsPerBlock * 32, 0, st>>>(a);
-        return cudaGetLastError();
+        return sub(6, [&] {
+            vb_group_prune_kernel<D><<<group_grid, kWarpsPerBlock * 32, 0, st>>>(a);
+            return cudaGetLastError();
+        });
     }
 
     cudaError_t check_error() {
@@ -1011,6 +1288,17 @@ struct Builder {
     // refinement phases to stderr; it synchronises around every stage.
     bool trace = false;
     double t_stage[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    double t_sub[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // back-edge sub-stages
+    template <typename F>
+    cudaError_t sub(int k, F f) {
+        if (!trace) return f();
+        VB_TRY(cudaStreamSynchronize(st));
+        const auto t0 = std::chrono::steady_clock::now();
+        VB_TRY(f());
+        VB_TRY(cudaStreamSynchronize(st));
+        t_sub[k] += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return cudaSuccess;
+    }
     template <typename F>
     cudaError_t timed(int phase, int stage, F f) {
         if (!trace) return f();
@@ -1063,6 +1351,11 @@ struct Builder {
                          "vamana build: bulk search %.3f s prune %.3f s back-edges %.3f s | refine search %.3f s "
                          "prune %.3f s back-edges %.3f s\n",
                          t_stage[0][0], t_stage[0][1], t_stage[0][2], t_stage[1][0], t_stage[1][1], t_stage[1][2]);
+        if (trace)
+            std::fprintf(stderr,
+                         "  back-edges: count %.3f scan %.3f scatter+append %.3f gram %.3f gram-big %.3f need-scan "
+                         "%.3f warp-prune %.3f s\n",
+                         t_sub[0], t_sub[1], t_sub[2], t_sub[3], t_sub[4], t_sub[5], t_sub[6]);
         return cudaSuccess;
     }
 };
