@@ -85,6 +85,11 @@ bool rabitq_encode_full(const void *space, const float *raw, void *encoded_out);
 bool rabitq_copy_compact(const void *space, const void *full_encoded, void *compact_out);
 /* rabitq_bridge.cpp:214-222 */
 bool rabitq_copy_residual_record(const void *space, const void *full_encoded, void *residual_out);
+/* The rotation's sign vector (code_dim floats, +-1/sqrt(D)): read it, or replace it as
+ * RaBitQSpace::loadState does with stored signs (space_rabitq.h:3318-3336; a set centre is
+ * re-rotated). Used to save and load the EXRBTQ31 space state. */
+bool qg_space_signs(const void *space, float *out);
+bool qg_space_set_signs(void *space, const float *signs);
 /* rabitq_bridge.cpp:224-303: the reference's Vamana build (bulk insertion in batches,
  * refinement passes, grouped back-edges, robust_prune_4bit over the symmetric 4-bit estimator),
  * run on the GPU; the same graph as the reference for the same arguments. Host buffers; also

@@ -368,6 +368,20 @@ class Reference:
                                                 C.c_size_t(residual.shape[1]), _p(long_d), _p(out))
         return out
 
+    def save_state(self) -> bytes:
+        """RaBitQSpace::saveState of the reference space."""
+        self.lib.qgref_save_state.restype = C.c_size_t
+        buf = np.zeros(1 << 22, np.uint8)
+        n = self.lib.qgref_save_state(self.space, _p(buf), C.c_size_t(buf.size))
+        if n == 0:
+            raise RuntimeError("reference saveState failed")
+        return bytes(buf[:n])
+
+    def load_state(self, state: bytes) -> bool:
+        """RaBitQSpace::loadState into the reference space; False when the reference rejects it."""
+        b = np.frombuffer(state, np.uint8).copy()
+        return bool(self.lib.qgref_load_state(self.space, _p(b), C.c_size_t(b.size)))
+
     def build_graph(self, compact, r=32, l_build=100, alpha=1.2, beam=1, batch=4096, refine=1,
                     cap=256, stop_hops=2):
         compact = np.ascontiguousarray(compact)

@@ -6,6 +6,8 @@
 // kernels, so that golden search results come from the reference's kernels.
 #include <cstdint>
 #include <cstring>
+#include <sstream>
+#include <string>
 #include <vector>
 
 #include <omp.h>
@@ -53,6 +55,33 @@ void qgref_prepared_export(const void *prepared, size_t code_dim, float *rotated
 
 void qgref_rotate(const void *space, const float *raw, float *out) {
     static_cast<const hnswlib::RaBitQSpace *>(space)->rotate(raw, out);
+}
+
+// The reference's RaBitQSpace::saveState (space_rabitq.h:3139-3198) into a buffer; returns the
+// byte count (0 when it does not fit or fails).
+size_t qgref_save_state(const void *space, uint8_t *out, size_t cap) {
+    try {
+        std::ostringstream os(std::ios::binary);
+        static_cast<const hnswlib::RaBitQSpace *>(space)->saveState(os);
+        const std::string bytes = os.str();
+        if (bytes.size() > cap) return 0;
+        std::memcpy(out, bytes.data(), bytes.size());
+        return bytes.size();
+    } catch (...) {
+        return 0;
+    }
+}
+
+// RaBitQSpace::loadState (space_rabitq.h:3200-3345) from a buffer into an existing space;
+// returns 1 on success, 0 when the reference rejects the state.
+int qgref_load_state(void *space, const uint8_t *in, size_t n) {
+    try {
+        std::istringstream is(std::string(reinterpret_cast<const char *>(in), n), std::ios::binary);
+        static_cast<hnswlib::RaBitQSpace *>(space)->loadState(is);
+        return 1;
+    } catch (...) {
+        return 0;
+    }
 }
 
 }  // extern "C"

@@ -117,6 +117,8 @@ _SIGS = {
     "qg_center_mean": (C.c_int, [P, SZ, SZ, P, SZ, P, P]),
     "qg_encode_batch": (C.c_int, [P, P, SZ, P, P, P]),
     "qg_export_sidecar_device": (C.c_int, [P, P, SZ, SZ, P, P, P]),
+    "qg_space_signs": (C.c_bool, [P, P]),
+    "qg_space_set_signs": (C.c_bool, [P, P]),
     "qg_build_vamana_device": (C.c_int, [P, P, SZ, SZ, SZ, SZ, C.c_float, SZ, SZ, SZ, SZ, SZ, P, P, SZ, P, P]),
     "qg_prune_candidates": (C.c_int, [P, P, SZ, SZ, P, SZ, SZ, C.c_float, P, P, SZ, P]),
     "qg_prepare_batch": (C.c_int, [P, P, SZ, P, P, P, P, P]),

@@ -391,6 +391,33 @@ bool rabitq_space_set_center(void *space, const float *center) {
     }
 }
 
+// The rotation's sign vector (+-1/sqrt(D), code_dim floats): read, or replaced as
+// RaBitQSpace::loadState does with the stored fht_signs_ (space_rabitq.h:3318-3336); a set
+// centre is re-rotated with the new signs.
+bool qg_space_signs(const void *space, float *out) {
+    const Space *s = as_space(space);
+    if (!s || !out) return false;
+    std::copy(s->signs.begin(), s->signs.end(), out);
+    return true;
+}
+
+bool qg_space_set_signs(void *space, const float *signs) {
+    try {
+        auto *s = static_cast<Space *>(space);
+        if (!s || !signs) return false;
+        std::copy(signs, signs + s->code_dim, s->signs.begin());
+        if (!cuda_ok(cudaMemcpy(s->d_signs, signs, s->code_dim * 4, cudaMemcpyHostToDevice), "signs upload"))
+            return false;
+        if (s->center_set) {
+            std::vector<float> c(s->center);
+            return rabitq_space_set_center(space, c.data());
+        }
+        return true;
+    } catch (...) {
+        return false;
+    }
+}
+
 bool rabitq_space_set_centroids(void *space, const float *centroids, size_t centroid_count) {
     if (centroid_count != 1) {
         set_error("only one centroid is supported");

@@ -71,6 +71,7 @@ class RabitqSpace:
         if not self.lib.rabitq_space_set_center(self.ptr, center.ctypes.data):
             raise RuntimeError(f"rabitq_space_set_center failed: {N.last_error()}")
         self.center = center
+        self.seed = int(seed)
         self.lib.rabitq_set_query_coarse_codec(self.ptr, codec)
         self.code_dim = self.lib.rabitq_paper_msb_code_bytes(self.ptr) * 8
 

@@ -11,7 +11,7 @@ ours_diskann.rs:1539-1986 (which cannot be built here) is driven over the refere
 bridge kernels (oracle/ref_probe.cpp).
 
 Inputs are regenerated from numpy seeds in the tests; a checksum of each input is stored
-to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants]
+to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants | space_states]
 """
 from __future__ import annotations
 
@@ -131,12 +131,28 @@ def build_variants():
     np.savez_compressed(os.path.join(HERE, "build_variants.npz"), **out)
 
 
+def space_states():
+    """RaBitQSpace::saveState output of the reference for the kernel fixtures' spaces (seed 100,
+    their centres): the EXRBTQ31 bytes a saved space must equal and a loaded one must encode
+    like."""
+    out = {}
+    for name in ("kernels_d128", "kernels_d960", "kernels_d1536"):
+        g = np.load(os.path.join(HERE, name + ".npz"))
+        ref = oracle_py.Reference(int(g["dim"]), g["center"])
+        out[name] = np.frombuffer(ref.save_state(), np.uint8)
+        print(name, "state", out[name].size, "bytes")
+    np.savez_compressed(os.path.join(HERE, "space_states.npz"), **out)
+
+
 def main():
     oracle_py.build(ref=True)
     if not oracle_py.reference_available():
         raise SystemExit("the reference library could not be built")
     if sys.argv[1:] == ["build_variants"]:
         build_variants()
+        return
+    if sys.argv[1:] == ["space_states"]:
+        space_states()
         return
     kernel_case("kernels_d128", 128, 64, 8, seed=20260813, center_value=0.05)
     kernel_case("kernels_d100", 100, 48, 4, seed=5, center_value=None)
@@ -150,6 +166,7 @@ def main():
     search_case("search_c3", c3_data, 1536, 1000, 16, 31, M=32, l_build=64, refine=1, cap=256, stop=2,
                 batch=256, Ls=(40,))
     build_variants()
+    space_states()
     with open(os.path.join(HERE, "PROVENANCE.txt"), "w") as f:
         f.write(f"generated by tests/golden/make_golden.py on {platform.machine()} {platform.processor()}\n")
         f.write(f"reference bridge compiled with: {FLAGS}\n")
