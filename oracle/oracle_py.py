@@ -63,9 +63,9 @@ class _Lib:
 
 
 class Oracle:
-    """The restatement: one space (seed 100 by default), INT8 query codec."""
+    """The restatement: one space (seed 100 by default), INT8 query codec (or INT4, codec=2)."""
 
-    def __init__(self, dim: int, center: np.ndarray, seed: int = 100):
+    def __init__(self, dim: int, center: np.ndarray, seed: int = 100, codec: int = 3):
         self.lib = lib = _Lib.load(ORACLE_SO)
         lib.qgo_space_new.restype = C.c_void_p
         lib.qgo_space_new.argtypes = [C.c_size_t, C.c_uint32]
@@ -91,6 +91,8 @@ class Oracle:
         self.residual_bytes = lib.qgo_residual_bytes(self.space)
         self.msb_bytes = lib.qgo_msb_bytes(self.space)
         self.prep = C.c_void_p(lib.qgo_prepared_new(self.space))
+        if lib.qgo_space_set_query_codec(self.space, C.c_int(codec)) != 0:
+            raise ValueError("the oracle prepares Int8 (3) and Int4 (2) queries")
 
     def __del__(self):
         try:
@@ -253,7 +255,7 @@ def _search(fn, lead_args, queries, index, k, L, eps, rerank, beam, early_stop, 
 class Reference:
     """The reference's own bridge (rabitq_* entry points) plus the probe accessors."""
 
-    def __init__(self, dim: int, center: np.ndarray, seed: int = 100):
+    def __init__(self, dim: int, center: np.ndarray, seed: int = 100, codec: int = 3):
         self.lib = lib = _Lib.load(REF_SO)
         lib.rabitq_space_new.restype = C.c_void_p
         lib.rabitq_space_new.argtypes = [C.c_size_t, C.c_uint32, C.c_size_t, C.c_size_t, C.c_size_t,
@@ -275,7 +277,7 @@ class Reference:
         self.space = C.c_void_p(lib.rabitq_space_new(dim, seed, 1, 4, 16, True, True))
         self.center = np.ascontiguousarray(center, dtype=np.float32)
         assert lib.rabitq_space_set_center(self.space, _p(self.center))
-        lib.rabitq_set_query_coarse_codec(self.space, C.c_int(3))  # Int8
+        lib.rabitq_set_query_coarse_codec(self.space, C.c_int(codec))  # 3 = Int8, 2 = Int4
         self.full_bytes = lib.rabitq_full_record_bytes(self.space)
         self.compact_bytes = lib.rabitq_compact_record_bytes(self.space)
         self.residual_bytes = lib.rabitq_residual_record_bytes(self.space)

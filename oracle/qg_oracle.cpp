@@ -123,6 +123,7 @@ struct qgo_space {
     size_t residual_bytes = 0;
     size_t msb_bytes = 0;
     uint32_t seed = 100;
+    int query_bits = 8;  // Int8 (codec 3) or Int4 (codec 2)
     std::vector<float> signs;
     std::vector<float> center;
     std::vector<float> rotated_center;
@@ -684,7 +685,8 @@ void qgo_dither_draws(uint64_t seed, size_t count, double *out) {
     for (size_t i = 0; i < count; ++i) out[i] = u01(rng);
 }
 
-// initializePreparedQuery + buildCentroidQuery (space_rabitq.h:3429-3698), INT8 codec.
+// initializePreparedQuery + buildCentroidQuery (space_rabitq.h:3429-3698), INT8 or INT4 codec
+// (qgo_space_set_query_codec); the integer codes of either live in int8_code.
 int qgo_prepare(const qgo_space *sp, const float *query, qgo_prepared *p) {
     const qgo_space &s = *sp;
     const size_t D = s.code_dim;
@@ -712,15 +714,20 @@ int qgo_prepare(const qgo_space *sp, const float *query, qgo_prepared *p) {
     p->code_sum = 0;
     std::fill(p->int8_code.begin(), p->int8_code.end(), 0);
     if (max_abs > 0.0f) {
-        p->int8_scale = max_abs / 128.0f;
+        // Int8: scale max/128, codes in [-128, 127], the first of the two draws per dimension;
+        // Int4: scale max/8, codes in [-8, 7], the second (space_rabitq.h:3538-3655)
+        const bool int4 = s.query_bits == 4;
+        p->int8_scale = max_abs / (int4 ? 8.0f : 128.0f);
+        const int32_t lo = int4 ? -8 : -128, hi = int4 ? 7 : 127;
         std::mt19937_64 rng(qgo_dither_seed(query, s.dim, 0));
         std::uniform_real_distribution<double> u01(0.0, 1.0);
         for (size_t i = 0; i < D; ++i) {
             const double u8 = u01(rng);
-            (void)u01(rng);  // the INT4 draw is consumed too (space_rabitq.h:3630-3631)
+            const double u4 = u01(rng);
             int32_t x = static_cast<int32_t>(std::floor(
-                static_cast<double>(p->rotated_residual[i]) / static_cast<double>(p->int8_scale) + u8));
-            x = std::max(-128, std::min(127, x));
+                static_cast<double>(p->rotated_residual[i]) / static_cast<double>(p->int8_scale) +
+                (int4 ? u4 : u8)));
+            x = std::max(lo, std::min(hi, x));
             p->int8_code[i] = static_cast<int8_t>(x);
             p->code_sum += x;
         }
@@ -1389,5 +1396,12 @@ extern "C" int qgo_build_vamana(const qgo_space *space, const uint8_t *compact, 
         std::copy(st.graph[id].begin(), st.graph[id].end(), edges + id * edge_stride);
     }
     if (evals_out != nullptr) *evals_out = st.evals;
+    return 0;
+}
+
+// rabitq_set_query_coarse_codec for the oracle: 3 = Int8, 2 = Int4; others return -1.
+extern "C" int qgo_space_set_query_codec(qgo_space *space, int codec) {
+    if (!space || (codec != 2 && codec != 3)) return -1;
+    space->query_bits = codec == 2 ? 4 : 8;
     return 0;
 }

@@ -85,7 +85,9 @@ int qgo_export_sidecar(const qgo_space *space, const uint8_t *compact, size_t n,
                        uint8_t *msb_out, void *factors_out);
 float qgo_symmetric_distance(const qgo_space *space, const uint8_t *lhs, const uint8_t *rhs);
 
-/* ---- query preparation (space_rabitq.h:3429-3706), INT8 codec ---- */
+/* ---- query preparation (space_rabitq.h:3429-3706), INT8 codec, or INT4 after
+ * qgo_space_set_query_codec(space, 2) ---- */
+int qgo_space_set_query_codec(qgo_space *space, int codec);
 qgo_prepared *qgo_prepared_new(const qgo_space *space);
 void qgo_prepared_delete(qgo_prepared *prepared);
 int qgo_prepare(const qgo_space *space, const float *query, qgo_prepared *prepared);

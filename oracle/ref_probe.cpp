@@ -37,20 +37,22 @@ bool rabitq_residual_distance_batch(const void *space, const void *prepared,
                                     size_t residual_stride, const float *long_distances,
                                     RabitqDistanceInterval *out);
 
-// scalars: [query_norm_sqr, query_norm, half_sum_residual, int8_scale]
+// scalars: [query_norm_sqr, query_norm, half_sum_residual, int8 (or int4) scale]
 void qgref_prepared_export(const void *prepared, size_t code_dim, float *rotated_residual,
                            int8_t *codes, float *scalars, int64_t *code_sum) {
     const auto &p = *static_cast<const hnswlib::RaBitQSpace::PreparedQuery *>(prepared);
     const auto &q = p.centroid_queries[0];
+    const bool int4 = p.query_coarse_codec == hnswlib::QueryCoarseCodec::Int4;
+    const auto &ic = int4 ? q.int4_code : q.int8_code;
     if (rotated_residual) std::memcpy(rotated_residual, q.rotated_residual.data(), code_dim * 4);
-    if (codes && q.int8_code.size() >= code_dim) std::memcpy(codes, q.int8_code.data(), code_dim);
+    if (codes && ic.size() >= code_dim) std::memcpy(codes, ic.data(), code_dim);
     if (scalars) {
         scalars[0] = q.query_norm_sqr;
         scalars[1] = q.query_norm;
         scalars[2] = q.half_sum_residual;
-        scalars[3] = q.int8_scale;
+        scalars[3] = int4 ? q.int4_scale : q.int8_scale;
     }
-    if (code_sum) *code_sum = q.int8_code_sum;
+    if (code_sum) *code_sum = int4 ? q.int4_code_sum : q.int8_code_sum;
 }
 
 void qgref_rotate(const void *space, const float *raw, float *out) {

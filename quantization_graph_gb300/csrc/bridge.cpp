@@ -630,8 +630,8 @@ const void *rabitq_prepare_query(const void *space, const float *query) {
     try {
         const Space *s = as_space(space);
         if (!s || !query) return nullptr;
-        if (s->codec != 3) {
-            set_error("the GPU query path implements the Int8 query codec (3) only");
+        if (s->codec != 3 && s->codec != 2) {
+            set_error("the GPU query path implements the Int8 (3) and Int4 (2) query codecs");
             return nullptr;
         }
         Prepared &p = t_prepared;
@@ -1000,10 +1000,15 @@ int qg_prepare_batch(const void *space, const float *d_queries, size_t nq, float
         set_error("set the centre before preparing queries");
         return QG_ERR_INVALID;
     }
+    if (!space_query_bits(s)) {
+        set_error("the GPU query path implements the Int8 (3) and Int4 (2) query codecs");
+        return QG_ERR_INVALID;
+    }
     PrepArgs a{d_queries, s->dim, static_cast<int>(nq), static_cast<int>(s->dim),
                static_cast<int>(s->code_dim), s->d_signs, s->d_center, s->d_rotated_center,
                s->d_center_norm, d_rotated, d_codes, reinterpret_cast<float4 *>(d_scalars),
                reinterpret_cast<long long *>(d_code_sum)};
+    a.qbits = space_query_bits(s);
     if (!cuda_ok(launch_prepare(a, static_cast<cudaStream_t>(stream)), "prepare kernel")) return QG_ERR_CUDA;
     return QG_OK;
 }
@@ -1449,9 +1454,14 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
     }
     if (nq == 0) return QG_OK;
     {
+        if (!space_query_bits(s)) {
+            set_error("the GPU query path implements the Int8 (3) and Int4 (2) query codecs");
+            return QG_ERR_INVALID;
+        }
         PrepArgs pa{d_queries, s->dim, static_cast<int>(nq), static_cast<int>(s->dim),
                     static_cast<int>(s->code_dim), s->d_signs, s->d_center, s->d_rotated_center,
                     s->d_center_norm, index->q.rr, index->q.codes, index->q.scal, index->q.csum, d_nq};
+        pa.qbits = space_query_bits(s);
         if (!cuda_ok(launch_prepare(pa, st), "prepare kernel")) return QG_ERR_CUDA;
     }
     if (!cuda_ok(cudaMemsetAsync(index->counter, 0, 4, st), "counter reset") ||

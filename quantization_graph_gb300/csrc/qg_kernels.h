@@ -26,6 +26,7 @@ struct PrepArgs {
     float4 *scal;
     long long *csum;
     const int *nq_dev;  // optional: the batch size read on the device (CUDA-graph replay)
+    int qbits = 8;      // 8: Int8 query codec; 4: Int4 (scale max/8, codes in [-8, 7], second draw)
 };
 
 struct SearchArgs {

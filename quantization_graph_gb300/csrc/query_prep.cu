@@ -286,19 +286,23 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(PrepArgs a) {
 
     const float qn2 = s_qn2;
     const float max_abs = s_max;
-    const float scale = max_abs > 0.0f ? max_abs / 128.0f : 1.0f;
+    const bool int4 = a.qbits == 4;  // Int4: max/8, [-8, 7], the second draw (space_rabitq.h:3538-3655)
+    const float scale = max_abs > 0.0f ? max_abs / (int4 ? 8.0f : 128.0f) : 1.0f;
+    const int vlo = int4 ? -8 : -128, vhi = int4 ? 7 : 127;
     // below this the quotient's FMA remainder may underflow: take the double expression
     const bool fast = scale >= 0x1p-100f;
     int csum = 0;
     int8_t *codes = a.codes + static_cast<size_t>(q) * D;
     if (max_abs > 0.0f) {
-        // Two draws per dimension, the first used by INT8 (space_rabitq.h:3625-3643).
+        // Two draws per dimension, the first used by INT8, the second by INT4
+        // (space_rabitq.h:3625-3655).
         const int draws = 2 * D;
+        const int parity = int4 ? 1 : 0;
         for (int base = 0; base < draws; base += kMtN) {
             mt_twist(mt);
             for (int p = threadIdx.x; p < kMtN; p += 128) {
                 const int j = base + p;
-                if (j < draws && (j & 1) == 0) {
+                if (j < draws && (j & 1) == parity) {
                     const int i = j >> 1;
                     const unsigned long long K = mt_temper(mt[p]);
                     bool undecided = !fast;
@@ -307,7 +311,7 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(PrepArgs a) {
                         const double u = canonical_u01(K);
                         v = static_cast<int>(floor(static_cast<double>(x[i]) / static_cast<double>(scale) + u));
                     }
-                    v = max(-128, min(127, v));
+                    v = max(vlo, min(vhi, v));
                     codes[i] = static_cast<int8_t>(v);
                     csum += v;
                 }

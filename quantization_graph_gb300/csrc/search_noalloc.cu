@@ -142,10 +142,13 @@ extern "C" int qg_search_batch_noalloc(qg_index *index, const float *d_queries, 
         (e = cudaMemsetAsync(sb + o_tags, 0, slots * row_bytes, st)) != cudaSuccess)
         return fail(QG_ERR_CUDA, std::string("qg_search_batch_noalloc: clear: ") + cudaGetErrorString(e));
 
+    if (!space_query_bits(s))
+        return fail(QG_ERR_INVALID, "qg_search_batch_noalloc: the Int8 (3) and Int4 (2) query codecs only");
     PrepArgs pa{d_queries, s->dim, static_cast<int>(nq), static_cast<int>(s->dim), static_cast<int>(D),
                 s->d_signs, s->d_center, s->d_rotated_center, s->d_center_norm,
                 reinterpret_cast<float *>(sb + o_rr), reinterpret_cast<int8_t *>(sb + o_codes),
                 reinterpret_cast<float4 *>(sb + o_scal), reinterpret_cast<long long *>(sb + o_csum)};
+    pa.qbits = space_query_bits(s);
     if ((e = launch_prepare(pa, st)) != cudaSuccess)
         return fail(QG_ERR_CUDA, std::string("qg_search_batch_noalloc: prepare: ") + cudaGetErrorString(e));
 

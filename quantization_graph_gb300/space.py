@@ -123,7 +123,8 @@ class RabitqSpace:
         return msb, factors
 
     def prepare(self, queries: torch.Tensor) -> dict:
-        """Batched INT8 query preparation (prepare_query, space_rabitq.h:3700)."""
+        """Batched INT8 (or INT4, by the space's codec) query preparation (prepare_query,
+        space_rabitq.h:3700)."""
         q = _cuda(queries, torch.float32)
         nq = q.shape[0]
         D = self.code_dim

@@ -11,7 +11,7 @@ ours_diskann.rs:1539-1986 (which cannot be built here) is driven over the refere
 bridge kernels (oracle/ref_probe.cpp).
 
 Inputs are regenerated from numpy seeds in the tests; a checksum of each input is stored
-to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants | space_states]
+to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants | space_states | int4]
 """
 from __future__ import annotations
 
@@ -38,17 +38,17 @@ def sha(a: np.ndarray) -> str:
     return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
-def kernel_case(name: str, dim: int, n: int, nq: int, seed: int, center_value: float | None):
-    """Kernel-level golden vectors for every query x every record."""
+def kernel_case(name: str, dim: int, n: int, nq: int, seed: int, center_value: float | None, codec: int = 3):
+    """Kernel-level golden vectors for every query x every record (codec 3 = Int8, 2 = Int4)."""
     X, Q = kernel_inputs(dim, n, nq, seed)
     center = (np.full(dim, center_value, np.float32) if center_value is not None
               else X.mean(0).astype(np.float32))
-    ref = oracle_py.Reference(dim, center)
+    ref = oracle_py.Reference(dim, center, codec=codec)
     full = np.stack([ref.encode_full(x) for x in X])
     compact, residual = ref.encode(X)
     msb, factors = ref.sidecar(compact)
     ids = np.arange(n, dtype=np.uint32)
-    out = dict(dim=dim, n=n, nq=nq, seed=seed, center=center, x_sha=sha(X), q_sha=sha(Q), full=full,
+    out = dict(dim=dim, n=n, nq=nq, seed=seed, codec=codec, center=center, x_sha=sha(X), q_sha=sha(Q), full=full,
                compact=compact, residual=residual, msb=msb, factors=factors)
     rr, codes, scal, csum, gate, d2, d0, res, dsingle = [], [], [], [], [], [], [], [], []
     for q in Q:
@@ -131,6 +131,26 @@ def build_variants():
     np.savez_compressed(os.path.join(HERE, "build_variants.npz"), **out)
 
 
+def int4_cases():
+    """The Int4 query codec (an ablation in the reference): kernel vectors for 128-d and 1536-d,
+    and search results on the search_c1 index."""
+    kernel_case("kernels_d128_int4", 128, 64, 8, seed=20260813, center_value=0.05, codec=2)
+    kernel_case("kernels_d1536_int4", 1536, 64, 3, seed=7, center_value=None, codec=2)
+    g = np.load(os.path.join(HERE, "search_c1.npz"))
+    _, Q = c1_data()
+    ref = oracle_py.Reference(128, g["center"], codec=2)
+    index = dict(compact=g["compact"], residual=g["residual"], msb=g["msb"], factors=g["factors"],
+                 degrees=g["degrees"], edges=g["edges"], total_points=int(g["n"]), base_points=int(g["n"]))
+    out = {}
+    for L in (20, 40, 80):
+        ids, dists, stats = ref.search(Q, index, k=10, L=L, eps=1.9, rerank=100)
+        out[f"ids_L{L}"] = ids
+        out[f"dists_L{L}"] = dists
+        out[f"stats_L{L}"] = stats.view(np.uint64).reshape(len(Q), -1)
+    np.savez_compressed(os.path.join(HERE, "search_c1_int4.npz"), **out)
+    print("search_c1_int4 written")
+
+
 def space_states():
     """RaBitQSpace::saveState output of the reference for the kernel fixtures' spaces (seed 100,
     their centres): the EXRBTQ31 bytes a saved space must equal and a loaded one must encode
@@ -154,6 +174,9 @@ def main():
     if sys.argv[1:] == ["space_states"]:
         space_states()
         return
+    if sys.argv[1:] == ["int4"]:
+        int4_cases()
+        return
     kernel_case("kernels_d128", 128, 64, 8, seed=20260813, center_value=0.05)
     kernel_case("kernels_d100", 100, 48, 4, seed=5, center_value=None)
     kernel_case("kernels_d960", 960, 96, 4, seed=6, center_value=None)
@@ -167,6 +190,7 @@ def main():
                 batch=256, Ls=(40,))
     build_variants()
     space_states()
+    int4_cases()
     with open(os.path.join(HERE, "PROVENANCE.txt"), "w") as f:
         f.write(f"generated by tests/golden/make_golden.py on {platform.machine()} {platform.processor()}\n")
         f.write(f"reference bridge compiled with: {FLAGS}\n")

@@ -1,8 +1,9 @@
 """The drop-in boundary itself: the reference bridge's rabitq_* entry points of this library,
 called exactly as the Rust side calls the reference's (ours_diskann.rs:45-242), against the
 golden vectors the reference produced (encode, copies, sidecar, symmetric distance, the
-batched gate / distance / residual kernels, the single-record restore) and against the
-reference's sentinels for what is not built."""
+batched gate / distance / residual kernels, the single-record restore; Int8 and Int4 query
+codecs) and against the reference's sentinels for what is not built (the B1 / Full codecs).
+rabitq_build_vamana_graph is covered by test_gpu_vamana_build.py."""
 import ctypes as C
 
 import numpy as np
@@ -13,7 +14,8 @@ from conftest import load_golden
 
 pytestmark = pytest.mark.gpu
 
-KERNEL_CASES = ["kernels_d128", "kernels_d100", "kernels_d960", "kernels_d1536"]
+KERNEL_CASES = ["kernels_d128", "kernels_d100", "kernels_d960", "kernels_d1536", "kernels_d128_int4",
+                "kernels_d1536_int4"]
 
 
 def _p(a):
@@ -31,12 +33,12 @@ def lib(cuda):
     return N.load()
 
 
-def _space(lib, dim, center):
+def _space(lib, dim, center, codec=3):
     sp = C.c_void_p(lib.rabitq_space_new(dim, 100, 1, 4, 16, True, True))
     assert sp.value
     c = np.ascontiguousarray(center, np.float32)
     assert lib.rabitq_space_set_center(sp, _p(c))
-    lib.rabitq_set_query_coarse_codec(sp, 3)  # Int8, as the formal path sets it
+    lib.rabitq_set_query_coarse_codec(sp, codec)  # Int8 (3), as the formal path sets it, or Int4 (2)
     return sp
 
 
@@ -84,7 +86,7 @@ def test_prepared_query_kernels(lib, name):
     g = load_golden(name)
     dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
     _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
-    sp = _space(lib, dim, g["center"])
+    sp = _space(lib, dim, g["center"], int(g.get("codec", 3)))
     try:
         compact, residual, msb, factors = g["compact"], g["residual"], g["msb"], g["factors"]
         ids = np.arange(n, dtype=np.uint32)
@@ -132,13 +134,5 @@ def test_sentinels_of_what_is_not_built(lib):
         assert np.isinf(lib.rabitq_query_distance_with_paper(sp, prep, _p(rec), C.c_float(0.0)))
         lib.rabitq_set_query_coarse_codec(sp, 1)  # B1: not built, no prepared query
         assert not C.c_void_p(lib.rabitq_prepare_query(sp, _p(query))).value
-        n = int(g["n"])
-        deg = np.zeros(n, np.uint32)
-        edges = np.zeros((n, 8), np.uint32)
-        ms, fbytes, ev = C.c_size_t(0), C.c_size_t(0), C.c_uint64(0)
-        assert not lib.rabitq_build_vamana_graph(
-            sp, _p(g["compact"]), n, g["compact"].shape[1], 8, 32, C.c_float(1.2), 1, 64, 1, 256, 2, _p(deg),
-            _p(edges), 8, _p(np.zeros((n, 16), np.uint8)), _p(np.zeros((n, 20), np.uint8)), C.byref(ms),
-            C.byref(fbytes), C.byref(ev))
     finally:
         lib.rabitq_space_delete(sp)

@@ -10,17 +10,18 @@ from conftest import load_golden
 
 pytestmark = pytest.mark.gpu
 
-KERNEL_CASES = ["kernels_d128", "kernels_d100", "kernels_d960", "kernels_d1536"]
+KERNEL_CASES = ["kernels_d128", "kernels_d100", "kernels_d960", "kernels_d1536", "kernels_d128_int4",
+                "kernels_d1536_int4"]
 
 
 def bits(a):
     return np.ascontiguousarray(a).view(np.uint32)
 
 
-def _space(torch, dim, center):
+def _space(torch, dim, center, codec=3):
     from quantization_graph_gb300.space import RabitqSpace
 
-    return RabitqSpace(dim, center)
+    return RabitqSpace(dim, center, codec=codec)
 
 
 @pytest.mark.parametrize("name", KERNEL_CASES)
@@ -43,7 +44,7 @@ def test_prepare_gate_distance_residual_bit_exact(cuda, name):
     g = load_golden(name)
     dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
     _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
-    sp = _space(torch, dim, g["center"])
+    sp = _space(torch, dim, g["center"], int(g.get("codec", 3)))
     p = sp.prepare(torch.from_numpy(Q).cuda())
     np.testing.assert_array_equal(bits(p["rotated_residual"].cpu().numpy()), bits(g["rotated_residual"]))
     np.testing.assert_array_equal(p["codes"].cpu().numpy(), g["codes"])

@@ -163,3 +163,23 @@ def test_other_code_dims_match_oracle(cuda, oracle, dim):
         np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), oi)
         np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(od))
         np.testing.assert_array_equal(stats_matrix(r.stats), stats_matrix(os_))
+
+
+def test_int4_codec_search_matches_reference(cuda):
+    """The Int4 query codec (an ablation in the reference: scale max/8, codes in [-8, 7], the
+    second dither draw) through the batched GPU search, against the reference's own kernels."""
+    torch = cuda
+    from quantization_graph_gb300.index import OursIndex
+    from quantization_graph_gb300.space import RabitqSpace
+
+    g = load_golden("search_c1")
+    v = load_golden("search_c1_int4")
+    _, Q = SEARCH_CASES["search_c1"]()
+    sp = RabitqSpace(128, g["center"], codec=2)
+    ix = OursIndex(sp, g["compact"], g["residual"], g["msb"], g["factors"], g["degrees"], g["edges"])
+    q = torch.from_numpy(Q).cuda()
+    for L in (20, 40, 80):
+        r = ix.search(q, k=10, l_value=L, with_stats=True)
+        np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), v[f"ids_L{L}"])
+        np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(v[f"dists_L{L}"]))
+        np.testing.assert_array_equal(stats_matrix(r.stats), v[f"stats_L{L}"])

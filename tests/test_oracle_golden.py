@@ -9,7 +9,8 @@ import pytest
 from cases import SEARCH_CASES, kernel_inputs
 from conftest import golden_index, load_golden, sha
 
-KERNEL_CASES = ["kernels_d128", "kernels_d100", "kernels_d960", "kernels_d1536"]
+KERNEL_CASES = ["kernels_d128", "kernels_d100", "kernels_d960", "kernels_d1536", "kernels_d128_int4",
+                "kernels_d1536_int4"]
 
 
 def bits(a):
@@ -22,7 +23,7 @@ def test_kernels_bit_exact(oracle, name):
     dim, n, nq, seed = int(g["dim"]), int(g["n"]), int(g["nq"]), int(g["seed"])
     X, Q = kernel_inputs(dim, n, nq, seed)
     assert sha(X) == str(g["x_sha"]) and sha(Q) == str(g["q_sha"]), "input generator drifted"
-    o = oracle.Oracle(dim, g["center"])
+    o = oracle.Oracle(dim, g["center"], codec=int(g.get("codec", 3)))
     full = np.stack([o.encode_full(x) for x in X])
     np.testing.assert_array_equal(full, g["full"])
     compact, residual = o.encode(X)
@@ -151,3 +152,17 @@ def test_vamana_build_variants_match_reference(oracle):
         deg, edges, evals = o.build_graph(g["compact"], **kw)
         _graph_equal(deg, edges, v[f"{name}_degrees"], v[f"{name}_edges"])
         assert evals == int(v[f"{name}_evals"]), name
+
+
+def test_search_loop_int4_bit_exact(oracle):
+    """The Int4 query codec (scale max/8, codes in [-8, 7], the second dither draw) through the
+    whole search, against the reference's own kernels with codec 2."""
+    g = load_golden("search_c1")
+    v = load_golden("search_c1_int4")
+    _, Q = SEARCH_CASES["search_c1"]()
+    o = oracle.Oracle(128, g["center"], codec=2)
+    for L in (20, 40, 80):
+        ids, dists, stats = o.search(Q, golden_index(g), k=10, L=L, eps=1.9, rerank=100)
+        np.testing.assert_array_equal(ids, v[f"ids_L{L}"])
+        np.testing.assert_array_equal(bits(dists), bits(v[f"dists_L{L}"]))
+        np.testing.assert_array_equal(stats.view(np.uint64).reshape(len(Q), -1), v[f"stats_L{L}"])
