@@ -32,7 +32,7 @@ assert PAPER_ESTIMATE.itemsize == 24 and INTERVAL.itemsize == 12
 class SearchParams(C.Structure):
     _fields_ = [("k", C.c_size_t), ("l_value", C.c_size_t), ("beam_width", C.c_size_t),
                 ("epsilon0", C.c_float), ("rerank_candidates", C.c_size_t),
-                ("early_stop_hops", C.c_size_t), ("kth_stop", C.c_int)]
+                ("early_stop_hops", C.c_size_t), ("kth_stop", C.c_int), ("codec", C.c_int)]
 
 
 def _p(a):
@@ -92,7 +92,8 @@ class Oracle:
         self.msb_bytes = lib.qgo_msb_bytes(self.space)
         self.prep = C.c_void_p(lib.qgo_prepared_new(self.space))
         if lib.qgo_space_set_query_codec(self.space, C.c_int(codec)) != 0:
-            raise ValueError("the oracle prepares Int8 (3) and Int4 (2) queries")
+            raise ValueError("the oracle prepares Int8 (3), Int4 (2) and B1 (1) queries")
+        self.codec = codec
 
     def __del__(self):
         try:
@@ -157,8 +158,15 @@ class Oracle:
         sc = np.empty(4, np.float32)
         cs = np.zeros(1, np.int64)
         self.lib.qgo_prepared_export(self.prep, _p(rr), _p(codes), _p(sc), _p(cs))
-        return dict(rotated_residual=rr, codes=codes, query_norm_sqr=sc[0], query_norm=sc[1],
-                    half_sum=sc[2], scale=sc[3], code_sum=int(cs[0]))
+        out = dict(rotated_residual=rr, codes=codes, query_norm_sqr=sc[0], query_norm=sc[1],
+                   half_sum=sc[2], scale=sc[3], code_sum=int(cs[0]))
+        if self.codec == 1:
+            bits = np.zeros(self.msb_bytes, np.uint8)
+            b1 = np.zeros(3, np.float32)
+            ss = np.zeros(1, np.int64)
+            self.lib.qgo_prepared_export_b1(self.prep, _p(bits), _p(b1), _p(ss))
+            out.update(b1_bits=bits, b1_scalars=b1, b1_signed_sum=int(ss[0]))
+        return out
 
     def dither_seed(self, q):
         q = np.ascontiguousarray(q, np.float32)
@@ -199,7 +207,7 @@ class Oracle:
     def search(self, queries, index, k=10, L=40, eps=1.9, rerank=100, beam=1, early_stop=0,
                kth_stop=False, threads=0):
         return _search(self.lib.qgo_search_batch, [self.space], queries, index, k, L, eps,
-                       rerank, beam, early_stop, kth_stop, threads)
+                       rerank, beam, early_stop, kth_stop, threads, codec=self.codec)
 
     def build_graph(self, compact, r=32, l_build=100, alpha=1.2, beam=1, batch=4096, refine=1,
                     cap=256, stop_hops=2, threads=0):
@@ -230,10 +238,10 @@ class Oracle:
 
 
 def _search(fn, lead_args, queries, index, k, L, eps, rerank, beam, early_stop, kth_stop, threads,
-            dim_arg=None):
+            dim_arg=None, codec=3):
     queries = np.ascontiguousarray(queries, np.float32)
     nq = queries.shape[0]
-    prm = SearchParams(k, L, beam, eps, rerank, early_stop, 1 if kth_stop else 0)
+    prm = SearchParams(k, L, beam, eps, rerank, early_stop, 1 if kth_stop else 0, codec)
     ids = np.zeros((nq, k), np.uint32)
     dists = np.zeros((nq, k), np.float32)
     stats = np.zeros(nq, STATS)
@@ -277,7 +285,8 @@ class Reference:
         self.space = C.c_void_p(lib.rabitq_space_new(dim, seed, 1, 4, 16, True, True))
         self.center = np.ascontiguousarray(center, dtype=np.float32)
         assert lib.rabitq_space_set_center(self.space, _p(self.center))
-        lib.rabitq_set_query_coarse_codec(self.space, C.c_int(codec))  # 3 = Int8, 2 = Int4
+        lib.rabitq_set_query_coarse_codec(self.space, C.c_int(codec))  # 3 = Int8, 2 = Int4, 1 = B1
+        self.codec = codec
         self.full_bytes = lib.rabitq_full_record_bytes(self.space)
         self.compact_bytes = lib.rabitq_compact_record_bytes(self.space)
         self.residual_bytes = lib.rabitq_residual_record_bytes(self.space)
@@ -337,8 +346,15 @@ class Reference:
         sc = np.empty(4, np.float32)
         cs = np.zeros(1, np.int64)
         self.lib.qgref_prepared_export(self.prep, C.c_size_t(self.D), _p(rr), _p(codes), _p(sc), _p(cs))
-        return dict(rotated_residual=rr, codes=codes, query_norm_sqr=sc[0], query_norm=sc[1],
-                    half_sum=sc[2], scale=sc[3], code_sum=int(cs[0]))
+        out = dict(rotated_residual=rr, codes=codes, query_norm_sqr=sc[0], query_norm=sc[1],
+                   half_sum=sc[2], scale=sc[3], code_sum=int(cs[0]))
+        if self.codec == 1:
+            bits = np.zeros(self.msb_bytes, np.uint8)
+            b1 = np.zeros(3, np.float32)
+            ss = np.zeros(1, np.int64)
+            self.lib.qgref_prepared_export_b1(self.prep, C.c_size_t(self.D), _p(bits), _p(b1), _p(ss))
+            out.update(b1_bits=bits, b1_scalars=b1, b1_signed_sum=int(ss[0]))
+        return out
 
     def gate(self, ids, msb, factors, eps=1.9):
         ids = np.ascontiguousarray(ids, np.uint32)
@@ -408,4 +424,4 @@ class Reference:
     def search(self, queries, index, k=10, L=40, eps=1.9, rerank=100, beam=1, early_stop=0,
                kth_stop=False, threads=0):
         return _search(self.lib.qgref_search_batch, [self.space], queries, index, k, L, eps, rerank,
-                       beam, early_stop, kth_stop, threads, dim_arg=self.dim)
+                       beam, early_stop, kth_stop, threads, dim_arg=self.dim, codec=self.codec)

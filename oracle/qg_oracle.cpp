@@ -123,7 +123,7 @@ struct qgo_space {
     size_t residual_bytes = 0;
     size_t msb_bytes = 0;
     uint32_t seed = 100;
-    int query_bits = 8;  // Int8 (codec 3) or Int4 (codec 2)
+    int query_bits = 8;  // Int8 (codec 3), Int4 (codec 2) or B1 (codec 1, sign bits)
     std::vector<float> signs;
     std::vector<float> center;
     std::vector<float> rotated_center;
@@ -149,6 +149,12 @@ struct qgo_prepared {
     float half_sum = 0.0f;
     float int8_scale = 1.0f;
     int64_t code_sum = 0;
+    // B1 codec (space_rabitq.h:3493-3523): sign bits of q', scales of the 1-bit estimator
+    std::vector<uint8_t> b1_code;
+    int64_t b1_signed_sum = 0;
+    float b1_short_scale = 0.0f;
+    float b1_error_scale = 0.0f;
+    float b1_alpha = 0.0f;
 };
 
 namespace {
@@ -367,6 +373,33 @@ qgo_paper_estimate gate_one(const qgo_space &s, const qgo_prepared &q, const uin
     const float short_ip =
         0.5f * q.int8_scale * static_cast<float>(static_cast<int64_t>(2) * selected - q.code_sum);
     return finish_gate(q, short_ip, f, eps);
+}
+
+// compute_b1_paper_prune_estimate_batch_by_id + finish_b1_paper_prune_estimate
+// (space_rabitq.h:4607-4695, 4727-4753): popcount of the sign-code mismatches, the symmetric
+// 1-bit cross term, and a bound with the database and the query error terms added.
+qgo_paper_estimate gate_b1_one(const qgo_space &s, const qgo_prepared &q, const uint8_t *msb,
+                               const Factors &f, float eps) {
+    qgo_paper_estimate r{};
+    const bool query_valid = q.b1_short_scale > 0.0f && std::isfinite(q.b1_short_scale) && q.query_norm > 0.0f;
+    if (!query_valid || !f.valid || f.cross_scale <= 0.0f || !std::isfinite(f.cross_scale) || f.data_norm <= 0.0f)
+        return r;
+    uint64_t mism = 0;
+    for (size_t j = 0; j < s.msb_bytes; ++j)
+        mism += static_cast<uint64_t>(__builtin_popcount(static_cast<unsigned>(q.b1_code[j] ^ msb[j])));
+    const float signed_dot = static_cast<float>(s.code_dim) - 2.0f * static_cast<float>(mism);
+    const float short_ip = signed_dot * q.b1_short_scale / 8.0f;
+    const float cross = short_ip * f.cross_scale;
+    const float max_cross = 2.0f * f.data_norm * q.query_norm;
+    const float err_sum = std::fma(f.error_cross_scale, q.query_norm, q.b1_error_scale * f.data_norm);  // FMA
+    const float upper = std::max(-max_cross, std::min(max_cross, cross + eps * err_sum));
+    r.lower_bound = f.norm_sqr + q.query_norm_sqr - upper;
+    r.short_ip = short_ip;
+    r.alpha = q.b1_alpha;
+    r.ip_hat = max_cross > 0.0f ? cross / max_cross : 0.0f;
+    r.error_bound = max_cross > 0.0f ? eps * err_sum / max_cross : 0.0f;
+    r.valid = std::isfinite(r.lower_bound) ? 1 : 0;
+    return r;
 }
 
 // compute_residual_distance_intervals_batch_by_id AVX2 path (space_rabitq.h:5432-5548):
@@ -713,6 +746,32 @@ int qgo_prepare(const qgo_space *sp, const float *query, qgo_prepared *p) {
     p->int8_scale = 1.0f;
     p->code_sum = 0;
     std::fill(p->int8_code.begin(), p->int8_code.end(), 0);
+    if (s.query_bits == 1) {  // B1: sign bits and the 1-bit estimator's scales (no integer codes)
+        p->b1_code.assign(s.msb_bytes, 0);
+        p->b1_signed_sum = 0;
+        p->b1_short_scale = p->b1_error_scale = p->b1_alpha = 0.0f;
+        float abs_sum = 0.0f;
+        for (size_t i = 0; i < D; ++i) {
+            const float r = p->rotated_residual[i];
+            abs_sum += std::fabs(r);
+            if (r > 0.0f) {
+                p->b1_code[i >> 3U] = static_cast<uint8_t>(p->b1_code[i >> 3U] | (1U << (i & 7U)));
+                p->b1_signed_sum += 1;
+            } else {
+                p->b1_signed_sum -= 1;
+            }
+        }
+        if (p->query_norm > 0.0f && abs_sum > 0.0f && D > 1) {
+            const float a_q = abs_sum / p->query_norm;
+            const float alpha_q = std::min(1.0f, a_q / std::sqrt(static_cast<float>(D)));
+            const float alpha2 = alpha_q * alpha_q;
+            p->b1_alpha = alpha_q;
+            p->b1_short_scale = 4.0f * p->query_norm / a_q;
+            p->b1_error_scale = 2.0f * p->query_norm * std::sqrt(std::max(0.0f, (1.0f - alpha2) / alpha2)) /
+                                std::sqrt(static_cast<float>(D - 1));
+        }
+        return 0;
+    }
     if (max_abs > 0.0f) {
         // Int8: scale max/128, codes in [-128, 127], the first of the two draws per dimension;
         // Int4: scale max/8, codes in [-8, 7], the second (space_rabitq.h:3538-3655)
@@ -756,7 +815,8 @@ void qgo_gate_batch(const qgo_space *s, const qgo_prepared *q, const uint32_t *i
     for (size_t i = 0; i < count; ++i) {
         Factors f;
         std::memcpy(&f, fb + static_cast<size_t>(ids[i]) * factors_stride, sizeof(Factors));
-        out[i] = gate_one(*s, *q, msb_base + static_cast<size_t>(ids[i]) * msb_stride, f, eps);
+        const uint8_t *msb = msb_base + static_cast<size_t>(ids[i]) * msb_stride;
+        out[i] = s->query_bits == 1 ? gate_b1_one(*s, *q, msb, f, eps) : gate_one(*s, *q, msb, f, eps);
     }
 }
 
@@ -935,7 +995,9 @@ extern "C" int qgo_search_one_with(const qgo_kernel_table *kt, const float *quer
                 }
                 f.ids.push_back(fresh[slot]);
                 f.slots.push_back(slot);
-                f.modes.push_back(paper.valid ? 2 : 0);
+                // survivors: the quantized traversal for the integer codecs, the FP32 restore
+                // for B1 and invalid estimates (ours_diskann.rs:1731-1748)
+                f.modes.push_back(paper.valid && prm->codec != 1 ? 2 : 0);
                 f.short_ips.push_back(paper.short_ip);
                 if (f.ids.size() >= kDistBatch) flush_batch(kt, prep, pool, l_value, est, f, st);
             }
@@ -1401,7 +1463,18 @@ extern "C" int qgo_build_vamana(const qgo_space *space, const uint8_t *compact, 
 
 // rabitq_set_query_coarse_codec for the oracle: 3 = Int8, 2 = Int4; others return -1.
 extern "C" int qgo_space_set_query_codec(qgo_space *space, int codec) {
-    if (!space || (codec != 2 && codec != 3)) return -1;
-    space->query_bits = codec == 2 ? 4 : 8;
+    if (!space || (codec != 1 && codec != 2 && codec != 3)) return -1;
+    space->query_bits = codec == 1 ? 1 : (codec == 2 ? 4 : 8);
     return 0;
+}
+
+// The B1 prepared fields: sign bits [D/8], {short scale, error scale, alpha}, signed sum.
+extern "C" void qgo_prepared_export_b1(const qgo_prepared *p, uint8_t *bits, float *scalars, int64_t *signed_sum) {
+    if (bits) std::copy(p->b1_code.begin(), p->b1_code.end(), bits);
+    if (scalars) {
+        scalars[0] = p->b1_short_scale;
+        scalars[1] = p->b1_error_scale;
+        scalars[2] = p->b1_alpha;
+    }
+    if (signed_sum) *signed_sum = p->b1_signed_sum;
 }

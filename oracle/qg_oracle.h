@@ -88,6 +88,7 @@ float qgo_symmetric_distance(const qgo_space *space, const uint8_t *lhs, const u
 /* ---- query preparation (space_rabitq.h:3429-3706), INT8 codec, or INT4 after
  * qgo_space_set_query_codec(space, 2) ---- */
 int qgo_space_set_query_codec(qgo_space *space, int codec);
+void qgo_prepared_export_b1(const qgo_prepared *prepared, uint8_t *bits, float *scalars, int64_t *signed_sum);
 qgo_prepared *qgo_prepared_new(const qgo_space *space);
 void qgo_prepared_delete(qgo_prepared *prepared);
 int qgo_prepare(const qgo_space *space, const float *query, qgo_prepared *prepared);
@@ -122,6 +123,7 @@ typedef struct {
     size_t rerank_candidates;
     size_t early_stop_hops;
     int kth_stop;
+    int codec; /* 3 Int8, 2 Int4 (quantized traversal), 1 B1 (survivors by the FP32 restore) */
 } qgo_search_params;
 
 int qgo_search_batch(const qgo_space *space, const float *queries, size_t nq,

@@ -55,6 +55,20 @@ void qgref_prepared_export(const void *prepared, size_t code_dim, float *rotated
     if (code_sum) *code_sum = int4 ? q.int4_code_sum : q.int8_code_sum;
 }
 
+// The B1 prepared fields (space_rabitq.h:3493-3523): sign bits [D/8], {short scale, error
+// scale, alpha}, signed sum.
+void qgref_prepared_export_b1(const void *prepared, size_t code_dim, uint8_t *bits, float *scalars,
+                              int64_t *signed_sum) {
+    const auto &q = static_cast<const hnswlib::RaBitQSpace::PreparedQuery *>(prepared)->centroid_queries[0];
+    if (bits && q.b1_code.size() >= (code_dim + 7) / 8) std::memcpy(bits, q.b1_code.data(), (code_dim + 7) / 8);
+    if (scalars) {
+        scalars[0] = q.b1_short_scale;
+        scalars[1] = q.b1_error_scale;
+        scalars[2] = q.b1_alpha;
+    }
+    if (signed_sum) *signed_sum = q.b1_signed_sum;
+}
+
 void qgref_rotate(const void *space, const float *raw, float *out) {
     static_cast<const hnswlib::RaBitQSpace *>(space)->rotate(raw, out);
 }

@@ -11,7 +11,7 @@ ours_diskann.rs:1539-1986 (which cannot be built here) is driven over the refere
 bridge kernels (oracle/ref_probe.cpp).
 
 Inputs are regenerated from numpy seeds in the tests; a checksum of each input is stored
-to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants | space_states | int4]
+to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants | space_states | int4 | b1]
 """
 from __future__ import annotations
 
@@ -151,6 +151,42 @@ def int4_cases():
     print("search_c1_int4 written")
 
 
+def b1_cases():
+    """The B1 query codec (sign bits; an ablation in the reference): per query the sign bits
+    and the 1-bit estimator's scales, the B1 gate over every record of the kernel fixtures, and
+    whole searches (survivors scored by the FP32 restore) on the search_c1 index."""
+    out = {}
+    for name in ("kernels_d128", "kernels_d1536"):
+        g = np.load(os.path.join(HERE, name + ".npz"))
+        dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+        _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+        ref = oracle_py.Reference(dim, g["center"], codec=1)
+        ids = np.arange(n, dtype=np.uint32)
+        bits, scal, ssum, gate = [], [], [], []
+        for q in Q:
+            p = ref.prepare(q)
+            bits.append(p["b1_bits"])
+            scal.append(p["b1_scalars"])
+            ssum.append(p["b1_signed_sum"])
+            gate.append(ref.gate(ids, g["msb"], g["factors"], 1.9).view(np.uint8).reshape(n, -1))
+        out[f"{name}_bits"] = np.array(bits)
+        out[f"{name}_scalars"] = np.array(scal, np.float32)
+        out[f"{name}_signed_sum"] = np.array(ssum, np.int64)
+        out[f"{name}_gate"] = np.array(gate)
+    g = np.load(os.path.join(HERE, "search_c1.npz"))
+    _, Q = c1_data()
+    ref = oracle_py.Reference(128, g["center"], codec=1)
+    index = dict(compact=g["compact"], residual=g["residual"], msb=g["msb"], factors=g["factors"],
+                 degrees=g["degrees"], edges=g["edges"], total_points=int(g["n"]), base_points=int(g["n"]))
+    for L in (20, 40, 80):
+        ids, dists, stats = ref.search(Q, index, k=10, L=L, eps=1.9, rerank=100)
+        out[f"search_c1_ids_L{L}"] = ids
+        out[f"search_c1_dists_L{L}"] = dists
+        out[f"search_c1_stats_L{L}"] = stats.view(np.uint64).reshape(len(Q), -1)
+    np.savez_compressed(os.path.join(HERE, "b1_codec.npz"), **out)
+    print("b1_codec written")
+
+
 def space_states():
     """RaBitQSpace::saveState output of the reference for the kernel fixtures' spaces (seed 100,
     their centres): the EXRBTQ31 bytes a saved space must equal and a loaded one must encode
@@ -177,6 +213,9 @@ def main():
     if sys.argv[1:] == ["int4"]:
         int4_cases()
         return
+    if sys.argv[1:] == ["b1"]:
+        b1_cases()
+        return
     kernel_case("kernels_d128", 128, 64, 8, seed=20260813, center_value=0.05)
     kernel_case("kernels_d100", 100, 48, 4, seed=5, center_value=None)
     kernel_case("kernels_d960", 960, 96, 4, seed=6, center_value=None)
@@ -191,6 +230,7 @@ def main():
     build_variants()
     space_states()
     int4_cases()
+    b1_cases()
     with open(os.path.join(HERE, "PROVENANCE.txt"), "w") as f:
         f.write(f"generated by tests/golden/make_golden.py on {platform.machine()} {platform.processor()}\n")
         f.write(f"reference bridge compiled with: {FLAGS}\n")

@@ -166,3 +166,34 @@ def test_search_loop_int4_bit_exact(oracle):
         np.testing.assert_array_equal(ids, v[f"ids_L{L}"])
         np.testing.assert_array_equal(bits(dists), bits(v[f"dists_L{L}"]))
         np.testing.assert_array_equal(stats.view(np.uint64).reshape(len(Q), -1), v[f"stats_L{L}"])
+
+
+@pytest.mark.parametrize("name", ["kernels_d128", "kernels_d1536"])
+def test_b1_codec_prepare_and_gate_bit_exact(oracle, name):
+    """The B1 codec: sign bits, the 1-bit estimator's scales and the B1 gate (popcount, then the
+    bound with the query's error term added) against the reference with codec 1."""
+    g = load_golden(name)
+    v = load_golden("b1_codec")
+    dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+    _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+    o = oracle.Oracle(dim, g["center"], codec=1)
+    ids = np.arange(n, dtype=np.uint32)
+    for qi in range(nq):
+        p = o.prepare(Q[qi])
+        np.testing.assert_array_equal(p["b1_bits"], v[f"{name}_bits"][qi])
+        np.testing.assert_array_equal(bits(p["b1_scalars"]), bits(v[f"{name}_scalars"][qi]))
+        assert p["b1_signed_sum"] == int(v[f"{name}_signed_sum"][qi])
+        est = o.gate(ids, g["msb"], g["factors"])
+        np.testing.assert_array_equal(est.view(np.uint8).reshape(n, -1)[:, :21], v[f"{name}_gate"][qi][:, :21])
+
+
+def test_b1_codec_search_bit_exact(oracle):
+    g = load_golden("search_c1")
+    v = load_golden("b1_codec")
+    _, Q = SEARCH_CASES["search_c1"]()
+    o = oracle.Oracle(128, g["center"], codec=1)
+    for L in (20, 40, 80):
+        ids, dists, stats = o.search(Q, golden_index(g), k=10, L=L, eps=1.9, rerank=100)
+        np.testing.assert_array_equal(ids, v[f"search_c1_ids_L{L}"])
+        np.testing.assert_array_equal(bits(dists), bits(v[f"search_c1_dists_L{L}"]))
+        np.testing.assert_array_equal(stats.view(np.uint64).reshape(len(Q), -1), v[f"search_c1_stats_L{L}"])
