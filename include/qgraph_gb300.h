@@ -117,8 +117,10 @@ float rabitq_symmetric_distance(const void *space, const void *lhs, const void *
  * valid until that thread's next prepare call, as in the reference (space_rabitq.h:3700). */
 const void *rabitq_prepare_query(const void *space, const float *query);
 /* rabitq_bridge.cpp:364-370. Codec ids: Full=0 B1=1 Int4=2 Int8=3 B1Main=4 FullStaged=5
- * FullRerankScalar=6 (space_rabitq.h:36-44). The GPU path implements Int8 (the formal codec)
- * and Int4; prepare_query returns NULL, and the batched qg_* search fails, for the others. */
+ * FullRerankScalar=6 (space_rabitq.h:36-44). The GPU path implements Int8 (the formal codec),
+ * Int4 and B1; prepare_query returns NULL, and the batched qg_* search fails, for the others.
+ * With B1 the prepared codes hold the sign bits, the scale slot the 1-bit short scale and the
+ * code-sum slot the error scale (low word) and alpha (high word). */
 void rabitq_set_query_coarse_codec(void *space, int codec);
 /* rabitq_bridge.cpp:372-378 (no-op, as in the reference) */
 void rabitq_release_query(const void *space, const void *prepared);

@@ -61,6 +61,38 @@ __global__ void gate_pairs_kernel(const int8_t *codes, const float4 *scal, const
     }
 }
 
+// compute_b1_paper_prune_estimate_batch_by_id (space_rabitq.h:4607-4695): popcount of the
+// query's sign bits against the MSB plane, then finish_b1_paper_prune_estimate.
+template <int D>
+__global__ void gate_b1_pairs_kernel(const int8_t *codes, const float4 *scal, const long long *csum,
+                                     const uint32_t *qidx, const uint32_t *ids, size_t count,
+                                     const uint8_t *msb, size_t msb_stride, const uint8_t *factors,
+                                     size_t factor_stride, float eps, RabitqPaperEstimate *out) {
+    const size_t pair = (static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (pair >= count) return;
+    const uint32_t q = qidx[pair], id = ids[pair];
+    const uint8_t *qb = reinterpret_cast<const uint8_t *>(codes + static_cast<size_t>(q) * D);
+    const uint8_t *m = msb + static_cast<size_t>(id) * msb_stride;
+    int mism = 0;
+    for (int j = lane; j < D / 8; j += 32) mism += __popc(static_cast<uint32_t>(qb[j] ^ m[j]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mism += __shfl_xor_sync(0xffffffffu, mism, o);
+    if (lane == 0) {
+        const float4 pf = load_factors(factors + static_cast<size_t>(id) * factor_stride);
+        const float4 s = scal[q];
+        const GateOut g = finish_gate_b1(mism, pf, s.w, b1_error_scale(csum[q]), s.y, s.x, eps, D);
+        RabitqPaperEstimate r;
+        r.lower_bound = g.lower_bound;
+        r.short_ip = g.short_ip;
+        r.alpha = g.reached ? b1_alpha(csum[q]) : 0.0f;
+        r.ip_hat = g.ip_hat;
+        r.error_bound = g.error_bound;
+        r.valid = g.valid ? 1 : 0;
+        out[pair] = r;
+    }
+}
+
 template <int D>
 __global__ void distance_pairs_kernel(const float *rr, const int8_t *codes, const float4 *scal,
                                       const long long *csum, const uint32_t *qidx,
@@ -241,11 +273,17 @@ cudaError_t launch_gate_pairs(int code_dim, const int8_t *codes, const float4 *s
                               const long long *csum, const uint32_t *qidx, const uint32_t *ids,
                               size_t count, const uint8_t *msb, size_t msb_stride,
                               const uint8_t *factors, size_t factor_stride, float eps,
-                              RabitqPaperEstimate *out, cudaStream_t stream) {
+                              RabitqPaperEstimate *out, cudaStream_t stream, bool b1) {
     if (count == 0) return cudaSuccess;
-    QG_DISPATCH_D(code_dim, gate_pairs_kernel<kD><<<warp_grid(count), 256, 0, stream>>>(
-                                codes, scal, csum, qidx, ids, count, msb, msb_stride, factors,
-                                factor_stride, eps, out));
+    if (b1) {
+        QG_DISPATCH_D(code_dim, gate_b1_pairs_kernel<kD><<<warp_grid(count), 256, 0, stream>>>(
+                                    codes, scal, csum, qidx, ids, count, msb, msb_stride, factors,
+                                    factor_stride, eps, out));
+    } else {
+        QG_DISPATCH_D(code_dim, gate_pairs_kernel<kD><<<warp_grid(count), 256, 0, stream>>>(
+                                    codes, scal, csum, qidx, ids, count, msb, msb_stride, factors,
+                                    factor_stride, eps, out));
+    }
     return cudaGetLastError();
 }
 

@@ -181,7 +181,7 @@ bool gate_host(const Space *s, const uint32_t *ids, size_t count, const uint8_t 
     if (!cuda_ok(launch_gate_pairs(static_cast<int>(s->code_dim), t_prepared.d_codes, t_prepared.d_scal,
                                    t_prepared.d_csum, reinterpret_cast<uint32_t *>(d + o_q),
                                    reinterpret_cast<uint32_t *>(d + o_i), count, d + o_m, mb, d + o_f, 20,
-                                   eps, reinterpret_cast<RabitqPaperEstimate *>(d + o_o), st),
+                                   eps, reinterpret_cast<RabitqPaperEstimate *>(d + o_o), st, s->codec == 1),
                  "gate kernel"))
         return false;
     if (!cuda_ok(cudaMemcpyAsync(h + o_o, d + o_o, count * sizeof(RabitqPaperEstimate),
@@ -630,8 +630,8 @@ const void *rabitq_prepare_query(const void *space, const float *query) {
     try {
         const Space *s = as_space(space);
         if (!s || !query) return nullptr;
-        if (s->codec != 3 && s->codec != 2) {
-            set_error("the GPU query path implements the Int8 (3) and Int4 (2) query codecs");
+        if (!space_query_bits(s)) {
+            set_error("the GPU query path implements the Int8 (3), Int4 (2) and B1 (1) query codecs");
             return nullptr;
         }
         Prepared &p = t_prepared;
@@ -1001,7 +1001,7 @@ int qg_prepare_batch(const void *space, const float *d_queries, size_t nq, float
         return QG_ERR_INVALID;
     }
     if (!space_query_bits(s)) {
-        set_error("the GPU query path implements the Int8 (3) and Int4 (2) query codecs");
+        set_error("the GPU query path implements the Int8 (3), Int4 (2) and B1 (1) query codecs");
         return QG_ERR_INVALID;
     }
     PrepArgs a{d_queries, s->dim, static_cast<int>(nq), static_cast<int>(s->dim),
@@ -1044,7 +1044,8 @@ int qg_gate_pairs(const void *space, const int8_t *d_codes, const float *d_scala
                                    reinterpret_cast<const float4 *>(d_scalars),
                                    reinterpret_cast<const long long *>(d_code_sum), d_qidx, d_ids, count,
                                    d_msb, msb_stride, static_cast<const uint8_t *>(d_factors),
-                                   factor_stride, epsilon0, d_out, static_cast<cudaStream_t>(stream)),
+                                   factor_stride, epsilon0, d_out, static_cast<cudaStream_t>(stream),
+                                   s->codec == 1),
                  "gate kernel"))
         return QG_ERR_CUDA;
     return QG_OK;
@@ -1455,7 +1456,7 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
     if (nq == 0) return QG_OK;
     {
         if (!space_query_bits(s)) {
-            set_error("the GPU query path implements the Int8 (3) and Int4 (2) query codecs");
+            set_error("the GPU query path implements the Int8 (3), Int4 (2) and B1 (1) query codecs");
             return QG_ERR_INVALID;
         }
         PrepArgs pa{d_queries, s->dim, static_cast<int>(nq), static_cast<int>(s->dim),
@@ -1485,6 +1486,7 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
     a.rerank = params->rerank_candidates;
     a.early_stop_hops = params->early_stop_hops;
     a.kth_stop = params->kth_stop;
+    a.b1 = space_query_bits(s) == 1 ? 1 : 0;
     a.ids_out = d_ids;
     a.dists_out = d_dists;
     a.stats_out = d_stats;

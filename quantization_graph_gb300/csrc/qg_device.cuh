@@ -89,6 +89,7 @@ struct GateOut {
     float ip_hat;
     float error_bound;
     bool valid;
+    bool reached;  // the estimate was computed (not refused by the validity checks)
 };
 
 // compute_paper_prune_estimate_int_msb_gate + finish_paper_prune_estimate_sidecar
@@ -96,9 +97,10 @@ struct GateOut {
 // validity folded into cross_scale (NaN when the factors are invalid).
 __device__ __forceinline__ GateOut finish_gate(int32_t selected, const float4 pf, float scale,
                                                int64_t code_sum, float qn, float qn2, float eps) {
-    GateOut r{0.0f, 0.0f, 0.0f, 0.0f, false};
+    GateOut r{0.0f, 0.0f, 0.0f, 0.0f, false, false};
     const float cross_scale = pf.z;
     if (!(cross_scale > 0.0f) || !f_isfinite(cross_scale) || qn <= 0.0f) return r;
+    r.reached = true;
     const float short_ip =
         0.5f * scale * static_cast<float>(static_cast<int64_t>(2) * selected - code_sum);
     const float cross = short_ip * cross_scale;
@@ -110,6 +112,40 @@ __device__ __forceinline__ GateOut finish_gate(int32_t selected, const float4 pf
     r.error_bound = max_cross > 0.0f ? eps * pf.w * qn / max_cross : 0.0f;
     r.valid = f_isfinite(r.lower_bound);
     return r;
+}
+
+// compute_b1_paper_prune_estimate_batch_by_id + finish_b1_paper_prune_estimate
+// (space_rabitq.h:4607-4695, 4727-4753): the sign codes' mismatch count gives the symmetric
+// 1-bit cross term; the bound adds the query's error term to the database's (the reference
+// contracts the database product into the sum).
+__device__ __forceinline__ GateOut finish_gate_b1(int32_t mismatches, const float4 pf, float short_scale,
+                                                  float error_scale, float qn, float qn2, float eps, int D) {
+    GateOut r{0.0f, 0.0f, 0.0f, 0.0f, false, false};
+    const float cross_scale = pf.z;
+    if (!(short_scale > 0.0f) || !f_isfinite(short_scale) || !(qn > 0.0f) || !(cross_scale > 0.0f) ||
+        !f_isfinite(cross_scale) || !(pf.y > 0.0f))
+        return r;
+    r.reached = true;
+    const float signed_dot = static_cast<float>(D) - 2.0f * static_cast<float>(mismatches);
+    const float short_ip = signed_dot * short_scale / 8.0f;
+    const float cross = short_ip * cross_scale;
+    const float max_cross = 2.0f * pf.y * qn;
+    const float err = __fmaf_rn(pf.w, qn, error_scale * pf.y);
+    const float up = fmaxf(-max_cross, fminf(max_cross, cross + eps * err));
+    r.lower_bound = pf.x + qn2 - up;
+    r.short_ip = short_ip;
+    r.ip_hat = max_cross > 0.0f ? cross / max_cross : 0.0f;
+    r.error_bound = max_cross > 0.0f ? eps * err / max_cross : 0.0f;
+    r.valid = f_isfinite(r.lower_bound);
+    return r;
+}
+
+// B1 prepared scalars packed in the code-sum slot: error scale (low word), alpha (high word).
+__device__ __forceinline__ float b1_error_scale(long long packed) {
+    return __uint_as_float(static_cast<uint32_t>(static_cast<unsigned long long>(packed)));
+}
+__device__ __forceinline__ float b1_alpha(long long packed) {
+    return __uint_as_float(static_cast<uint32_t>(static_cast<unsigned long long>(packed) >> 32));
 }
 
 // Residual rerank interval (compute_residual_distance_intervals_batch_by_id AVX2 path,

@@ -42,6 +42,7 @@ struct SearchArgs {
     const int *l_per_q;
     int k_stride;
     int l_cap;       // pool capacity per warp (>= every L and k)
+    int b1;          // 1: B1 query codec (codes hold sign bits; popcount gate; survivors by the FP32 restore)
     int beam_width;
     float eps;
     int rerank;
@@ -129,7 +130,7 @@ cudaError_t launch_gate_pairs(int code_dim, const int8_t *codes, const float4 *s
                               const long long *csum, const uint32_t *qidx, const uint32_t *ids,
                               size_t count, const uint8_t *msb, size_t msb_stride,
                               const uint8_t *factors, size_t factor_stride, float eps,
-                              RabitqPaperEstimate *out, cudaStream_t stream);
+                              RabitqPaperEstimate *out, cudaStream_t stream, bool b1 = false);
 cudaError_t launch_distance_pairs(int code_dim, const float *rr, const int8_t *codes,
                                   const float4 *scal, const long long *csum,
                                   const uint32_t *qidx, const uint32_t *ids,

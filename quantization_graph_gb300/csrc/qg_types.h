@@ -38,9 +38,11 @@ struct Space {
     float center_norm_sqr = 0.0f;
 };
 
-// Bits of the query codes of the space's codec: Int8 (3) -> 8, Int4 (2) -> 4; 0 for the codecs
-// the GPU path does not build (Full, B1, B1Main and the staged variants).
-inline int space_query_bits(const Space *s) { return s->codec == 3 ? 8 : (s->codec == 2 ? 4 : 0); }
+// Bits of the query codes of the space's codec: Int8 (3) -> 8, Int4 (2) -> 4, B1 (1) -> 1 (sign
+// bits); 0 for the codecs the GPU path does not build (Full, B1Main and the staged variants).
+inline int space_query_bits(const Space *s) {
+    return s->codec == 3 ? 8 : (s->codec == 2 ? 4 : (s->codec == 1 ? 1 : 0));
+}
 
 // Device-resident index: structure-of-arrays, every row 16-byte aligned.
 struct DevIndex {

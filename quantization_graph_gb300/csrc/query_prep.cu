@@ -286,6 +286,36 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(PrepArgs a) {
 
     const float qn2 = s_qn2;
     const float max_abs = s_max;
+    if (a.qbits == 1) {
+        // B1 (space_rabitq.h:3493-3523): sign bits of q' into the code buffer (bit i of byte
+        // i / 8), |q'| summed in dimension order on one thread, the 1-bit estimator's scales:
+        // short scale in the scale slot, error scale and alpha packed in the code-sum slot.
+        int8_t *bits = a.codes + static_cast<size_t>(q) * D;
+        for (int b = threadIdx.x; b < D / 8; b += 128) {
+            uint32_t byte = 0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) byte |= (x[8 * b + k] > 0.0f ? 1u : 0u) << k;
+            bits[b] = static_cast<int8_t>(byte);
+        }
+        if (threadIdx.x == 0) {
+            float abs_sum = 0.0f;
+            for (int i = 0; i < D; ++i) abs_sum += fabsf(x[i]);
+            const float qn = sqrtf(qn2);
+            float ss = 0.0f, es = 0.0f, al = 0.0f;
+            if (qn > 0.0f && abs_sum > 0.0f && D > 1) {
+                const float a_q = abs_sum / qn;
+                const float alpha_q = fminf(1.0f, a_q / sqrtf(static_cast<float>(D)));
+                const float alpha2 = alpha_q * alpha_q;
+                al = alpha_q;
+                ss = 4.0f * qn / a_q;
+                es = 2.0f * qn * sqrtf(fmaxf(0.0f, (1.0f - alpha2) / alpha2)) / sqrtf(static_cast<float>(D - 1));
+            }
+            a.scal[q] = make_float4(qn2, qn, s_half * 0.5f, ss);
+            a.csum[q] = static_cast<long long>((static_cast<unsigned long long>(__float_as_uint(al)) << 32) |
+                                               __float_as_uint(es));
+        }
+        return;
+    }
     const bool int4 = a.qbits == 4;  // Int4: max/8, [-8, 7], the second draw (space_rabitq.h:3538-3655)
     const float scale = max_abs > 0.0f ? max_abs / (int4 ? 8.0f : 128.0f) : 1.0f;
     const int vlo = int4 ? -8 : -128, vhi = int4 ? 7 : 127;

@@ -280,7 +280,10 @@ __device__ __forceinline__ void load_query(QueryRegs<D> &r, const int8_t *codes,
 
 // ---- the per-query search ------------------------------------------------------------
 
-template <int D>
+// kB1: the B1 query codec (sign bits; an ablation in the reference): the gate counts sign
+// mismatches against the MSB plane (finish_gate_b1) and every survivor takes the FP32 restore
+// (mode 0, as the Rust loop assigns, ours_diskann.rs:1731-1748).
+template <int D, bool kB1>
 __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int lane,
                            uint16_t *tags, uint32_t tag, const uint32_t *stop_smem) {
     using L = Lay<D>;
@@ -320,7 +323,15 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
     }
 
     QueryRegs<D> qr;
-    load_query<D>(qr, a.codes + static_cast<size_t>(q) * D, sub);
+    if constexpr (kB1) {
+        // the sign-bit word of each 32-dim chunk this lane gates
+        const uint32_t *bw = reinterpret_cast<const uint32_t *>(a.codes + static_cast<size_t>(q) * D);
+#pragma unroll
+        for (int j = 0; j < L::CPL; ++j) qr.xg[j][0] = static_cast<int>(bw[sub + L::LPN * j]);
+    } else {
+        load_query<D>(qr, a.codes + static_cast<size_t>(q) * D, sub);
+    }
+    const float b1_es = kB1 ? b1_error_scale(csum) : 0.0f;
 
     int pn = 0;  // pool size (warp-uniform)
     if (ix.n_base != 0) {
@@ -500,13 +511,19 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                     for (int g = 0; g < G; ++g) {
                         int acc = 0;
 #pragma unroll
-                        for (int j = 0; j < L::CPL; ++j) acc = gate_chunk(w[g][j], qr.xg[j], acc);
+                        for (int j = 0; j < L::CPL; ++j) {
+                            if constexpr (kB1)
+                                acc += __popc(w[g][j] ^ static_cast<uint32_t>(qr.xg[j][0]));
+                            else
+                                acc = gate_chunk(w[g][j], qr.xg[j], acc);
+                        }
                         p[g] = acc;
                     }
                     const int tot = reduce_scatter<G>(p, lane);
                     const int f = gb + lane;
                     if (lane < G && f < F) {
-                        const GateOut go = finish_gate(tot, s.fpf[f], scale, csum, qn, qn2, a.eps);
+                        const GateOut go = kB1 ? finish_gate_b1(tot, s.fpf[f], scale, b1_es, qn, qn2, a.eps, D)
+                                               : finish_gate(tot, s.fpf[f], scale, csum, qn, qn2, a.eps);
                         s.flb[f] = go.lower_bound;
                         s.fsip[f] = go.short_ip;
                         s.fval[f] = go.valid ? 1 : 0;
@@ -529,12 +546,13 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                     }
 #pragma unroll
                     for (int pp = 0; pp < P; ++pp) {
-                        int acc = gate_chunk(w[pp], qr.xg[0], 0);
+                        int acc = kB1 ? __popc(w[pp] ^ static_cast<uint32_t>(qr.xg[0][0])) : gate_chunk(w[pp], qr.xg[0], 0);
 #pragma unroll
                         for (int o = 1; o < L::LPN; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
                         const int f = fb + pp * L::NBP + grp;
                         if (sub == 0 && f < F) {
-                            const GateOut go = finish_gate(acc, s.fpf[f], scale, csum, qn, qn2, a.eps);
+                            const GateOut go = kB1 ? finish_gate_b1(acc, s.fpf[f], scale, b1_es, qn, qn2, a.eps, D)
+                                                   : finish_gate(acc, s.fpf[f], scale, csum, qn, qn2, a.eps);
                             s.flb[f] = go.lower_bound;
                             s.fsip[f] = go.short_ip;
                             s.fval[f] = go.valid ? 1 : 0;
@@ -586,81 +604,93 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                 const float4 h = ix.hdr[s.sid[i]];
                 s.shdr[i] = make_float2(h.x, h.y);
             }
-            bool any_full = false;
-            if constexpr (L::LPN == 32) {
-                constexpr int G = L::GT;
-                for (int gb = 0; gb < S; gb += G) {
-                    uint4 c[G][L::CPL];
-#pragma unroll
-                    for (int g = 0; g < G; ++g) {
-                        const int i = gb + g < S ? gb + g : gb;
-                        const uint4 *row = reinterpret_cast<const uint4 *>(
-                            ix.codes + static_cast<size_t>(s.sid[i]) * (D / 2));
-#pragma unroll
-                        for (int j = 0; j < L::CPL; ++j) c[g][j] = row_load(row + lane + 32 * j);
-                    }
-#if QG_TRAV_PREFETCH == 1
-                    if (gb + G < S)
-                        prefetch_rows_l1(ix.codes, s.sid + gb + G, S - gb - G < G ? S - gb - G : G, D / 2, D / 2,
-                                         lane);
-#endif
-                    int p[G];
-#pragma unroll
-                    for (int g = 0; g < G; ++g) {
-                        int acc = 0;
-#pragma unroll
-                        for (int j = 0; j < L::CPL; ++j) acc = trav_chunk(c[g][j], qr.xe[j], qr.xo[j], acc);
-                        p[g] = acc;
-                    }
-                    const int tot = reduce_scatter<G>(p, lane);
-                    const int i = gb + lane;
-                    if (lane < G && i < S) s.sdist[i] = __int_as_float(tot);  // finished below
+            if constexpr (kB1) {
+                // B1: every survivor by the FP32 restore, two per pass (one per half-warp)
+                for (int base = 0; base < S; base += 2) {
+                    const int i = base + (lane >> 4);
+                    const int ii = i < S ? i : base;
+                    const float2 h = s.shdr[ii];
+                    const float d = restore_distance_hw<D>(ix.codes + static_cast<size_t>(s.sid[ii]) * (D / 2), rr,
+                                                           h.x, h.y, half_sum, qn2, lane & 15);
+                    if ((lane & 15) == 0 && i < S) s.sdist[i] = d;
                 }
+                __syncwarp();
             } else {
-                constexpr int P = L::PG;
-                for (int ib = 0; ib < S; ib += P * L::NBP) {
-                    uint4 c[P];
-#pragma unroll
-                    for (int pp = 0; pp < P; ++pp) {
-                        int i = ib + pp * L::NBP + grp;
-                        i = i < S ? i : ib;
-                        const uint4 *row = reinterpret_cast<const uint4 *>(
-                            ix.codes + static_cast<size_t>(s.sid[i]) * (D / 2));
-                        c[pp] = __ldg(row + sub);
+                bool any_full = false;
+                if constexpr (L::LPN == 32) {
+                    constexpr int G = L::GT;
+                    for (int gb = 0; gb < S; gb += G) {
+                        uint4 c[G][L::CPL];
+    #pragma unroll
+                        for (int g = 0; g < G; ++g) {
+                            const int i = gb + g < S ? gb + g : gb;
+                            const uint4 *row = reinterpret_cast<const uint4 *>(
+                                ix.codes + static_cast<size_t>(s.sid[i]) * (D / 2));
+    #pragma unroll
+                            for (int j = 0; j < L::CPL; ++j) c[g][j] = row_load(row + lane + 32 * j);
+                        }
+    #if QG_TRAV_PREFETCH == 1
+                        if (gb + G < S)
+                            prefetch_rows_l1(ix.codes, s.sid + gb + G, S - gb - G < G ? S - gb - G : G, D / 2, D / 2,
+                                             lane);
+    #endif
+                        int p[G];
+    #pragma unroll
+                        for (int g = 0; g < G; ++g) {
+                            int acc = 0;
+    #pragma unroll
+                            for (int j = 0; j < L::CPL; ++j) acc = trav_chunk(c[g][j], qr.xe[j], qr.xo[j], acc);
+                            p[g] = acc;
+                        }
+                        const int tot = reduce_scatter<G>(p, lane);
+                        const int i = gb + lane;
+                        if (lane < G && i < S) s.sdist[i] = __int_as_float(tot);  // finished below
                     }
-#pragma unroll
-                    for (int pp = 0; pp < P; ++pp) {
-                        int acc = trav_chunk(c[pp], qr.xe[0], qr.xo[0], 0);
-#pragma unroll
-                        for (int o = 1; o < L::LPN; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-                        const int i = ib + pp * L::NBP + grp;
-                        if (sub == 0 && i < S) s.sdist[i] = __int_as_float(acc);  // finished below
+                } else {
+                    constexpr int P = L::PG;
+                    for (int ib = 0; ib < S; ib += P * L::NBP) {
+                        uint4 c[P];
+    #pragma unroll
+                        for (int pp = 0; pp < P; ++pp) {
+                            int i = ib + pp * L::NBP + grp;
+                            i = i < S ? i : ib;
+                            const uint4 *row = reinterpret_cast<const uint4 *>(
+                                ix.codes + static_cast<size_t>(s.sid[i]) * (D / 2));
+                            c[pp] = __ldg(row + sub);
+                        }
+    #pragma unroll
+                        for (int pp = 0; pp < P; ++pp) {
+                            int acc = trav_chunk(c[pp], qr.xe[0], qr.xo[0], 0);
+    #pragma unroll
+                            for (int o = 1; o < L::LPN; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                            const int i = ib + pp * L::NBP + grp;
+                            if (sub == 0 && i < S) s.sdist[i] = __int_as_float(acc);  // finished below
+                        }
                     }
                 }
-            }
-            __syncwarp();
-            // finish every survivor at once, one lane each (finishQuantizedTraversalDistance)
-            for (int i = lane; i < S; i += 32) {
-                const float2 h = s.shdr[i];
-                s.sdist[i] = finish_traversal(h.x, h.y, s.fsip[s.sslot[i]], __float_as_int(s.sdist[i]), scale,
-                                              csum, qn2);
-            }
-            __syncwarp();
-            // survivors whose gate was invalid use the full FP32 restore (mode 0)
-            for (int i = 0; i < S; ++i) any_full |= s.fval[s.sslot[i]] == 0;
-            if (any_full) {
-                for (int i = 0; i < S; ++i) {
-                    if (s.fval[s.sslot[i]]) continue;
-                    const uint32_t id = s.sid[i];
+                __syncwarp();
+                // finish every survivor at once, one lane each (finishQuantizedTraversalDistance)
+                for (int i = lane; i < S; i += 32) {
                     const float2 h = s.shdr[i];
-                    const float d = restore_distance_hw<D>(ix.codes + static_cast<size_t>(id) * (D / 2),
-                                                           rr, h.x, h.y, half_sum, qn2, lane & 15);
-                    if (lane == 0) s.sdist[i] = d;
-                    __syncwarp();
+                    s.sdist[i] = finish_traversal(h.x, h.y, s.fsip[s.sslot[i]], __float_as_int(s.sdist[i]), scale,
+                                                  csum, qn2);
                 }
+                __syncwarp();
+                // survivors whose gate was invalid use the full FP32 restore (mode 0)
+                for (int i = 0; i < S; ++i) any_full |= s.fval[s.sslot[i]] == 0;
+                if (any_full) {
+                    for (int i = 0; i < S; ++i) {
+                        if (s.fval[s.sslot[i]]) continue;
+                        const uint32_t id = s.sid[i];
+                        const float2 h = s.shdr[i];
+                        const float d = restore_distance_hw<D>(ix.codes + static_cast<size_t>(id) * (D / 2),
+                                                               rr, h.x, h.y, half_sum, qn2, lane & 15);
+                        if (lane == 0) s.sdist[i] = d;
+                        __syncwarp();
+                    }
+                }
+                __syncwarp();
             }
-            __syncwarp();
-
             // ---- re-check and sorted insert in adjacency order (ours_diskann.rs:1944-1979) ----
             for (int i = 0; i < S; ++i) {
                 const uint32_t slot = s.sslot[i];
@@ -889,7 +919,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
 #ifndef QG_SEARCH_THREADS
 #define QG_SEARCH_THREADS 256
 #endif
-template <int D>
+template <int D, bool kB1>
 __global__ void __launch_bounds__(QG_SEARCH_THREADS, QG_SEARCH_MINBLOCKS) search_kernel(SearchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -918,7 +948,7 @@ __global__ void __launch_bounds__(QG_SEARCH_THREADS, QG_SEARCH_MINBLOCKS) search
             e += 1;
         }
         if (lane == 0) a.epochs[slot] = e;
-        search_one<D>(a, s, q, lane, tags, e & 0xFFFFu, stop_smem);
+        search_one<D, kB1>(a, s, q, lane, tags, e & 0xFFFFu, stop_smem);
         __syncwarp();
     }
 }
@@ -935,14 +965,19 @@ int search_supported_dim(int code_dim) {
            code_dim == 1024 || code_dim == 2048;
 }
 
-template <int D>
-static cudaError_t launch_d(const SearchArgs &a, int grid, int wpb, cudaStream_t stream) {
+template <int D, bool kB1>
+static cudaError_t launch_dc(const SearchArgs &a, int grid, int wpb, cudaStream_t stream) {
     const size_t smem = search_block_smem(a.l_cap, wpb, a.stop_w != nullptr);
-    cudaError_t e = cudaFuncSetAttribute(search_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(search_kernel<D, kB1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    search_kernel<D><<<grid, wpb * 32, smem, stream>>>(a);
+    search_kernel<D, kB1><<<grid, wpb * 32, smem, stream>>>(a);
     return cudaGetLastError();
+}
+
+template <int D>
+static cudaError_t launch_d(const SearchArgs &a, int grid, int wpb, cudaStream_t stream) {
+    return a.b1 ? launch_dc<D, true>(a, grid, wpb, stream) : launch_dc<D, false>(a, grid, wpb, stream);
 }
 
 size_t search_block_smem(int l_cap, int wpb, bool stop_model) {
@@ -952,11 +987,13 @@ size_t search_block_smem(int l_cap, int wpb, bool stop_model) {
 template <int D>
 static int blocks_per_sm_d(int l_cap, int wpb, bool stop_model) {
     const size_t smem = search_block_smem(l_cap, wpb, stop_model);
-    if (cudaFuncSetAttribute(search_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    // the B1 instantiation shares the launch bounds and shared memory of the Int8 one
+    if (cudaFuncSetAttribute(search_kernel<D, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(smem)) != cudaSuccess)
         return 0;
     int blocks = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, search_kernel<D>, wpb * 32, smem) != cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, search_kernel<D, false>, wpb * 32, smem) !=
+        cudaSuccess)
         return 0;
     return blocks;
 }

@@ -2,7 +2,8 @@
 called exactly as the Rust side calls the reference's (ours_diskann.rs:45-242), against the
 golden vectors the reference produced (encode, copies, sidecar, symmetric distance, the
 batched gate / distance / residual kernels, the single-record restore; Int8 and Int4 query
-codecs) and against the reference's sentinels for what is not built (the B1 / Full codecs).
+codecs) and against the reference's sentinels for what is not built (the Full and B1Main
+codecs).
 rabitq_build_vamana_graph is covered by test_gpu_vamana_build.py."""
 import ctypes as C
 
@@ -132,7 +133,8 @@ def test_sentinels_of_what_is_not_built(lib):
         rec = np.ascontiguousarray(g["compact"][0])
         assert np.isinf(lib.rabitq_query_distance_b1(sp, prep, _p(rec)))
         assert np.isinf(lib.rabitq_query_distance_with_paper(sp, prep, _p(rec), C.c_float(0.0)))
-        lib.rabitq_set_query_coarse_codec(sp, 1)  # B1: not built, no prepared query
-        assert not C.c_void_p(lib.rabitq_prepare_query(sp, _p(query))).value
+        for codec in (0, 4, 5, 6):  # Full, B1Main, FullStaged, FullRerankScalar: not built, no prepared query
+            lib.rabitq_set_query_coarse_codec(sp, codec)
+            assert not C.c_void_p(lib.rabitq_prepare_query(sp, _p(query))).value
     finally:
         lib.rabitq_space_delete(sp)

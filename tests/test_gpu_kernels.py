@@ -231,3 +231,29 @@ def test_round_quotient_decision_near_half_integers(cuda):
     u8 = und.cpu().numpy()
     assert u8[:200].sum() > 0
     assert u8[m:].sum() <= 2
+
+
+@pytest.mark.parametrize("name", ["kernels_d128", "kernels_d1536"])
+def test_b1_codec_prepare_and_gate_bit_exact(cuda, name):
+    """The B1 query codec on the GPU: sign bits (in the code buffer), the 1-bit estimator's
+    scales (short scale in the scale slot, error scale and alpha packed in the code-sum slot)
+    and the popcount gate against the reference with codec 1."""
+    torch = cuda
+    g = load_golden(name)
+    v = load_golden("b1_codec")
+    dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+    _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+    sp = _space(torch, dim, g["center"], codec=1)
+    p = sp.prepare(torch.from_numpy(Q).cuda())
+    D = sp.code_dim
+    np.testing.assert_array_equal(p["codes"].cpu().numpy().view(np.uint8)[:, :D // 8], v[f"{name}_bits"])
+    sc = p["scalars"].cpu().numpy()
+    packed = p["code_sum"].cpu().numpy().view(np.uint32).reshape(nq, 2)
+    np.testing.assert_array_equal(bits(sc[:, 3]), bits(v[f"{name}_scalars"][:, 0]))
+    np.testing.assert_array_equal(packed[:, 0], bits(v[f"{name}_scalars"][:, 1]))
+    np.testing.assert_array_equal(packed[:, 1], bits(v[f"{name}_scalars"][:, 2]))
+    qidx = np.repeat(np.arange(nq), n).astype(np.int32)
+    ids = np.tile(np.arange(n), nq).astype(np.int32)
+    gate = sp.gate_pairs(p, qidx, ids, torch.from_numpy(g["msb"]).cuda(), torch.from_numpy(g["factors"]).cuda(),
+                         1.9).cpu().numpy()
+    np.testing.assert_array_equal(gate[:, :21], v[f"{name}_gate"].reshape(nq * n, -1)[:, :21])

@@ -183,3 +183,23 @@ def test_int4_codec_search_matches_reference(cuda):
         np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), v[f"ids_L{L}"])
         np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(v[f"dists_L{L}"]))
         np.testing.assert_array_equal(stats_matrix(r.stats), v[f"stats_L{L}"])
+
+
+def test_b1_codec_search_matches_reference(cuda):
+    """The B1 query codec through the batched GPU search (popcount gate, FP32-restore survivors)
+    against the reference's own kernels with codec 1: ids, distance bits and the counters."""
+    torch = cuda
+    from quantization_graph_gb300.index import OursIndex
+    from quantization_graph_gb300.space import RabitqSpace
+
+    g = load_golden("search_c1")
+    v = load_golden("b1_codec")
+    _, Q = SEARCH_CASES["search_c1"]()
+    sp = RabitqSpace(128, g["center"], codec=1)
+    ix = OursIndex(sp, g["compact"], g["residual"], g["msb"], g["factors"], g["degrees"], g["edges"])
+    q = torch.from_numpy(Q).cuda()
+    for L in (20, 40, 80):
+        r = ix.search(q, k=10, l_value=L, with_stats=True)
+        np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), v[f"search_c1_ids_L{L}"])
+        np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(v[f"search_c1_dists_L{L}"]))
+        np.testing.assert_array_equal(stats_matrix(r.stats), v[f"search_c1_stats_L{L}"])
