@@ -54,3 +54,20 @@ BUILD_VARIANTS = {
     "d960_r24": dict(src="search_c2", r=24, l_build=48, alpha=1.2, beam=1, batch=4096, refine=1, cap=32,
                      stop_hops=2),
 }
+
+
+def build_edge_data():
+    """Duplicates, near-duplicates (1e-7 apart) and zero vectors among 128-d Gaussians: equal
+    codes, zero and invalid-record distances, ties broken by id."""
+    rng = np.random.default_rng(5)
+    base = rng.standard_normal((300, 128)).astype(np.float32)
+    X = np.concatenate([base, base[:150], base[:75] + np.float32(1e-7), np.zeros((10, 128), np.float32)])
+    rng.shuffle(X)
+    return X
+
+
+BUILD_EDGE_ARGS = {
+    "edge_r16": dict(r=16, l_build=32, alpha=1.2, beam=1, batch=64, refine=1, cap=24, stop_hops=2),
+    "edge_r8_beam2": dict(r=8, l_build=16, alpha=1.0, beam=2, batch=1000, refine=0, cap=0, stop_hops=0),
+    "edge_n3": dict(n=3, r=4, l_build=8, alpha=1.2, beam=1, batch=4, refine=1, cap=0, stop_hops=0),
+}

@@ -11,7 +11,7 @@ ours_diskann.rs:1539-1986 (which cannot be built here) is driven over the refere
 bridge kernels (oracle/ref_probe.cpp).
 
 Inputs are regenerated from numpy seeds in the tests; a checksum of each input is stored
-to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants | space_states | int4 | b1]
+to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants | space_states | int4 | b1 | build_edges]
 """
 from __future__ import annotations
 
@@ -29,7 +29,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 import oracle_py  # noqa: E402
 sys.path.insert(0, HERE)
-from cases import BUILD_VARIANTS, c1_data, c2_data, c3_data, kernel_inputs  # noqa: E402
+from cases import BUILD_EDGE_ARGS, BUILD_VARIANTS, build_edge_data, c1_data, c2_data, c3_data, kernel_inputs  # noqa: E402
 
 FLAGS = "g++ -std=c++20 -O3 -march=native -fopenmp (experiments/02_diskann_fair/build.rs:22-36)"
 
@@ -151,6 +151,23 @@ def int4_cases():
     print("search_c1_int4 written")
 
 
+def build_edges():
+    """Reference graphs for duplicate / near-duplicate / zero vectors and a 3-node index."""
+    X = build_edge_data()
+    center = X.mean(0).astype(np.float32)
+    ref = oracle_py.Reference(128, center)
+    compact, _ = ref.encode(X)
+    out = dict(center=center, compact=compact)
+    for name, kw in BUILD_EDGE_ARGS.items():
+        kw = dict(kw)
+        n = kw.pop("n", len(compact))
+        deg, edges = ref.build_graph(compact[:n], **kw)
+        out[f"{name}_degrees"] = deg
+        out[f"{name}_edges"] = edges
+    np.savez_compressed(os.path.join(HERE, "build_edges.npz"), **out)
+    print("build_edges written")
+
+
 def b1_cases():
     """The B1 query codec (sign bits; an ablation in the reference): per query the sign bits
     and the 1-bit estimator's scales, the B1 gate over every record of the kernel fixtures, and
@@ -216,6 +233,9 @@ def main():
     if sys.argv[1:] == ["b1"]:
         b1_cases()
         return
+    if sys.argv[1:] == ["build_edges"]:
+        build_edges()
+        return
     kernel_case("kernels_d128", 128, 64, 8, seed=20260813, center_value=0.05)
     kernel_case("kernels_d100", 100, 48, 4, seed=5, center_value=None)
     kernel_case("kernels_d960", 960, 96, 4, seed=6, center_value=None)
@@ -231,6 +251,7 @@ def main():
     space_states()
     int4_cases()
     b1_cases()
+    build_edges()
     with open(os.path.join(HERE, "PROVENANCE.txt"), "w") as f:
         f.write(f"generated by tests/golden/make_golden.py on {platform.machine()} {platform.processor()}\n")
         f.write(f"reference bridge compiled with: {FLAGS}\n")

@@ -113,3 +113,16 @@ def test_build_matches_oracle_at_scale(cuda, oracle, case):
     gdeg, gedges, _ = o.build_graph(compact, **kw)
     deg, edges, _ = _gpu_build(cuda, RabitqSpace(X.shape[1], center), compact, **kw)
     _assert_same_graph(deg, edges, gdeg, gedges, case)
+
+
+@pytest.mark.parametrize("name", ["edge_r16", "edge_r8_beam2", "edge_n3"])
+def test_build_edge_cases_match_reference(cuda, name):
+    """Duplicate / near-duplicate / zero vectors and a 3-node index on the GPU."""
+    from cases import BUILD_EDGE_ARGS
+
+    v = load_golden("build_edges")
+    kw = dict(BUILD_EDGE_ARGS[name])
+    n = kw.pop("n", len(v["compact"]))
+    g = dict(dim=128, center=v["center"])
+    deg, edges, _ = _gpu_build(cuda, _space(g), v["compact"][:n], **kw)
+    _assert_same_graph(deg, edges, v[f"{name}_degrees"], v[f"{name}_edges"], name)

@@ -197,3 +197,20 @@ def test_b1_codec_search_bit_exact(oracle):
         np.testing.assert_array_equal(ids, v[f"search_c1_ids_L{L}"])
         np.testing.assert_array_equal(bits(dists), bits(v[f"search_c1_dists_L{L}"]))
         np.testing.assert_array_equal(stats.view(np.uint64).reshape(len(Q), -1), v[f"search_c1_stats_L{L}"])
+
+
+@pytest.mark.parametrize("name", ["edge_r16", "edge_r8_beam2", "edge_n3"])
+def test_vamana_build_edge_cases_match_reference(oracle, name):
+    """Duplicates, near-duplicates and zero vectors (ties, zero and invalid distances) and a
+    3-node index, against the reference's graphs."""
+    from cases import BUILD_EDGE_ARGS, build_edge_data
+
+    v = load_golden("build_edges")
+    X = build_edge_data()
+    kw = dict(BUILD_EDGE_ARGS[name])
+    n = kw.pop("n", len(X))
+    o = oracle.Oracle(128, v["center"])
+    compact, _ = o.encode(X)
+    np.testing.assert_array_equal(compact, v["compact"])
+    deg, edges, _ = o.build_graph(compact[:n], **kw)
+    _graph_equal(deg, edges, v[f"{name}_degrees"], v[f"{name}_edges"])
