@@ -160,7 +160,7 @@ class Oracle:
         self.lib.qgo_prepared_export(self.prep, _p(rr), _p(codes), _p(sc), _p(cs))
         out = dict(rotated_residual=rr, codes=codes, query_norm_sqr=sc[0], query_norm=sc[1],
                    half_sum=sc[2], scale=sc[3], code_sum=int(cs[0]))
-        if self.codec == 1:
+        if self.codec in (1, 4):
             bits = np.zeros(self.msb_bytes, np.uint8)
             b1 = np.zeros(3, np.float32)
             ss = np.zeros(1, np.int64)
@@ -176,6 +176,12 @@ class Oracle:
         out = np.empty(count, np.float64)
         self.lib.qgo_dither_draws(C.c_uint64(seed), C.c_size_t(count), _p(out))
         return out
+
+    def distance_b1(self, record):
+        """query_distance_b1 (B1 / B1Main codecs) on the most recently prepared query."""
+        self.lib.qgo_distance_b1.restype = C.c_float
+        self.lib.qgo_distance_b1.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        return self.lib.qgo_distance_b1(self.space, self.prep, _p(np.ascontiguousarray(record)))
 
     # The batched kernels act on the most recently prepared query.
     def gate(self, ids, msb, factors, eps=1.9):
@@ -348,7 +354,7 @@ class Reference:
         self.lib.qgref_prepared_export(self.prep, C.c_size_t(self.D), _p(rr), _p(codes), _p(sc), _p(cs))
         out = dict(rotated_residual=rr, codes=codes, query_norm_sqr=sc[0], query_norm=sc[1],
                    half_sum=sc[2], scale=sc[3], code_sum=int(cs[0]))
-        if self.codec == 1:
+        if self.codec in (1, 4):
             bits = np.zeros(self.msb_bytes, np.uint8)
             b1 = np.zeros(3, np.float32)
             ss = np.zeros(1, np.int64)
@@ -373,6 +379,12 @@ class Reference:
                                              C.c_size_t(len(ids)), _p(records),
                                              C.c_size_t(records.shape[1]), _p(short_ips), _p(out))
         return out
+
+    def distance_b1(self, record):
+        """rabitq_query_distance_b1 on the most recently prepared query (B1 / B1Main codecs)."""
+        self.lib.rabitq_query_distance_b1.restype = C.c_float
+        self.lib.rabitq_query_distance_b1.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        return self.lib.rabitq_query_distance_b1(self.space, self.prep, _p(np.ascontiguousarray(record)))
 
     def distance_single(self, record):
         return self.lib.rabitq_query_distance(self.space, self.prep, _p(np.ascontiguousarray(record)))

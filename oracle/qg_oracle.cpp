@@ -328,6 +328,23 @@ float finish_traversal(const qgo_prepared &q, float norm_sqr, float long_scale, 
            static_cast<float>(static_cast<double>(long_scale) * signed_long);
 }
 
+// query_distance_b1 (space_rabitq.h:3741-3753): the 4-bit long code dotted with the query's
+// sign code (exact in integers), centred by 7.5 * the sign sum, scaled by long_scale in double.
+float distance_b1(const qgo_space &s, const qgo_prepared &q, const uint8_t *record) {
+    const float norm_sqr = get_f32(record);
+    const float long_scale = get_f32(record + 4);
+    if (!(long_scale > 0.0f) || !std::isfinite(long_scale)) return norm_sqr + q.query_norm_sqr;
+    const uint8_t *code = record + s.off_code_compact();
+    int64_t dot = 0;
+    for (size_t i = 0; i < s.code_dim; ++i) {
+        const int c = (code[i >> 1U] >> (4U * (i & 1U))) & 0x0F;
+        dot += ((q.b1_code[i >> 3U] >> (i & 7U)) & 1U) ? c : -c;
+    }
+    const double signed_long_ip = static_cast<double>(dot) - 7.5 * static_cast<double>(q.b1_signed_sum);
+    const double est_ip = static_cast<double>(long_scale) * signed_long_ip;
+    return norm_sqr + q.query_norm_sqr - static_cast<float>(est_ip);
+}
+
 // query_distance_with_quantized_paper_msb (space_rabitq.h:4207-4232).
 float traversal_distance(const qgo_space &s, const qgo_prepared &q, const uint8_t *record,
                          float short_ip) {
@@ -979,6 +996,15 @@ extern "C" int qgo_search_one_with(const qgo_kernel_table *kt, const float *quer
             }
             if (fresh.empty()) continue;
             st.visited_nodes += fresh.size();
+            if (prm->codec == 4) {  // B1Main: no gate, every fresh neighbour (ours_diskann.rs:1661-1682)
+                for (uint32_t id : fresh) {
+                    const float d = kt->distance_b1(kt->ctx, prep, id);
+                    st.distance_computations++;
+                    st.paper_remaining_kernel_calls++;
+                    insert_sorted(pool, Candidate{d, id, false, std::numeric_limits<float>::max()}, l_value);
+                }
+                continue;
+            }
             est.assign(fresh.size(), qgo_paper_estimate{});
             kt->gate(kt->ctx, prep, fresh.data(), fresh.size(), prm->epsilon0, est.data());
             st.paper_msb_kernel_calls += fresh.size();
@@ -1093,6 +1119,10 @@ void ok_dist(void *ctx, const void *p, const uint32_t *ids, const uint8_t *modes
     qgo_distance_batch(c->space, static_cast<const qgo_prepared *>(p), ids, modes, n, c->records,
                        c->record_stride, sips, out);
 }
+float ok_distance_b1(void *ctx, const void *p, uint32_t id) {
+    auto *c = static_cast<OracleCtx *>(ctx);
+    return distance_b1(*c->space, *static_cast<const qgo_prepared *>(p), c->records + static_cast<size_t>(id) * c->record_stride);
+}
 void ok_res(void *ctx, const void *p, const uint32_t *ids, size_t n, const float *ld,
             qgo_interval *out) {
     auto *c = static_cast<OracleCtx *>(ctx);
@@ -1119,7 +1149,7 @@ extern "C" int qgo_search_batch(const qgo_space *space, const float *queries, si
     {
         OracleCtx ctx{space, qgo_prepared_new(space), records, record_stride, residual,
                       residual_stride, msb, msb_stride, factors, factor_stride};
-        qgo_kernel_table kt{&ctx, ok_prepare, ok_distance, ok_gate, ok_dist, ok_res};
+        qgo_kernel_table kt{&ctx, ok_prepare, ok_distance, ok_gate, ok_dist, ok_res, ok_distance_b1};
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 1)
 #endif
@@ -1463,9 +1493,13 @@ extern "C" int qgo_build_vamana(const qgo_space *space, const uint8_t *compact, 
 
 // rabitq_set_query_coarse_codec for the oracle: 3 = Int8, 2 = Int4; others return -1.
 extern "C" int qgo_space_set_query_codec(qgo_space *space, int codec) {
-    if (!space || (codec != 1 && codec != 2 && codec != 3)) return -1;
-    space->query_bits = codec == 1 ? 1 : (codec == 2 ? 4 : 8);
+    if (!space || (codec != 1 && codec != 2 && codec != 3 && codec != 4)) return -1;
+    space->query_bits = (codec == 1 || codec == 4) ? 1 : (codec == 2 ? 4 : 8);  // B1Main prepares like B1
     return 0;
+}
+
+extern "C" float qgo_distance_b1(const qgo_space *space, const qgo_prepared *prepared, const uint8_t *record) {
+    return distance_b1(*space, *prepared, record);
 }
 
 // The B1 prepared fields: sign bits [D/8], {short scale, error scale, alpha}, signed sum.

@@ -123,7 +123,8 @@ typedef struct {
     size_t rerank_candidates;
     size_t early_stop_hops;
     int kth_stop;
-    int codec; /* 3 Int8, 2 Int4 (quantized traversal), 1 B1 (survivors by the FP32 restore) */
+    int codec; /* 3 Int8, 2 Int4 (quantized traversal), 1 B1 (survivors by the FP32 restore),
+                  4 B1Main (no gate: every fresh neighbour by the 4-bit x 1-bit distance) */
 } qgo_search_params;
 
 int qgo_search_batch(const qgo_space *space, const float *queries, size_t nq,
@@ -147,6 +148,8 @@ typedef struct {
                            const uint8_t *modes, size_t n, const float *short_ips, float *out);
     void (*residual_batch)(void *ctx, const void *prepared, const uint32_t *ids, size_t n,
                            const float *long_d, qgo_interval *out);
+    /* 4-bit data x 1-bit query distance (B1Main; query_distance_b1, space_rabitq.h:3741-3753) */
+    float (*distance_b1)(void *ctx, const void *prepared, uint32_t id);
 } qgo_kernel_table;
 
 int qgo_search_one_with(const qgo_kernel_table *kt, const float *query,

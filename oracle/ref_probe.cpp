@@ -22,6 +22,7 @@ struct RabitqDistanceInterval;
 
 const void *rabitq_prepare_query(const void *space, const float *query);
 float rabitq_query_distance(const void *space, const void *prepared, const void *encoded);
+float rabitq_query_distance_b1(const void *space, const void *prepared, const void *encoded);
 bool rabitq_paper_estimate_batch_sidecar(const void *space, const void *prepared,
                                          const uint32_t *ids, size_t count,
                                          const uint8_t *msb_base, size_t msb_stride,
@@ -135,6 +136,10 @@ void rk_dist(void *ctx, const void *p, const uint32_t *ids, const uint8_t *modes
     auto *c = static_cast<RefCtx *>(ctx);
     rabitq_query_distance_batch(c->space, p, ids, modes, n, c->records, c->record_stride, sips, out);
 }
+float rk_distance_b1(void *ctx, const void *p, uint32_t id) {
+    auto *c = static_cast<RefCtx *>(ctx);
+    return rabitq_query_distance_b1(c->space, p, c->records + static_cast<size_t>(id) * c->record_stride);
+}
 void rk_res(void *ctx, const void *p, const uint32_t *ids, size_t n, const float *ld,
             qgo_interval *out) {
     auto *c = static_cast<RefCtx *>(ctx);
@@ -160,7 +165,7 @@ extern "C" int qgref_search_batch(const void *space, size_t dim, const float *qu
     {
         RefCtx ctx{space, records, record_stride, residual, residual_stride,
                    msb, msb_stride, factors, factor_stride};
-        qgo_kernel_table kt{&ctx, rk_prepare, rk_distance, rk_gate, rk_dist, rk_res};
+        qgo_kernel_table kt{&ctx, rk_prepare, rk_distance, rk_gate, rk_dist, rk_res, rk_distance_b1};
 #pragma omp for schedule(dynamic, 1)
         for (long long q = 0; q < static_cast<long long>(nq); ++q) {
             const size_t qi = static_cast<size_t>(q);

@@ -11,7 +11,7 @@ ours_diskann.rs:1539-1986 (which cannot be built here) is driven over the refere
 bridge kernels (oracle/ref_probe.cpp).
 
 Inputs are regenerated from numpy seeds in the tests; a checksum of each input is stored
-to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants | space_states | int4 | b1 | build_edges]
+to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants | space_states | int4 | b1 | build_edges | b1main]
 """
 from __future__ import annotations
 
@@ -151,6 +151,36 @@ def int4_cases():
     print("search_c1_int4 written")
 
 
+def b1main_cases():
+    """The B1Main codec (no gate; every fresh neighbour by the 4-bit x 1-bit distance): the
+    distance for every query x record of the kernel fixtures, and whole searches on the
+    search_c1 and search_c2 indexes."""
+    out = {}
+    for name in ("kernels_d128", "kernels_d1536"):
+        g = np.load(os.path.join(HERE, name + ".npz"))
+        dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+        _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+        ref = oracle_py.Reference(dim, g["center"], codec=4)
+        d = []
+        for q in Q:
+            ref.prepare(q)
+            d.append([ref.distance_b1(g["compact"][i]) for i in range(n)])
+        out[f"{name}_distance_b1"] = np.array(d, np.float32)
+    for name, fn in (("search_c1", c1_data), ("search_c2", c2_data)):
+        g = np.load(os.path.join(HERE, name + ".npz"))
+        _, Q = fn()
+        ref = oracle_py.Reference(int(g["dim"]), g["center"], codec=4)
+        index = dict(compact=g["compact"], residual=g["residual"], msb=g["msb"], factors=g["factors"],
+                     degrees=g["degrees"], edges=g["edges"], total_points=int(g["n"]), base_points=int(g["n"]))
+        for L in (20, 40, 80):
+            ids, dists, stats = ref.search(Q, index, k=10, L=L, eps=1.9, rerank=100)
+            out[f"{name}_ids_L{L}"] = ids
+            out[f"{name}_dists_L{L}"] = dists
+            out[f"{name}_stats_L{L}"] = stats.view(np.uint64).reshape(len(Q), -1)
+    np.savez_compressed(os.path.join(HERE, "b1main_codec.npz"), **out)
+    print("b1main_codec written")
+
+
 def build_edges():
     """Reference graphs for duplicate / near-duplicate / zero vectors and a 3-node index."""
     X = build_edge_data()
@@ -236,6 +266,9 @@ def main():
     if sys.argv[1:] == ["build_edges"]:
         build_edges()
         return
+    if sys.argv[1:] == ["b1main"]:
+        b1main_cases()
+        return
     kernel_case("kernels_d128", 128, 64, 8, seed=20260813, center_value=0.05)
     kernel_case("kernels_d100", 100, 48, 4, seed=5, center_value=None)
     kernel_case("kernels_d960", 960, 96, 4, seed=6, center_value=None)
@@ -252,6 +285,7 @@ def main():
     int4_cases()
     b1_cases()
     build_edges()
+    b1main_cases()
     with open(os.path.join(HERE, "PROVENANCE.txt"), "w") as f:
         f.write(f"generated by tests/golden/make_golden.py on {platform.machine()} {platform.processor()}\n")
         f.write(f"reference bridge compiled with: {FLAGS}\n")

@@ -214,3 +214,31 @@ def test_vamana_build_edge_cases_match_reference(oracle, name):
     np.testing.assert_array_equal(compact, v["compact"])
     deg, edges, _ = o.build_graph(compact[:n], **kw)
     _graph_equal(deg, edges, v[f"{name}_degrees"], v[f"{name}_edges"])
+
+
+@pytest.mark.parametrize("name", ["kernels_d128", "kernels_d1536"])
+def test_b1main_distance_bit_exact(oracle, name):
+    """query_distance_b1 (the 4-bit data x 1-bit query estimator) for every query x record."""
+    g = load_golden(name)
+    v = load_golden("b1main_codec")
+    dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+    _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+    o = oracle.Oracle(dim, g["center"], codec=4)
+    for qi in range(nq):
+        o.prepare(Q[qi])
+        d = np.array([o.distance_b1(g["compact"][i]) for i in range(n)], np.float32)
+        np.testing.assert_array_equal(bits(d), bits(v[f"{name}_distance_b1"][qi]))
+
+
+@pytest.mark.parametrize("name", ["search_c1", "search_c2"])
+def test_b1main_search_bit_exact(oracle, name):
+    """The B1Main loop (no gate, every fresh neighbour scored) against the reference's kernels."""
+    g = load_golden(name)
+    v = load_golden("b1main_codec")
+    _, Q = SEARCH_CASES[name]()
+    o = oracle.Oracle(int(g["dim"]), g["center"], codec=4)
+    for L in (20, 40, 80):
+        ids, dists, stats = o.search(Q, golden_index(g), k=10, L=L, eps=1.9, rerank=100)
+        np.testing.assert_array_equal(ids, v[f"{name}_ids_L{L}"])
+        np.testing.assert_array_equal(bits(dists), bits(v[f"{name}_dists_L{L}"]))
+        np.testing.assert_array_equal(stats.view(np.uint64).reshape(len(Q), -1), v[f"{name}_stats_L{L}"])
