@@ -118,7 +118,8 @@ float rabitq_symmetric_distance(const void *space, const void *lhs, const void *
 const void *rabitq_prepare_query(const void *space, const float *query);
 /* rabitq_bridge.cpp:364-370. Codec ids: Full=0 B1=1 Int4=2 Int8=3 B1Main=4 FullStaged=5
  * FullRerankScalar=6 (space_rabitq.h:36-44). The GPU path implements Int8 (the formal codec),
- * Int4 and B1; prepare_query returns NULL, and the batched qg_* search fails, for the others.
+ * Int4, B1 and B1Main; prepare_query returns NULL, and the batched qg_* search fails, for the
+ * others. B1Main prepared codes are +-1 bytes with the sign sum in the code-sum slot.
  * With B1 the prepared codes hold the sign bits, the scale slot the 1-bit short scale and the
  * code-sum slot the error scale (low word) and alpha (high word). */
 void rabitq_set_query_coarse_codec(void *space, int codec);
@@ -126,7 +127,9 @@ void rabitq_set_query_coarse_codec(void *space, int codec);
 void rabitq_release_query(const void *space, const void *prepared);
 /* rabitq_bridge.cpp:380-387 (full FP32 4-bit restore) */
 float rabitq_query_distance(const void *space, const void *prepared, const void *encoded);
-/* rabitq_bridge.cpp:389-396 / 398-423: B1Main codec; returns +inf (codec not built) */
+/* rabitq_bridge.cpp:389-396 / 398-423: the 4-bit x 1-bit distance (query_distance_b1,
+ * space_rabitq.h:3741-3753) for a B1Main prepared query; +inf otherwise (the batch form fills
+ * +inf and returns true, as the reference does for failed items) */
 float rabitq_query_distance_b1(const void *space, const void *prepared, const void *encoded);
 bool rabitq_query_distance_b1_batch(const void *space, const void *prepared, const uint32_t *ids,
                                     size_t count, const void *encoded_base, size_t encoded_stride,

@@ -93,6 +93,28 @@ __global__ void gate_b1_pairs_kernel(const int8_t *codes, const float4 *scal, co
     }
 }
 
+// query_distance_b1 over (query, record) pairs, one warp per pair; codes are the B1Main +-1
+// bytes, csum the sign sum.
+template <int D>
+__global__ void distance_b1_pairs_kernel(const int8_t *codes, const float4 *scal, const long long *csum,
+                                         const uint32_t *qidx, const uint32_t *ids, size_t count,
+                                         const uint8_t *records, size_t record_stride, float *out) {
+    const size_t pair = (static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (pair >= count) return;
+    const uint32_t q = qidx[pair], id = ids[pair];
+    const int8_t *x = codes + static_cast<size_t>(q) * D;
+    const uint8_t *rec = records + static_cast<size_t>(id) * record_stride;
+    int dot = 0;
+    for (int p = lane; p < D / 2; p += 32) {
+        const int b = rec[16 + p];
+        dot += (b & 15) * x[2 * p] + (b >> 4) * x[2 * p + 1];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+    if (lane == 0) out[pair] = finish_b1main(ld_f32(rec), ld_f32(rec + 4), dot, csum[q], scal[q].x);
+}
+
 template <int D>
 __global__ void distance_pairs_kernel(const float *rr, const int8_t *codes, const float4 *scal,
                                       const long long *csum, const uint32_t *qidx,
@@ -284,6 +306,15 @@ cudaError_t launch_gate_pairs(int code_dim, const int8_t *codes, const float4 *s
                                     codes, scal, csum, qidx, ids, count, msb, msb_stride, factors,
                                     factor_stride, eps, out));
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_distance_b1_pairs(int code_dim, const int8_t *codes, const float4 *scal, const long long *csum,
+                                     const uint32_t *qidx, const uint32_t *ids, size_t count, const uint8_t *records,
+                                     size_t record_stride, float *out, cudaStream_t stream) {
+    if (count == 0) return cudaSuccess;
+    QG_DISPATCH_D(code_dim, distance_b1_pairs_kernel<kD><<<warp_grid(count), 256, 0, stream>>>(
+                                codes, scal, csum, qidx, ids, count, records, record_stride, out));
     return cudaGetLastError();
 }
 

@@ -222,6 +222,33 @@ bool distance_host(const Space *s, const uint32_t *ids, const uint8_t *modes, si
     return true;
 }
 
+// query_distance_b1 for the records ids[i] (rows gathered like distance_host); the prepared
+// query must be a B1Main one (+-1 codes, sign sum in the code-sum slot).
+bool distance_b1_host(const Space *s, const uint32_t *ids, size_t count, const uint8_t *rec_base, size_t rec_stride,
+                      float *out) {
+    const size_t rb = s->compact_bytes;
+    Carve c;
+    const size_t o_q = c.take(count * 4), o_i = c.take(count * 4), o_r = c.take(count * rb),
+                 o_o = c.take(count * 4);
+    if (!t_stage.reserve(c.off)) return false;
+    uint8_t *h = static_cast<uint8_t *>(t_stage.h), *d = static_cast<uint8_t *>(t_stage.d);
+    fill_pairs(reinterpret_cast<uint32_t *>(h + o_q), reinterpret_cast<uint32_t *>(h + o_i), count);
+    gather_rows(h + o_r, rec_base, rec_stride, ids, count, rb);
+    cudaStream_t st = t_stage.stream;
+    if (!cuda_ok(cudaMemcpyAsync(d, h, o_o, cudaMemcpyHostToDevice, st), "b1 distance upload")) return false;
+    if (!cuda_ok(launch_distance_b1_pairs(static_cast<int>(s->code_dim), t_prepared.d_codes, t_prepared.d_scal,
+                                          t_prepared.d_csum, reinterpret_cast<uint32_t *>(d + o_q),
+                                          reinterpret_cast<uint32_t *>(d + o_i), count, d + o_r, rb,
+                                          reinterpret_cast<float *>(d + o_o), st),
+                 "b1 distance kernel"))
+        return false;
+    if (!cuda_ok(cudaMemcpyAsync(h + o_o, d + o_o, count * 4, cudaMemcpyDeviceToHost, st), "b1 distance download"))
+        return false;
+    if (!cuda_ok(cudaStreamSynchronize(st), "b1 distance sync")) return false;
+    std::memcpy(out, h + o_o, count * 4);
+    return true;
+}
+
 bool residual_host(const Space *s, const uint32_t *ids, size_t count, const uint8_t *res_base,
                    size_t res_stride, const float *long_d, RabitqDistanceInterval *out) {
     const size_t rb = s->residual_bytes;
@@ -678,15 +705,43 @@ float rabitq_query_distance(const void *space, const void *prepared, const void 
     }
 }
 
-float rabitq_query_distance_b1(const void *, const void *, const void *) {
-    set_error("the B1Main codec is not built");
-    return std::numeric_limits<float>::infinity();
+float rabitq_query_distance_b1(const void *space, const void *prepared, const void *encoded) {
+    const float inf = std::numeric_limits<float>::infinity();
+    try {
+        const Space *s = as_space(space);
+        if (!check_prepared(s, prepared) || !encoded) return inf;
+        if (s->codec != 4) {
+            set_error("rabitq_query_distance_b1: prepare the query with the B1Main codec (4)");
+            return inf;
+        }
+        const uint32_t id = 0;
+        float out = inf;
+        if (!distance_b1_host(s, &id, 1, static_cast<const uint8_t *>(encoded), s->compact_bytes, &out)) return inf;
+        return out;
+    } catch (...) {
+        return inf;
+    }
 }
 
-bool rabitq_query_distance_b1_batch(const void *, const void *, const uint32_t *, size_t count,
-                                    const void *, size_t, float *out_distances) {
-    for (size_t i = 0; i < count; ++i) out_distances[i] = std::numeric_limits<float>::infinity();
-    return true;
+bool rabitq_query_distance_b1_batch(const void *space, const void *prepared, const uint32_t *ids, size_t count,
+                                    const void *encoded_base, size_t encoded_stride, float *out_distances) {
+    const float inf = std::numeric_limits<float>::infinity();
+    try {
+        const Space *s = as_space(space);
+        if (!out_distances) return false;
+        bool ok = check_prepared(s, prepared) && ids && encoded_base && s->codec == 4;
+        for (size_t b = 0; ok && b < count; b += 4096) {
+            const size_t n = std::min<size_t>(4096, count - b);
+            ok = distance_b1_host(s, ids + b, n, static_cast<const uint8_t *>(encoded_base), encoded_stride,
+                                  out_distances + b);
+        }
+        if (!ok)
+            for (size_t i = 0; i < count; ++i) out_distances[i] = inf;  // the reference's failure sentinel
+        return true;
+    } catch (...) {
+        for (size_t i = 0; i < count; ++i) out_distances[i] = inf;
+        return true;
+    }
 }
 
 RabitqPaperEstimate rabitq_paper_estimate_sidecar(const void *space, const void *prepared,
@@ -1486,7 +1541,7 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
     a.rerank = params->rerank_candidates;
     a.early_stop_hops = params->early_stop_hops;
     a.kth_stop = params->kth_stop;
-    a.b1 = space_query_bits(s) == 1 ? 1 : 0;
+    a.mode = space_search_mode(s);
     a.ids_out = d_ids;
     a.dists_out = d_dists;
     a.stats_out = d_stats;

@@ -140,6 +140,18 @@ __device__ __forceinline__ GateOut finish_gate_b1(int32_t mismatches, const floa
     return r;
 }
 
+// query_distance_b1 (space_rabitq.h:3741-3753): dot = sum of the 4-bit codes times the query's
+// +-1 signs (exact), then norm_sqr + qn2 - float(long_scale * (dot - 7.5 * sign_sum)) in double;
+// a degenerate long_scale gives norm_sqr + qn2.
+__device__ __forceinline__ float finish_b1main(float norm_sqr, float long_scale, int32_t dot, long long sign_sum,
+                                               float qn2) {
+    if (!(long_scale > 0.0f) || !f_isfinite(long_scale)) return norm_sqr + qn2;
+    const double signed_long_ip =
+        __dsub_rn(static_cast<double>(dot), __dmul_rn(7.5, static_cast<double>(sign_sum)));
+    const double est = __dmul_rn(static_cast<double>(long_scale), signed_long_ip);
+    return (norm_sqr + qn2) - __double2float_rn(est);
+}
+
 // B1 prepared scalars packed in the code-sum slot: error scale (low word), alpha (high word).
 __device__ __forceinline__ float b1_error_scale(long long packed) {
     return __uint_as_float(static_cast<uint32_t>(static_cast<unsigned long long>(packed)));

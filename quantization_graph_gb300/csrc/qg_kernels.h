@@ -26,7 +26,8 @@ struct PrepArgs {
     float4 *scal;
     long long *csum;
     const int *nq_dev;  // optional: the batch size read on the device (CUDA-graph replay)
-    int qbits = 8;      // 8: Int8 query codec; 4: Int4 (scale max/8, codes in [-8, 7], second draw)
+    int qbits = 8;      // 8: Int8; 4: Int4 (scale max/8, codes in [-8, 7], second draw); 1: B1 (sign
+                        // bits); 2: B1Main (+-1 bytes, the sign sum in the code-sum slot)
 };
 
 struct SearchArgs {
@@ -42,7 +43,8 @@ struct SearchArgs {
     const int *l_per_q;
     int k_stride;
     int l_cap;       // pool capacity per warp (>= every L and k)
-    int b1;          // 1: B1 query codec (codes hold sign bits; popcount gate; survivors by the FP32 restore)
+    int mode;        // 0 Int8 / Int4; 1 B1 (sign bits, popcount gate, survivors by the FP32 restore);
+                     // 2 B1Main (+-1 codes, no gate, every fresh neighbour by the 4-bit x 1-bit distance)
     int beam_width;
     float eps;
     int rerank;
@@ -144,6 +146,10 @@ cudaError_t launch_residual_pairs(int code_dim, const float *rr, const float4 *s
                                   cudaStream_t stream);
 cudaError_t launch_symmetric_pairs(int code_dim, const uint8_t *lhs, const uint8_t *rhs,
                                    size_t count, size_t stride, float *out, cudaStream_t stream);
+// query_distance_b1 (space_rabitq.h:3741-3753) over (query, record) pairs; codes = B1Main +-1 bytes.
+cudaError_t launch_distance_b1_pairs(int code_dim, const int8_t *codes, const float4 *scal, const long long *csum,
+                                     const uint32_t *qidx, const uint32_t *ids, size_t count, const uint8_t *records,
+                                     size_t record_stride, float *out, cudaStream_t stream);
 
 // rabitq_build_vamana_graph arguments (rabitq_bridge.cpp:224-303)
 struct VbBuildParams {

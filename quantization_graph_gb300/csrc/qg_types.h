@@ -38,11 +38,15 @@ struct Space {
     float center_norm_sqr = 0.0f;
 };
 
-// Bits of the query codes of the space's codec: Int8 (3) -> 8, Int4 (2) -> 4, B1 (1) -> 1 (sign
-// bits); 0 for the codecs the GPU path does not build (Full, B1Main and the staged variants).
+// Query code layout of the space's codec: Int8 (3) -> 8, Int4 (2) -> 4 (integer codes), B1 (1) ->
+// 1 (sign bits), B1Main (4) -> 2 (+-1 bytes); 0 for the codecs the GPU path does not build (Full
+// and the staged variants).
 inline int space_query_bits(const Space *s) {
-    return s->codec == 3 ? 8 : (s->codec == 2 ? 4 : (s->codec == 1 ? 1 : 0));
+    return s->codec == 3 ? 8 : (s->codec == 2 ? 4 : (s->codec == 1 ? 1 : (s->codec == 4 ? 2 : 0)));
 }
+// Search mode of the codec: 0 integer codes (Int8 / Int4), 1 B1 (popcount gate), 2 B1Main (no
+// gate; every fresh neighbour by the 4-bit x 1-bit distance).
+inline int space_search_mode(const Space *s) { return s->codec == 1 ? 1 : (s->codec == 4 ? 2 : 0); }
 
 // Device-resident index: structure-of-arrays, every row 16-byte aligned.
 struct DevIndex {

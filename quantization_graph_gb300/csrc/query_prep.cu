@@ -286,6 +286,27 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(PrepArgs a) {
 
     const float qn2 = s_qn2;
     const float max_abs = s_max;
+    if (a.qbits == 2) {
+        // B1Main (space_rabitq.h:3493-3510): +-1 per dimension (r > 0 -> +1) as integer codes,
+        // the sign sum in the code-sum slot
+        int8_t *codes = a.codes + static_cast<size_t>(q) * D;
+        int pos = 0;
+        for (int i = threadIdx.x; i < D; i += 128) {
+            const bool p = x[i] > 0.0f;
+            codes[i] = p ? 1 : -1;
+            pos += p ? 1 : 0;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) pos += __shfl_xor_sync(0xffffffffu, pos, o);
+        if (lane == 0) s_csum_part[warp] = pos;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int p = s_csum_part[0] + s_csum_part[1] + s_csum_part[2] + s_csum_part[3];
+            a.scal[q] = make_float4(qn2, sqrtf(qn2), s_half * 0.5f, 1.0f);
+            a.csum[q] = static_cast<long long>(2 * p - D);
+        }
+        return;
+    }
     if (a.qbits == 1) {
         // B1 (space_rabitq.h:3493-3523): sign bits of q' into the code buffer (bit i of byte
         // i / 8), |q'| summed in dimension order on one thread, the 1-bit estimator's scales:

@@ -183,14 +183,17 @@ __device__ __forceinline__ int gate_chunk(uint32_t w, const int (&xg)[8], int ac
     return acc;
 }
 
-// Integer traversal partial over one 32-dim chunk: sum of (code & 7) * x.
+// Integer traversal partial over one 32-dim chunk: sum of (code & 7) * x, or of the whole 4-bit
+// code times x (kFull: the B1Main distance, x = +-1).
+template <bool kFull = false>
 __device__ __forceinline__ int trav_chunk(const uint4 c, const int (&xe)[4], const int (&xo)[4],
                                           int acc) {
+    constexpr uint32_t kMask = kFull ? 0x0F0F0F0Fu : 0x07070707u;
     const uint32_t w[4] = {c.x, c.y, c.z, c.w};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        acc = __dp4a(static_cast<int>(w[k] & 0x07070707u), xe[k], acc);
-        acc = __dp4a(static_cast<int>((w[k] >> 4) & 0x07070707u), xo[k], acc);
+        acc = __dp4a(static_cast<int>(w[k] & kMask), xe[k], acc);
+        acc = __dp4a(static_cast<int>((w[k] >> 4) & kMask), xo[k], acc);
     }
     return acc;
 }
@@ -280,10 +283,12 @@ __device__ __forceinline__ void load_query(QueryRegs<D> &r, const int8_t *codes,
 
 // ---- the per-query search ------------------------------------------------------------
 
-// kB1: the B1 query codec (sign bits; an ablation in the reference): the gate counts sign
-// mismatches against the MSB plane (finish_gate_b1) and every survivor takes the FP32 restore
-// (mode 0, as the Rust loop assigns, ours_diskann.rs:1731-1748).
-template <int D, bool kB1>
+// kMode 0: Int8 / Int4 query codes. kMode 1, the B1 codec (sign bits; an ablation in the
+// reference): the gate counts sign mismatches against the MSB plane (finish_gate_b1) and every
+// survivor takes the FP32 restore (mode 0, as the Rust loop assigns, ours_diskann.rs:1731-1748).
+// kMode 2, B1Main: no gate; every fresh neighbour is scored by the 4-bit x 1-bit distance
+// (query_distance_b1) from +-1 query bytes and inserted (ours_diskann.rs:1661-1682).
+template <int D, int kMode>
 __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int lane,
                            uint16_t *tags, uint32_t tag, const uint32_t *stop_smem) {
     using L = Lay<D>;
@@ -323,6 +328,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
     }
 
     QueryRegs<D> qr;
+    constexpr bool kB1 = kMode == 1;
     if constexpr (kB1) {
         // the sign-bit word of each 32-dim chunk this lane gates
         const uint32_t *bw = reinterpret_cast<const uint32_t *>(a.codes + static_cast<size_t>(q) * D);
@@ -442,125 +448,131 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                 break;
             }
             if (F == 0) continue;
-            bump((1u << VIS) | (1u << MSBC), static_cast<unsigned>(F));
+            bump((1u << VIS) | (kMode == 2 ? 0u : (1u << MSBC)), static_cast<unsigned>(F));
 
-            // ---- gate (paper-prune lower bound) for every fresh neighbour ----
-            // all MSB rows and factor rows are requested at once, then consumed group by group
-#if QG_GATE_ASYNC
-            if constexpr (L::LPN != 32) prefetch_rows_l1(ix.msb, s.fid, F, D / 8, D / 8, lane);
-#elif QG_GATE_PREFETCH == 0
-            prefetch_rows_l1(ix.msb, s.fid, F, D / 8, D / 8, lane);
-#else
-            if constexpr (L::LPN == 32)
-                prefetch_rows_l1(ix.msb, s.fid, F < L::GG ? F : L::GG, D / 8, D / 8, lane);
-            else
-                prefetch_rows_l1(ix.msb, s.fid, F, D / 8, D / 8, lane);
-#endif
-            prefetch_rows_l1(reinterpret_cast<const uint8_t *>(ix.pf), s.fid, F, 16, 16, lane);
-            for (int f = lane; f < F; f += 32) s.fpf[f] = ix.pf[s.fid[f]];
-            if constexpr (L::LPN == 32) {
-                constexpr int G = L::GG;
-#if QG_GATE_ASYNC
-                // rows of gate group `grp_i` to stage (grp_i & 1): G rows of D/8 bytes, 16-byte
-                // pieces spread over the lanes; rows past F are not copied
-                static_assert(G * (D / 8) <= QG_GATE_GROUP * 128, "gate stage size");
-                auto stage_rows = [&](int gbase, int st) {
-                    constexpr int kPieces = G * (D / 8) / 16;
-                    uint8_t *dst = s.gstage + st * (QG_GATE_GROUP * 128);
-#pragma unroll
-                    for (int c = lane; c < kPieces; c += 32) {
-                        const int r = c / (D / 128), off = (c % (D / 128)) * 16;
-                        if (gbase + r < F)
-                            cp_async16(dst + r * (D / 8) + off, ix.msb + static_cast<size_t>(s.fid[gbase + r]) * (D / 8) + off);
-                    }
-                    cp_async_commit();
-                };
-                stage_rows(0, 0);
-                stage_rows(G, 1);
-#endif
-                for (int gb = 0, st = 0; gb < F; gb += G, st ^= 1) {
-                    uint32_t w[G][L::CPL];
-#if QG_GATE_ASYNC
-                    cp_async_wait<1>();
-                    __syncwarp();
-                    const uint32_t *stage = reinterpret_cast<const uint32_t *>(s.gstage + st * (QG_GATE_GROUP * 128));
-#pragma unroll
-                    for (int g = 0; g < G; ++g) {
-#pragma unroll
-                        for (int j = 0; j < L::CPL; ++j) w[g][j] = stage[g * (D / 32) + lane + 32 * j];
-                    }
-                    __syncwarp();
-                    stage_rows(gb + 2 * G, st);
-#else
-#pragma unroll
-                    for (int g = 0; g < G; ++g) {
-                        const int f = gb + g < F ? gb + g : gb;
-                        const uint32_t *row = reinterpret_cast<const uint32_t *>(
-                            ix.msb + static_cast<size_t>(s.fid[f]) * (D / 8));
-#pragma unroll
-                        for (int j = 0; j < L::CPL; ++j) w[g][j] = row_load(row + lane + 32 * j);
-                    }
-#endif
-#if QG_GATE_PREFETCH == 1
-                    if (gb + G < F)
-                        prefetch_rows_l1(ix.msb, s.fid + gb + G, F - gb - G < G ? F - gb - G : G, D / 8, D / 8,
-                                         lane);
-#endif
-                    int p[G];
-#pragma unroll
-                    for (int g = 0; g < G; ++g) {
-                        int acc = 0;
-#pragma unroll
-                        for (int j = 0; j < L::CPL; ++j) {
-                            if constexpr (kB1)
-                                acc += __popc(w[g][j] ^ static_cast<uint32_t>(qr.xg[j][0]));
-                            else
-                                acc = gate_chunk(w[g][j], qr.xg[j], acc);
-                        }
-                        p[g] = acc;
-                    }
-                    const int tot = reduce_scatter<G>(p, lane);
-                    const int f = gb + lane;
-                    if (lane < G && f < F) {
-                        const GateOut go = kB1 ? finish_gate_b1(tot, s.fpf[f], scale, b1_es, qn, qn2, a.eps, D)
-                                               : finish_gate(tot, s.fpf[f], scale, csum, qn, qn2, a.eps);
-                        s.flb[f] = go.lower_bound;
-                        s.fsip[f] = go.short_ip;
-                        s.fval[f] = go.valid ? 1 : 0;
-                    }
-                }
-#if QG_GATE_ASYNC
-                cp_async_wait<0>();  // nothing is left in flight (the last groups copy no rows)
-#endif
+            if constexpr (kMode == 2) {
+                // B1Main: no gate; every fresh neighbour goes on, none can be pruned
+                for (int f = lane; f < F; f += 32) s.fval[f] = 0;
+                __syncwarp();
             } else {
-                constexpr int P = L::PG;
-                for (int fb = 0; fb < F; fb += P * L::NBP) {
-                    uint32_t w[P];
-#pragma unroll
-                    for (int pp = 0; pp < P; ++pp) {
-                        int f = fb + pp * L::NBP + grp;
-                        f = f < F ? f : fb;
-                        const uint32_t *row = reinterpret_cast<const uint32_t *>(
-                            ix.msb + static_cast<size_t>(s.fid[f]) * (D / 8));
-                        w[pp] = __ldg(row + sub);
-                    }
-#pragma unroll
-                    for (int pp = 0; pp < P; ++pp) {
-                        int acc = kB1 ? __popc(w[pp] ^ static_cast<uint32_t>(qr.xg[0][0])) : gate_chunk(w[pp], qr.xg[0], 0);
-#pragma unroll
-                        for (int o = 1; o < L::LPN; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-                        const int f = fb + pp * L::NBP + grp;
-                        if (sub == 0 && f < F) {
-                            const GateOut go = kB1 ? finish_gate_b1(acc, s.fpf[f], scale, b1_es, qn, qn2, a.eps, D)
-                                                   : finish_gate(acc, s.fpf[f], scale, csum, qn, qn2, a.eps);
+                // ---- gate (paper-prune lower bound) for every fresh neighbour ----
+                // all MSB rows and factor rows are requested at once, then consumed group by group
+    #if QG_GATE_ASYNC
+                if constexpr (L::LPN != 32) prefetch_rows_l1(ix.msb, s.fid, F, D / 8, D / 8, lane);
+    #elif QG_GATE_PREFETCH == 0
+                prefetch_rows_l1(ix.msb, s.fid, F, D / 8, D / 8, lane);
+    #else
+                if constexpr (L::LPN == 32)
+                    prefetch_rows_l1(ix.msb, s.fid, F < L::GG ? F : L::GG, D / 8, D / 8, lane);
+                else
+                    prefetch_rows_l1(ix.msb, s.fid, F, D / 8, D / 8, lane);
+    #endif
+                prefetch_rows_l1(reinterpret_cast<const uint8_t *>(ix.pf), s.fid, F, 16, 16, lane);
+                for (int f = lane; f < F; f += 32) s.fpf[f] = ix.pf[s.fid[f]];
+                if constexpr (L::LPN == 32) {
+                    constexpr int G = L::GG;
+    #if QG_GATE_ASYNC
+                    // rows of gate group `grp_i` to stage (grp_i & 1): G rows of D/8 bytes, 16-byte
+                    // pieces spread over the lanes; rows past F are not copied
+                    static_assert(G * (D / 8) <= QG_GATE_GROUP * 128, "gate stage size");
+                    auto stage_rows = [&](int gbase, int st) {
+                        constexpr int kPieces = G * (D / 8) / 16;
+                        uint8_t *dst = s.gstage + st * (QG_GATE_GROUP * 128);
+    #pragma unroll
+                        for (int c = lane; c < kPieces; c += 32) {
+                            const int r = c / (D / 128), off = (c % (D / 128)) * 16;
+                            if (gbase + r < F)
+                                cp_async16(dst + r * (D / 8) + off, ix.msb + static_cast<size_t>(s.fid[gbase + r]) * (D / 8) + off);
+                        }
+                        cp_async_commit();
+                    };
+                    stage_rows(0, 0);
+                    stage_rows(G, 1);
+    #endif
+                    for (int gb = 0, st = 0; gb < F; gb += G, st ^= 1) {
+                        uint32_t w[G][L::CPL];
+    #if QG_GATE_ASYNC
+                        cp_async_wait<1>();
+                        __syncwarp();
+                        const uint32_t *stage = reinterpret_cast<const uint32_t *>(s.gstage + st * (QG_GATE_GROUP * 128));
+    #pragma unroll
+                        for (int g = 0; g < G; ++g) {
+    #pragma unroll
+                            for (int j = 0; j < L::CPL; ++j) w[g][j] = stage[g * (D / 32) + lane + 32 * j];
+                        }
+                        __syncwarp();
+                        stage_rows(gb + 2 * G, st);
+    #else
+    #pragma unroll
+                        for (int g = 0; g < G; ++g) {
+                            const int f = gb + g < F ? gb + g : gb;
+                            const uint32_t *row = reinterpret_cast<const uint32_t *>(
+                                ix.msb + static_cast<size_t>(s.fid[f]) * (D / 8));
+    #pragma unroll
+                            for (int j = 0; j < L::CPL; ++j) w[g][j] = row_load(row + lane + 32 * j);
+                        }
+    #endif
+    #if QG_GATE_PREFETCH == 1
+                        if (gb + G < F)
+                            prefetch_rows_l1(ix.msb, s.fid + gb + G, F - gb - G < G ? F - gb - G : G, D / 8, D / 8,
+                                             lane);
+    #endif
+                        int p[G];
+    #pragma unroll
+                        for (int g = 0; g < G; ++g) {
+                            int acc = 0;
+    #pragma unroll
+                            for (int j = 0; j < L::CPL; ++j) {
+                                if constexpr (kB1)
+                                    acc += __popc(w[g][j] ^ static_cast<uint32_t>(qr.xg[j][0]));
+                                else
+                                    acc = gate_chunk(w[g][j], qr.xg[j], acc);
+                            }
+                            p[g] = acc;
+                        }
+                        const int tot = reduce_scatter<G>(p, lane);
+                        const int f = gb + lane;
+                        if (lane < G && f < F) {
+                            const GateOut go = kB1 ? finish_gate_b1(tot, s.fpf[f], scale, b1_es, qn, qn2, a.eps, D)
+                                                   : finish_gate(tot, s.fpf[f], scale, csum, qn, qn2, a.eps);
                             s.flb[f] = go.lower_bound;
                             s.fsip[f] = go.short_ip;
                             s.fval[f] = go.valid ? 1 : 0;
                         }
                     }
+    #if QG_GATE_ASYNC
+                    cp_async_wait<0>();  // nothing is left in flight (the last groups copy no rows)
+    #endif
+                } else {
+                    constexpr int P = L::PG;
+                    for (int fb = 0; fb < F; fb += P * L::NBP) {
+                        uint32_t w[P];
+    #pragma unroll
+                        for (int pp = 0; pp < P; ++pp) {
+                            int f = fb + pp * L::NBP + grp;
+                            f = f < F ? f : fb;
+                            const uint32_t *row = reinterpret_cast<const uint32_t *>(
+                                ix.msb + static_cast<size_t>(s.fid[f]) * (D / 8));
+                            w[pp] = __ldg(row + sub);
+                        }
+    #pragma unroll
+                        for (int pp = 0; pp < P; ++pp) {
+                            int acc = kB1 ? __popc(w[pp] ^ static_cast<uint32_t>(qr.xg[0][0])) : gate_chunk(w[pp], qr.xg[0], 0);
+    #pragma unroll
+                            for (int o = 1; o < L::LPN; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+                            const int f = fb + pp * L::NBP + grp;
+                            if (sub == 0 && f < F) {
+                                const GateOut go = kB1 ? finish_gate_b1(acc, s.fpf[f], scale, b1_es, qn, qn2, a.eps, D)
+                                                       : finish_gate(acc, s.fpf[f], scale, csum, qn, qn2, a.eps);
+                                s.flb[f] = go.lower_bound;
+                                s.fsip[f] = go.short_ip;
+                                s.fval[f] = go.valid ? 1 : 0;
+                            }
+                        }
+                    }
                 }
+                __syncwarp();
             }
-            __syncwarp();
 
             // ---- first check against the pool tail (ours_diskann.rs:1708-1725) ----
             int S = 0;
@@ -639,7 +651,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                         for (int g = 0; g < G; ++g) {
                             int acc = 0;
     #pragma unroll
-                            for (int j = 0; j < L::CPL; ++j) acc = trav_chunk(c[g][j], qr.xe[j], qr.xo[j], acc);
+                            for (int j = 0; j < L::CPL; ++j) acc = trav_chunk<kMode == 2>(c[g][j], qr.xe[j], qr.xo[j], acc);
                             p[g] = acc;
                         }
                         const int tot = reduce_scatter<G>(p, lane);
@@ -660,7 +672,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                         }
     #pragma unroll
                         for (int pp = 0; pp < P; ++pp) {
-                            int acc = trav_chunk(c[pp], qr.xe[0], qr.xo[0], 0);
+                            int acc = trav_chunk<kMode == 2>(c[pp], qr.xe[0], qr.xo[0], 0);
     #pragma unroll
                             for (int o = 1; o < L::LPN; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
                             const int i = ib + pp * L::NBP + grp;
@@ -672,12 +684,16 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                 // finish every survivor at once, one lane each (finishQuantizedTraversalDistance)
                 for (int i = lane; i < S; i += 32) {
                     const float2 h = s.shdr[i];
-                    s.sdist[i] = finish_traversal(h.x, h.y, s.fsip[s.sslot[i]], __float_as_int(s.sdist[i]), scale,
-                                                  csum, qn2);
+                    if constexpr (kMode == 2)
+                        s.sdist[i] = finish_b1main(h.x, h.y, __float_as_int(s.sdist[i]), csum, qn2);
+                    else
+                        s.sdist[i] = finish_traversal(h.x, h.y, s.fsip[s.sslot[i]], __float_as_int(s.sdist[i]),
+                                                      scale, csum, qn2);
                 }
                 __syncwarp();
                 // survivors whose gate was invalid use the full FP32 restore (mode 0)
-                for (int i = 0; i < S; ++i) any_full |= s.fval[s.sslot[i]] == 0;
+                if constexpr (kMode != 2)
+                    for (int i = 0; i < S; ++i) any_full |= s.fval[s.sslot[i]] == 0;
                 if (any_full) {
                     for (int i = 0; i < S; ++i) {
                         if (s.fval[s.sslot[i]]) continue;
@@ -919,7 +935,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
 #ifndef QG_SEARCH_THREADS
 #define QG_SEARCH_THREADS 256
 #endif
-template <int D, bool kB1>
+template <int D, int kMode>
 __global__ void __launch_bounds__(QG_SEARCH_THREADS, QG_SEARCH_MINBLOCKS) search_kernel(SearchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -948,7 +964,7 @@ __global__ void __launch_bounds__(QG_SEARCH_THREADS, QG_SEARCH_MINBLOCKS) search
             e += 1;
         }
         if (lane == 0) a.epochs[slot] = e;
-        search_one<D, kB1>(a, s, q, lane, tags, e & 0xFFFFu, stop_smem);
+        search_one<D, kMode>(a, s, q, lane, tags, e & 0xFFFFu, stop_smem);
         __syncwarp();
     }
 }
@@ -965,19 +981,23 @@ int search_supported_dim(int code_dim) {
            code_dim == 1024 || code_dim == 2048;
 }
 
-template <int D, bool kB1>
+template <int D, int kMode>
 static cudaError_t launch_dc(const SearchArgs &a, int grid, int wpb, cudaStream_t stream) {
     const size_t smem = search_block_smem(a.l_cap, wpb, a.stop_w != nullptr);
-    cudaError_t e = cudaFuncSetAttribute(search_kernel<D, kB1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(search_kernel<D, kMode>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    search_kernel<D, kB1><<<grid, wpb * 32, smem, stream>>>(a);
+    search_kernel<D, kMode><<<grid, wpb * 32, smem, stream>>>(a);
     return cudaGetLastError();
 }
 
 template <int D>
 static cudaError_t launch_d(const SearchArgs &a, int grid, int wpb, cudaStream_t stream) {
-    return a.b1 ? launch_dc<D, true>(a, grid, wpb, stream) : launch_dc<D, false>(a, grid, wpb, stream);
+    switch (a.mode) {
+        case 1: return launch_dc<D, 1>(a, grid, wpb, stream);
+        case 2: return launch_dc<D, 2>(a, grid, wpb, stream);
+        default: return launch_dc<D, 0>(a, grid, wpb, stream);
+    }
 }
 
 size_t search_block_smem(int l_cap, int wpb, bool stop_model) {
@@ -987,12 +1007,12 @@ size_t search_block_smem(int l_cap, int wpb, bool stop_model) {
 template <int D>
 static int blocks_per_sm_d(int l_cap, int wpb, bool stop_model) {
     const size_t smem = search_block_smem(l_cap, wpb, stop_model);
-    // the B1 instantiation shares the launch bounds and shared memory of the Int8 one
-    if (cudaFuncSetAttribute(search_kernel<D, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    // the B1 and B1Main instantiations share the launch bounds and shared memory of the Int8 one
+    if (cudaFuncSetAttribute(search_kernel<D, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(smem)) != cudaSuccess)
         return 0;
     int blocks = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, search_kernel<D, false>, wpb * 32, smem) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, search_kernel<D, 0>, wpb * 32, smem) !=
         cudaSuccess)
         return 0;
     return blocks;

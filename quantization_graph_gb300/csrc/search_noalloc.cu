@@ -170,7 +170,7 @@ extern "C" int qg_search_batch_noalloc(qg_index *index, const float *d_queries, 
     a.rerank = params->rerank_candidates;
     a.early_stop_hops = params->early_stop_hops;
     a.kth_stop = params->kth_stop;
-    a.b1 = space_query_bits(s) == 1 ? 1 : 0;
+    a.mode = space_search_mode(s);
     a.ids_out = d_ids;
     a.dists_out = d_dists;
     a.stats_out = d_stats;

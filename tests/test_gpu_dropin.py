@@ -2,8 +2,8 @@
 called exactly as the Rust side calls the reference's (ours_diskann.rs:45-242), against the
 golden vectors the reference produced (encode, copies, sidecar, symmetric distance, the
 batched gate / distance / residual kernels, the single-record restore; Int8 and Int4 query
-codecs) and against the reference's sentinels for what is not built (the Full and B1Main
-codecs).
+codecs; B1Main's 4-bit x 1-bit distance) and against the reference's sentinels for what is not
+built (the Full codecs).
 rabitq_build_vamana_graph is covered by test_gpu_vamana_build.py."""
 import ctypes as C
 
@@ -133,8 +133,33 @@ def test_sentinels_of_what_is_not_built(lib):
         rec = np.ascontiguousarray(g["compact"][0])
         assert np.isinf(lib.rabitq_query_distance_b1(sp, prep, _p(rec)))
         assert np.isinf(lib.rabitq_query_distance_with_paper(sp, prep, _p(rec), C.c_float(0.0)))
-        for codec in (0, 4, 5, 6):  # Full, B1Main, FullStaged, FullRerankScalar: not built, no prepared query
+        for codec in (0, 5, 6):  # Full, FullStaged, FullRerankScalar: not built, no prepared query
             lib.rabitq_set_query_coarse_codec(sp, codec)
             assert not C.c_void_p(lib.rabitq_prepare_query(sp, _p(query))).value
+    finally:
+        lib.rabitq_space_delete(sp)
+
+
+@pytest.mark.parametrize("name", ["kernels_d128", "kernels_d1536"])
+def test_b1main_distance_entry_points(lib, name):
+    """rabitq_query_distance_b1 and its batch form with a B1Main prepared query, against the
+    reference's query_distance_b1 for every query x record."""
+    g = load_golden(name)
+    v = load_golden("b1main_codec")
+    dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+    _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+    sp = _space(lib, dim, g["center"], 4)
+    try:
+        compact = g["compact"]
+        ids = np.arange(n, dtype=np.uint32)
+        for q in range(nq):
+            prep = C.c_void_p(lib.rabitq_prepare_query(sp, _p(np.ascontiguousarray(Q[q]))))
+            assert prep.value
+            single = np.array([lib.rabitq_query_distance_b1(sp, prep, C.c_void_p(compact[i].ctypes.data))
+                               for i in range(n)], np.float32)
+            np.testing.assert_array_equal(bits(single), bits(v[f"{name}_distance_b1"][q]))
+            out = np.zeros(n, np.float32)
+            assert lib.rabitq_query_distance_b1_batch(sp, prep, _p(ids), n, _p(compact), compact.shape[1], _p(out))
+            np.testing.assert_array_equal(bits(out), bits(v[f"{name}_distance_b1"][q]))
     finally:
         lib.rabitq_space_delete(sp)

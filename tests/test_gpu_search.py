@@ -203,3 +203,24 @@ def test_b1_codec_search_matches_reference(cuda):
         np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), v[f"search_c1_ids_L{L}"])
         np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(v[f"search_c1_dists_L{L}"]))
         np.testing.assert_array_equal(stats_matrix(r.stats), v[f"search_c1_stats_L{L}"])
+
+
+@pytest.mark.parametrize("name", ["search_c1", "search_c2"])
+def test_b1main_codec_search_matches_reference(cuda, name):
+    """The B1Main codec (no gate; every fresh neighbour by the 4-bit x 1-bit distance) through the
+    batched GPU search, against the reference: ids, distance bits, counters."""
+    torch = cuda
+    from quantization_graph_gb300.index import OursIndex
+    from quantization_graph_gb300.space import RabitqSpace
+
+    g = load_golden(name)
+    v = load_golden("b1main_codec")
+    _, Q = SEARCH_CASES[name]()
+    sp = RabitqSpace(int(g["dim"]), g["center"], codec=4)
+    ix = OursIndex(sp, g["compact"], g["residual"], g["msb"], g["factors"], g["degrees"], g["edges"])
+    q = torch.from_numpy(Q).cuda()
+    for L in (20, 40, 80):
+        r = ix.search(q, k=10, l_value=L, with_stats=True)
+        np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), v[f"{name}_ids_L{L}"])
+        np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(v[f"{name}_dists_L{L}"]))
+        np.testing.assert_array_equal(stats_matrix(r.stats), v[f"{name}_stats_L{L}"])
