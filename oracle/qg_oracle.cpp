@@ -123,7 +123,7 @@ struct qgo_space {
     size_t residual_bytes = 0;
     size_t msb_bytes = 0;
     uint32_t seed = 100;
-    int query_bits = 8;  // Int8 (codec 3), Int4 (codec 2) or B1 (codec 1, sign bits)
+    int query_bits = 8;  // Int8 (codec 3), Int4 (codec 2), B1 / B1Main (1, sign bits), Full (0: 32)
     std::vector<float> signs;
     std::vector<float> center;
     std::vector<float> rotated_center;
@@ -317,6 +317,27 @@ float restore_distance(const qgo_space &s, const qgo_prepared &q, const uint8_t 
     return finish_long(q, norm_sqr, long_scale, short_ip, remaining);
 }
 
+// query_distance_with_paper_msb (space_rabitq.h:3961-3966, 1609-1619): the restore's
+// remaining-bit sum (dotRemainingUint8FloatAvx512, :1052-1073: the same 16 lanes and
+// contractions) with the gate's FP32 short ip reused.
+float full_reuse_distance(const qgo_space &s, const qgo_prepared &q, const uint8_t *record, float short_ip) {
+    const float norm_sqr = get_f32(record);
+    const float long_scale = get_f32(record + 4);
+    if (long_scale <= 0.0f || !std::isfinite(long_scale)) return norm_sqr + q.query_norm_sqr;
+    const uint8_t *code = record + s.off_code_compact();
+    float rem[16] = {};
+    const float *r = q.rotated_residual.data();
+    for (size_t base = 0; base < s.pair_count; base += 16) {
+        for (int l = 0; l < 16; ++l) {
+            const size_t pair = base + l;
+            const uint8_t packed = code[pair];
+            rem[l] = std::fma(static_cast<float>(packed & 7U), r[2 * pair], rem[l]);           // FMA
+            rem[l] = std::fma(static_cast<float>((packed >> 4U) & 7U), r[2 * pair + 1], rem[l]);  // FMA
+        }
+    }
+    return finish_long(q, norm_sqr, long_scale, short_ip, reduce16(rem));
+}
+
 // finishQuantizedTraversalDistance (space_rabitq.h:4342-4358); every product is exact.
 float finish_traversal(const qgo_prepared &q, float norm_sqr, float long_scale, float short_ip,
                        int64_t remaining_dot) {
@@ -417,6 +438,21 @@ qgo_paper_estimate gate_b1_one(const qgo_space &s, const qgo_prepared &q, const 
     r.error_bound = max_cross > 0.0f ? eps * err_sum / max_cross : 0.0f;
     r.valid = std::isfinite(r.lower_bound) ? 1 : 0;
     return r;
+}
+
+// compute_full_paper_prune_estimate_batch_by_id AVX-512 path (space_rabitq.h:4427-4505): lane t
+// adds the rotated residual of dims 16k + t whose MSB bit is set (masked adds), the lanes are
+// reduced by the _mm512_reduce_add_ps tree, short ip = selected - half sum, then the sidecar finish.
+qgo_paper_estimate gate_full_one(const qgo_space &s, const qgo_prepared &q, const uint8_t *msb,
+                                 const Factors &f, float eps) {
+    float acc[16] = {};
+    const float *r = q.rotated_residual.data();
+    for (size_t dim = 0; dim < s.code_dim; dim += 16)
+        for (int t = 0; t < 16; ++t) {
+            const size_t i = dim + t;
+            acc[t] = acc[t] + (((msb[i >> 3U] >> (i & 7U)) & 1U) ? r[i] : 0.0f);
+        }
+    return finish_gate(q, reduce16(acc) - q.half_sum, f, eps);
 }
 
 // compute_residual_distance_intervals_batch_by_id AVX2 path (space_rabitq.h:5432-5548):
@@ -763,6 +799,7 @@ int qgo_prepare(const qgo_space *sp, const float *query, qgo_prepared *p) {
     p->int8_scale = 1.0f;
     p->code_sum = 0;
     std::fill(p->int8_code.begin(), p->int8_code.end(), 0);
+    if (s.query_bits == 32) return 0;  // Full: the FP32 residual only (space_rabitq.h:3489-3492)
     if (s.query_bits == 1) {  // B1: sign bits and the 1-bit estimator's scales (no integer codes)
         p->b1_code.assign(s.msb_bytes, 0);
         p->b1_signed_sum = 0;
@@ -833,19 +870,23 @@ void qgo_gate_batch(const qgo_space *s, const qgo_prepared *q, const uint32_t *i
         Factors f;
         std::memcpy(&f, fb + static_cast<size_t>(ids[i]) * factors_stride, sizeof(Factors));
         const uint8_t *msb = msb_base + static_cast<size_t>(ids[i]) * msb_stride;
-        out[i] = s->query_bits == 1 ? gate_b1_one(*s, *q, msb, f, eps) : gate_one(*s, *q, msb, f, eps);
+        out[i] = s->query_bits == 1    ? gate_b1_one(*s, *q, msb, f, eps)
+                 : s->query_bits == 32 ? gate_full_one(*s, *q, msb, f, eps)
+                                       : gate_one(*s, *q, msb, f, eps);
     }
 }
 
-// rabitq_query_distance_batch (rabitq_bridge.cpp:885-970): mode 2 = INT8 traversal reusing
-// the gate's short_ip, anything else here = full FP32 restore (mode 0).
+// rabitq_query_distance_batch (rabitq_bridge.cpp:885-970): mode 2 = integer traversal reusing
+// the gate's short_ip, modes 1 / 3 = the FP32 remaining bits reusing the Full gate's short ip,
+// anything else = full FP32 restore (mode 0).
 void qgo_distance_batch(const qgo_space *s, const qgo_prepared *q, const uint32_t *ids,
                         const uint8_t *modes, size_t count, const uint8_t *records,
                         size_t stride, const float *short_ips, float *out) {
     for (size_t i = 0; i < count; ++i) {
         const uint8_t *rec = records + static_cast<size_t>(ids[i]) * stride;
-        out[i] = modes[i] == 2 ? traversal_distance(*s, *q, rec, short_ips[i])
-                               : restore_distance(*s, *q, rec);
+        out[i] = modes[i] == 2                     ? traversal_distance(*s, *q, rec, short_ips[i])
+                 : (modes[i] == 1 || modes[i] == 3) ? full_reuse_distance(*s, *q, rec, short_ips[i])
+                                                    : restore_distance(*s, *q, rec);
     }
 }
 
@@ -1023,7 +1064,7 @@ extern "C" int qgo_search_one_with(const qgo_kernel_table *kt, const float *quer
                 f.slots.push_back(slot);
                 // survivors: the quantized traversal for the integer codecs, the FP32 restore
                 // for B1 and invalid estimates (ours_diskann.rs:1731-1748)
-                f.modes.push_back(paper.valid && prm->codec != 1 ? 2 : 0);
+                f.modes.push_back(!paper.valid ? 0 : prm->codec == 0 ? 1 : prm->codec == 1 ? 0 : 2);
                 f.short_ips.push_back(paper.short_ip);
                 if (f.ids.size() >= kDistBatch) flush_batch(kt, prep, pool, l_value, est, f, st);
             }
@@ -1493,8 +1534,9 @@ extern "C" int qgo_build_vamana(const qgo_space *space, const uint8_t *compact, 
 
 // rabitq_set_query_coarse_codec for the oracle: 3 = Int8, 2 = Int4; others return -1.
 extern "C" int qgo_space_set_query_codec(qgo_space *space, int codec) {
-    if (!space || (codec != 1 && codec != 2 && codec != 3 && codec != 4)) return -1;
-    space->query_bits = (codec == 1 || codec == 4) ? 1 : (codec == 2 ? 4 : 8);  // B1Main prepares like B1
+    if (!space || codec < 0 || codec > 4) return -1;
+    // B1Main prepares like B1; Full (0) keeps only the FP32 residual
+    space->query_bits = codec == 0 ? 32 : (codec == 1 || codec == 4) ? 1 : (codec == 2 ? 4 : 8);
     return 0;
 }
 

@@ -124,7 +124,8 @@ typedef struct {
     size_t early_stop_hops;
     int kth_stop;
     int codec; /* 3 Int8, 2 Int4 (quantized traversal), 1 B1 (survivors by the FP32 restore),
-                  4 B1Main (no gate: every fresh neighbour by the 4-bit x 1-bit distance) */
+                  4 B1Main (no gate: every fresh neighbour by the 4-bit x 1-bit distance),
+                  0 Full (FP32 gate; survivors by the remaining bits with the gate's short ip) */
 } qgo_search_params;
 
 int qgo_search_batch(const qgo_space *space, const float *queries, size_t nq,

@@ -11,7 +11,7 @@ ours_diskann.rs:1539-1986 (which cannot be built here) is driven over the refere
 bridge kernels (oracle/ref_probe.cpp).
 
 Inputs are regenerated from numpy seeds in the tests; a checksum of each input is stored
-to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants | space_states | int4 | b1 | build_edges | b1main]
+to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants | space_states | int4 | b1 | build_edges | b1main | full]
 """
 from __future__ import annotations
 
@@ -181,6 +181,40 @@ def b1main_cases():
     print("b1main_codec written")
 
 
+def full_cases():
+    """The Full query codec (FP32 query against the MSB plane; survivors by the FP32 remaining
+    bits reusing the gate's short ip, mode 1): gate and mode-1 distances for every query x record
+    of three kernel fixtures, and whole searches on the three search indexes."""
+    out = {}
+    for name in ("kernels_d128", "kernels_d960", "kernels_d1536"):
+        g = np.load(os.path.join(HERE, name + ".npz"))
+        dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+        _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+        ref = oracle_py.Reference(dim, g["center"], codec=0)
+        ids = np.arange(n, dtype=np.uint32)
+        gate, d1 = [], []
+        for q in Q:
+            ref.prepare(q)
+            est = ref.gate(ids, g["msb"], g["factors"], 1.9)
+            gate.append(est.view(np.uint8).reshape(n, -1))
+            d1.append(ref.distance(ids, np.full(n, 1, np.uint8), g["compact"], est["short_ip"]))
+        out[f"{name}_gate"] = np.array(gate)
+        out[f"{name}_dist_mode1"] = np.array(d1)
+    for name, fn in (("search_c1", c1_data), ("search_c2", c2_data), ("search_c3", c3_data)):
+        g = np.load(os.path.join(HERE, name + ".npz"))
+        _, Q = fn()
+        ref = oracle_py.Reference(int(g["dim"]), g["center"], codec=0)
+        index = dict(compact=g["compact"], residual=g["residual"], msb=g["msb"], factors=g["factors"],
+                     degrees=g["degrees"], edges=g["edges"], total_points=int(g["n"]), base_points=int(g["n"]))
+        for L in (20, 40):
+            ids, dists, stats = ref.search(Q, index, k=10, L=L, eps=1.9, rerank=100)
+            out[f"{name}_ids_L{L}"] = ids
+            out[f"{name}_dists_L{L}"] = dists
+            out[f"{name}_stats_L{L}"] = stats.view(np.uint64).reshape(len(Q), -1)
+    np.savez_compressed(os.path.join(HERE, "full_codec.npz"), **out)
+    print("full_codec written")
+
+
 def build_edges():
     """Reference graphs for duplicate / near-duplicate / zero vectors and a 3-node index."""
     X = build_edge_data()
@@ -269,6 +303,9 @@ def main():
     if sys.argv[1:] == ["b1main"]:
         b1main_cases()
         return
+    if sys.argv[1:] == ["full"]:
+        full_cases()
+        return
     kernel_case("kernels_d128", 128, 64, 8, seed=20260813, center_value=0.05)
     kernel_case("kernels_d100", 100, 48, 4, seed=5, center_value=None)
     kernel_case("kernels_d960", 960, 96, 4, seed=6, center_value=None)
@@ -286,6 +323,7 @@ def main():
     b1_cases()
     build_edges()
     b1main_cases()
+    full_cases()
     with open(os.path.join(HERE, "PROVENANCE.txt"), "w") as f:
         f.write(f"generated by tests/golden/make_golden.py on {platform.machine()} {platform.processor()}\n")
         f.write(f"reference bridge compiled with: {FLAGS}\n")

@@ -242,3 +242,34 @@ def test_b1main_search_bit_exact(oracle, name):
         np.testing.assert_array_equal(ids, v[f"{name}_ids_L{L}"])
         np.testing.assert_array_equal(bits(dists), bits(v[f"{name}_dists_L{L}"]))
         np.testing.assert_array_equal(stats.view(np.uint64).reshape(len(Q), -1), v[f"{name}_stats_L{L}"])
+
+
+@pytest.mark.parametrize("name", ["kernels_d128", "kernels_d960", "kernels_d1536"])
+def test_full_codec_gate_and_mode1_bit_exact(oracle, name):
+    """The Full codec: the FP32 masked gate (16 lanes over dimensions, the reduce tree) and the
+    mode-1 distance (remaining bits, the gate's short ip reused) against the reference."""
+    g = load_golden(name)
+    v = load_golden("full_codec")
+    dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+    _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+    o = oracle.Oracle(dim, g["center"], codec=0)
+    ids = np.arange(n, dtype=np.uint32)
+    for qi in range(nq):
+        o.prepare(Q[qi])
+        est = o.gate(ids, g["msb"], g["factors"])
+        np.testing.assert_array_equal(est.view(np.uint8).reshape(n, -1)[:, :21], v[f"{name}_gate"][qi][:, :21])
+        d1 = o.distance(ids, np.full(n, 1, np.uint8), g["compact"], est["short_ip"])
+        np.testing.assert_array_equal(bits(d1), bits(v[f"{name}_dist_mode1"][qi]))
+
+
+@pytest.mark.parametrize("name", ["search_c1", "search_c2", "search_c3"])
+def test_full_codec_search_bit_exact(oracle, name):
+    g = load_golden(name)
+    v = load_golden("full_codec")
+    _, Q = SEARCH_CASES[name]()
+    o = oracle.Oracle(int(g["dim"]), g["center"], codec=0)
+    for L in (20, 40):
+        ids, dists, stats = o.search(Q, golden_index(g), k=10, L=L, eps=1.9, rerank=100)
+        np.testing.assert_array_equal(ids, v[f"{name}_ids_L{L}"])
+        np.testing.assert_array_equal(bits(dists), bits(v[f"{name}_dists_L{L}"]))
+        np.testing.assert_array_equal(stats.view(np.uint64).reshape(len(Q), -1), v[f"{name}_stats_L{L}"])
