@@ -32,7 +32,8 @@ assert PAPER_ESTIMATE.itemsize == 24 and INTERVAL.itemsize == 12
 class SearchParams(C.Structure):
     _fields_ = [("k", C.c_size_t), ("l_value", C.c_size_t), ("beam_width", C.c_size_t),
                 ("epsilon0", C.c_float), ("rerank_candidates", C.c_size_t),
-                ("early_stop_hops", C.c_size_t), ("kth_stop", C.c_int), ("codec", C.c_int)]
+                ("early_stop_hops", C.c_size_t), ("kth_stop", C.c_int), ("codec", C.c_int),
+                ("fused_int_rerank", C.c_int)]
 
 
 def _p(a):
@@ -211,9 +212,23 @@ class Oracle:
         return out
 
     def search(self, queries, index, k=10, L=40, eps=1.9, rerank=100, beam=1, early_stop=0,
-               kth_stop=False, threads=0):
+               kth_stop=False, threads=0, fused=False):
+        """fused: the rerank of an Int8 / Int4 traversal by the fused restore + residual kernel
+        (the RABITQ_ENABLE_FUSED_INT_RERANK ablation)."""
         return _search(self.lib.qgo_search_batch, [self.space], queries, index, k, L, eps,
-                       rerank, beam, early_stop, kth_stop, threads, codec=self.codec)
+                       rerank, beam, early_stop, kth_stop, threads, codec=self.codec, fused=fused)
+
+    def full_residual(self, ids, records, residual):
+        """The fused restore + residual rerank (compute_full_residual_distance_intervals_batch_by_id,
+        space_rabitq.h:5557-5778) on the prepared query: [n, 3] (estimate, lower, upper)."""
+        ids = np.ascontiguousarray(ids, np.uint32)
+        records = np.ascontiguousarray(records)
+        residual = np.ascontiguousarray(residual)
+        out = np.zeros((len(ids), 3), np.float32)
+        self.lib.qgo_full_residual_batch(self.space, self.prep, _p(ids), C.c_size_t(len(ids)), _p(records),
+                                         C.c_size_t(records.shape[1]), _p(residual),
+                                         C.c_size_t(residual.shape[1]), _p(out))
+        return out
 
     def build_graph(self, compact, r=32, l_build=100, alpha=1.2, beam=1, batch=4096, refine=1,
                     cap=256, stop_hops=2, threads=0):
@@ -244,10 +259,10 @@ class Oracle:
 
 
 def _search(fn, lead_args, queries, index, k, L, eps, rerank, beam, early_stop, kth_stop, threads,
-            dim_arg=None, codec=3):
+            dim_arg=None, codec=3, fused=False):
     queries = np.ascontiguousarray(queries, np.float32)
     nq = queries.shape[0]
-    prm = SearchParams(k, L, beam, eps, rerank, early_stop, 1 if kth_stop else 0, codec)
+    prm = SearchParams(k, L, beam, eps, rerank, early_stop, 1 if kth_stop else 0, codec, 1 if fused else 0)
     ids = np.zeros((nq, k), np.uint32)
     dists = np.zeros((nq, k), np.float32)
     stats = np.zeros(nq, STATS)
@@ -380,6 +395,16 @@ class Reference:
                                              C.c_size_t(records.shape[1]), _p(short_ips), _p(out))
         return out
 
+    def full_residual(self, ids, records, residual):
+        """rabitq_full_residual_distance_batch (the fused FP32 restore + residual rerank kernel,
+        space_rabitq.h:5557-5778) on the most recently prepared query: [n, 3] (est, lo, hi)."""
+        ids = np.ascontiguousarray(ids, np.uint32)
+        out = np.zeros((len(ids), 3), np.float32)
+        self.lib.rabitq_full_residual_distance_batch(
+            self.space, self.prep, _p(ids), C.c_size_t(len(ids)), _p(records), C.c_size_t(records.shape[1]),
+            _p(residual), C.c_size_t(residual.shape[1]), _p(out))
+        return out
+
     def distance_b1(self, record):
         """rabitq_query_distance_b1 on the most recently prepared query (B1 / B1Main codecs)."""
         self.lib.rabitq_query_distance_b1.restype = C.c_float
@@ -434,6 +459,6 @@ class Reference:
         return degrees, edges
 
     def search(self, queries, index, k=10, L=40, eps=1.9, rerank=100, beam=1, early_stop=0,
-               kth_stop=False, threads=0):
+               kth_stop=False, threads=0, fused=False):
         return _search(self.lib.qgref_search_batch, [self.space], queries, index, k, L, eps, rerank,
-                       beam, early_stop, kth_stop, threads, dim_arg=self.dim, codec=self.codec)
+                       beam, early_stop, kth_stop, threads, dim_arg=self.dim, codec=self.codec, fused=fused)

@@ -458,8 +458,12 @@ qgo_paper_estimate gate_full_one(const qgo_space &s, const qgo_prepared &q, cons
 // compute_residual_distance_intervals_batch_by_id AVX2 path (space_rabitq.h:5432-5548):
 // per 16-dim block, 8 lanes of lo*qe + hi*qo (the add contracted), summed lane 0..7 in
 // order, then ips += scale * block_ip (contracted).
+// fused: the residual half of compute_full_residual_distance_intervals_batch_by_id
+// (space_rabitq.h:5700-5743, the AVX-512 build), where the compiler contracts the other
+// product of the pair: fma(lo, qe, hi*qo) instead of fma(hi, qo, lo*qe). The two orders
+// differ by one ulp on rare records.
 qgo_interval residual_interval(const qgo_space &s, const qgo_prepared &q, const uint8_t *res,
-                               float long_d) {
+                               float long_d, bool fused = false) {
     const uint8_t *scales = res + 8;
     const uint8_t *codes = res + 8 + s.scale_bytes;
     const float *r = q.rotated_residual.data();
@@ -478,8 +482,9 @@ qgo_interval residual_interval(const qgo_space &s, const qgo_prepared &q, const 
             int lo = packed & 0x0F, hi = packed >> 4;
             if (lo > 7) lo -= 16;
             if (hi > 7) hi -= 16;
-            const float prod = std::fma(static_cast<float>(hi), r[2 * pair + 1],
-                                        static_cast<float>(lo) * r[2 * pair]);  // FMA
+            const float prod =
+                fused ? std::fma(static_cast<float>(lo), r[2 * pair], static_cast<float>(hi) * r[2 * pair + 1])
+                      : std::fma(static_cast<float>(hi), r[2 * pair + 1], static_cast<float>(lo) * r[2 * pair]);
             block_ip += prod;
         }
         ips = std::fma(scale, block_ip, ips);  // FMA
@@ -901,6 +906,20 @@ void qgo_residual_batch(const qgo_space *s, const qgo_prepared *q, const uint32_
                                    long_d[i]);
 }
 
+// compute_full_residual_distance_intervals_batch_by_id (space_rabitq.h:5557-5778) behind
+// rabitq_full_residual_distance_batch (rabitq_bridge.cpp:1044-1084): the FP32 restore (its
+// long distance equals mode 0's, invalid records included) and the residual in the fused
+// kernel's product order.
+void qgo_full_residual_batch(const qgo_space *s, const qgo_prepared *q, const uint32_t *ids,
+                             size_t count, const uint8_t *records, size_t record_stride,
+                             const uint8_t *residual, size_t residual_stride, qgo_interval *out) {
+    for (size_t i = 0; i < count; ++i) {
+        const float long_d = restore_distance(*s, *q, records + static_cast<size_t>(ids[i]) * record_stride);
+        out[i] = residual_interval(*s, *q, residual + static_cast<size_t>(ids[i]) * residual_stride,
+                                   long_d, true);
+    }
+}
+
 }  // extern "C"
 
 // ------------------------------------------------------------------------------------------
@@ -1084,8 +1103,10 @@ extern "C" int qgo_search_one_with(const qgo_kernel_table *kt, const float *quer
             if (stall >= prm->early_stop_hops) break;
         }
     }
-    // rerank (ours_diskann.rs:1813-1902): INT8 traversal -> recompute the rerank set with
-    // the full FP32 restore (mode 0), then the residual correction, sort by (estimate, id).
+    // rerank (ours_diskann.rs:1813-1902): the residual correction of the pool distances, sorted
+    // by (estimate, id). After an INT8 / INT4 traversal the rerank set is first recomputed with
+    // the FP32 restore (mode 0), or, with the fused rerank switched on, both run as one kernel;
+    // the other codecs correct the distances the traversal left in the pool.
     size_t in_base = 0;
     for (const auto &c : pool) in_base += c.id < base_points ? 1 : 0;
     const size_t rerank_count = std::max(std::min(in_base, std::max(prm->rerank_candidates, k)), k);
@@ -1099,11 +1120,18 @@ extern "C" int qgo_search_one_with(const qgo_kernel_table *kt, const float *quer
     }
     std::vector<qgo_interval> iv(rids.size());
     if (!rids.empty()) {
-        std::vector<uint8_t> modes(rids.size(), 0);
-        std::vector<float> zeros(rids.size(), 0.0f);
-        kt->distance_batch(kt->ctx, prep, rids.data(), modes.data(), rids.size(), zeros.data(),
-                           rlong.data());
-        kt->residual_batch(kt->ctx, prep, rids.data(), rids.size(), rlong.data(), iv.data());
+        const bool int_query = prm->codec == 2 || prm->codec == 3;
+        if (int_query && prm->fused_int_rerank) {
+            kt->full_residual_batch(kt->ctx, prep, rids.data(), rids.size(), iv.data());
+        } else {
+            if (int_query) {
+                std::vector<uint8_t> modes(rids.size(), 0);
+                std::vector<float> zeros(rids.size(), 0.0f);
+                kt->distance_batch(kt->ctx, prep, rids.data(), modes.data(), rids.size(), zeros.data(),
+                                   rlong.data());
+            }
+            kt->residual_batch(kt->ctx, prep, rids.data(), rids.size(), rlong.data(), iv.data());
+        }
     }
     std::vector<std::pair<float, uint32_t>> rr(rids.size());
     for (size_t i = 0; i < rids.size(); ++i) rr[i] = {iv[i].estimate, rids[i]};
@@ -1170,6 +1198,11 @@ void ok_res(void *ctx, const void *p, const uint32_t *ids, size_t n, const float
     qgo_residual_batch(c->space, static_cast<const qgo_prepared *>(p), ids, n, c->records,
                        c->record_stride, c->residual, c->residual_stride, ld, out);
 }
+void ok_full_res(void *ctx, const void *p, const uint32_t *ids, size_t n, qgo_interval *out) {
+    auto *c = static_cast<OracleCtx *>(ctx);
+    qgo_full_residual_batch(c->space, static_cast<const qgo_prepared *>(p), ids, n, c->records,
+                            c->record_stride, c->residual, c->residual_stride, out);
+}
 
 }  // namespace
 
@@ -1190,7 +1223,7 @@ extern "C" int qgo_search_batch(const qgo_space *space, const float *queries, si
     {
         OracleCtx ctx{space, qgo_prepared_new(space), records, record_stride, residual,
                       residual_stride, msb, msb_stride, factors, factor_stride};
-        qgo_kernel_table kt{&ctx, ok_prepare, ok_distance, ok_gate, ok_dist, ok_res, ok_distance_b1};
+        qgo_kernel_table kt{&ctx, ok_prepare, ok_distance, ok_gate, ok_dist, ok_res, ok_distance_b1, ok_full_res};
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 1)
 #endif
@@ -1554,3 +1587,4 @@ extern "C" void qgo_prepared_export_b1(const qgo_prepared *p, uint8_t *bits, flo
     }
     if (signed_sum) *signed_sum = p->b1_signed_sum;
 }
+

@@ -111,6 +111,11 @@ void qgo_residual_batch(const qgo_space *space, const qgo_prepared *prepared,
                         const uint32_t *ids, size_t count, const uint8_t *records,
                         size_t record_stride, const uint8_t *residual, size_t residual_stride,
                         const float *long_distances, qgo_interval *out);
+/* compute_full_residual_distance_intervals_batch_by_id (space_rabitq.h:5557-5778) */
+void qgo_full_residual_batch(const qgo_space *space, const qgo_prepared *prepared,
+                             const uint32_t *ids, size_t count, const uint8_t *records,
+                             size_t record_stride, const uint8_t *residual, size_t residual_stride,
+                             qgo_interval *out);
 
 /* ---- search loop (ours_diskann.rs:1539-1986), batch of queries, OpenMP over queries ----
  * adjacency: fixed stride `edge_stride`, degrees[i] valid entries per row.
@@ -126,6 +131,8 @@ typedef struct {
     int codec; /* 3 Int8, 2 Int4 (quantized traversal), 1 B1 (survivors by the FP32 restore),
                   4 B1Main (no gate: every fresh neighbour by the 4-bit x 1-bit distance),
                   0 Full (FP32 gate; survivors by the remaining bits with the gate's short ip) */
+    int fused_int_rerank; /* Int8 / Int4: rerank by the fused restore + residual kernel
+                             (RABITQ_ENABLE_FUSED_INT_RERANK, ours_diskann.rs:1166-1172, 1831-1848) */
 } qgo_search_params;
 
 int qgo_search_batch(const qgo_space *space, const float *queries, size_t nq,
@@ -151,6 +158,9 @@ typedef struct {
                            const float *long_d, qgo_interval *out);
     /* 4-bit data x 1-bit query distance (B1Main; query_distance_b1, space_rabitq.h:3741-3753) */
     float (*distance_b1)(void *ctx, const void *prepared, uint32_t id);
+    /* fused FP32 restore + residual (rabitq_full_residual_distance_batch, rabitq_bridge.cpp:1044-1084) */
+    void (*full_residual_batch)(void *ctx, const void *prepared, const uint32_t *ids, size_t n,
+                                qgo_interval *out);
 } qgo_kernel_table;
 
 int qgo_search_one_with(const qgo_kernel_table *kt, const float *query,

@@ -37,6 +37,10 @@ bool rabitq_residual_distance_batch(const void *space, const void *prepared,
                                     size_t encoded_stride, const void *residual_base,
                                     size_t residual_stride, const float *long_distances,
                                     RabitqDistanceInterval *out);
+bool rabitq_full_residual_distance_batch(const void *space, const void *prepared,
+                                         const uint32_t *ids, size_t count, const void *encoded_base,
+                                         size_t encoded_stride, const void *residual_base,
+                                         size_t residual_stride, RabitqDistanceInterval *out);
 
 // scalars: [query_norm_sqr, query_norm, half_sum_residual, int8 (or int4) scale]
 void qgref_prepared_export(const void *prepared, size_t code_dim, float *rotated_residual,
@@ -147,6 +151,11 @@ void rk_res(void *ctx, const void *p, const uint32_t *ids, size_t n, const float
                                    c->residual_stride, ld,
                                    reinterpret_cast<RabitqDistanceInterval *>(out));
 }
+void rk_full_res(void *ctx, const void *p, const uint32_t *ids, size_t n, qgo_interval *out) {
+    auto *c = static_cast<RefCtx *>(ctx);
+    rabitq_full_residual_distance_batch(c->space, p, ids, n, c->records, c->record_stride, c->residual,
+                                        c->residual_stride, reinterpret_cast<RabitqDistanceInterval *>(out));
+}
 
 }  // namespace
 
@@ -165,7 +174,7 @@ extern "C" int qgref_search_batch(const void *space, size_t dim, const float *qu
     {
         RefCtx ctx{space, records, record_stride, residual, residual_stride,
                    msb, msb_stride, factors, factor_stride};
-        qgo_kernel_table kt{&ctx, rk_prepare, rk_distance, rk_gate, rk_dist, rk_res, rk_distance_b1};
+        qgo_kernel_table kt{&ctx, rk_prepare, rk_distance, rk_gate, rk_dist, rk_res, rk_distance_b1, rk_full_res};
 #pragma omp for schedule(dynamic, 1)
         for (long long q = 0; q < static_cast<long long>(nq); ++q) {
             const size_t qi = static_cast<size_t>(q);

@@ -11,7 +11,7 @@ ours_diskann.rs:1539-1986 (which cannot be built here) is driven over the refere
 bridge kernels (oracle/ref_probe.cpp).
 
 Inputs are regenerated from numpy seeds in the tests; a checksum of each input is stored
-to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants | space_states | int4 | b1 | build_edges | b1main | full]
+to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants | space_states | int4 | b1 | build_edges | b1main | full | fused]
 """
 from __future__ import annotations
 
@@ -215,6 +215,38 @@ def full_cases():
     print("full_codec written")
 
 
+def fused_rerank_cases():
+    """rabitq_full_residual_distance_batch, the reference's fused FP32 restore + residual rerank
+    kernel, for every query x record of three kernel fixtures, and whole Int8 / Int4 searches
+    with the fused rerank switched on (RABITQ_ENABLE_FUSED_INT_RERANK) on the search indexes."""
+    out = {}
+    for name in ("kernels_d128", "kernels_d960", "kernels_d1536"):
+        g = np.load(os.path.join(HERE, name + ".npz"))
+        dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+        _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+        ref = oracle_py.Reference(dim, g["center"])
+        ids = np.arange(n, dtype=np.uint32)
+        res = []
+        for q in Q:
+            ref.prepare(q)
+            res.append(ref.full_residual(ids, np.ascontiguousarray(g["compact"]), np.ascontiguousarray(g["residual"])))
+        out[name] = np.array(res)
+    for name, fn in (("search_c1", c1_data), ("search_c2", c2_data), ("search_c3", c3_data)):
+        g = np.load(os.path.join(HERE, name + ".npz"))
+        _, Q = fn()
+        index = dict(compact=g["compact"], residual=g["residual"], msb=g["msb"], factors=g["factors"],
+                     degrees=g["degrees"], edges=g["edges"], total_points=int(g["n"]), base_points=int(g["n"]))
+        for codec in (3, 2):
+            ref = oracle_py.Reference(int(g["dim"]), g["center"], codec=codec)
+            for L in (20, 40):
+                ids, dists, stats = ref.search(Q, index, k=10, L=L, eps=1.9, rerank=100, fused=True)
+                out[f"{name}_c{codec}_ids_L{L}"] = ids
+                out[f"{name}_c{codec}_dists_L{L}"] = dists
+                out[f"{name}_c{codec}_stats_L{L}"] = stats.view(np.uint64).reshape(len(Q), -1)
+    np.savez_compressed(os.path.join(HERE, "fused_rerank.npz"), **out)
+    print("fused_rerank written")
+
+
 def build_edges():
     """Reference graphs for duplicate / near-duplicate / zero vectors and a 3-node index."""
     X = build_edge_data()
@@ -306,6 +338,9 @@ def main():
     if sys.argv[1:] == ["full"]:
         full_cases()
         return
+    if sys.argv[1:] == ["fused"]:
+        fused_rerank_cases()
+        return
     kernel_case("kernels_d128", 128, 64, 8, seed=20260813, center_value=0.05)
     kernel_case("kernels_d100", 100, 48, 4, seed=5, center_value=None)
     kernel_case("kernels_d960", 960, 96, 4, seed=6, center_value=None)
@@ -324,6 +359,7 @@ def main():
     build_edges()
     b1main_cases()
     full_cases()
+    fused_rerank_cases()
     with open(os.path.join(HERE, "PROVENANCE.txt"), "w") as f:
         f.write(f"generated by tests/golden/make_golden.py on {platform.machine()} {platform.processor()}\n")
         f.write(f"reference bridge compiled with: {FLAGS}\n")

@@ -273,3 +273,45 @@ def test_full_codec_search_bit_exact(oracle, name):
         np.testing.assert_array_equal(ids, v[f"{name}_ids_L{L}"])
         np.testing.assert_array_equal(bits(dists), bits(v[f"{name}_dists_L{L}"]))
         np.testing.assert_array_equal(stats.view(np.uint64).reshape(len(Q), -1), v[f"{name}_stats_L{L}"])
+
+
+@pytest.mark.parametrize("name", ["kernels_d128", "kernels_d960", "kernels_d1536"])
+def test_fused_rerank_bit_exact(oracle, name):
+    """The fused restore + residual rerank (rabitq_full_residual_distance_batch) against the
+    reference's outputs for every query x record. Its long distance is the FP32 restore's; its
+    residual contracts the other product of each code pair, so on rare records it differs by one
+    ulp from restore-then-residual (the path of the default rerank), which is checked too."""
+    g = load_golden(name)
+    v = load_golden("fused_rerank")
+    dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+    _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+    o = oracle.Oracle(dim, g["center"])
+    ids = np.arange(n, dtype=np.uint32)
+    unfused_differs = 0
+    for qi in range(nq):
+        o.prepare(Q[qi])
+        iv = o.full_residual(ids, g["compact"], g["residual"])
+        np.testing.assert_array_equal(bits(iv), bits(v[name][qi]))
+        d0 = o.distance(ids, np.zeros(n, np.uint8), g["compact"], np.zeros(n, np.float32))
+        iv0 = o.residual(ids, g["compact"], g["residual"], d0).view(np.float32).reshape(n, 3)
+        unfused_differs += int((bits(iv0) != bits(iv)).any(1).sum())
+        assert np.all(np.abs(iv0.astype(np.float64) - iv) <= np.spacing(np.abs(iv)) * 1.01)
+    if name == "kernels_d128":
+        assert unfused_differs > 0  # the fixture holds a record where the two orders part
+
+
+@pytest.mark.parametrize("name", ["search_c1", "search_c2", "search_c3"])
+@pytest.mark.parametrize("codec", [3, 2])
+def test_fused_rerank_search_bit_exact(oracle, name, codec):
+    """Int8 / Int4 searches with the fused rerank switched on (RABITQ_ENABLE_FUSED_INT_RERANK,
+    ours_diskann.rs:1831-1848) against the reference's kernels: same traversal, the rerank by
+    rabitq_full_residual_distance_batch."""
+    g = load_golden(name)
+    v = load_golden("fused_rerank")
+    _, Q = SEARCH_CASES[name]()
+    o = oracle.Oracle(int(g["dim"]), g["center"], codec=codec)
+    for L in (20, 40):
+        ids, dists, stats = o.search(Q, golden_index(g), k=10, L=L, eps=1.9, rerank=100, fused=True)
+        np.testing.assert_array_equal(ids, v[f"{name}_c{codec}_ids_L{L}"])
+        np.testing.assert_array_equal(bits(dists), bits(v[f"{name}_c{codec}_dists_L{L}"]))
+        np.testing.assert_array_equal(stats.view(np.uint64).reshape(len(Q), -1), v[f"{name}_c{codec}_stats_L{L}"])
