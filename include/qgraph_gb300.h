@@ -189,7 +189,9 @@ bool rabitq_residual_distance_batch(const void *space, const void *prepared, con
                                     size_t encoded_stride, const void *residual_base,
                                     size_t residual_stride, const float *long_distances,
                                     RabitqDistanceInterval *out);
-/* rabitq_bridge.cpp:1044-1084 (fused restore + residual) */
+/* rabitq_bridge.cpp:1044-1084 (fused restore + residual; its residual contracts the other
+ * product of each code pair, space_rabitq.h:5700-5743, so it can differ by one ulp from
+ * rabitq_query_distance_batch mode 0 followed by rabitq_residual_distance_batch) */
 bool rabitq_full_residual_distance_batch(const void *space, const void *prepared,
                                          const uint32_t *ids, size_t count,
                                          const void *encoded_base, size_t encoded_stride,
@@ -220,6 +222,9 @@ typedef struct qg_search_params {
     int rerank_candidates;  /* residual rerank set size (reference 100) */
     int early_stop_hops;    /* stall stop (0 = off) */
     int kth_stop;           /* k-th bound stop (0 = off) */
+    int fused_int_rerank;   /* Int8 / Int4: rerank by the fused restore + residual kernel's
+                               arithmetic (RABITQ_ENABLE_FUSED_INT_RERANK, ours_diskann.rs:1166-1172,
+                               1831-1848; 0 = the two-kernel default) */
 } qg_search_params;
 
 /* The counters that verify_search_parity compares (ours_diskann.rs:1988-2066). */

@@ -25,7 +25,8 @@ SZ = C.c_size_t
 class SearchParams(C.Structure):
     """qg_search_params"""
     _fields_ = [("k", C.c_int), ("l_value", C.c_int), ("beam_width", C.c_int), ("epsilon0", C.c_float),
-                ("rerank_candidates", C.c_int), ("early_stop_hops", C.c_int), ("kth_stop", C.c_int)]
+                ("rerank_candidates", C.c_int), ("early_stop_hops", C.c_int), ("kth_stop", C.c_int),
+                ("fused_int_rerank", C.c_int)]
 
 
 class PaperEstimate(C.Structure):

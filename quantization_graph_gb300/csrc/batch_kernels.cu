@@ -151,7 +151,7 @@ __global__ void distance_pairs_kernel(const float *rr, const int8_t *codes, cons
 template <int D>
 __global__ void residual_pairs_kernel(const float *rr, const float4 *scal, const uint32_t *qidx,
                                       const uint32_t *ids, size_t count, const uint8_t *residual,
-                                      size_t residual_stride, const float *long_d,
+                                      size_t residual_stride, const float *long_d, bool fused,
                                       RabitqDistanceInterval *out) {
     const size_t pair = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (pair >= count) return;
@@ -161,7 +161,7 @@ __global__ void residual_pairs_kernel(const float *rr, const float4 *scal, const
     const uint8_t *rc = rec + 8 + 2 * (D / 16);
     float est, lo, hi;
     residual_interval_thread<D>(scales, rc, rr + static_cast<size_t>(q) * D, long_d[pair],
-                                scal[q].y, &est, &lo, &hi);
+                                scal[q].y, fused, &est, &lo, &hi);
     out[pair] = RabitqDistanceInterval{est, lo, hi};
 }
 
@@ -334,12 +334,12 @@ cudaError_t launch_distance_pairs(int code_dim, const float *rr, const int8_t *c
 cudaError_t launch_residual_pairs(int code_dim, const float *rr, const float4 *scal,
                                   const uint32_t *qidx, const uint32_t *ids, size_t count,
                                   const uint8_t *residual, size_t residual_stride,
-                                  const float *long_d, RabitqDistanceInterval *out,
+                                  const float *long_d, bool fused, RabitqDistanceInterval *out,
                                   cudaStream_t stream) {
     if (count == 0) return cudaSuccess;
     const unsigned int grid = static_cast<unsigned int>((count + 127) / 128);
     QG_DISPATCH_D(code_dim, residual_pairs_kernel<kD><<<grid, 128, 0, stream>>>(
-                                rr, scal, qidx, ids, count, residual, residual_stride, long_d, out));
+                                rr, scal, qidx, ids, count, residual, residual_stride, long_d, fused, out));
     return cudaGetLastError();
 }
 

@@ -250,7 +250,8 @@ bool distance_b1_host(const Space *s, const uint32_t *ids, size_t count, const u
 }
 
 bool residual_host(const Space *s, const uint32_t *ids, size_t count, const uint8_t *res_base,
-                   size_t res_stride, const float *long_d, RabitqDistanceInterval *out) {
+                   size_t res_stride, const float *long_d, RabitqDistanceInterval *out,
+                   bool fused = false) {
     const size_t rb = s->residual_bytes;
     Carve c;
     const size_t o_q = c.take(count * 4), o_i = c.take(count * 4), o_l = c.take(count * 4),
@@ -265,7 +266,7 @@ bool residual_host(const Space *s, const uint32_t *ids, size_t count, const uint
     if (!cuda_ok(launch_residual_pairs(static_cast<int>(s->code_dim), t_prepared.d_rr, t_prepared.d_scal,
                                        reinterpret_cast<uint32_t *>(d + o_q),
                                        reinterpret_cast<uint32_t *>(d + o_i), count, d + o_r, rb,
-                                       reinterpret_cast<float *>(d + o_l),
+                                       reinterpret_cast<float *>(d + o_l), fused,
                                        reinterpret_cast<RabitqDistanceInterval *>(d + o_o), st),
                  "residual kernel"))
         return false;
@@ -910,19 +911,15 @@ RabitqDistanceInterval rabitq_residual_distance_from_record(const void *space,
     }
 }
 
-bool rabitq_residual_distance_batch(const void *space, const void *prepared, const uint32_t *ids,
-                                    size_t count, const void *encoded_base,
-                                    size_t encoded_stride, const void *residual_base,
-                                    size_t residual_stride, const float *long_distances,
-                                    RabitqDistanceInterval *out) {
-    (void)encoded_base;
-    (void)encoded_stride;
+static bool residual_batch(const void *space, const void *prepared, const uint32_t *ids, size_t count,
+                           const void *residual_base, size_t residual_stride, const float *long_distances,
+                           RabitqDistanceInterval *out, bool fused) {
     try {
         const Space *s = as_space(space);
         bool ok = check_prepared(s, prepared) && ids && residual_base && long_distances;
         if (ok && count)
             ok = residual_host(s, ids, count, static_cast<const uint8_t *>(residual_base), residual_stride,
-                               long_distances, out);
+                               long_distances, out, fused);
         if (!ok)
             for (size_t i = 0; i < count; ++i)
                 out[i] = RabitqDistanceInterval{long_distances[i], long_distances[i], long_distances[i]};
@@ -932,6 +929,17 @@ bool rabitq_residual_distance_batch(const void *space, const void *prepared, con
             out[i] = RabitqDistanceInterval{long_distances[i], long_distances[i], long_distances[i]};
         return true;
     }
+}
+
+bool rabitq_residual_distance_batch(const void *space, const void *prepared, const uint32_t *ids,
+                                    size_t count, const void *encoded_base,
+                                    size_t encoded_stride, const void *residual_base,
+                                    size_t residual_stride, const float *long_distances,
+                                    RabitqDistanceInterval *out) {
+    (void)encoded_base;
+    (void)encoded_stride;
+    return residual_batch(space, prepared, ids, count, residual_base, residual_stride, long_distances, out,
+                          false);
 }
 
 bool rabitq_full_residual_distance_batch(const void *space, const void *prepared,
@@ -951,8 +959,9 @@ bool rabitq_full_residual_distance_batch(const void *space, const void *prepared
             for (size_t i = 0; i < count; ++i) out[i] = RabitqDistanceInterval{inf, inf, inf};
             return true;
         }
-        return rabitq_residual_distance_batch(space, prepared, ids, count, encoded_base, encoded_stride,
-                                              residual_base, residual_stride, longd.data(), out);
+        // the residual in the fused kernel's product order (space_rabitq.h:5700-5743)
+        return residual_batch(space, prepared, ids, count, residual_base, residual_stride, longd.data(), out,
+                              true);
     } catch (...) {
         for (size_t i = 0; i < count; ++i) out[i] = RabitqDistanceInterval{inf, inf, inf};
         return true;
@@ -1132,7 +1141,7 @@ int qg_residual_pairs(const void *space, const float *d_rotated, const float *d_
     if (!s) return QG_ERR_INVALID;
     if (!cuda_ok(launch_residual_pairs(static_cast<int>(s->code_dim), d_rotated,
                                        reinterpret_cast<const float4 *>(d_scalars), d_qidx, d_ids, count,
-                                       d_residual, residual_stride, d_long_distances, d_out,
+                                       d_residual, residual_stride, d_long_distances, false, d_out,
                                        static_cast<cudaStream_t>(stream)),
                  "residual kernel"))
         return QG_ERR_CUDA;
@@ -1541,6 +1550,7 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
     a.rerank = params->rerank_candidates;
     a.early_stop_hops = params->early_stop_hops;
     a.kth_stop = params->kth_stop;
+    a.fused_rerank = params->fused_int_rerank != 0 ? 1 : 0;  // used by mode 0 only
     a.mode = space_search_mode(s);
     a.ids_out = d_ids;
     a.dists_out = d_dists;

@@ -163,12 +163,15 @@ __device__ __forceinline__ float b1_alpha(long long packed) {
 // Residual rerank interval (compute_residual_distance_intervals_batch_by_id AVX2 path,
 // space_rabitq.h:5432-5548), one thread per record: per 16-dim block, eight lanes of
 // fma(hi, qo, lo*qe) summed in lane order, then ips = fma(scale, block_ip, ips).
+// fused: the product order of the fused restore + residual kernel
+// (compute_full_residual_distance_intervals_batch_by_id, space_rabitq.h:5700-5743),
+// fma(lo, qe, hi*qo); the two orders differ by one ulp on rare records.
 template <int D>
 __device__ __forceinline__ void residual_interval_thread(const uint16_t *__restrict__ scales,
                                                          const uint8_t *__restrict__ codes,
                                                          const float *__restrict__ rr, float long_d,
-                                                         float qn, float *est, float *lo_out,
-                                                         float *hi_out) {
+                                                         float qn, bool fused, float *est,
+                                                         float *lo_out, float *hi_out) {
     constexpr int kBlocks = D / 16;
     float ips = 0.0f;
     double err_sqr = 0.0;
@@ -188,7 +191,8 @@ __device__ __forceinline__ void residual_interval_thread(const uint16_t *__restr
             const float4 q = q4[j >> 1];
             const float qe = (j & 1) ? q.z : q.x;
             const float qo = (j & 1) ? q.w : q.y;
-            const float prod = __fmaf_rn(static_cast<float>(hi), qo, static_cast<float>(lo) * qe);
+            const float fl = static_cast<float>(lo), fh = static_cast<float>(hi);
+            const float prod = fused ? __fmaf_rn(fl, qe, __fmul_rn(fh, qo)) : __fmaf_rn(fh, qo, __fmul_rn(fl, qe));
             block_ip = block_ip + prod;
         }
         ips = __fmaf_rn(scale, block_ip, ips);

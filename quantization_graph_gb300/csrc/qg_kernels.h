@@ -50,6 +50,7 @@ struct SearchArgs {
     int rerank;
     int early_stop_hops;
     int kth_stop;
+    int fused_rerank;    // mode 0: rerank residual in the fused kernel's product order
     uint32_t *ids_out;
     float *dists_out;
     qg_search_stats *stats_out;
@@ -139,10 +140,11 @@ cudaError_t launch_distance_pairs(int code_dim, const float *rr, const int8_t *c
                                   const uint8_t *modes, size_t count, const uint8_t *records,
                                   size_t record_stride, const float *short_ips, float *out,
                                   cudaStream_t stream);
+// fused: the product order of the fused restore + residual rerank kernel
 cudaError_t launch_residual_pairs(int code_dim, const float *rr, const float4 *scal,
                                   const uint32_t *qidx, const uint32_t *ids, size_t count,
                                   const uint8_t *residual, size_t residual_stride,
-                                  const float *long_d, RabitqDistanceInterval *out,
+                                  const float *long_d, bool fused, RabitqDistanceInterval *out,
                                   cudaStream_t stream);
 cudaError_t launch_symmetric_pairs(int code_dim, const uint8_t *lhs, const uint8_t *rhs,
                                    size_t count, size_t stride, float *out, cudaStream_t stream);

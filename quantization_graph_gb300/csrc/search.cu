@@ -884,27 +884,32 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
         __syncwarp();
     }
     if (m > want) m = want;
-    prefetch_rows_l2(ix.codes, s.pid, m, D / 2, D / 2, lane);
+    if constexpr (kMode != 2) prefetch_rows_l2(ix.codes, s.pid, m, D / 2, D / 2, lane);
     prefetch_rows_l2(reinterpret_cast<const uint8_t *>(ix.res_scales), s.pid, m, D / 8, D / 8, lane);
     prefetch_rows_l2(ix.res_codes, s.pid, m, D / 2, D / 2, lane);
-    // FP32 4-bit restore (mode 0), two records per pass (one per half-warp)
-    for (int base = 0; base < m; base += 2) {
-        const int e = base + (lane >> 4);
-        const int ee = e < m ? e : base;
-        const uint32_t id = s.pid[ee];
-        const float4 h = ix.hdr[id];
-        const float d = restore_distance_hw<D>(ix.codes + static_cast<size_t>(id) * (D / 2), rr,
-                                               h.x, h.y, half_sum, qn2, lane & 15);
-        if ((lane & 15) == 0 && e < m) s.pd[e] = d;
+    // Int8 / Int4: the rerank set is recomputed by the FP32 4-bit restore (mode 0), two records
+    // per pass (one per half-warp). B1's pool already holds that distance (recomputing it changes
+    // nothing); B1Main's residual corrects the 4-bit x 1-bit distances in the pool
+    // (ours_diskann.rs:1849-1883).
+    if constexpr (kMode != 2) {
+        for (int base = 0; base < m; base += 2) {
+            const int e = base + (lane >> 4);
+            const int ee = e < m ? e : base;
+            const uint32_t id = s.pid[ee];
+            const float4 h = ix.hdr[id];
+            const float d = restore_distance_hw<D>(ix.codes + static_cast<size_t>(id) * (D / 2), rr,
+                                                   h.x, h.y, half_sum, qn2, lane & 15);
+            if ((lane & 15) == 0 && e < m) s.pd[e] = d;
+        }
+        __syncwarp();
     }
-    __syncwarp();
     // residual correction, one record per lane
     for (int e = lane; e < m; e += 32) {
         const uint32_t id = s.pid[e];
         float est, lo, hi;
         residual_interval_thread<D>(ix.res_scales + static_cast<size_t>(id) * (D / 16),
                                     ix.res_codes + static_cast<size_t>(id) * (D / 2), rr, s.pd[e],
-                                    qn, &est, &lo, &hi);
+                                    qn, kMode == 0 && a.fused_rerank != 0, &est, &lo, &hi);
         s.plb[e] = est;
     }
     __syncwarp();

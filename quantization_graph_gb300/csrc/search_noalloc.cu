@@ -170,6 +170,7 @@ extern "C" int qg_search_batch_noalloc(qg_index *index, const float *d_queries, 
     a.rerank = params->rerank_candidates;
     a.early_stop_hops = params->early_stop_hops;
     a.kth_stop = params->kth_stop;
+    a.fused_rerank = params->fused_int_rerank != 0 ? 1 : 0;  // used by mode 0 only
     a.mode = space_search_mode(s);
     a.ids_out = d_ids;
     a.dists_out = d_dists;

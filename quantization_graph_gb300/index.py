@@ -7,6 +7,7 @@ search_ours_paper_active's knobs (ours_diskann.rs:1174-1227).
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -73,10 +74,15 @@ class OursIndex:
                     k: int = 10, l_value: int = 100, beam_width: int = 1, epsilon0: float = 1.9,
                     rerank_candidates: int = 100, early_stop_hops: int = 0, kth_stop: bool = False,
                     stats_out: torch.Tensor | None = None, k_per_query: torch.Tensor | None = None,
-                    l_per_query: torch.Tensor | None = None) -> None:
-        """Stream-ordered search writing into preallocated CUDA outputs (no host sync)."""
+                    l_per_query: torch.Tensor | None = None, fused_int_rerank: bool | None = None) -> None:
+        """Stream-ordered search writing into preallocated CUDA outputs (no host sync).
+        fused_int_rerank: rerank an Int8 / Int4 traversal with the fused restore + residual
+        kernel's arithmetic; None reads RABITQ_ENABLE_FUSED_INT_RERANK as the reference does
+        (ours_diskann.rs:1166-1172)."""
+        if fused_int_rerank is None:
+            fused_int_rerank = os.environ.get("RABITQ_ENABLE_FUSED_INT_RERANK") is not None
         params = N.SearchParams(k, l_value, beam_width, epsilon0, rerank_candidates, early_stop_hops,
-                                1 if kth_stop else 0)
+                                1 if kth_stop else 0, 1 if fused_int_rerank else 0)
         N.check(self.lib.qg_search_batch(self.handle, _ptr(queries), queries.shape[0], C.byref(params),
                                          _ptr(k_per_query), _ptr(l_per_query), ids_out.shape[1], _ptr(ids_out),
                                          _ptr(dists_out), _ptr(stats_out), _stream()), "qg_search_batch")
@@ -96,8 +102,8 @@ class OursIndex:
     def search(self, queries, k: int = 10, l_value: int = 100, beam_width: int = 1,
                epsilon0: float = 1.9, rerank_candidates: int = 100, early_stop_hops: int = 0,
                kth_stop: bool = False, with_stats: bool = True, k_per_query=None,
-               l_per_query=None) -> SearchResult:
-        """Batched search_ours_paper_active with the Int8 codec; checks the device status."""
+               l_per_query=None, fused_int_rerank: bool | None = None) -> SearchResult:
+        """Batched search_ours_paper_active with the space's query codec; checks the device status."""
         q = _cuda(queries, torch.float32)
         nq = q.shape[0]
         kmax = int(max(k, int(torch.as_tensor(k_per_query).max())) if k_per_query is not None else k)
@@ -109,7 +115,8 @@ class OursIndex:
         stats = torch.empty((nq, 9), dtype=torch.int64, device="cuda") if with_stats else None
         self.search_into(q, ids, dists, k=kmax, l_value=lmax, beam_width=beam_width, epsilon0=epsilon0,
                          rerank_candidates=rerank_candidates, early_stop_hops=early_stop_hops,
-                         kth_stop=kth_stop, stats_out=stats, k_per_query=kq, l_per_query=lq)
+                         kth_stop=kth_stop, stats_out=stats, k_per_query=kq, l_per_query=lq,
+                         fused_int_rerank=fused_int_rerank)
         N.check(self.lib.qg_search_status(self.handle, _stream()), "search status")
         st = None
         if stats is not None:

@@ -163,3 +163,30 @@ def test_b1main_distance_entry_points(lib, name):
             np.testing.assert_array_equal(bits(out), bits(v[f"{name}_distance_b1"][q]))
     finally:
         lib.rabitq_space_delete(sp)
+
+
+@pytest.mark.parametrize("name", ["kernels_d128", "kernels_d960", "kernels_d1536"])
+def test_fused_rerank_entry_point(lib, name):
+    """rabitq_full_residual_distance_batch (the fused restore + residual rerank, in that kernel's
+    product order) against the reference's outputs for every query x record."""
+    from quantization_graph_gb300 import _native as N
+
+    g = load_golden(name)
+    v = load_golden("fused_rerank")
+    dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+    _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+    sp = _space(lib, dim, g["center"])
+    try:
+        compact, residual = g["compact"], g["residual"]
+        ids = np.arange(n, dtype=np.uint32)
+        for q in range(nq):
+            prep = C.c_void_p(lib.rabitq_prepare_query(sp, _p(np.ascontiguousarray(Q[q]))))
+            assert prep.value
+            iv = (N.DistanceInterval * n)()
+            assert lib.rabitq_full_residual_distance_batch(sp, prep, _p(ids), n, _p(compact), compact.shape[1],
+                                                           _p(residual), residual.shape[1], iv)
+            got = np.frombuffer(bytes(iv), np.float32).reshape(n, 3)
+            np.testing.assert_array_equal(bits(got), bits(v[name][q]))
+            lib.rabitq_release_query(sp, prep)
+    finally:
+        lib.rabitq_space_delete(sp)
