@@ -118,8 +118,10 @@ float rabitq_symmetric_distance(const void *space, const void *lhs, const void *
 const void *rabitq_prepare_query(const void *space, const float *query);
 /* rabitq_bridge.cpp:364-370. Codec ids: Full=0 B1=1 Int4=2 Int8=3 B1Main=4 FullStaged=5
  * FullRerankScalar=6 (space_rabitq.h:36-44). The GPU path implements Int8 (the formal codec),
- * Int4, B1 and B1Main; prepare_query returns NULL, and the batched qg_* search fails, for the
- * others. B1Main prepared codes are +-1 bytes with the sign sum in the code-sum slot.
+ * Int4, B1, B1Main and Full; prepare_query returns NULL, and the batched qg_* search fails, for
+ * the others. A new space starts with Full, as in the reference. B1Main prepared codes are +-1
+ * bytes with the sign sum in the code-sum slot; Full prepares no codes (the rotated residual and
+ * the scalars only, scale 1).
  * With B1 the prepared codes hold the sign bits, the scale slot the 1-bit short scale and the
  * code-sum slot the error scale (low word) and alpha (high word). */
 void rabitq_set_query_coarse_codec(void *space, int codec);
@@ -152,7 +154,8 @@ bool rabitq_paper_estimate_codec_batch(const void *space, const void *prepared,
                                        const uint8_t *msb_base, size_t msb_stride,
                                        const void *factors_base, size_t factors_stride,
                                        float epsilon0, RabitqPaperEstimate *out);
-/* rabitq_bridge.cpp:582-593: Full-codec reuse (mode 1); returns +inf (codec not built) */
+/* rabitq_bridge.cpp:582-593: Full-codec reuse (mode 1): the remaining bits with the given FP32
+ * short ip (query_distance_with_paper_msb, space_rabitq.h:3961-3966) */
 float rabitq_query_distance_with_paper(const void *space, const void *prepared,
                                        const void *encoded, float short_ip);
 /* rabitq_bridge.cpp:595-607 (mode 2: INT8 x remaining 3 bits) */
@@ -178,7 +181,7 @@ bool rabitq_paper_estimate_batch_sidecar(const void *space, const void *prepared
                                          const uint8_t *msb_base, size_t msb_stride,
                                          const void *factors_base, size_t factors_stride,
                                          float epsilon0, RabitqPaperEstimate *out);
-/* rabitq_bridge.cpp:885-970 (hot-loop flush and rerank restore; modes 0 and 2) */
+/* rabitq_bridge.cpp:885-970 (hot-loop flush and rerank restore; modes 0, 1 / 3 and 2) */
 bool rabitq_query_distance_batch(const void *space, const void *prepared, const uint32_t *ids,
                                  const uint8_t *modes, size_t count, const void *encoded_base,
                                  size_t encoded_stride, const float *short_ips,
@@ -391,7 +394,7 @@ int qg_build_vamana_device(const void *space, const uint8_t *d_compact, size_t n
 int qg_export_sidecar_device(const void *space, const uint8_t *d_compact, size_t n,
                              size_t compact_stride, uint8_t *d_msb, void *d_factors,
                              void *stream);
-/* GPU query preparation (space_rabitq.h:3429-3706, INT8 codec) for nq queries: rotated
+/* GPU query preparation (space_rabitq.h:3429-3706, by the space's codec) for nq queries: rotated
  * residual [nq x D] f32, int8 codes [nq x D], scalars [nq x 4] = {query_norm_sqr,
  * query_norm, half_sum_residual, int8_scale}, code sums [nq] int64. */
 int qg_prepare_batch(const void *space, const float *d_queries, size_t nq, float *d_rotated,
@@ -417,6 +420,12 @@ int qg_gate_pairs(const void *space, const int8_t *d_codes, const float *d_scala
                   const int64_t *d_code_sum, const uint32_t *d_qidx, const uint32_t *d_ids,
                   size_t count, const uint8_t *d_msb, size_t msb_stride, const void *d_factors,
                   size_t factor_stride, float epsilon0, RabitqPaperEstimate *d_out, void *stream);
+/* The Full codec's gate over pairs: the FP32 rotated residual (qg_prepare_batch's d_rotated)
+ * against the MSB plane (qg_gate_pairs refuses the Full codec). */
+int qg_gate_full_pairs(const void *space, const float *d_rotated, const float *d_scalars, const uint32_t *d_qidx,
+                       const uint32_t *d_ids, size_t count, const uint8_t *d_msb, size_t msb_stride,
+                       const void *d_factors, size_t factor_stride, float epsilon0, RabitqPaperEstimate *d_out,
+                       void *stream);
 int qg_distance_pairs(const void *space, const float *d_rotated, const int8_t *d_codes,
                       const float *d_scalars, const int64_t *d_code_sum, const uint32_t *d_qidx,
                       const uint32_t *d_ids, const uint8_t *d_modes, size_t count,

@@ -126,6 +126,7 @@ _SIGS = {
     "qg_dither_floor_pairs": (C.c_int, [P, P, P, SZ, P, P, P]),
     "qg_round_quotient_pairs": (C.c_int, [P, P, SZ, P, P, P]),
     "qg_gate_pairs": (C.c_int, [P, P, P, P, P, P, SZ, P, SZ, P, SZ, C.c_float, P, P]),
+    "qg_gate_full_pairs": (C.c_int, [P, P, P, P, P, SZ, P, SZ, P, SZ, C.c_float, P, P]),
     "qg_distance_pairs": (C.c_int, [P, P, P, P, P, P, P, P, SZ, P, SZ, P, P, P]),
     "qg_residual_pairs": (C.c_int, [P, P, P, P, P, SZ, P, SZ, P, P, P]),
 }

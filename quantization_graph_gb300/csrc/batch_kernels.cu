@@ -3,9 +3,9 @@
 // device re-layout of an uploaded index and the MSB sidecar extraction.
 //
 //   gate      rabitq_paper_estimate_batch_sidecar, Int8 branch (rabitq_bridge.cpp:747-778 ->
-//             space_rabitq.h:4991-5093, 4701-4721)
-//   distance  rabitq_query_distance_batch modes 2 and 0 (rabitq_bridge.cpp:885-970 ->
-//             space_rabitq.h:4234-4358, 4080-4202)
+//             space_rabitq.h:4991-5093, 4701-4721), B1 (:4607-4695) and Full (:4427-4505)
+//   distance  rabitq_query_distance_batch modes 2, 1 / 3 and 0 (rabitq_bridge.cpp:885-970 ->
+//             space_rabitq.h:4234-4358, 3961-3966, 4080-4202)
 //   residual  rabitq_residual_distance_batch (rabitq_bridge.cpp:972-1017 ->
 //             space_rabitq.h:5432-5548)
 //   sidecar   extract_paper_prune_sidecar (space_rabitq.h:4364-4392)
@@ -24,10 +24,16 @@ __device__ __forceinline__ float ld_f32(const uint8_t *p) {
     return __uint_as_float(v);
 }
 
-// PaperPruneFactors (20 bytes) -> device float4 with validity folded into cross_scale.
+// PaperPruneFactors (20 bytes) -> device float4 with validity folded into cross_scale and
+// error_cross_scale: both NaN when the valid flag is 0. A set flag implies a finite error cross
+// scale (extract_paper_prune_sidecar, space_rabitq.h:4364-4392), so a NaN there marks exactly the
+// records whose flag is 0.
 __device__ __forceinline__ float4 load_factors(const uint8_t *f) {
     float4 pf = make_float4(ld_f32(f), ld_f32(f + 4), ld_f32(f + 8), ld_f32(f + 12));
-    if (f[16] == 0) pf.z = __int_as_float(0x7fc00000);
+    if (f[16] == 0) {
+        pf.z = __int_as_float(0x7fc00000);
+        pf.w = __int_as_float(0x7fc00000);
+    }
     return pf;
 }
 
@@ -93,6 +99,35 @@ __global__ void gate_b1_pairs_kernel(const int8_t *codes, const float4 *scal, co
     }
 }
 
+// compute_full_paper_prune_estimate_batch_by_id (space_rabitq.h:4427-4505): the FP32 rotated
+// residual against the MSB plane, 16 lanes over dimensions and the reduce tree (each half-warp
+// computes the same sum), then the sidecar finish. One warp per pair.
+template <int D>
+__global__ void gate_full_pairs_kernel(const float *rr, const float4 *scal, const uint32_t *qidx,
+                                       const uint32_t *ids, size_t count, const uint8_t *msb, size_t msb_stride,
+                                       const uint8_t *factors, size_t factor_stride, float eps,
+                                       RabitqPaperEstimate *out) {
+    const size_t pair = (static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (pair >= count) return;
+    const uint32_t q = qidx[pair], id = ids[pair];
+    const float sel = full_gate_selected_hw<D>(msb + static_cast<size_t>(id) * msb_stride,
+                                               rr + static_cast<size_t>(q) * D, lane & 15);
+    if (lane == 0) {
+        const float4 pf = load_factors(factors + static_cast<size_t>(id) * factor_stride);
+        const float4 s = scal[q];
+        const GateOut g = finish_gate_full(sel - s.z, pf, s.y, s.x, eps);
+        RabitqPaperEstimate r;
+        r.lower_bound = g.lower_bound;
+        r.short_ip = g.short_ip;
+        r.alpha = 0.0f;
+        r.ip_hat = g.ip_hat;
+        r.error_bound = g.error_bound;
+        r.valid = g.valid ? 1 : 0;
+        out[pair] = r;
+    }
+}
+
 // query_distance_b1 over (query, record) pairs, one warp per pair; codes are the B1Main +-1
 // bytes, csum the sign sum.
 template <int D>
@@ -141,6 +176,11 @@ __global__ void distance_pairs_kernel(const float *rr, const int8_t *codes, cons
         for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
         if (lane == 0)
             out[pair] = finish_traversal(norm_sqr, long_scale, short_ips[pair], dot, s.w, csum[q], s.x);
+    } else if (modes[pair] == 1 || modes[pair] == 3) {
+        // query_distance_with_paper_msb: the remaining bits with the given FP32 short ip
+        const float d = full_distance_hw<D>(code, rr + static_cast<size_t>(q) * D, norm_sqr, long_scale, s.z,
+                                            s.x, true, short_ips[pair], lane & 15);
+        if (lane == 0) out[pair] = d;
     } else {
         const float d = restore_distance_hw<D>(code, rr + static_cast<size_t>(q) * D, norm_sqr,
                                                 long_scale, s.z, s.x, lane & 15);
@@ -306,6 +346,16 @@ cudaError_t launch_gate_pairs(int code_dim, const int8_t *codes, const float4 *s
                                     codes, scal, csum, qidx, ids, count, msb, msb_stride, factors,
                                     factor_stride, eps, out));
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gate_full_pairs(int code_dim, const float *rr, const float4 *scal, const uint32_t *qidx,
+                                   const uint32_t *ids, size_t count, const uint8_t *msb, size_t msb_stride,
+                                   const uint8_t *factors, size_t factor_stride, float eps, RabitqPaperEstimate *out,
+                                   cudaStream_t stream) {
+    if (count == 0) return cudaSuccess;
+    QG_DISPATCH_D(code_dim, gate_full_pairs_kernel<kD><<<warp_grid(count), 256, 0, stream>>>(
+                                rr, scal, qidx, ids, count, msb, msb_stride, factors, factor_stride, eps, out));
     return cudaGetLastError();
 }
 

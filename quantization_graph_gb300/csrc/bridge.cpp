@@ -178,12 +178,17 @@ bool gate_host(const Space *s, const uint32_t *ids, size_t count, const uint8_t 
     gather_rows(h + o_f, factors_base, factor_stride, ids, count, 20);
     cudaStream_t st = t_stage.stream;
     if (!cuda_ok(cudaMemcpyAsync(d, h, o_o, cudaMemcpyHostToDevice, st), "gate upload")) return false;
-    if (!cuda_ok(launch_gate_pairs(static_cast<int>(s->code_dim), t_prepared.d_codes, t_prepared.d_scal,
-                                   t_prepared.d_csum, reinterpret_cast<uint32_t *>(d + o_q),
-                                   reinterpret_cast<uint32_t *>(d + o_i), count, d + o_m, mb, d + o_f, 20,
-                                   eps, reinterpret_cast<RabitqPaperEstimate *>(d + o_o), st, s->codec == 1),
-                 "gate kernel"))
-        return false;
+    const cudaError_t ge =
+        s->codec == 0
+            ? launch_gate_full_pairs(static_cast<int>(s->code_dim), t_prepared.d_rr, t_prepared.d_scal,
+                                     reinterpret_cast<uint32_t *>(d + o_q), reinterpret_cast<uint32_t *>(d + o_i),
+                                     count, d + o_m, mb, d + o_f, 20, eps,
+                                     reinterpret_cast<RabitqPaperEstimate *>(d + o_o), st)
+            : launch_gate_pairs(static_cast<int>(s->code_dim), t_prepared.d_codes, t_prepared.d_scal,
+                                t_prepared.d_csum, reinterpret_cast<uint32_t *>(d + o_q),
+                                reinterpret_cast<uint32_t *>(d + o_i), count, d + o_m, mb, d + o_f, 20, eps,
+                                reinterpret_cast<RabitqPaperEstimate *>(d + o_o), st, s->codec == 1);
+    if (!cuda_ok(ge, "gate kernel")) return false;
     if (!cuda_ok(cudaMemcpyAsync(h + o_o, d + o_o, count * sizeof(RabitqPaperEstimate),
                                  cudaMemcpyDeviceToHost, st), "gate download"))
         return false;
@@ -659,7 +664,8 @@ const void *rabitq_prepare_query(const void *space, const float *query) {
         const Space *s = as_space(space);
         if (!s || !query) return nullptr;
         if (!space_query_bits(s)) {
-            set_error("the GPU query path implements the Int8 (3), Int4 (2) and B1 (1) query codecs");
+            set_error("the GPU query path implements the Full (0), B1 (1), Int4 (2), Int8 (3) and B1Main (4) "
+                      "query codecs");
             return nullptr;
         }
         Prepared &p = t_prepared;
@@ -840,9 +846,22 @@ bool rabitq_paper_estimate_batch(const void *space, const void *prepared, const 
     }
 }
 
-float rabitq_query_distance_with_paper(const void *, const void *, const void *, float) {
-    set_error("the Full-codec MSB reuse (mode 1) is not built");
-    return std::numeric_limits<float>::infinity();
+float rabitq_query_distance_with_paper(const void *space, const void *prepared, const void *encoded,
+                                       float short_ip) {
+    const float inf = std::numeric_limits<float>::infinity();
+    try {
+        const Space *s = as_space(space);
+        if (!check_prepared(s, prepared) || !encoded) return inf;
+        const uint32_t id = 0;
+        const uint8_t mode = 1;
+        float out = inf;
+        if (!distance_host(s, &id, &mode, 1, static_cast<const uint8_t *>(encoded), s->compact_bytes, &short_ip,
+                           &out))
+            return inf;
+        return out;
+    } catch (...) {
+        return inf;
+    }
 }
 
 float rabitq_query_distance_with_quantized_paper(const void *space, const void *prepared,
@@ -875,9 +894,6 @@ bool rabitq_query_distance_batch(const void *space, const void *prepared, const 
             ok = distance_host(s, ids, modes, count, static_cast<const uint8_t *>(encoded_base),
                                encoded_stride, short_ips, out_distances);
         if (!ok) std::fill(out_distances, out_distances + count, inf);
-        // modes 1 and 3 (Full-codec reuse) are not built: +inf, like a failed item
-        for (size_t i = 0; ok && i < count; ++i)
-            if (modes[i] == 1 || modes[i] == 3) out_distances[i] = inf;
         return true;
     } catch (...) {
         std::fill(out_distances, out_distances + count, inf);
@@ -1065,7 +1081,7 @@ int qg_prepare_batch(const void *space, const float *d_queries, size_t nq, float
         return QG_ERR_INVALID;
     }
     if (!space_query_bits(s)) {
-        set_error("the GPU query path implements the Int8 (3), Int4 (2) and B1 (1) query codecs");
+        set_error("the GPU query path implements the Full (0), B1 (1), Int4 (2), Int8 (3) and B1Main (4) query codecs");
         return QG_ERR_INVALID;
     }
     PrepArgs a{d_queries, s->dim, static_cast<int>(nq), static_cast<int>(s->dim),
@@ -1104,12 +1120,31 @@ int qg_gate_pairs(const void *space, const int8_t *d_codes, const float *d_scala
                   size_t factor_stride, float epsilon0, RabitqPaperEstimate *d_out, void *stream) {
     const Space *s = as_space(space);
     if (!s) return QG_ERR_INVALID;
+    if (s->codec == 0) {
+        set_error("qg_gate_pairs: the Full codec's gate reads the rotated residual; use qg_gate_full_pairs");
+        return QG_ERR_INVALID;
+    }
     if (!cuda_ok(launch_gate_pairs(static_cast<int>(s->code_dim), d_codes,
                                    reinterpret_cast<const float4 *>(d_scalars),
                                    reinterpret_cast<const long long *>(d_code_sum), d_qidx, d_ids, count,
                                    d_msb, msb_stride, static_cast<const uint8_t *>(d_factors),
                                    factor_stride, epsilon0, d_out, static_cast<cudaStream_t>(stream),
                                    s->codec == 1),
+                 "gate kernel"))
+        return QG_ERR_CUDA;
+    return QG_OK;
+}
+
+int qg_gate_full_pairs(const void *space, const float *d_rotated, const float *d_scalars, const uint32_t *d_qidx,
+                       const uint32_t *d_ids, size_t count, const uint8_t *d_msb, size_t msb_stride,
+                       const void *d_factors, size_t factor_stride, float epsilon0, RabitqPaperEstimate *d_out,
+                       void *stream) {
+    const Space *s = as_space(space);
+    if (!s) return QG_ERR_INVALID;
+    if (!cuda_ok(launch_gate_full_pairs(static_cast<int>(s->code_dim), d_rotated,
+                                        reinterpret_cast<const float4 *>(d_scalars), d_qidx, d_ids, count, d_msb,
+                                        msb_stride, static_cast<const uint8_t *>(d_factors), factor_stride, epsilon0,
+                                        d_out, static_cast<cudaStream_t>(stream)),
                  "gate kernel"))
         return QG_ERR_CUDA;
     return QG_OK;
@@ -1520,7 +1555,8 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
     if (nq == 0) return QG_OK;
     {
         if (!space_query_bits(s)) {
-            set_error("the GPU query path implements the Int8 (3), Int4 (2) and B1 (1) query codecs");
+            set_error("the GPU query path implements the Full (0), B1 (1), Int4 (2), Int8 (3) and B1Main (4) "
+                      "query codecs");
             return QG_ERR_INVALID;
         }
         PrepArgs pa{d_queries, s->dim, static_cast<int>(nq), static_cast<int>(s->dim),

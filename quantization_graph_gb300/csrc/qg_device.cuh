@@ -70,6 +70,52 @@ __device__ __forceinline__ float restore_distance_hw(const uint8_t *__restrict__
     return out;
 }
 
+// The Full codec's survivor distance: the restore's 16-lane sums with the gate's FP32 short ip
+// reused when `reuse` (query_distance_with_paper_msb, space_rabitq.h:3961-3966, 1609-1619; its
+// remaining-bit sum, dotRemainingUint8FloatAvx512 :1052-1073, has the restore's lanes and
+// contractions), else the restore itself (mode 0, invalid gates). Half-warp like
+// restore_distance_hw; every lane runs the same loop and shuffles whichever result is taken.
+template <int D>
+__device__ __forceinline__ float full_distance_hw(const uint8_t *__restrict__ code,
+                                                  const float *__restrict__ rr, float norm_sqr,
+                                                  float long_scale, float half_sum, float qn2, bool reuse,
+                                                  float gate_short_ip, int t) {
+    constexpr int kPairs = D / 2;
+    float sel = 0.0f, rem = 0.0f;
+#pragma unroll 8
+    for (int base = 0; base < kPairs; base += 16) {
+        const int pair = base + t;
+        const uint32_t packed = code[pair];
+        const uint32_t lo = packed & 0x0Fu, hi = packed >> 4;
+        const float2 q = *reinterpret_cast<const float2 *>(rr + 2 * pair);
+        rem = __fmaf_rn(static_cast<float>(lo & 7u), q.x, rem);
+        rem = __fmaf_rn(static_cast<float>(hi & 7u), q.y, rem);
+        if (lo > 7u) sel = sel + q.x;
+        if (hi > 7u) sel = sel + q.y;
+    }
+    sel = reduce16_tree(sel);
+    rem = reduce16_tree(rem);
+    const float short_ip = reuse ? gate_short_ip : sel - half_sum;
+    float out = finish_long(norm_sqr, long_scale, short_ip, rem, half_sum, qn2);
+    if (!(long_scale > 0.0f) || !f_isfinite(long_scale)) out = norm_sqr + qn2;
+    return out;
+}
+
+// The Full codec's gate sum (compute_full_paper_prune_estimate_batch_by_id AVX-512 path,
+// space_rabitq.h:4427-4505): lane t of a half-warp adds the rotated residual of dims 16k + t whose
+// MSB bit is set, then the _mm512_reduce_add_ps tree; lane 0 of the half-warp holds the sum.
+template <int D>
+__device__ __forceinline__ float full_gate_selected_hw(const uint8_t *__restrict__ msb,
+                                                       const float *__restrict__ rr, int t) {
+    float acc = 0.0f;
+#pragma unroll 8
+    for (int k = 0; k < D; k += 16) {
+        const int i = k + t;
+        acc = acc + (((static_cast<uint32_t>(msb[i >> 3]) >> (i & 7)) & 1u) ? rr[i] : 0.0f);
+    }
+    return reduce16_tree(acc);
+}
+
 // finishQuantizedTraversalDistance (space_rabitq.h:4342-4358); every product is exact. The
 // search calls it for all survivors of a hop in one warp-wide pass, so the double latency is
 // paid once per hop rather than once per group of survivors.
@@ -94,7 +140,7 @@ struct GateOut {
 
 // compute_paper_prune_estimate_int_msb_gate + finish_paper_prune_estimate_sidecar
 // (space_rabitq.h:4873-4899, 4701-4721). `pf` is the device copy of PaperPruneFactors with
-// validity folded into cross_scale (NaN when the factors are invalid).
+// validity folded into cross_scale and error_cross_scale (both NaN when the factors are invalid).
 __device__ __forceinline__ GateOut finish_gate(int32_t selected, const float4 pf, float scale,
                                                int64_t code_sum, float qn, float qn2, float eps) {
     GateOut r{0.0f, 0.0f, 0.0f, 0.0f, false, false};
@@ -104,6 +150,25 @@ __device__ __forceinline__ GateOut finish_gate(int32_t selected, const float4 pf
     const float short_ip =
         0.5f * scale * static_cast<float>(static_cast<int64_t>(2) * selected - code_sum);
     const float cross = short_ip * cross_scale;
+    const float max_cross = 2.0f * pf.y * qn;
+    const float up = fmaxf(-max_cross, fminf(max_cross, cross + eps * pf.w * qn));
+    r.lower_bound = pf.x + qn2 - up;
+    r.short_ip = short_ip;
+    r.ip_hat = max_cross > 0.0f ? cross / max_cross : 0.0f;
+    r.error_bound = max_cross > 0.0f ? eps * pf.w * qn / max_cross : 0.0f;
+    r.valid = f_isfinite(r.lower_bound);
+    return r;
+}
+
+// finish_paper_prune_estimate_sidecar (space_rabitq.h:4701-4721) for the Full codec's FP32 short
+// ip (selected sum - half sum): only the sidecar's valid flag is checked. `pf.w` (the error cross
+// scale, finite whenever that flag is set) is NaN exactly when the flag is 0.
+__device__ __forceinline__ GateOut finish_gate_full(float short_ip, const float4 pf, float qn, float qn2,
+                                                    float eps) {
+    GateOut r{0.0f, 0.0f, 0.0f, 0.0f, false, false};
+    if (!f_isfinite(pf.w)) return r;
+    r.reached = true;
+    const float cross = short_ip * pf.z;
     const float max_cross = 2.0f * pf.y * qn;
     const float up = fmaxf(-max_cross, fminf(max_cross, cross + eps * pf.w * qn));
     r.lower_bound = pf.x + qn2 - up;

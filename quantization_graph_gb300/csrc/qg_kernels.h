@@ -27,7 +27,8 @@ struct PrepArgs {
     long long *csum;
     const int *nq_dev;  // optional: the batch size read on the device (CUDA-graph replay)
     int qbits = 8;      // 8: Int8; 4: Int4 (scale max/8, codes in [-8, 7], second draw); 1: B1 (sign
-                        // bits); 2: B1Main (+-1 bytes, the sign sum in the code-sum slot)
+                        // bits); 2: B1Main (+-1 bytes, the sign sum in the code-sum slot); 32: Full
+                        // (the FP32 residual and scalars only)
 };
 
 struct SearchArgs {
@@ -44,7 +45,8 @@ struct SearchArgs {
     int k_stride;
     int l_cap;       // pool capacity per warp (>= every L and k)
     int mode;        // 0 Int8 / Int4; 1 B1 (sign bits, popcount gate, survivors by the FP32 restore);
-                     // 2 B1Main (+-1 codes, no gate, every fresh neighbour by the 4-bit x 1-bit distance)
+                     // 2 B1Main (+-1 codes, no gate, every fresh neighbour by the 4-bit x 1-bit distance);
+                     // 3 Full (FP32 gate, survivors by the remaining bits with the gate's short ip)
     int beam_width;
     float eps;
     int rerank;
@@ -134,6 +136,11 @@ cudaError_t launch_gate_pairs(int code_dim, const int8_t *codes, const float4 *s
                               size_t count, const uint8_t *msb, size_t msb_stride,
                               const uint8_t *factors, size_t factor_stride, float eps,
                               RabitqPaperEstimate *out, cudaStream_t stream, bool b1 = false);
+// the Full codec's gate: the FP32 rotated residual (rr) against the MSB plane
+cudaError_t launch_gate_full_pairs(int code_dim, const float *rr, const float4 *scal, const uint32_t *qidx,
+                                   const uint32_t *ids, size_t count, const uint8_t *msb, size_t msb_stride,
+                                   const uint8_t *factors, size_t factor_stride, float eps, RabitqPaperEstimate *out,
+                                   cudaStream_t stream);
 cudaError_t launch_distance_pairs(int code_dim, const float *rr, const int8_t *codes,
                                   const float4 *scal, const long long *csum,
                                   const uint32_t *qidx, const uint32_t *ids,

@@ -39,14 +39,18 @@ struct Space {
 };
 
 // Query code layout of the space's codec: Int8 (3) -> 8, Int4 (2) -> 4 (integer codes), B1 (1) ->
-// 1 (sign bits), B1Main (4) -> 2 (+-1 bytes); 0 for the codecs the GPU path does not build (Full
-// and the staged variants).
+// 1 (sign bits), B1Main (4) -> 2 (+-1 bytes), Full (0) -> 32 (the FP32 residual only); 0 for the
+// codecs the GPU path does not build (the staged and scalar Full variants).
 inline int space_query_bits(const Space *s) {
-    return s->codec == 3 ? 8 : (s->codec == 2 ? 4 : (s->codec == 1 ? 1 : (s->codec == 4 ? 2 : 0)));
+    return s->codec == 3 ? 8
+                         : (s->codec == 2 ? 4 : (s->codec == 1 ? 1 : (s->codec == 4 ? 2 : (s->codec == 0 ? 32 : 0))));
 }
 // Search mode of the codec: 0 integer codes (Int8 / Int4), 1 B1 (popcount gate), 2 B1Main (no
-// gate; every fresh neighbour by the 4-bit x 1-bit distance).
-inline int space_search_mode(const Space *s) { return s->codec == 1 ? 1 : (s->codec == 4 ? 2 : 0); }
+// gate; every fresh neighbour by the 4-bit x 1-bit distance), 3 Full (FP32 gate; survivors by the
+// remaining bits with the gate's short ip).
+inline int space_search_mode(const Space *s) {
+    return s->codec == 1 ? 1 : (s->codec == 4 ? 2 : (s->codec == 0 ? 3 : 0));
+}
 
 // Device-resident index: structure-of-arrays, every row 16-byte aligned.
 struct DevIndex {

@@ -286,6 +286,14 @@ __global__ void __launch_bounds__(128) prepare_queries_kernel(PrepArgs a) {
 
     const float qn2 = s_qn2;
     const float max_abs = s_max;
+    if (a.qbits == 32) {
+        // Full (space_rabitq.h:3489-3492): the FP32 residual and the scalars, no query codes
+        if (threadIdx.x == 0) {
+            a.scal[q] = make_float4(qn2, sqrtf(qn2), s_half * 0.5f, 1.0f);
+            a.csum[q] = 0;
+        }
+        return;
+    }
     if (a.qbits == 2) {
         // B1Main (space_rabitq.h:3493-3510): +-1 per dimension (r > 0 -> +1) as integer codes,
         // the sign sum in the code-sum slot

@@ -288,6 +288,9 @@ __device__ __forceinline__ void load_query(QueryRegs<D> &r, const int8_t *codes,
 // survivor takes the FP32 restore (mode 0, as the Rust loop assigns, ours_diskann.rs:1731-1748).
 // kMode 2, B1Main: no gate; every fresh neighbour is scored by the 4-bit x 1-bit distance
 // (query_distance_b1) from +-1 query bytes and inserted (ours_diskann.rs:1661-1682).
+// kMode 3, Full: the FP32 rotated residual against the MSB plane (16 lanes over dimensions and
+// the reduce tree, half a warp per neighbour) gates; survivors with a valid gate take the
+// remaining bits with the gate's short ip (mode 1), the others the FP32 restore (mode 0).
 template <int D, int kMode>
 __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int lane,
                            uint16_t *tags, uint32_t tag, const uint32_t *stop_smem) {
@@ -334,7 +337,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
         const uint32_t *bw = reinterpret_cast<const uint32_t *>(a.codes + static_cast<size_t>(q) * D);
 #pragma unroll
         for (int j = 0; j < L::CPL; ++j) qr.xg[j][0] = static_cast<int>(bw[sub + L::LPN * j]);
-    } else {
+    } else if constexpr (kMode != 3) {
         load_query<D>(qr, a.codes + static_cast<size_t>(q) * D, sub);
     }
     const float b1_es = kB1 ? b1_error_scale(csum) : 0.0f;
@@ -453,6 +456,23 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             if constexpr (kMode == 2) {
                 // B1Main: no gate; every fresh neighbour goes on, none can be pruned
                 for (int f = lane; f < F; f += 32) s.fval[f] = 0;
+                __syncwarp();
+            } else if constexpr (kMode == 3) {
+                // Full: FP32 gate, two neighbours per pass (one per half-warp)
+                for (int f = lane; f < F; f += 32) s.fpf[f] = ix.pf[s.fid[f]];
+                __syncwarp();
+                for (int base = 0; base < F; base += 2) {
+                    const int f = base + (lane >> 4);
+                    const int ff = f < F ? f : base;
+                    const float sel = full_gate_selected_hw<D>(ix.msb + static_cast<size_t>(s.fid[ff]) * (D / 8), rr,
+                                                               lane & 15);
+                    if ((lane & 15) == 0 && f < F) {
+                        const GateOut go = finish_gate_full(sel - half_sum, s.fpf[f], qn, qn2, a.eps);
+                        s.flb[f] = go.lower_bound;
+                        s.fsip[f] = go.short_ip;
+                        s.fval[f] = go.valid ? 1 : 0;
+                    }
+                }
                 __syncwarp();
             } else {
                 // ---- gate (paper-prune lower bound) for every fresh neighbour ----
@@ -616,7 +636,21 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                 const float4 h = ix.hdr[s.sid[i]];
                 s.shdr[i] = make_float2(h.x, h.y);
             }
-            if constexpr (kB1) {
+            __syncwarp();  // the survivor passes below read headers other lanes loaded
+            if constexpr (kMode == 3) {
+                // Full: mode 1 (the gate's short ip reused) for valid gates, mode 0 otherwise; two
+                // survivors per pass (one per half-warp)
+                for (int base = 0; base < S; base += 2) {
+                    const int i = base + (lane >> 4);
+                    const int ii = i < S ? i : base;
+                    const float2 h = s.shdr[ii];
+                    const uint32_t slot = s.sslot[ii];
+                    const float d = full_distance_hw<D>(ix.codes + static_cast<size_t>(s.sid[ii]) * (D / 2), rr, h.x,
+                                                        h.y, half_sum, qn2, s.fval[slot] != 0, s.fsip[slot], lane & 15);
+                    if ((lane & 15) == 0 && i < S) s.sdist[i] = d;
+                }
+                __syncwarp();
+            } else if constexpr (kB1) {
                 // B1: every survivor by the FP32 restore, two per pass (one per half-warp)
                 for (int base = 0; base < S; base += 2) {
                     const int i = base + (lane >> 4);
@@ -884,14 +918,14 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
         __syncwarp();
     }
     if (m > want) m = want;
-    if constexpr (kMode != 2) prefetch_rows_l2(ix.codes, s.pid, m, D / 2, D / 2, lane);
+    if constexpr (kMode <= 1) prefetch_rows_l2(ix.codes, s.pid, m, D / 2, D / 2, lane);
     prefetch_rows_l2(reinterpret_cast<const uint8_t *>(ix.res_scales), s.pid, m, D / 8, D / 8, lane);
     prefetch_rows_l2(ix.res_codes, s.pid, m, D / 2, D / 2, lane);
     // Int8 / Int4: the rerank set is recomputed by the FP32 4-bit restore (mode 0), two records
     // per pass (one per half-warp). B1's pool already holds that distance (recomputing it changes
-    // nothing); B1Main's residual corrects the 4-bit x 1-bit distances in the pool
-    // (ours_diskann.rs:1849-1883).
-    if constexpr (kMode != 2) {
+    // nothing); B1Main's and Full's residuals correct the distances in the pool (4-bit x 1-bit,
+    // mode 1) (ours_diskann.rs:1849-1883).
+    if constexpr (kMode <= 1) {
         for (int base = 0; base < m; base += 2) {
             const int e = base + (lane >> 4);
             const int ee = e < m ? e : base;
@@ -1001,6 +1035,7 @@ static cudaError_t launch_d(const SearchArgs &a, int grid, int wpb, cudaStream_t
     switch (a.mode) {
         case 1: return launch_dc<D, 1>(a, grid, wpb, stream);
         case 2: return launch_dc<D, 2>(a, grid, wpb, stream);
+        case 3: return launch_dc<D, 3>(a, grid, wpb, stream);
         default: return launch_dc<D, 0>(a, grid, wpb, stream);
     }
 }
@@ -1012,7 +1047,7 @@ size_t search_block_smem(int l_cap, int wpb, bool stop_model) {
 template <int D>
 static int blocks_per_sm_d(int l_cap, int wpb, bool stop_model) {
     const size_t smem = search_block_smem(l_cap, wpb, stop_model);
-    // the B1 and B1Main instantiations share the launch bounds and shared memory of the Int8 one
+    // the B1, B1Main and Full instantiations share the launch bounds and shared memory of the Int8 one
     if (cudaFuncSetAttribute(search_kernel<D, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(smem)) != cudaSuccess)
         return 0;

@@ -143,7 +143,7 @@ extern "C" int qg_search_batch_noalloc(qg_index *index, const float *d_queries, 
         return fail(QG_ERR_CUDA, std::string("qg_search_batch_noalloc: clear: ") + cudaGetErrorString(e));
 
     if (!space_query_bits(s))
-        return fail(QG_ERR_INVALID, "qg_search_batch_noalloc: the Int8 (3), Int4 (2) and B1 (1) query codecs only");
+        return fail(QG_ERR_INVALID, "qg_search_batch_noalloc: the Full (0), B1 (1), Int4 (2), Int8 (3) and B1Main (4) query codecs only");
     PrepArgs pa{d_queries, s->dim, static_cast<int>(nq), static_cast<int>(s->dim), static_cast<int>(D),
                 s->d_signs, s->d_center, s->d_rotated_center, s->d_center_norm,
                 reinterpret_cast<float *>(sb + o_rr), reinterpret_cast<int8_t *>(sb + o_codes),

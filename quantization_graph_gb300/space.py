@@ -15,7 +15,7 @@ import torch
 
 from . import _native as N
 
-CODEC_FULL, CODEC_B1, CODEC_INT4, CODEC_INT8 = 0, 1, 2, 3
+CODEC_FULL, CODEC_B1, CODEC_INT4, CODEC_INT8, CODEC_B1MAIN = 0, 1, 2, 3, 4
 
 
 def _ptr(t: torch.Tensor | None) -> C.c_void_p:
@@ -72,6 +72,7 @@ class RabitqSpace:
             raise RuntimeError(f"rabitq_space_set_center failed: {N.last_error()}")
         self.center = center
         self.seed = int(seed)
+        self.codec = int(codec)
         self.lib.rabitq_set_query_coarse_codec(self.ptr, codec)
         self.code_dim = self.lib.rabitq_paper_msb_code_bytes(self.ptr) * 8
 
@@ -98,6 +99,7 @@ class RabitqSpace:
         return self.lib.rabitq_paper_factor_bytes()
 
     def set_query_coarse_codec(self, codec: int) -> None:
+        self.codec = int(codec)
         self.lib.rabitq_set_query_coarse_codec(self.ptr, codec)
 
     def encode(self, data: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
@@ -123,8 +125,9 @@ class RabitqSpace:
         return msb, factors
 
     def prepare(self, queries: torch.Tensor) -> dict:
-        """Batched INT8 (or INT4, by the space's codec) query preparation (prepare_query,
-        space_rabitq.h:3700)."""
+        """Batched query preparation by the space's codec (prepare_query, space_rabitq.h:3700):
+        INT8 / INT4 codes, B1 sign bits, B1Main +-1 bytes; the Full codec writes no codes (only
+        the rotated residual and the scalars)."""
         q = _cuda(queries, torch.float32)
         nq = q.shape[0]
         D = self.code_dim
@@ -142,6 +145,12 @@ class RabitqSpace:
         ids = _cuda(ids, torch.int32)
         n = ids.shape[0]
         out = torch.empty((n, 24), dtype=torch.uint8, device="cuda")
+        if self.codec == CODEC_FULL:
+            N.check(self.lib.qg_gate_full_pairs(self.ptr, _ptr(prepared["rotated_residual"]),
+                                                _ptr(prepared["scalars"]), _ptr(qidx), _ptr(ids), n, _ptr(msb),
+                                                msb.shape[1], _ptr(factors), factors.shape[1], epsilon0, _ptr(out),
+                                                _stream()), "qg_gate_full_pairs")
+            return out
         N.check(self.lib.qg_gate_pairs(self.ptr, _ptr(prepared["codes"]), _ptr(prepared["scalars"]),
                                        _ptr(prepared["code_sum"]), _ptr(qidx), _ptr(ids), n, _ptr(msb),
                                        msb.shape[1], _ptr(factors), factors.shape[1], epsilon0, _ptr(out),

@@ -2,8 +2,9 @@
 called exactly as the Rust side calls the reference's (ours_diskann.rs:45-242), against the
 golden vectors the reference produced (encode, copies, sidecar, symmetric distance, the
 batched gate / distance / residual kernels, the single-record restore; Int8 and Int4 query
-codecs; B1Main's 4-bit x 1-bit distance) and against the reference's sentinels for what is not
-built (the Full codecs).
+codecs; B1Main's 4-bit x 1-bit distance; the Full codec's FP32 gate and mode-1 distance; the
+fused rerank) and against the reference's sentinels for what is not built (the staged Full
+variants).
 rabitq_build_vamana_graph is covered by test_gpu_vamana_build.py."""
 import ctypes as C
 
@@ -131,9 +132,8 @@ def test_sentinels_of_what_is_not_built(lib):
         query = np.ascontiguousarray(Q[0])
         prep = C.c_void_p(lib.rabitq_prepare_query(sp, _p(query)))
         rec = np.ascontiguousarray(g["compact"][0])
-        assert np.isinf(lib.rabitq_query_distance_b1(sp, prep, _p(rec)))
-        assert np.isinf(lib.rabitq_query_distance_with_paper(sp, prep, _p(rec), C.c_float(0.0)))
-        for codec in (0, 5, 6):  # Full, FullStaged, FullRerankScalar: not built, no prepared query
+        assert np.isinf(lib.rabitq_query_distance_b1(sp, prep, _p(rec)))  # needs a B1Main prepared query
+        for codec in (5, 6):  # FullStaged, FullRerankScalar: not built, no prepared query
             lib.rabitq_set_query_coarse_codec(sp, codec)
             assert not C.c_void_p(lib.rabitq_prepare_query(sp, _p(query))).value
     finally:
@@ -187,6 +187,49 @@ def test_fused_rerank_entry_point(lib, name):
                                                            _p(residual), residual.shape[1], iv)
             got = np.frombuffer(bytes(iv), np.float32).reshape(n, 3)
             np.testing.assert_array_equal(bits(got), bits(v[name][q]))
+            lib.rabitq_release_query(sp, prep)
+    finally:
+        lib.rabitq_space_delete(sp)
+
+
+@pytest.mark.parametrize("name", ["kernels_d128", "kernels_d960", "kernels_d1536"])
+def test_full_codec_entry_points(lib, name):
+    """The Full codec: the FP32 MSB gate (rabitq_paper_estimate_batch_sidecar) and the mode-1
+    distance with the gate's short ip (rabitq_query_distance_batch, all-mode-1 and mixed with
+    mode 0, and rabitq_query_distance_with_paper) against the reference for every query x record."""
+    from quantization_graph_gb300 import _native as N
+
+    g = load_golden(name)
+    v = load_golden("full_codec")
+    dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+    _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+    sp = _space(lib, dim, g["center"], 0)
+    try:
+        compact, msb, factors = g["compact"], g["msb"], g["factors"]
+        ids = np.arange(n, dtype=np.uint32)
+        for q in range(nq):
+            prep = C.c_void_p(lib.rabitq_prepare_query(sp, _p(np.ascontiguousarray(Q[q]))))
+            assert prep.value, N.last_error()
+            est = (N.PaperEstimate * n)()
+            assert lib.rabitq_paper_estimate_batch_sidecar(sp, prep, _p(ids), n, _p(msb), msb.shape[1],
+                                                           _p(factors), factors.shape[1], C.c_float(1.9), est)
+            got = np.frombuffer(bytes(est), np.uint8).reshape(n, -1)
+            np.testing.assert_array_equal(got[:, :21], v[f"{name}_gate"][q][:, :21])
+            sip = np.array([e.short_ip for e in est], np.float32)
+            out = np.zeros(n, np.float32)
+            assert lib.rabitq_query_distance_batch(sp, prep, _p(ids), _p(np.ones(n, np.uint8)), n, _p(compact),
+                                                   compact.shape[1], _p(sip), _p(out))
+            np.testing.assert_array_equal(bits(out), bits(v[f"{name}_dist_mode1"][q]))
+            modes = (ids % 2).astype(np.uint8)  # mixed batch: odd records mode 1, even mode 0
+            mixed = np.zeros(n, np.float32)
+            assert lib.rabitq_query_distance_batch(sp, prep, _p(ids), _p(modes), n, _p(compact), compact.shape[1],
+                                                   _p(sip), _p(mixed))
+            want = np.where(modes == 1, v[f"{name}_dist_mode1"][q], g["dist_mode0"][q]).astype(np.float32)
+            np.testing.assert_array_equal(bits(mixed), bits(want))
+            single = np.array([lib.rabitq_query_distance_with_paper(sp, prep, C.c_void_p(compact[i].ctypes.data),
+                                                                    C.c_float(sip[i])) for i in range(0, n, 7)],
+                              np.float32)
+            np.testing.assert_array_equal(bits(single), bits(v[f"{name}_dist_mode1"][q][::7]))
             lib.rabitq_release_query(sp, prep)
     finally:
         lib.rabitq_space_delete(sp)

@@ -246,3 +246,25 @@ def test_fused_int_rerank_search_matches_reference(cuda, name, codec):
         np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), v[f"{name}_c{codec}_ids_L{L}"])
         np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(v[f"{name}_c{codec}_dists_L{L}"]))
         np.testing.assert_array_equal(stats_matrix(r.stats), v[f"{name}_c{codec}_stats_L{L}"])
+
+
+@pytest.mark.parametrize("name", list(SEARCH_CASES))
+def test_full_codec_search_matches_reference(cuda, name):
+    """The Full codec through the batched GPU search (FP32 gate against the MSB plane, survivors
+    by the remaining bits with the gate's short ip, the rerank correcting those distances)
+    against the reference's kernels: ids, distance bits, counters."""
+    torch = cuda
+    from quantization_graph_gb300.index import OursIndex
+    from quantization_graph_gb300.space import RabitqSpace
+
+    g = load_golden(name)
+    v = load_golden("full_codec")
+    _, Q = SEARCH_CASES[name]()
+    sp = RabitqSpace(int(g["dim"]), g["center"], codec=0)
+    ix = OursIndex(sp, g["compact"], g["residual"], g["msb"], g["factors"], g["degrees"], g["edges"])
+    q = torch.from_numpy(Q).cuda()
+    for L in (20, 40):
+        r = ix.search(q, k=10, l_value=L, with_stats=True)
+        np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), v[f"{name}_ids_L{L}"])
+        np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(v[f"{name}_dists_L{L}"]))
+        np.testing.assert_array_equal(stats_matrix(r.stats), v[f"{name}_stats_L{L}"])
