@@ -18,25 +18,6 @@
 namespace qg {
 namespace {
 
-__device__ __forceinline__ float ld_f32(const uint8_t *p) {
-    const uint32_t v = static_cast<uint32_t>(p[0]) | (static_cast<uint32_t>(p[1]) << 8) |
-                       (static_cast<uint32_t>(p[2]) << 16) | (static_cast<uint32_t>(p[3]) << 24);
-    return __uint_as_float(v);
-}
-
-// PaperPruneFactors (20 bytes) -> device float4 with validity folded into cross_scale and
-// error_cross_scale: both NaN when the valid flag is 0. A set flag implies a finite error cross
-// scale (extract_paper_prune_sidecar, space_rabitq.h:4364-4392), so a NaN there marks exactly the
-// records whose flag is 0.
-__device__ __forceinline__ float4 load_factors(const uint8_t *f) {
-    float4 pf = make_float4(ld_f32(f), ld_f32(f + 4), ld_f32(f + 8), ld_f32(f + 12));
-    if (f[16] == 0) {
-        pf.z = __int_as_float(0x7fc00000);
-        pf.w = __int_as_float(0x7fc00000);
-    }
-    return pf;
-}
-
 template <int D>
 __global__ void gate_pairs_kernel(const int8_t *codes, const float4 *scal, const long long *csum,
                                   const uint32_t *qidx, const uint32_t *ids, size_t count,

@@ -21,6 +21,26 @@ constexpr float kFltMax = 3.402823466e+38f;
 __device__ __forceinline__ float f_inf() { return __int_as_float(0x7f800000); }
 __device__ __forceinline__ bool f_isfinite(float x) { return isfinite(x); }
 
+// A little-endian f32 at any byte address (the reference's records are unaligned).
+__device__ __forceinline__ float ld_f32(const uint8_t *p) {
+    const uint32_t v = static_cast<uint32_t>(p[0]) | (static_cast<uint32_t>(p[1]) << 8) |
+                       (static_cast<uint32_t>(p[2]) << 16) | (static_cast<uint32_t>(p[3]) << 24);
+    return __uint_as_float(v);
+}
+
+// PaperPruneFactors (20 bytes) -> device float4 with validity folded into cross_scale and
+// error_cross_scale: both NaN when the valid flag is 0. A set flag implies a finite error cross
+// scale (extract_paper_prune_sidecar, space_rabitq.h:4364-4392), so a NaN there marks exactly the
+// records whose flag is 0.
+__device__ __forceinline__ float4 load_factors(const uint8_t *f) {
+    float4 pf = make_float4(ld_f32(f), ld_f32(f + 4), ld_f32(f + 8), ld_f32(f + 12));
+    if (f[16] == 0) {
+        pf.z = __int_as_float(0x7fc00000);
+        pf.w = __int_as_float(0x7fc00000);
+    }
+    return pf;
+}
+
 // _mm512_reduce_add_ps tree over the 16 lanes of a half-warp (lane t = AVX-512 lane t):
 // (v[8+j] + v[j]) -> (a[4+j] + a[j]) -> (b0 + b2, b1 + b3) -> c0 + c1. Every lane of the
 // half-warp must call it; lane 0 of the half-warp holds the result.
