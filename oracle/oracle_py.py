@@ -64,7 +64,8 @@ class _Lib:
 
 
 class Oracle:
-    """The restatement: one space (seed 100 by default), INT8 query codec (or INT4, codec=2)."""
+    """The restatement: one space (seed 100 by default), INT8 query codec by default (codec: 0 Full,
+    1 B1, 2 Int4, 3 Int8, 4 B1Main, 5 FullStaged, 6 FullRerankScalar, 7 FullScalar)."""
 
     def __init__(self, dim: int, center: np.ndarray, seed: int = 100, codec: int = 3):
         self.lib = lib = _Lib.load(ORACLE_SO)
@@ -92,8 +93,9 @@ class Oracle:
         self.residual_bytes = lib.qgo_residual_bytes(self.space)
         self.msb_bytes = lib.qgo_msb_bytes(self.space)
         self.prep = C.c_void_p(lib.qgo_prepared_new(self.space))
-        if lib.qgo_space_set_query_codec(self.space, C.c_int(codec)) != 0:
-            raise ValueError("the oracle prepares Int8 (3), Int4 (2) and B1 (1) queries")
+        # 7 = FullScalar: a Rust-side switch (distance mode 3) over the Full prepared query
+        if lib.qgo_space_set_query_codec(self.space, C.c_int(0 if codec == 7 else codec)) != 0:
+            raise ValueError("the oracle prepares the codecs 0..6 (and FullScalar, 7)")
         self.codec = codec
 
     def __del__(self):
@@ -306,7 +308,8 @@ class Reference:
         self.space = C.c_void_p(lib.rabitq_space_new(dim, seed, 1, 4, 16, True, True))
         self.center = np.ascontiguousarray(center, dtype=np.float32)
         assert lib.rabitq_space_set_center(self.space, _p(self.center))
-        lib.rabitq_set_query_coarse_codec(self.space, C.c_int(codec))  # 3 = Int8, 2 = Int4, 1 = B1
+        # native codec ids 0..6 (space_rabitq.h:36-44); 7 = FullScalar prepares as Full (ours_diskann.rs:300-310)
+        lib.rabitq_set_query_coarse_codec(self.space, C.c_int(0 if codec == 7 else codec))
         self.codec = codec
         self.full_bytes = lib.rabitq_full_record_bytes(self.space)
         self.compact_bytes = lib.rabitq_compact_record_bytes(self.space)

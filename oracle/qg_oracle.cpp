@@ -123,7 +123,8 @@ struct qgo_space {
     size_t residual_bytes = 0;
     size_t msb_bytes = 0;
     uint32_t seed = 100;
-    int query_bits = 8;  // Int8 (codec 3), Int4 (codec 2), B1 / B1Main (1, sign bits), Full (0: 32)
+    int query_bits = 8;  // Int8 (codec 3), Int4 (codec 2), B1 / B1Main (1, sign bits), Full (0, 5, 6: 32)
+    int codec = 3;       // the query codec id (rabitq_set_query_coarse_codec)
     std::vector<float> signs;
     std::vector<float> center;
     std::vector<float> rotated_center;
@@ -895,15 +896,20 @@ void qgo_distance_batch(const qgo_space *s, const qgo_prepared *q, const uint32_
     }
 }
 
+// rabitq_residual_distance_batch (rabitq_bridge.cpp:972-1042): the AVX2 batch path, or, when the
+// space's codec is FullRerankScalar (6), the per-record path (computeResidualDistanceIntervalFromRecord
+// -> residualInt4IpAvx2, space_rabitq.h:1723-1734, 2278-2325), whose compiled products take the
+// fused kernel's order.
 void qgo_residual_batch(const qgo_space *s, const qgo_prepared *q, const uint32_t *ids,
                         size_t count, const uint8_t *records, size_t record_stride,
                         const uint8_t *residual, size_t residual_stride,
                         const float *long_d, qgo_interval *out) {
     (void)records;
     (void)record_stride;
+    const bool per_record = s->codec == 6;
     for (size_t i = 0; i < count; ++i)
         out[i] = residual_interval(*s, *q, residual + static_cast<size_t>(ids[i]) * residual_stride,
-                                   long_d[i]);
+                                   long_d[i], per_record);
 }
 
 // compute_full_residual_distance_intervals_batch_by_id (space_rabitq.h:5557-5778) behind
@@ -1083,7 +1089,16 @@ extern "C" int qgo_search_one_with(const qgo_kernel_table *kt, const float *quer
                 f.slots.push_back(slot);
                 // survivors: the quantized traversal for the integer codecs, the FP32 restore
                 // for B1 and invalid estimates (ours_diskann.rs:1731-1748)
-                f.modes.push_back(!paper.valid ? 0 : prm->codec == 0 ? 1 : prm->codec == 1 ? 0 : 2);
+                // DIST_MODE_* of ours_diskann.rs:1734-1749: invalid gate -> recompute (0); Full,
+                // FullStaged, FullRerankScalar -> reuse the FP32 short ip (1); FullScalar (7, a
+                // Rust-side switch over the Full prepared query) -> its scalar twin (3); Int4 /
+                // Int8 -> the quantized remaining bits (2); B1 -> recompute (0)
+                const int c = prm->codec;
+                f.modes.push_back(!paper.valid                        ? 0
+                                  : (c == 0 || c == 5 || c == 6)      ? 1
+                                  : c == 7                            ? 3
+                                  : (c == 2 || c == 3)                ? 2
+                                                                      : 0);
                 f.short_ips.push_back(paper.short_ip);
                 if (f.ids.size() >= kDistBatch) flush_batch(kt, prep, pool, l_value, est, f, st);
             }
@@ -1565,11 +1580,14 @@ extern "C" int qgo_build_vamana(const qgo_space *space, const uint8_t *compact, 
     return 0;
 }
 
-// rabitq_set_query_coarse_codec for the oracle: 3 = Int8, 2 = Int4; others return -1.
+// rabitq_set_query_coarse_codec for the oracle: 0 Full, 1 B1, 2 Int4, 3 Int8, 4 B1Main, 5 FullStaged,
+// 6 FullRerankScalar; others return -1. The space's routines branch only on B1 / B1Main / Int4 /
+// Int8 (space_rabitq.h:3464-3469, 4519-4531), so 5 and 6 prepare and gate as Full.
 extern "C" int qgo_space_set_query_codec(qgo_space *space, int codec) {
-    if (!space || codec < 0 || codec > 4) return -1;
-    // B1Main prepares like B1; Full (0) keeps only the FP32 residual
-    space->query_bits = codec == 0 ? 32 : (codec == 1 || codec == 4) ? 1 : (codec == 2 ? 4 : 8);
+    if (!space || codec < 0 || codec > 6) return -1;
+    // B1Main prepares like B1; the Full codecs keep only the FP32 residual
+    space->query_bits = (codec == 1 || codec == 4) ? 1 : codec == 2 ? 4 : codec == 3 ? 8 : 32;
+    space->codec = codec;
     return 0;
 }
 

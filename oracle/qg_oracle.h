@@ -130,7 +130,9 @@ typedef struct {
     int kth_stop;
     int codec; /* 3 Int8, 2 Int4 (quantized traversal), 1 B1 (survivors by the FP32 restore),
                   4 B1Main (no gate: every fresh neighbour by the 4-bit x 1-bit distance),
-                  0 Full (FP32 gate; survivors by the remaining bits with the gate's short ip) */
+                  0 Full (FP32 gate; survivors by the remaining bits with the gate's short ip);
+                  5 FullStaged and 6 FullRerankScalar run as Full; 7 FullScalar (a Rust-side
+                  switch over a Full prepared query) takes distance mode 3, which computes mode 1 */
     int fused_int_rerank; /* Int8 / Int4: rerank by the fused restore + residual kernel
                              (RABITQ_ENABLE_FUSED_INT_RERANK, ours_diskann.rs:1166-1172, 1831-1848) */
 } qgo_search_params;

@@ -108,6 +108,7 @@ struct Prepared {
     long long *d_csum = nullptr;
     float4 h_scal{};
     long long h_csum = 0;
+    int codec = 0;  // the space's codec when the query was prepared (PreparedQuery::query_coarse_codec)
     bool valid = false;
     ~Prepared() { release(); }
     void release() {
@@ -178,8 +179,9 @@ bool gate_host(const Space *s, const uint32_t *ids, size_t count, const uint8_t 
     gather_rows(h + o_f, factors_base, factor_stride, ids, count, 20);
     cudaStream_t st = t_stage.stream;
     if (!cuda_ok(cudaMemcpyAsync(d, h, o_o, cudaMemcpyHostToDevice, st), "gate upload")) return false;
+    const int codec = t_prepared.codec;
     const cudaError_t ge =
-        s->codec == 0
+        codec_query_bits(codec) == 32
             ? launch_gate_full_pairs(static_cast<int>(s->code_dim), t_prepared.d_rr, t_prepared.d_scal,
                                      reinterpret_cast<uint32_t *>(d + o_q), reinterpret_cast<uint32_t *>(d + o_i),
                                      count, d + o_m, mb, d + o_f, 20, eps,
@@ -187,7 +189,7 @@ bool gate_host(const Space *s, const uint32_t *ids, size_t count, const uint8_t 
             : launch_gate_pairs(static_cast<int>(s->code_dim), t_prepared.d_codes, t_prepared.d_scal,
                                 t_prepared.d_csum, reinterpret_cast<uint32_t *>(d + o_q),
                                 reinterpret_cast<uint32_t *>(d + o_i), count, d + o_m, mb, d + o_f, 20, eps,
-                                reinterpret_cast<RabitqPaperEstimate *>(d + o_o), st, s->codec == 1);
+                                reinterpret_cast<RabitqPaperEstimate *>(d + o_o), st, codec == 1);
     if (!cuda_ok(ge, "gate kernel")) return false;
     if (!cuda_ok(cudaMemcpyAsync(h + o_o, d + o_o, count * sizeof(RabitqPaperEstimate),
                                  cudaMemcpyDeviceToHost, st), "gate download"))
@@ -679,6 +681,7 @@ const void *rabitq_prepare_query(const void *space, const float *query) {
             return nullptr;
         if (!cuda_ok(cudaMemcpy(&p.h_csum, p.d_csum, 8, cudaMemcpyDeviceToHost), "prepare download")) return nullptr;
         p.space = s;
+        p.codec = s->codec;
         p.valid = true;
         return &p;
     } catch (...) {
@@ -687,7 +690,8 @@ const void *rabitq_prepare_query(const void *space, const float *query) {
 }
 
 void rabitq_set_query_coarse_codec(void *space, int codec) {
-    if (space) static_cast<Space *>(space)->codec = codec;
+    // the reference stores static_cast<QueryCoarseCodec>(codec), an 8-bit enum
+    if (space) static_cast<Space *>(space)->codec = static_cast<uint8_t>(codec);
 }
 
 void rabitq_release_query(const void *space, const void *prepared) {
@@ -717,7 +721,7 @@ float rabitq_query_distance_b1(const void *space, const void *prepared, const vo
     try {
         const Space *s = as_space(space);
         if (!check_prepared(s, prepared) || !encoded) return inf;
-        if (s->codec != 4) {
+        if (t_prepared.codec != 4) {
             set_error("rabitq_query_distance_b1: prepare the query with the B1Main codec (4)");
             return inf;
         }
@@ -736,7 +740,7 @@ bool rabitq_query_distance_b1_batch(const void *space, const void *prepared, con
     try {
         const Space *s = as_space(space);
         if (!out_distances) return false;
-        bool ok = check_prepared(s, prepared) && ids && encoded_base && s->codec == 4;
+        bool ok = check_prepared(s, prepared) && ids && encoded_base && t_prepared.codec == 4;
         for (size_t b = 0; ok && b < count; b += 4096) {
             const size_t n = std::min<size_t>(4096, count - b);
             ok = distance_b1_host(s, ids + b, n, static_cast<const uint8_t *>(encoded_base), encoded_stride,
@@ -869,7 +873,7 @@ float rabitq_query_distance_with_quantized_paper(const void *space, const void *
     const float inf = std::numeric_limits<float>::infinity();
     try {
         const Space *s = as_space(space);
-        if (!check_prepared(s, prepared) || !encoded) return inf;
+        if (!check_prepared(s, prepared) || !encoded || codec_search_mode(t_prepared.codec) != 0) return inf;
         const uint32_t id = 0;
         const uint8_t mode = 2;
         float out = inf;
@@ -894,6 +898,9 @@ bool rabitq_query_distance_batch(const void *space, const void *prepared, const 
             ok = distance_host(s, ids, modes, count, static_cast<const uint8_t *>(encoded_base),
                                encoded_stride, short_ips, out_distances);
         if (!ok) std::fill(out_distances, out_distances + count, inf);
+        // mode 2 reads the integer query codes, which only Int8 / Int4 prepare
+        for (size_t i = 0; ok && i < count; ++i)
+            if (modes[i] == 2 && codec_search_mode(t_prepared.codec) != 0) out_distances[i] = inf;
         return true;
     } catch (...) {
         std::fill(out_distances, out_distances + count, inf);
@@ -918,8 +925,10 @@ RabitqDistanceInterval rabitq_residual_distance_from_record(const void *space,
         if (!check_prepared(s, prepared) || !residual_record) return fallback;
         const uint32_t id = 0;
         RabitqDistanceInterval out = fallback;
+        // compute_residual_distance_interval_from_record: the per-record path, whose products take
+        // the fused kernel's order (residualInt4IpAvx2, space_rabitq.h:2278-2325)
         if (!residual_host(s, &id, 1, static_cast<const uint8_t *>(residual_record), s->residual_bytes,
-                           &long_distance, &out))
+                           &long_distance, &out, true))
             return fallback;
         return out;
     } catch (...) {
@@ -954,8 +963,10 @@ bool rabitq_residual_distance_batch(const void *space, const void *prepared, con
                                     RabitqDistanceInterval *out) {
     (void)encoded_base;
     (void)encoded_stride;
+    // FullRerankScalar (6) takes the per-record path (rabitq_bridge.cpp:987-1040), in the fused order
+    const Space *s = as_space(space);
     return residual_batch(space, prepared, ids, count, residual_base, residual_stride, long_distances, out,
-                          false);
+                          s && s->codec == 6);
 }
 
 bool rabitq_full_residual_distance_batch(const void *space, const void *prepared,
@@ -1120,7 +1131,7 @@ int qg_gate_pairs(const void *space, const int8_t *d_codes, const float *d_scala
                   size_t factor_stride, float epsilon0, RabitqPaperEstimate *d_out, void *stream) {
     const Space *s = as_space(space);
     if (!s) return QG_ERR_INVALID;
-    if (s->codec == 0) {
+    if (space_query_bits(s) == 32) {
         set_error("qg_gate_pairs: the Full codec's gate reads the rotated residual; use qg_gate_full_pairs");
         return QG_ERR_INVALID;
     }
@@ -1586,7 +1597,9 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
     a.rerank = params->rerank_candidates;
     a.early_stop_hops = params->early_stop_hops;
     a.kth_stop = params->kth_stop;
-    a.fused_rerank = params->fused_int_rerank != 0 ? 1 : 0;  // used by mode 0 only
+    // the rerank residual in the fused kernel's order: the fused Int8 / Int4 rerank, or
+    // FullRerankScalar's per-record residual path
+    a.fused_rerank = ((space_search_mode(s) == 0 && params->fused_int_rerank != 0) || s->codec == 6) ? 1 : 0;
     a.mode = space_search_mode(s);
     a.ids_out = d_ids;
     a.dists_out = d_dists;

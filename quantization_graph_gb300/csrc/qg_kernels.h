@@ -52,7 +52,8 @@ struct SearchArgs {
     int rerank;
     int early_stop_hops;
     int kth_stop;
-    int fused_rerank;    // mode 0: rerank residual in the fused kernel's product order
+    int fused_rerank;    // rerank residual in the fused kernel's product order (the fused Int8 / Int4
+                         // rerank, or FullRerankScalar's per-record residual)
     uint32_t *ids_out;
     float *dists_out;
     qg_search_stats *stats_out;

@@ -38,19 +38,17 @@ struct Space {
     float center_norm_sqr = 0.0f;
 };
 
-// Query code layout of the space's codec: Int8 (3) -> 8, Int4 (2) -> 4 (integer codes), B1 (1) ->
-// 1 (sign bits), B1Main (4) -> 2 (+-1 bytes), Full (0) -> 32 (the FP32 residual only); 0 for the
-// codecs the GPU path does not build (the staged and scalar Full variants).
-inline int space_query_bits(const Space *s) {
-    return s->codec == 3 ? 8
-                         : (s->codec == 2 ? 4 : (s->codec == 1 ? 1 : (s->codec == 4 ? 2 : (s->codec == 0 ? 32 : 0))));
-}
-// Search mode of the codec: 0 integer codes (Int8 / Int4), 1 B1 (popcount gate), 2 B1Main (no
-// gate; every fresh neighbour by the 4-bit x 1-bit distance), 3 Full (FP32 gate; survivors by the
-// remaining bits with the gate's short ip).
-inline int space_search_mode(const Space *s) {
-    return s->codec == 1 ? 1 : (s->codec == 4 ? 2 : (s->codec == 0 ? 3 : 0));
-}
+// Query code layout of a codec id: Int8 (3) -> 8, Int4 (2) -> 4 (integer codes), B1 (1) -> 1 (sign
+// bits), B1Main (4) -> 2 (+-1 bytes), and 32 (the FP32 residual only) for every other id: Full (0),
+// FullStaged (5), FullRerankScalar (6) and any value outside the enum, which the reference's space
+// handles as Full (space_rabitq.h:3464-3469, 4519-4531).
+inline int codec_query_bits(int c) { return c == 3 ? 8 : (c == 2 ? 4 : (c == 1 ? 1 : (c == 4 ? 2 : 32))); }
+// Search mode of a codec id: 0 integer codes (Int8 / Int4), 1 B1 (popcount gate), 2 B1Main (no gate;
+// every fresh neighbour by the 4-bit x 1-bit distance), 3 the Full codecs (FP32 gate; survivors by
+// the remaining bits with the gate's short ip).
+inline int codec_search_mode(int c) { return c == 1 ? 1 : (c == 4 ? 2 : (c == 2 || c == 3 ? 0 : 3)); }
+inline int space_query_bits(const Space *s) { return codec_query_bits(s->codec); }
+inline int space_search_mode(const Space *s) { return codec_search_mode(s->codec); }
 
 // Device-resident index: structure-of-arrays, every row 16-byte aligned.
 struct DevIndex {

@@ -943,7 +943,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
         float est, lo, hi;
         residual_interval_thread<D>(ix.res_scales + static_cast<size_t>(id) * (D / 16),
                                     ix.res_codes + static_cast<size_t>(id) * (D / 2), rr, s.pd[e],
-                                    qn, kMode == 0 && a.fused_rerank != 0, &est, &lo, &hi);
+                                    qn, a.fused_rerank != 0, &est, &lo, &hi);
         s.plb[e] = est;
     }
     __syncwarp();

@@ -170,7 +170,9 @@ extern "C" int qg_search_batch_noalloc(qg_index *index, const float *d_queries, 
     a.rerank = params->rerank_candidates;
     a.early_stop_hops = params->early_stop_hops;
     a.kth_stop = params->kth_stop;
-    a.fused_rerank = params->fused_int_rerank != 0 ? 1 : 0;  // used by mode 0 only
+    // the rerank residual in the fused kernel's order: the fused Int8 / Int4 rerank, or
+    // FullRerankScalar's per-record residual path
+    a.fused_rerank = ((space_search_mode(s) == 0 && params->fused_int_rerank != 0) || s->codec == 6) ? 1 : 0;
     a.mode = space_search_mode(s);
     a.ids_out = d_ids;
     a.dists_out = d_dists;

@@ -184,7 +184,9 @@ def b1main_cases():
 def full_cases():
     """The Full query codec (FP32 query against the MSB plane; survivors by the FP32 remaining
     bits reusing the gate's short ip, mode 1): gate and mode-1 distances for every query x record
-    of three kernel fixtures, and whole searches on the three search indexes."""
+    of three kernel fixtures, and whole searches on the three search indexes; also whole searches
+    with FullRerankScalar (6), whose rerank takes the bridge's per-record residual path, and with
+    FullStaged (5) and FullScalar (7), stored only where they differ from Full's."""
     out = {}
     for name in ("kernels_d128", "kernels_d960", "kernels_d1536"):
         g = np.load(os.path.join(HERE, name + ".npz"))
@@ -211,6 +213,18 @@ def full_cases():
             out[f"{name}_ids_L{L}"] = ids
             out[f"{name}_dists_L{L}"] = dists
             out[f"{name}_stats_L{L}"] = stats.view(np.uint64).reshape(len(Q), -1)
+        for codec in (5, 6, 7):
+            other = oracle_py.Reference(int(g["dim"]), g["center"], codec=codec)
+            for L in (20, 40):
+                ids, dists, stats = other.search(Q, index, k=10, L=L, eps=1.9, rerank=100)
+                st = stats.view(np.uint64).reshape(len(Q), -1)
+                same = (np.array_equal(ids, out[f"{name}_ids_L{L}"]) and
+                        np.array_equal(dists.view(np.uint32), out[f"{name}_dists_L{L}"].view(np.uint32)) and
+                        np.array_equal(st, out[f"{name}_stats_L{L}"]))
+                if codec == 6 or not same:
+                    out[f"{name}_c{codec}_ids_L{L}"] = ids
+                    out[f"{name}_c{codec}_dists_L{L}"] = dists
+                    out[f"{name}_c{codec}_stats_L{L}"] = st
     np.savez_compressed(os.path.join(HERE, "full_codec.npz"), **out)
     print("full_codec written")
 

@@ -133,9 +133,17 @@ def test_sentinels_of_what_is_not_built(lib):
         prep = C.c_void_p(lib.rabitq_prepare_query(sp, _p(query)))
         rec = np.ascontiguousarray(g["compact"][0])
         assert np.isinf(lib.rabitq_query_distance_b1(sp, prep, _p(rec)))  # needs a B1Main prepared query
-        for codec in (5, 6):  # FullStaged, FullRerankScalar: not built, no prepared query
+        sip = np.zeros(1, np.float32)
+        out = np.zeros(1, np.float32)
+        lib.rabitq_set_query_coarse_codec(sp, 0)  # a Full prepared query has no integer codes for mode 2
+        prep = C.c_void_p(lib.rabitq_prepare_query(sp, _p(query)))
+        assert prep.value
+        assert lib.rabitq_query_distance_batch(sp, prep, _p(np.zeros(1, np.uint32)), _p(np.full(1, 2, np.uint8)), 1,
+                                               _p(g["compact"]), g["compact"].shape[1], _p(sip), _p(out))
+        assert np.isinf(out[0])
+        for codec in (5, 6, 0x105):  # FullStaged, FullRerankScalar, an id outside the enum: Full
             lib.rabitq_set_query_coarse_codec(sp, codec)
-            assert not C.c_void_p(lib.rabitq_prepare_query(sp, _p(query))).value
+            assert C.c_void_p(lib.rabitq_prepare_query(sp, _p(query))).value
     finally:
         lib.rabitq_space_delete(sp)
 
@@ -233,3 +241,38 @@ def test_full_codec_entry_points(lib, name):
             lib.rabitq_release_query(sp, prep)
     finally:
         lib.rabitq_space_delete(sp)
+
+
+@pytest.mark.parametrize("name", ["kernels_d128", "kernels_d960", "kernels_d1536"])
+def test_per_record_residual_paths(lib, name):
+    """The reference's per-record residual (rabitq_residual_distance_from_record, and
+    rabitq_residual_distance_batch when the codec is FullRerankScalar) takes the fused kernel's
+    product order; checked against the fused rerank's outputs for every query x record."""
+    from quantization_graph_gb300 import _native as N
+
+    g = load_golden(name)
+    v = load_golden("fused_rerank")
+    dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+    _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+    compact, residual = np.ascontiguousarray(g["compact"]), np.ascontiguousarray(g["residual"])
+    ids = np.arange(n, dtype=np.uint32)
+    for codec in (3, 6):
+        sp = _space(lib, dim, g["center"], codec)
+        try:
+            for q in range(nq):
+                prep = C.c_void_p(lib.rabitq_prepare_query(sp, _p(np.ascontiguousarray(Q[q]))))
+                assert prep.value
+                d0 = np.ascontiguousarray(g["dist_mode0"][q], np.float32)
+                if codec == 3:
+                    got = np.array([[x.estimate, x.lower_bound, x.upper_bound] for x in (
+                        lib.rabitq_residual_distance_from_record(sp, prep, _p(compact[i]), _p(residual[i]),
+                                                                 C.c_float(d0[i])) for i in range(n))], np.float32)
+                else:
+                    iv = (N.DistanceInterval * n)()
+                    assert lib.rabitq_residual_distance_batch(sp, prep, _p(ids), n, _p(compact), compact.shape[1],
+                                                              _p(residual), residual.shape[1], _p(d0), iv)
+                    got = np.frombuffer(bytes(iv), np.float32).reshape(n, 3)
+                np.testing.assert_array_equal(bits(got), bits(v[name][q]))
+                lib.rabitq_release_query(sp, prep)
+        finally:
+            lib.rabitq_space_delete(sp)

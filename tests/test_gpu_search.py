@@ -249,10 +249,12 @@ def test_fused_int_rerank_search_matches_reference(cuda, name, codec):
 
 
 @pytest.mark.parametrize("name", list(SEARCH_CASES))
-def test_full_codec_search_matches_reference(cuda, name):
+@pytest.mark.parametrize("codec", [0, 5, 6])
+def test_full_codec_search_matches_reference(cuda, name, codec):
     """The Full codec through the batched GPU search (FP32 gate against the MSB plane, survivors
     by the remaining bits with the gate's short ip, the rerank correcting those distances)
-    against the reference's kernels: ids, distance bits, counters."""
+    against the reference's kernels: ids, distance bits, counters. FullStaged (5) searches as Full;
+    FullRerankScalar (6) reranks in the per-record residual order."""
     torch = cuda
     from quantization_graph_gb300.index import OursIndex
     from quantization_graph_gb300.space import RabitqSpace
@@ -260,11 +262,12 @@ def test_full_codec_search_matches_reference(cuda, name):
     g = load_golden(name)
     v = load_golden("full_codec")
     _, Q = SEARCH_CASES[name]()
-    sp = RabitqSpace(int(g["dim"]), g["center"], codec=0)
+    sp = RabitqSpace(int(g["dim"]), g["center"], codec=codec)
     ix = OursIndex(sp, g["compact"], g["residual"], g["msb"], g["factors"], g["degrees"], g["edges"])
     q = torch.from_numpy(Q).cuda()
     for L in (20, 40):
+        key = f"{name}_c{codec}" if f"{name}_c{codec}_ids_L{L}" in v else name
         r = ix.search(q, k=10, l_value=L, with_stats=True)
-        np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), v[f"{name}_ids_L{L}"])
-        np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(v[f"{name}_dists_L{L}"]))
-        np.testing.assert_array_equal(stats_matrix(r.stats), v[f"{name}_stats_L{L}"])
+        np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), v[f"{key}_ids_L{L}"])
+        np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(v[f"{key}_dists_L{L}"]))
+        np.testing.assert_array_equal(stats_matrix(r.stats), v[f"{key}_stats_L{L}"])

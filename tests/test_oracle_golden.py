@@ -315,3 +315,21 @@ def test_fused_rerank_search_bit_exact(oracle, name, codec):
         np.testing.assert_array_equal(ids, v[f"{name}_c{codec}_ids_L{L}"])
         np.testing.assert_array_equal(bits(dists), bits(v[f"{name}_c{codec}_dists_L{L}"]))
         np.testing.assert_array_equal(stats.view(np.uint64).reshape(len(Q), -1), v[f"{name}_c{codec}_stats_L{L}"])
+
+
+@pytest.mark.parametrize("name", ["search_c1", "search_c2", "search_c3"])
+@pytest.mark.parametrize("codec", [5, 6, 7])
+def test_full_codec_variants_search_bit_exact(oracle, name, codec):
+    """FullStaged (5) and FullScalar (7, a Rust-side switch: distance mode 3 over a Full prepared
+    query) search as Full does; FullRerankScalar (6) reranks through the bridge's per-record
+    residual path (rabitq_bridge.cpp:987-1040). Against the reference's kernels."""
+    g = load_golden(name)
+    v = load_golden("full_codec")
+    _, Q = SEARCH_CASES[name]()
+    o = oracle.Oracle(int(g["dim"]), g["center"], codec=codec)
+    for L in (20, 40):
+        key = f"{name}_c{codec}" if f"{name}_c{codec}_ids_L{L}" in v else name
+        ids, dists, stats = o.search(Q, golden_index(g), k=10, L=L, eps=1.9, rerank=100)
+        np.testing.assert_array_equal(ids, v[f"{key}_ids_L{L}"])
+        np.testing.assert_array_equal(bits(dists), bits(v[f"{key}_dists_L{L}"]))
+        np.testing.assert_array_equal(stats.view(np.uint64).reshape(len(Q), -1), v[f"{key}_stats_L{L}"])
