@@ -117,11 +117,11 @@ float rabitq_symmetric_distance(const void *space, const void *lhs, const void *
  * valid until that thread's next prepare call, as in the reference (space_rabitq.h:3700). */
 const void *rabitq_prepare_query(const void *space, const float *query);
 /* rabitq_bridge.cpp:364-370. Codec ids: Full=0 B1=1 Int4=2 Int8=3 B1Main=4 FullStaged=5
- * FullRerankScalar=6 (space_rabitq.h:36-44). The GPU path implements Int8 (the formal codec),
- * Int4, B1, B1Main and Full; prepare_query returns NULL, and the batched qg_* search fails, for
- * the others. A new space starts with Full, as in the reference. B1Main prepared codes are +-1
- * bytes with the sign sum in the code-sum slot; Full prepares no codes (the rotated residual and
- * the scalars only, scale 1).
+ * FullRerankScalar=6 (space_rabitq.h:36-44). All are implemented; as in the reference, the id is
+ * stored as an 8-bit enum and every id other than 1-4 behaves as Full (FullRerankScalar also
+ * reranks in the per-record residual order). A new space starts with Full. B1Main prepared codes
+ * are +-1 bytes with the sign sum in the code-sum slot; the Full codecs prepare no codes (the
+ * rotated residual and the scalars only, scale 1).
  * With B1 the prepared codes hold the sign bits, the scale slot the 1-bit short scale and the
  * code-sum slot the error scale (low word) and alpha (high word). */
 void rabitq_set_query_coarse_codec(void *space, int codec);
@@ -165,7 +165,8 @@ float rabitq_query_distance_with_quantized_paper(const void *space, const void *
  * residuals external, so this returns {long,long,long}; use the _from_record form. */
 RabitqDistanceInterval rabitq_residual_distance(const void *space, const void *prepared,
                                                 const void *encoded, float long_distance);
-/* rabitq_bridge.cpp:629-648 */
+/* rabitq_bridge.cpp:644-663: the per-record residual (space_rabitq.h:1723-1734), whose products
+ * take the fused kernel's order */
 RabitqDistanceInterval rabitq_residual_distance_from_record(const void *space,
                                                             const void *prepared,
                                                             const void *encoded,
@@ -186,7 +187,8 @@ bool rabitq_query_distance_batch(const void *space, const void *prepared, const 
                                  const uint8_t *modes, size_t count, const void *encoded_base,
                                  size_t encoded_stride, const float *short_ips,
                                  float *out_distances);
-/* rabitq_bridge.cpp:972-1042 (rerank residual correction) */
+/* rabitq_bridge.cpp:972-1042 (rerank residual correction; the per-record order for
+ * FullRerankScalar) */
 bool rabitq_residual_distance_batch(const void *space, const void *prepared, const uint32_t *ids,
                                     size_t count, const void *encoded_base,
                                     size_t encoded_stride, const void *residual_base,
