@@ -220,6 +220,16 @@ class Oracle:
         return _search(self.lib.qgo_search_batch, [self.space], queries, index, k, L, eps,
                        rerank, beam, early_stop, kth_stop, threads, codec=self.codec, fused=fused)
 
+    def gate_encoded(self, ids, records, eps=1.9):
+        """compute_paper_prune_estimate (space_rabitq.h:3926-3959): the gate from the encoded
+        records (rabitq_paper_estimate / rabitq_paper_estimate_batch)."""
+        ids = np.ascontiguousarray(ids, np.uint32)
+        records = np.ascontiguousarray(records)
+        out = np.zeros(len(ids), PAPER_ESTIMATE)
+        self.lib.qgo_gate_encoded_batch(self.space, self.prep, _p(ids), C.c_size_t(len(ids)), _p(records),
+                                        C.c_size_t(records.shape[1]), C.c_float(eps), _p(out))
+        return out
+
     def full_residual(self, ids, records, residual):
         """The fused restore + residual rerank (compute_full_residual_distance_intervals_batch_by_id,
         space_rabitq.h:5557-5778) on the prepared query: [n, 3] (estimate, lower, upper)."""
@@ -406,6 +416,15 @@ class Reference:
         self.lib.rabitq_full_residual_distance_batch(
             self.space, self.prep, _p(ids), C.c_size_t(len(ids)), _p(records), C.c_size_t(records.shape[1]),
             _p(residual), C.c_size_t(residual.shape[1]), _p(out))
+        return out
+
+    def gate_encoded(self, ids, records, eps=1.9):
+        """rabitq_paper_estimate_batch: the gate from the encoded records."""
+        ids = np.ascontiguousarray(ids, np.uint32)
+        records = np.ascontiguousarray(records)
+        out = np.zeros(len(ids), PAPER_ESTIMATE)
+        self.lib.rabitq_paper_estimate_batch(self.space, self.prep, _p(ids), C.c_size_t(len(ids)), _p(records),
+                                             C.c_size_t(records.shape[1]), C.c_float(eps), _p(out))
         return out
 
     def distance_b1(self, record):

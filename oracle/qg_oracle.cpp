@@ -398,6 +398,51 @@ qgo_paper_estimate finish_gate(const qgo_prepared &q, float short_ip, const Fact
     return r;
 }
 
+// compute_paper_prune_estimate (space_rabitq.h:3926-3959), behind rabitq_paper_estimate and
+// rabitq_paper_estimate_batch: the gate from the encoded record itself, any codec. The short ip is
+// the FP32 restore's selected sum (shortCodeIpFromFullCodeAvx512, :1307-1329: the same 16 lanes
+// over pairs and reduce tree) minus the half sum; the bound is formed on the normalised inner
+// product and returns alpha; the reference build contracts the final lower bound as
+// fma(-two_norms, ip_upper, norm_sqr + qn2).
+qgo_paper_estimate gate_encoded_one(const qgo_space &s, const qgo_prepared &q, const uint8_t *record, float eps) {
+    qgo_paper_estimate r{};
+    const float norm_sqr = get_f32(record);
+    const float short_scale = get_f32(record + 8);
+    const size_t D = s.code_dim;
+    if (D <= 1 || eps < 0.0f || !std::isfinite(eps) || norm_sqr <= 0.0f || q.query_norm <= 0.0f ||
+        short_scale <= 0.0f || !std::isfinite(short_scale))
+        return r;
+    const float data_norm = std::sqrt(norm_sqr);
+    const float alpha_raw = 4.0f * data_norm / (short_scale * std::sqrt(static_cast<float>(D)));
+    if (!(alpha_raw > 0.0f) || !std::isfinite(alpha_raw)) return r;
+    const float alpha = std::min(1.0f, alpha_raw);
+    const uint8_t *code = record + s.off_code_compact();
+    float sel[16] = {};
+    const float *rr = q.rotated_residual.data();
+    for (size_t base = 0; base < s.pair_count; base += 16)
+        for (int l = 0; l < 16; ++l) {
+            const size_t pair = base + l;
+            const uint8_t packed = code[pair];
+            if ((packed & 0x0FU) > 7U) sel[l] = sel[l] + rr[2 * pair];
+            if ((packed >> 4U) > 7U) sel[l] = sel[l] + rr[2 * pair + 1];
+        }
+    const float short_ip = reduce16(sel) - q.half_sum;
+    const float cross = short_ip * short_scale;
+    const float two_norms = 2.0f * data_norm * q.query_norm;
+    const float ip_hat = cross / two_norms;
+    const float alpha2 = alpha * alpha;
+    const float error_bound =
+        std::sqrt(std::max(0.0f, (1.0f - alpha2) / alpha2)) * eps / std::sqrt(static_cast<float>(D - 1));
+    const float ip_upper = std::max(-1.0f, std::min(1.0f, ip_hat + error_bound));
+    r.lower_bound = std::fma(-two_norms, ip_upper, norm_sqr + q.query_norm_sqr);  // FMA
+    r.short_ip = short_ip;
+    r.alpha = alpha;
+    r.ip_hat = ip_hat;
+    r.error_bound = error_bound;
+    r.valid = std::isfinite(r.lower_bound) ? 1 : 0;
+    return r;
+}
+
 // compute_paper_prune_estimate_int_msb_gate (space_rabitq.h:4873-4899) and the by-id batch
 // (space_rabitq.h:4991-5093): integer masked sum, then the float finish.
 qgo_paper_estimate gate_one(const qgo_space &s, const qgo_prepared &q, const uint8_t *msb,
@@ -910,6 +955,13 @@ void qgo_residual_batch(const qgo_space *s, const qgo_prepared *q, const uint32_
     for (size_t i = 0; i < count; ++i)
         out[i] = residual_interval(*s, *q, residual + static_cast<size_t>(ids[i]) * residual_stride,
                                    long_d[i], per_record);
+}
+
+// rabitq_paper_estimate / rabitq_paper_estimate_batch (rabitq_bridge.cpp:425-446, 665-700)
+void qgo_gate_encoded_batch(const qgo_space *s, const qgo_prepared *q, const uint32_t *ids, size_t count,
+                            const uint8_t *records, size_t record_stride, float eps, qgo_paper_estimate *out) {
+    for (size_t i = 0; i < count; ++i)
+        out[i] = gate_encoded_one(*s, *q, records + static_cast<size_t>(ids[i]) * record_stride, eps);
 }
 
 // compute_full_residual_distance_intervals_batch_by_id (space_rabitq.h:5557-5778) behind

@@ -111,6 +111,10 @@ void qgo_residual_batch(const qgo_space *space, const qgo_prepared *prepared,
                         const uint32_t *ids, size_t count, const uint8_t *records,
                         size_t record_stride, const uint8_t *residual, size_t residual_stride,
                         const float *long_distances, qgo_interval *out);
+/* compute_paper_prune_estimate (space_rabitq.h:3926-3959): the gate from the encoded record */
+void qgo_gate_encoded_batch(const qgo_space *space, const qgo_prepared *prepared, const uint32_t *ids,
+                            size_t count, const uint8_t *records, size_t record_stride, float epsilon0,
+                            qgo_paper_estimate *out);
 /* compute_full_residual_distance_intervals_batch_by_id (space_rabitq.h:5557-5778) */
 void qgo_full_residual_batch(const qgo_space *space, const qgo_prepared *prepared,
                              const uint32_t *ids, size_t count, const uint8_t *records,

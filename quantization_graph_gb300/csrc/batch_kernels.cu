@@ -3,7 +3,8 @@
 // device re-layout of an uploaded index and the MSB sidecar extraction.
 //
 //   gate      rabitq_paper_estimate_batch_sidecar, Int8 branch (rabitq_bridge.cpp:747-778 ->
-//             space_rabitq.h:4991-5093, 4701-4721), B1 (:4607-4695) and Full (:4427-4505)
+//             space_rabitq.h:4991-5093, 4701-4721), B1 (:4607-4695) and Full (:4427-4505); and
+//             rabitq_paper_estimate(_batch), the gate from the encoded record (:3926-3959)
 //   distance  rabitq_query_distance_batch modes 2, 1 / 3 and 0 (rabitq_bridge.cpp:885-970 ->
 //             space_rabitq.h:4234-4358, 3961-3966, 4080-4202)
 //   residual  rabitq_residual_distance_batch (rabitq_bridge.cpp:972-1017 ->
@@ -102,6 +103,33 @@ __global__ void gate_full_pairs_kernel(const float *rr, const float4 *scal, cons
         r.lower_bound = g.lower_bound;
         r.short_ip = g.short_ip;
         r.alpha = 0.0f;
+        r.ip_hat = g.ip_hat;
+        r.error_bound = g.error_bound;
+        r.valid = g.valid ? 1 : 0;
+        out[pair] = r;
+    }
+}
+
+// compute_paper_prune_estimate over (query, record) pairs (the gate from the encoded record),
+// one warp per pair.
+template <int D>
+__global__ void gate_encoded_pairs_kernel(const float *rr, const float4 *scal, const uint32_t *qidx,
+                                          const uint32_t *ids, size_t count, const uint8_t *records,
+                                          size_t record_stride, float eps, RabitqPaperEstimate *out) {
+    const size_t pair = (static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (pair >= count) return;
+    const uint32_t q = qidx[pair], id = ids[pair];
+    const uint8_t *rec = records + static_cast<size_t>(id) * record_stride;
+    const float4 s = scal[q];
+    const float sip = encoded_short_ip_hw<D>(rec + 16, rr + static_cast<size_t>(q) * D, s.z, lane & 15);
+    if (lane == 0) {
+        float alpha;
+        const GateOut g = finish_gate_encoded(sip, ld_f32(rec), ld_f32(rec + 8), s.y, s.x, eps, D, &alpha);
+        RabitqPaperEstimate r;
+        r.lower_bound = g.lower_bound;
+        r.short_ip = g.short_ip;
+        r.alpha = alpha;
         r.ip_hat = g.ip_hat;
         r.error_bound = g.error_bound;
         r.valid = g.valid ? 1 : 0;
@@ -337,6 +365,15 @@ cudaError_t launch_gate_full_pairs(int code_dim, const float *rr, const float4 *
     if (count == 0) return cudaSuccess;
     QG_DISPATCH_D(code_dim, gate_full_pairs_kernel<kD><<<warp_grid(count), 256, 0, stream>>>(
                                 rr, scal, qidx, ids, count, msb, msb_stride, factors, factor_stride, eps, out));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gate_encoded_pairs(int code_dim, const float *rr, const float4 *scal, const uint32_t *qidx,
+                                      const uint32_t *ids, size_t count, const uint8_t *records, size_t record_stride,
+                                      float eps, RabitqPaperEstimate *out, cudaStream_t stream) {
+    if (count == 0) return cudaSuccess;
+    QG_DISPATCH_D(code_dim, gate_encoded_pairs_kernel<kD><<<warp_grid(count), 256, 0, stream>>>(
+                                rr, scal, qidx, ids, count, records, record_stride, eps, out));
     return cudaGetLastError();
 }
 

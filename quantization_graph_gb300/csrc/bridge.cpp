@@ -199,6 +199,32 @@ bool gate_host(const Space *s, const uint32_t *ids, size_t count, const uint8_t 
     return true;
 }
 
+// compute_paper_prune_estimate for the records ids[i] (compact rows gathered like distance_host).
+bool gate_encoded_host(const Space *s, const uint32_t *ids, size_t count, const uint8_t *rec_base,
+                       size_t rec_stride, float eps, RabitqPaperEstimate *out) {
+    const size_t rb = s->compact_bytes;
+    Carve c;
+    const size_t o_q = c.take(count * 4), o_i = c.take(count * 4), o_r = c.take(count * rb),
+                 o_o = c.take(count * sizeof(RabitqPaperEstimate));
+    if (!t_stage.reserve(c.off)) return false;
+    uint8_t *h = static_cast<uint8_t *>(t_stage.h), *d = static_cast<uint8_t *>(t_stage.d);
+    fill_pairs(reinterpret_cast<uint32_t *>(h + o_q), reinterpret_cast<uint32_t *>(h + o_i), count);
+    gather_rows(h + o_r, rec_base, rec_stride, ids, count, rb);
+    cudaStream_t st = t_stage.stream;
+    if (!cuda_ok(cudaMemcpyAsync(d, h, o_o, cudaMemcpyHostToDevice, st), "gate upload")) return false;
+    if (!cuda_ok(launch_gate_encoded_pairs(static_cast<int>(s->code_dim), t_prepared.d_rr, t_prepared.d_scal,
+                                           reinterpret_cast<uint32_t *>(d + o_q), reinterpret_cast<uint32_t *>(d + o_i),
+                                           count, d + o_r, rb, eps, reinterpret_cast<RabitqPaperEstimate *>(d + o_o), st),
+                 "gate kernel"))
+        return false;
+    if (!cuda_ok(cudaMemcpyAsync(h + o_o, d + o_o, count * sizeof(RabitqPaperEstimate), cudaMemcpyDeviceToHost, st),
+                 "gate download"))
+        return false;
+    if (!cuda_ok(cudaStreamSynchronize(st), "gate sync")) return false;
+    std::memcpy(out, h + o_o, count * sizeof(RabitqPaperEstimate));
+    return true;
+}
+
 bool distance_host(const Space *s, const uint32_t *ids, const uint8_t *modes, size_t count,
                    const uint8_t *rec_base, size_t rec_stride, const float *short_ips, float *out) {
     const size_t rb = s->compact_bytes;
@@ -208,7 +234,10 @@ bool distance_host(const Space *s, const uint32_t *ids, const uint8_t *modes, si
     if (!t_stage.reserve(c.off)) return false;
     uint8_t *h = static_cast<uint8_t *>(t_stage.h), *d = static_cast<uint8_t *>(t_stage.d);
     fill_pairs(reinterpret_cast<uint32_t *>(h + o_q), reinterpret_cast<uint32_t *>(h + o_i), count);
-    for (size_t i = 0; i < count; ++i) h[o_md + i] = modes ? (modes[i] == 2 ? 2 : 0) : 0;
+    // modes 2 (quantized remaining bits), 1 and 3 (FP32 remaining bits with the given short ip);
+    // every other value recomputes the FP32 restore, as the reference's dispatch does
+    for (size_t i = 0; i < count; ++i)
+        h[o_md + i] = modes ? (modes[i] == 2 ? 2 : (modes[i] == 1 || modes[i] == 3) ? 1 : 0) : 0;
     for (size_t i = 0; i < count; ++i)
         reinterpret_cast<float *>(h + o_s)[i] = short_ips ? short_ips[i] : 0.0f;
     gather_rows(h + o_r, rec_base, rec_stride, ids, count, rb);
@@ -772,15 +801,17 @@ RabitqPaperEstimate rabitq_paper_estimate_sidecar(const void *space, const void 
     }
 }
 
+// compute_paper_prune_estimate: the bound from the encoded record itself (not the sidecar gate)
 RabitqPaperEstimate rabitq_paper_estimate(const void *space, const void *prepared,
                                           const void *encoded, float epsilon0) {
     try {
         const Space *s = as_space(space);
         if (!check_prepared(s, prepared) || !encoded) return zero_estimate();
-        std::vector<uint8_t> msb(s->msb_bytes), f(20);
-        if (!rabitq_export_paper_sidecar(s, encoded, 1, s->compact_bytes, msb.data(), f.data()))
+        const uint32_t id = 0;
+        RabitqPaperEstimate out = zero_estimate();
+        if (!gate_encoded_host(s, &id, 1, static_cast<const uint8_t *>(encoded), s->compact_bytes, epsilon0, &out))
             return zero_estimate();
-        return rabitq_paper_estimate_sidecar(space, prepared, msb.data(), f.data(), epsilon0);
+        return out;
     } catch (...) {
         return zero_estimate();
     }
@@ -830,19 +861,14 @@ bool rabitq_paper_estimate_batch(const void *space, const void *prepared, const 
                                  float epsilon0, RabitqPaperEstimate *out) {
     try {
         const Space *s = as_space(space);
-        if (!check_prepared(s, prepared) || !ids || !encoded_base) {
-            for (size_t i = 0; i < count; ++i) out[i] = zero_estimate();
-            return true;
+        bool ok = check_prepared(s, prepared) && ids && encoded_base;
+        for (size_t b = 0; ok && b < count; b += 4096) {
+            const size_t n = std::min<size_t>(4096, count - b);
+            ok = gate_encoded_host(s, ids + b, n, static_cast<const uint8_t *>(encoded_base), encoded_stride,
+                                   epsilon0, out + b);
         }
-        std::vector<uint8_t> rows(count * s->compact_bytes), msb(count * s->msb_bytes), f(count * 20);
-        gather_rows(rows.data(), static_cast<const uint8_t *>(encoded_base), encoded_stride, ids, count,
-                    s->compact_bytes);
-        std::vector<uint32_t> local(count);
-        for (size_t i = 0; i < count; ++i) local[i] = static_cast<uint32_t>(i);
-        if (!rabitq_export_paper_sidecar(s, rows.data(), count, s->compact_bytes, msb.data(), f.data()) ||
-            !gate_host(s, local.data(), count, msb.data(), s->msb_bytes, f.data(), 20, epsilon0, out)) {
+        if (!ok)
             for (size_t i = 0; i < count; ++i) out[i] = zero_estimate();
-        }
         return true;
     } catch (...) {
         for (size_t i = 0; i < count; ++i) out[i] = zero_estimate();

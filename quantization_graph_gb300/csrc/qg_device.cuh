@@ -180,6 +180,56 @@ __device__ __forceinline__ GateOut finish_gate(int32_t selected, const float4 pf
     return r;
 }
 
+// compute_paper_prune_estimate (space_rabitq.h:3926-3959), the gate from the encoded record
+// (rabitq_paper_estimate, rabitq_paper_estimate_batch), any codec. Its short ip is the FP32
+// restore's selected sum (shortCodeIpFromFullCodeAvx512, :1307-1329: 16 lanes over pairs, the
+// reduce tree) minus the half sum; half-warp like restore_distance_hw, lane 0 holds the result.
+template <int D>
+__device__ __forceinline__ float encoded_short_ip_hw(const uint8_t *__restrict__ code, const float *__restrict__ rr,
+                                                     float half_sum, int t) {
+    constexpr int kPairs = D / 2;
+    float sel = 0.0f;
+#pragma unroll 8
+    for (int base = 0; base < kPairs; base += 16) {
+        const int pair = base + t;
+        const uint32_t packed = code[pair];
+        const float2 q = *reinterpret_cast<const float2 *>(rr + 2 * pair);
+        if ((packed & 0x0Fu) > 7u) sel = sel + q.x;
+        if ((packed >> 4) > 7u) sel = sel + q.y;
+    }
+    return reduce16_tree(sel) - half_sum;
+}
+
+// The bound of compute_paper_prune_estimate, formed on the normalised inner product; the
+// reference build contracts the last line as fma(-two_norms, ip_upper, norm_sqr + qn2).
+// `alpha` receives the estimate's alpha (0 when refused).
+__device__ __forceinline__ GateOut finish_gate_encoded(float short_ip, float norm_sqr, float short_scale, float qn,
+                                                       float qn2, float eps, int D, float *alpha) {
+    GateOut r{0.0f, 0.0f, 0.0f, 0.0f, false, false};
+    *alpha = 0.0f;
+    if (D <= 1 || eps < 0.0f || !f_isfinite(eps) || norm_sqr <= 0.0f || qn <= 0.0f || short_scale <= 0.0f ||
+        !f_isfinite(short_scale))
+        return r;
+    const float data_norm = sqrtf(norm_sqr);
+    const float alpha_raw = 4.0f * data_norm / (short_scale * sqrtf(static_cast<float>(D)));
+    if (!(alpha_raw > 0.0f) || !f_isfinite(alpha_raw)) return r;
+    const float a = fminf(1.0f, alpha_raw);
+    r.reached = true;
+    const float cross = short_ip * short_scale;
+    const float two_norms = 2.0f * data_norm * qn;
+    const float ip_hat = cross / two_norms;
+    const float a2 = a * a;
+    const float error_bound = sqrtf(fmaxf(0.0f, (1.0f - a2) / a2)) * eps / sqrtf(static_cast<float>(D - 1));
+    const float ip_upper = fmaxf(-1.0f, fminf(1.0f, ip_hat + error_bound));
+    r.lower_bound = __fmaf_rn(-two_norms, ip_upper, norm_sqr + qn2);
+    r.short_ip = short_ip;
+    r.ip_hat = ip_hat;
+    r.error_bound = error_bound;
+    r.valid = f_isfinite(r.lower_bound);
+    *alpha = a;
+    return r;
+}
+
 // finish_paper_prune_estimate_sidecar (space_rabitq.h:4701-4721) for the Full codec's FP32 short
 // ip (selected sum - half sum): only the sidecar's valid flag is checked. `pf.w` (the error cross
 // scale, finite whenever that flag is set) is NaN exactly when the flag is 0.

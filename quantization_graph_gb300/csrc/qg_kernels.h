@@ -137,6 +137,10 @@ cudaError_t launch_gate_pairs(int code_dim, const int8_t *codes, const float4 *s
                               size_t count, const uint8_t *msb, size_t msb_stride,
                               const uint8_t *factors, size_t factor_stride, float eps,
                               RabitqPaperEstimate *out, cudaStream_t stream, bool b1 = false);
+// the gate from the encoded record (compute_paper_prune_estimate), any codec
+cudaError_t launch_gate_encoded_pairs(int code_dim, const float *rr, const float4 *scal, const uint32_t *qidx,
+                                      const uint32_t *ids, size_t count, const uint8_t *records, size_t record_stride,
+                                      float eps, RabitqPaperEstimate *out, cudaStream_t stream);
 // the Full codec's gate: the FP32 rotated residual (rr) against the MSB plane
 cudaError_t launch_gate_full_pairs(int code_dim, const float *rr, const float4 *scal, const uint32_t *qidx,
                                    const uint32_t *ids, size_t count, const uint8_t *msb, size_t msb_stride,

@@ -11,7 +11,7 @@ ours_diskann.rs:1539-1986 (which cannot be built here) is driven over the refere
 bridge kernels (oracle/ref_probe.cpp).
 
 Inputs are regenerated from numpy seeds in the tests; a checksum of each input is stored
-to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants | space_states | int4 | b1 | build_edges | b1main | full | fused]
+to catch generator drift.  Usage:  python tests/golden/make_golden.py [build_variants | space_states | int4 | b1 | build_edges | b1main | full | fused | encoded_gate]
 """
 from __future__ import annotations
 
@@ -261,6 +261,26 @@ def fused_rerank_cases():
     print("fused_rerank written")
 
 
+def encoded_gate_cases():
+    """rabitq_paper_estimate_batch (the gate from the encoded record, compute_paper_prune_estimate)
+    for every query x record of four kernel fixtures, Int8 and Full prepared queries."""
+    out = {}
+    for name in ("kernels_d128", "kernels_d100", "kernels_d960", "kernels_d1536"):
+        g = np.load(os.path.join(HERE, name + ".npz"))
+        dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+        _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+        ids = np.arange(n, dtype=np.uint32)
+        for codec in (3, 0):
+            ref = oracle_py.Reference(dim, g["center"], codec=codec)
+            rows = []
+            for q in Q:
+                ref.prepare(q)
+                rows.append(ref.gate_encoded(ids, np.ascontiguousarray(g["compact"])).view(np.uint8).reshape(n, -1))
+            out[f"{name}_c{codec}"] = np.array(rows)
+    np.savez_compressed(os.path.join(HERE, "encoded_gate.npz"), **out)
+    print("encoded_gate written")
+
+
 def build_edges():
     """Reference graphs for duplicate / near-duplicate / zero vectors and a 3-node index."""
     X = build_edge_data()
@@ -355,6 +375,9 @@ def main():
     if sys.argv[1:] == ["fused"]:
         fused_rerank_cases()
         return
+    if sys.argv[1:] == ["encoded_gate"]:
+        encoded_gate_cases()
+        return
     kernel_case("kernels_d128", 128, 64, 8, seed=20260813, center_value=0.05)
     kernel_case("kernels_d100", 100, 48, 4, seed=5, center_value=None)
     kernel_case("kernels_d960", 960, 96, 4, seed=6, center_value=None)
@@ -374,6 +397,7 @@ def main():
     b1main_cases()
     full_cases()
     fused_rerank_cases()
+    encoded_gate_cases()
     with open(os.path.join(HERE, "PROVENANCE.txt"), "w") as f:
         f.write(f"generated by tests/golden/make_golden.py on {platform.machine()} {platform.processor()}\n")
         f.write(f"reference bridge compiled with: {FLAGS}\n")

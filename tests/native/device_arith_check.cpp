@@ -64,6 +64,24 @@ void full_gate(const uint8_t *msb, size_t ms, const uint8_t *fac, size_t fs, siz
 }
 
 template <int D>
+void encoded_gate(const uint8_t *rec, size_t rs, size_t n, const float *rr, float qn2, float qn, float half, float eps,
+                  float *out6) {
+    warp_emu::run_warp([&](int lane) {
+        for (size_t base = 0; base < n; base += 2) {
+            const size_t i = base + static_cast<size_t>(lane >> 4);
+            const size_t ii = i < n ? i : base;
+            const uint8_t *r = rec + ii * rs;
+            const float sip = encoded_short_ip_hw<D>(r + 16, rr, half, lane & 15);
+            if ((lane & 15) == 0 && i < n) {
+                float alpha;
+                const GateOut g = finish_gate_encoded(sip, ld_f32(r), ld_f32(r + 8), qn, qn2, eps, D, &alpha);
+                put_estimate(g, alpha, out6 + 6 * i);
+            }
+        }
+    });
+}
+
+template <int D>
 void residual(const uint8_t *res, size_t rs, size_t n, const float *rr, float qn, const float *long_d, bool fused,
               float *out3) {
     for (size_t i = 0; i < n; ++i) {
@@ -95,6 +113,12 @@ int emu_full_distance(int D, const uint8_t *rec, size_t rs, size_t n, const floa
 int emu_full_gate(int D, const uint8_t *msb, size_t ms, const uint8_t *fac, size_t fs, size_t n, const float *rr,
                   float qn2, float qn, float half, float eps, float *out6) {
     QG_EMU_DISPATCH(D, full_gate<kD>(msb, ms, fac, fs, n, rr, qn2, qn, half, eps, out6))
+}
+
+// The gate from the encoded record (compute_paper_prune_estimate); out6 as emu_full_gate
+int emu_encoded_gate(int D, const uint8_t *rec, size_t rs, size_t n, const float *rr, float qn2, float qn, float half,
+                     float eps, float *out6) {
+    QG_EMU_DISPATCH(D, encoded_gate<kD>(rec, rs, n, rr, qn2, qn, half, eps, out6))
 }
 
 // Residual interval (two-kernel order, or the fused kernel's); out3: [n x 3]

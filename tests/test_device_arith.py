@@ -2,7 +2,8 @@
 the host from the same source and run under a warp emulator (tests/native/warp_emu.h: 32 threads
 that meet at every shuffle), against the reference's own outputs in tests/golden: the FP32 restore,
 the Int8 / Int4 gate and traversal finishes, the residual interval in the two-kernel and the fused
-order, the B1 gate, the B1Main distance, and the Full codec's gate and mode-1 distance, for every
+order, the B1 gate, the B1Main distance, the Full codec's gate and mode-1 distance, and the gate
+from the encoded record (rabitq_paper_estimate), for every
 query x record of the kernel fixtures. The prepared queries are the reference's (the fixtures hold
 them), so nothing here depends on the oracle. This checks the routines' arithmetic and lane
 order; the kernels that call them are checked on the GPU by tests/test_gpu_*.py."""
@@ -160,3 +161,20 @@ def test_b1_gate_and_b1main_distance(lib, name):
         lib.emu_b1main(D, _p(rec), C.c_size_t(rec.shape[1]), C.c_size_t(n),
                        _p(np.ascontiguousarray(g["rotated_residual"][q])), C.c_float(qn2), _p(d))
         np.testing.assert_array_equal(bits(d), bits(b1m[f"{name}_distance_b1"][q]))
+
+
+@pytest.mark.parametrize("name", ["kernels_d128", "kernels_d100", "kernels_d960", "kernels_d1536"])
+def test_encoded_record_gate(lib, name):
+    """encoded_short_ip_hw + finish_gate_encoded (compute_paper_prune_estimate) against the
+    reference's rabitq_paper_estimate_batch."""
+    g = load_golden(name)
+    v = load_golden("encoded_gate")
+    D, n, nq = _code_dim(g), int(g["n"]), int(g["nq"])
+    rec = np.ascontiguousarray(g["compact"])
+    for q in range(nq):
+        qn2, qn, half, _ = (float(x) for x in g["scalars"][q])
+        est = np.zeros((n, 6), np.float32)
+        assert lib.emu_encoded_gate(D, _p(rec), C.c_size_t(rec.shape[1]), C.c_size_t(n),
+                                    _p(np.ascontiguousarray(g["rotated_residual"][q])), C.c_float(qn2), C.c_float(qn),
+                                    C.c_float(half), C.c_float(1.9), _p(est)) == 0
+        np.testing.assert_array_equal(_estimates(est), v[f"{name}_c3"][q][:, :21])

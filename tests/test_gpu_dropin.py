@@ -276,3 +276,35 @@ def test_per_record_residual_paths(lib, name):
                 lib.rabitq_release_query(sp, prep)
         finally:
             lib.rabitq_space_delete(sp)
+
+
+@pytest.mark.parametrize("name", ["kernels_d128", "kernels_d100", "kernels_d960", "kernels_d1536"])
+@pytest.mark.parametrize("codec", [3, 0])
+def test_encoded_record_gate_entry_points(lib, name, codec):
+    """rabitq_paper_estimate and rabitq_paper_estimate_batch: the gate computed from the encoded
+    record (compute_paper_prune_estimate, a different bound from the sidecar gate's) against the
+    reference for every query x record."""
+    from quantization_graph_gb300 import _native as N
+
+    g = load_golden(name)
+    v = load_golden("encoded_gate")
+    dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+    _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+    compact = np.ascontiguousarray(g["compact"])
+    ids = np.arange(n, dtype=np.uint32)
+    sp = _space(lib, dim, g["center"], codec)
+    try:
+        for q in range(nq):
+            prep = C.c_void_p(lib.rabitq_prepare_query(sp, _p(np.ascontiguousarray(Q[q]))))
+            assert prep.value
+            est = (N.PaperEstimate * n)()
+            assert lib.rabitq_paper_estimate_batch(sp, prep, _p(ids), n, _p(compact), compact.shape[1],
+                                                   C.c_float(1.9), est)
+            got = np.frombuffer(bytes(est), np.uint8).reshape(n, -1)
+            np.testing.assert_array_equal(got[:, :21], v[f"{name}_c{codec}"][q][:, :21])
+            single = np.array([np.frombuffer(bytes(lib.rabitq_paper_estimate(sp, prep, _p(compact[i]), C.c_float(1.9))),
+                                             np.uint8) for i in range(0, n, 5)])
+            np.testing.assert_array_equal(single[:, :21], v[f"{name}_c{codec}"][q][::5, :21])
+            lib.rabitq_release_query(sp, prep)
+    finally:
+        lib.rabitq_space_delete(sp)

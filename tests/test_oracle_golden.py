@@ -333,3 +333,20 @@ def test_full_codec_variants_search_bit_exact(oracle, name, codec):
         np.testing.assert_array_equal(ids, v[f"{key}_ids_L{L}"])
         np.testing.assert_array_equal(bits(dists), bits(v[f"{key}_dists_L{L}"]))
         np.testing.assert_array_equal(stats.view(np.uint64).reshape(len(Q), -1), v[f"{key}_stats_L{L}"])
+
+
+@pytest.mark.parametrize("name", ["kernels_d128", "kernels_d100", "kernels_d960", "kernels_d1536"])
+@pytest.mark.parametrize("codec", [3, 0])
+def test_encoded_record_gate_bit_exact(oracle, name, codec):
+    """compute_paper_prune_estimate (rabitq_paper_estimate / rabitq_paper_estimate_batch): the gate
+    from the encoded record, a different bound from the sidecar gate's, against the reference."""
+    g = load_golden(name)
+    v = load_golden("encoded_gate")
+    dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+    _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+    o = oracle.Oracle(dim, g["center"], codec=codec)
+    ids = np.arange(n, dtype=np.uint32)
+    for qi in range(nq):
+        o.prepare(Q[qi])
+        est = o.gate_encoded(ids, g["compact"])
+        np.testing.assert_array_equal(est.view(np.uint8).reshape(n, -1)[:, :21], v[f"{name}_c{codec}"][qi][:, :21])
