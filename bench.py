@@ -350,6 +350,20 @@ def learned_stop_select(torch, w, args, L_fixed, rec_fixed, log):
     return model, best, table, t_train
 
 
+def replica_aggregate(step_ms: float, e2e_ms: float, units_per_rank: int, world: int, device="cuda"):
+    """Replicas only: every rank times its own copy of the workload; the job's step time is the
+    slowest rank's (all_reduce MAX over the process group) and the job's throughput counts every
+    rank's units. Returns (step_ms, e2e_ms, value, e2e_value)."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([step_ms, e2e_ms], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    step_ms, e2e_ms = float(t[0]), float(t[1])
+    return step_ms, e2e_ms, world * units_per_rank / (step_ms / 1000.0), world * units_per_rank / (e2e_ms / 1000.0)
+
+
 def main():
     args = parse()
     if args.workload == "gist960" and args.dim == 1536:
@@ -468,13 +482,8 @@ def main():
             hd.copy_(dists, non_blocking=True)
 
         e2e_ms = device_ms(torch, e2e_step, args.steps)
-    t = torch.tensor([step_ms, e2e_ms], device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    step_ms, e2e_ms = float(t[0]), float(t[1])
+    step_ms, e2e_ms, value, e2e_value = replica_aggregate(step_ms, e2e_ms, nq, world)
     ok = bool((hid.to(torch.int64).cuda() == ids.to(torch.int64)).all())
-    value = world * nq / (step_ms / 1000.0)
-    e2e_value = world * nq / (e2e_ms / 1000.0)
     search_ms = max(step_ms - prep_ms, 1e-6)
     peaks = {}
     try:
