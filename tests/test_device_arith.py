@@ -178,3 +178,41 @@ def test_encoded_record_gate(lib, name):
                                     _p(np.ascontiguousarray(g["rotated_residual"][q])), C.c_float(qn2), C.c_float(qn),
                                     C.c_float(half), C.c_float(1.9), _p(est)) == 0
         np.testing.assert_array_equal(_estimates(est), v[f"{name}_c3"][q][:, :21])
+
+
+def test_invalid_factors_and_degenerate_records(lib, oracle):
+    """Rows the fixtures do not hold: sidecar factors whose valid flag is 0 (with finite values)
+    and records with zero, negative or NaN norms and zero, NaN or infinite short scales. The
+    device routines (Int8 gate, Full gate, encoded-record gate) must refuse exactly where the
+    oracle's restatement does and agree with it bit for bit elsewhere."""
+    from test_oracle_golden import edge_gate_inputs
+
+    g, rec, fac = edge_gate_inputs()  # the oracle is checked against the reference on the same rows
+    D, n = _code_dim(g), int(g["n"])
+    _, Q = kernel_inputs(int(g["dim"]), n, int(g["nq"]), int(g["seed"]))
+    msb = np.ascontiguousarray(g["msb"])
+    ids = np.arange(n, dtype=np.uint32)
+    for codec in (3, 0):
+        o = oracle.Oracle(int(g["dim"]), g["center"], codec=codec)
+        for q in range(2):
+            p = o.prepare(Q[q])
+            rr = np.ascontiguousarray(p["rotated_residual"])
+            qn2, qn, half = float(p["query_norm_sqr"]), float(p["query_norm"]), float(p["half_sum"])
+            want = o.gate(ids, msb, fac).view(np.uint8).reshape(n, -1)[:, :21]
+            est = np.zeros((n, 6), np.float32)
+            if codec == 3:
+                lib.emu_int_gate(D, _p(msb), C.c_size_t(msb.shape[1]), _p(fac), C.c_size_t(fac.shape[1]),
+                                 C.c_size_t(n), _p(np.ascontiguousarray(p["codes"])), C.c_float(qn2), C.c_float(qn),
+                                 C.c_float(float(p["scale"])), C.c_longlong(int(p["code_sum"])), C.c_float(1.9),
+                                 _p(est))
+            else:
+                assert lib.emu_full_gate(D, _p(msb), C.c_size_t(msb.shape[1]), _p(fac), C.c_size_t(fac.shape[1]),
+                                         C.c_size_t(n), _p(rr), C.c_float(qn2), C.c_float(qn), C.c_float(half),
+                                         C.c_float(1.9), _p(est)) == 0
+            np.testing.assert_array_equal(_estimates(est), want)
+            assert not want[::3, 20].any()  # the invalid rows were refused
+            want_enc = o.gate_encoded(ids, rec).view(np.uint8).reshape(n, -1)[:, :21]
+            assert lib.emu_encoded_gate(D, _p(rec), C.c_size_t(rec.shape[1]), C.c_size_t(n), _p(rr), C.c_float(qn2),
+                                        C.c_float(qn), C.c_float(half), C.c_float(1.9), _p(est)) == 0
+            np.testing.assert_array_equal(_estimates(est), want_enc)
+            assert not want_enc[[1, 4, 7, 10, 13, 16], 20].any()

@@ -350,3 +350,37 @@ def test_encoded_record_gate_bit_exact(oracle, name, codec):
         o.prepare(Q[qi])
         est = o.gate_encoded(ids, g["compact"])
         np.testing.assert_array_equal(est.view(np.uint8).reshape(n, -1)[:, :21], v[f"{name}_c{codec}"][qi][:, :21])
+
+
+def edge_gate_inputs():
+    """kernels_d128 with every third sidecar factor row marked invalid (values left in place) and
+    degenerate record headers: zero / negative / NaN norms, zero / NaN / infinite short scales."""
+    g = load_golden("kernels_d128")
+    rec = np.ascontiguousarray(g["compact"]).copy()
+    fac = np.ascontiguousarray(g["factors"]).copy()
+    fac[::3, 16] = 0
+    f32 = rec[:, :16].copy().view(np.float32)
+    f32[1, 0], f32[4, 0], f32[7, 0] = 0.0, -1.0, np.nan
+    f32[10, 2], f32[13, 2], f32[16, 2] = 0.0, np.nan, np.inf
+    rec[:, :16] = f32.view(np.uint8)
+    return g, rec, fac
+
+
+@pytest.mark.parametrize("codec", [3, 0, 1])
+def test_gates_on_invalid_and_degenerate_rows_match_reference(oracle, codec):
+    """The sidecar gate and the encoded-record gate on invalid factors and degenerate records,
+    oracle against the reference library (where it is built)."""
+    if not oracle.reference_available():
+        pytest.skip("reference tree not present on this host")
+    g, rec, fac = edge_gate_inputs()
+    n = int(g["n"])
+    _, Q = kernel_inputs(int(g["dim"]), n, int(g["nq"]), int(g["seed"]))
+    ids = np.arange(n, dtype=np.uint32)
+    o, r = oracle.Oracle(int(g["dim"]), g["center"], codec=codec), oracle.Reference(int(g["dim"]), g["center"], codec=codec)
+    for q in range(4):
+        o.prepare(Q[q])
+        r.prepare(Q[q])
+        for fo, fr in ((o.gate(ids, g["msb"], fac), r.gate(ids, g["msb"], fac)),
+                       (o.gate_encoded(ids, rec), r.gate_encoded(ids, rec))):
+            np.testing.assert_array_equal(fo.view(np.uint8).reshape(n, -1)[:, :21],
+                                          fr.view(np.uint8).reshape(n, -1)[:, :21])
