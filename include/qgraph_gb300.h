@@ -130,8 +130,9 @@ void rabitq_release_query(const void *space, const void *prepared);
 /* rabitq_bridge.cpp:380-387 (full FP32 4-bit restore) */
 float rabitq_query_distance(const void *space, const void *prepared, const void *encoded);
 /* rabitq_bridge.cpp:389-396 / 398-423: the 4-bit x 1-bit distance (query_distance_b1,
- * space_rabitq.h:3741-3753) for a B1Main prepared query; +inf otherwise (the batch form fills
- * +inf and returns true, as the reference does for failed items) */
+ * space_rabitq.h:3741-3753) for a B1Main or B1 prepared query (both prepare the query's signs);
+ * +inf otherwise (the batch form fills +inf and returns true). The reference reads a sign vector
+ * that the other codecs never prepare, so its value there depends on earlier calls. */
 float rabitq_query_distance_b1(const void *space, const void *prepared, const void *encoded);
 bool rabitq_query_distance_b1_batch(const void *space, const void *prepared, const uint32_t *ids,
                                     size_t count, const void *encoded_base, size_t encoded_stride,

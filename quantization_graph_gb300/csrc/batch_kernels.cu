@@ -138,25 +138,43 @@ __global__ void gate_encoded_pairs_kernel(const float *rr, const float4 *scal, c
 }
 
 // query_distance_b1 over (query, record) pairs, one warp per pair; codes are the B1Main +-1
-// bytes, csum the sign sum.
+// bytes with the sign sum in csum, or (sign_bits) a B1 prepared query's sign bits.
 template <int D>
 __global__ void distance_b1_pairs_kernel(const int8_t *codes, const float4 *scal, const long long *csum,
                                          const uint32_t *qidx, const uint32_t *ids, size_t count,
-                                         const uint8_t *records, size_t record_stride, float *out) {
+                                         const uint8_t *records, size_t record_stride, bool sign_bits, float *out) {
     const size_t pair = (static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (pair >= count) return;
     const uint32_t q = qidx[pair], id = ids[pair];
     const int8_t *x = codes + static_cast<size_t>(q) * D;
+    const uint8_t *qb = reinterpret_cast<const uint8_t *>(x);
     const uint8_t *rec = records + static_cast<size_t>(id) * record_stride;
     int dot = 0;
     for (int p = lane; p < D / 2; p += 32) {
         const int b = rec[16 + p];
-        dot += (b & 15) * x[2 * p] + (b >> 4) * x[2 * p + 1];
+        int x0, x1;
+        if (sign_bits) {  // B1: bit i of byte i / 8 set where q'_i > 0
+            const int i0 = 2 * p, i1 = 2 * p + 1;
+            x0 = ((qb[i0 >> 3] >> (i0 & 7)) & 1) ? 1 : -1;
+            x1 = ((qb[i1 >> 3] >> (i1 & 7)) & 1) ? 1 : -1;
+        } else {
+            x0 = x[2 * p];
+            x1 = x[2 * p + 1];
+        }
+        dot += (b & 15) * x0 + (b >> 4) * x1;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
-    if (lane == 0) out[pair] = finish_b1main(ld_f32(rec), ld_f32(rec + 4), dot, csum[q], scal[q].x);
+    long long sign_sum = csum[q];
+    if (sign_bits) {  // B1 keeps other scalars in the code-sum slot: count the positive signs
+        int pos = 0;
+        for (int j = lane; j < D / 8; j += 32) pos += __popc(static_cast<uint32_t>(qb[j]));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) pos += __shfl_xor_sync(0xffffffffu, pos, o);
+        sign_sum = 2LL * pos - D;
+    }
+    if (lane == 0) out[pair] = finish_b1main(ld_f32(rec), ld_f32(rec + 4), dot, sign_sum, scal[q].x);
 }
 
 template <int D>
@@ -379,10 +397,10 @@ cudaError_t launch_gate_encoded_pairs(int code_dim, const float *rr, const float
 
 cudaError_t launch_distance_b1_pairs(int code_dim, const int8_t *codes, const float4 *scal, const long long *csum,
                                      const uint32_t *qidx, const uint32_t *ids, size_t count, const uint8_t *records,
-                                     size_t record_stride, float *out, cudaStream_t stream) {
+                                     size_t record_stride, float *out, cudaStream_t stream, bool sign_bits) {
     if (count == 0) return cudaSuccess;
     QG_DISPATCH_D(code_dim, distance_b1_pairs_kernel<kD><<<warp_grid(count), 256, 0, stream>>>(
-                                codes, scal, csum, qidx, ids, count, records, record_stride, out));
+                                codes, scal, csum, qidx, ids, count, records, record_stride, sign_bits, out));
     return cudaGetLastError();
 }
 

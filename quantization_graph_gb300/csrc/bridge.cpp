@@ -275,7 +275,7 @@ bool distance_b1_host(const Space *s, const uint32_t *ids, size_t count, const u
     if (!cuda_ok(launch_distance_b1_pairs(static_cast<int>(s->code_dim), t_prepared.d_codes, t_prepared.d_scal,
                                           t_prepared.d_csum, reinterpret_cast<uint32_t *>(d + o_q),
                                           reinterpret_cast<uint32_t *>(d + o_i), count, d + o_r, rb,
-                                          reinterpret_cast<float *>(d + o_o), st),
+                                          reinterpret_cast<float *>(d + o_o), st, t_prepared.codec == 1),
                  "b1 distance kernel"))
         return false;
     if (!cuda_ok(cudaMemcpyAsync(h + o_o, d + o_o, count * 4, cudaMemcpyDeviceToHost, st), "b1 distance download"))
@@ -750,8 +750,8 @@ float rabitq_query_distance_b1(const void *space, const void *prepared, const vo
     try {
         const Space *s = as_space(space);
         if (!check_prepared(s, prepared) || !encoded) return inf;
-        if (t_prepared.codec != 4) {
-            set_error("rabitq_query_distance_b1: prepare the query with the B1Main codec (4)");
+        if (t_prepared.codec != 4 && t_prepared.codec != 1) {
+            set_error("rabitq_query_distance_b1: prepare the query with the B1Main (4) or B1 (1) codec");
             return inf;
         }
         const uint32_t id = 0;
@@ -769,7 +769,7 @@ bool rabitq_query_distance_b1_batch(const void *space, const void *prepared, con
     try {
         const Space *s = as_space(space);
         if (!out_distances) return false;
-        bool ok = check_prepared(s, prepared) && ids && encoded_base && t_prepared.codec == 4;
+        bool ok = check_prepared(s, prepared) && ids && encoded_base && (t_prepared.codec == 4 || t_prepared.codec == 1);
         for (size_t b = 0; ok && b < count; b += 4096) {
             const size_t n = std::min<size_t>(4096, count - b);
             ok = distance_b1_host(s, ids + b, n, static_cast<const uint8_t *>(encoded_base), encoded_stride,

@@ -160,10 +160,11 @@ cudaError_t launch_residual_pairs(int code_dim, const float *rr, const float4 *s
                                   cudaStream_t stream);
 cudaError_t launch_symmetric_pairs(int code_dim, const uint8_t *lhs, const uint8_t *rhs,
                                    size_t count, size_t stride, float *out, cudaStream_t stream);
-// query_distance_b1 (space_rabitq.h:3741-3753) over (query, record) pairs; codes = B1Main +-1 bytes.
+// query_distance_b1 (space_rabitq.h:3741-3753) over (query, record) pairs; codes = B1Main +-1 bytes,
+// or, with sign_bits, a B1 prepared query's sign bits.
 cudaError_t launch_distance_b1_pairs(int code_dim, const int8_t *codes, const float4 *scal, const long long *csum,
                                      const uint32_t *qidx, const uint32_t *ids, size_t count, const uint8_t *records,
-                                     size_t record_stride, float *out, cudaStream_t stream);
+                                     size_t record_stride, float *out, cudaStream_t stream, bool sign_bits = false);
 
 // rabitq_build_vamana_graph arguments (rabitq_bridge.cpp:224-303)
 struct VbBuildParams {

@@ -149,14 +149,16 @@ def test_sentinels_of_what_is_not_built(lib):
 
 
 @pytest.mark.parametrize("name", ["kernels_d128", "kernels_d1536"])
-def test_b1main_distance_entry_points(lib, name):
-    """rabitq_query_distance_b1 and its batch form with a B1Main prepared query, against the
-    reference's query_distance_b1 for every query x record."""
+@pytest.mark.parametrize("codec", [4, 1])
+def test_b1main_distance_entry_points(lib, name, codec):
+    """rabitq_query_distance_b1 and its batch form with a B1Main prepared query (or a B1 one: both
+    prepare the query's signs, and the reference gives the same values), against the reference's
+    query_distance_b1 for every query x record."""
     g = load_golden(name)
     v = load_golden("b1main_codec")
     dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
     _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
-    sp = _space(lib, dim, g["center"], 4)
+    sp = _space(lib, dim, g["center"], codec)
     try:
         compact = g["compact"]
         ids = np.arange(n, dtype=np.uint32)
