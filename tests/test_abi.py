@@ -76,3 +76,33 @@ def test_mlp_layout_constants_agree():
     assert int(m.group(1)) == mlp_ref.PARAMS == _native.MLP_PARAMS == 4801
     m = re.search(r"#define QG_NOALLOC_SCRATCH_BYTES \(\(size_t\)(\d+) << (\d+)\)", text)
     assert int(m.group(1)) << int(m.group(2)) == _native.QG_NOALLOC_SCRATCH_BYTES
+
+
+def test_train_centroids_matches_reference(oracle):
+    """rabitq_train_centroids (host k-means, rabitq_bridge.cpp:101-172) needs no GPU: called on the
+    CPU and compared bit for bit with the reference library's (where it is built)."""
+    import ctypes as C
+
+    from quantization_graph_gb300 import build
+
+    if not oracle.reference_available():
+        import pytest
+
+        pytest.skip("reference tree not present on this host")
+    ours = C.CDLL(build.build())
+    ref = oracle.Reference(64, np.zeros(64, np.float32)).lib
+    for lib in (ours, ref):
+        lib.rabitq_train_centroids.restype = C.c_bool
+        lib.rabitq_train_centroids.argtypes = [C.c_void_p, C.c_size_t, C.c_size_t, C.c_size_t, C.c_size_t,
+                                               C.c_uint32, C.c_int, C.c_void_p]
+    rng = np.random.default_rng(0)
+    for n, d, k in ((2000, 32, 8), (3000, 128, 64), (1500, 960, 4)):
+        X = (rng.standard_normal((n, d)) * rng.uniform(0.1, 2, d)).astype(np.float32)
+        a = np.zeros((k, d), np.float32)
+        b = np.zeros((k, d), np.float32)
+        assert ours.rabitq_train_centroids(X.ctypes.data, n, d, k, min(n, 2500), 7, 10, a.ctypes.data)
+        assert ref.rabitq_train_centroids(X.ctypes.data, n, d, k, min(n, 2500), 7, 10, b.ctypes.data)
+        np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
+    # the reference's argument checks
+    assert not ours.rabitq_train_centroids(X.ctypes.data, n, d, 257, 100, 7, 10, a.ctypes.data)
+    assert not ours.rabitq_train_centroids(X.ctypes.data, n, d, 4, 0, 7, 10, a.ctypes.data)
