@@ -103,12 +103,14 @@ def test_prepared_query_kernels(lib, name):
             np.testing.assert_array_equal(got[:, :21], g["gate"][q][:, :21])
             sip = np.array([e.short_ip for e in est], np.float32)
             out = np.zeros(n, np.float32)
-            assert lib.rabitq_query_distance_batch(sp, prep, _p(ids), _p(np.full(n, 2, np.uint8)), n, _p(compact),
+            mode2 = np.full(n, 2, np.uint8)
+            assert lib.rabitq_query_distance_batch(sp, prep, _p(ids), _p(mode2), n, _p(compact),
                                                    compact.shape[1], _p(sip), _p(out))
             np.testing.assert_array_equal(bits(out), bits(g["dist_mode2"][q]))
             d0 = np.zeros(n, np.float32)
-            assert lib.rabitq_query_distance_batch(sp, prep, _p(ids), _p(np.zeros(n, np.uint8)), n, _p(compact),
-                                                   compact.shape[1], _p(np.zeros(n, np.float32)), _p(d0))
+            mode0, zero_ips = np.zeros(n, np.uint8), np.zeros(n, np.float32)
+            assert lib.rabitq_query_distance_batch(sp, prep, _p(ids), _p(mode0), n, _p(compact),
+                                                   compact.shape[1], _p(zero_ips), _p(d0))
             np.testing.assert_array_equal(bits(d0), bits(g["dist_mode0"][q]))
             single = np.array([lib.rabitq_query_distance(sp, prep, C.c_void_p(compact[i].ctypes.data))
                                for i in range(n)], np.float32)
@@ -138,7 +140,8 @@ def test_sentinels_of_what_is_not_built(lib):
         lib.rabitq_set_query_coarse_codec(sp, 0)  # a Full prepared query has no integer codes for mode 2
         prep = C.c_void_p(lib.rabitq_prepare_query(sp, _p(query)))
         assert prep.value
-        assert lib.rabitq_query_distance_batch(sp, prep, _p(np.zeros(1, np.uint32)), _p(np.full(1, 2, np.uint8)), 1,
+        one_id, one_mode2 = np.zeros(1, np.uint32), np.full(1, 2, np.uint8)
+        assert lib.rabitq_query_distance_batch(sp, prep, _p(one_id), _p(one_mode2), 1,
                                                _p(g["compact"]), g["compact"].shape[1], _p(sip), _p(out))
         assert np.isinf(out[0])
         for codec in (5, 6, 0x105):  # FullStaged, FullRerankScalar, an id outside the enum: Full
@@ -227,7 +230,8 @@ def test_full_codec_entry_points(lib, name):
             np.testing.assert_array_equal(got[:, :21], v[f"{name}_gate"][q][:, :21])
             sip = np.array([e.short_ip for e in est], np.float32)
             out = np.zeros(n, np.float32)
-            assert lib.rabitq_query_distance_batch(sp, prep, _p(ids), _p(np.ones(n, np.uint8)), n, _p(compact),
+            mode1 = np.ones(n, np.uint8)
+            assert lib.rabitq_query_distance_batch(sp, prep, _p(ids), _p(mode1), n, _p(compact),
                                                    compact.shape[1], _p(sip), _p(out))
             np.testing.assert_array_equal(bits(out), bits(v[f"{name}_dist_mode1"][q]))
             modes = (ids % 2).astype(np.uint8)  # mixed batch: odd records mode 1, even mode 0
