@@ -921,9 +921,12 @@ void qgo_gate_batch(const qgo_space *s, const qgo_prepared *q, const uint32_t *i
         Factors f;
         std::memcpy(&f, fb + static_cast<size_t>(ids[i]) * factors_stride, sizeof(Factors));
         const uint8_t *msb = msb_base + static_cast<size_t>(ids[i]) * msb_stride;
-        out[i] = s->query_bits == 1    ? gate_b1_one(*s, *q, msb, f, eps)
-                 : s->query_bits == 32 ? gate_full_one(*s, *q, msb, f, eps)
-                                       : gate_one(*s, *q, msb, f, eps);
+        // compute_paper_prune_estimate_sidecar (space_rabitq.h:4510-4531): B1 -> the popcount gate,
+        // Int4 / Int8 -> the integer gate, every other codec (Full, B1Main, the Full variants) ->
+        // the FP32 Full gate
+        out[i] = s->codec == 1                     ? gate_b1_one(*s, *q, msb, f, eps)
+                 : (s->codec == 2 || s->codec == 3) ? gate_one(*s, *q, msb, f, eps)
+                                                    : gate_full_one(*s, *q, msb, f, eps);
     }
 }
 

@@ -179,9 +179,12 @@ bool gate_host(const Space *s, const uint32_t *ids, size_t count, const uint8_t 
     gather_rows(h + o_f, factors_base, factor_stride, ids, count, 20);
     cudaStream_t st = t_stage.stream;
     if (!cuda_ok(cudaMemcpyAsync(d, h, o_o, cudaMemcpyHostToDevice, st), "gate upload")) return false;
+    // compute_paper_prune_estimate_sidecar (space_rabitq.h:4510-4531): B1 -> the popcount gate,
+    // Int4 / Int8 -> the integer gate, every other codec (Full, B1Main, the Full variants) -> the
+    // FP32 Full gate
     const int codec = t_prepared.codec;
     const cudaError_t ge =
-        codec_query_bits(codec) == 32
+        (codec != 1 && codec_search_mode(codec) != 0)
             ? launch_gate_full_pairs(static_cast<int>(s->code_dim), t_prepared.d_rr, t_prepared.d_scal,
                                      reinterpret_cast<uint32_t *>(d + o_q), reinterpret_cast<uint32_t *>(d + o_i),
                                      count, d + o_m, mb, d + o_f, 20, eps,
@@ -1157,8 +1160,8 @@ int qg_gate_pairs(const void *space, const int8_t *d_codes, const float *d_scala
                   size_t factor_stride, float epsilon0, RabitqPaperEstimate *d_out, void *stream) {
     const Space *s = as_space(space);
     if (!s) return QG_ERR_INVALID;
-    if (space_query_bits(s) == 32) {
-        set_error("qg_gate_pairs: the Full codec's gate reads the rotated residual; use qg_gate_full_pairs");
+    if (s->codec != 1 && space_search_mode(s) != 0) {
+        set_error("qg_gate_pairs: this codec's gate (the Full gate) reads the rotated residual; use qg_gate_full_pairs");
         return QG_ERR_INVALID;
     }
     if (!cuda_ok(launch_gate_pairs(static_cast<int>(s->code_dim), d_codes,

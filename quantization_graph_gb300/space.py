@@ -145,7 +145,7 @@ class RabitqSpace:
         ids = _cuda(ids, torch.int32)
         n = ids.shape[0]
         out = torch.empty((n, 24), dtype=torch.uint8, device="cuda")
-        if self.codec == CODEC_FULL:
+        if self.codec not in (CODEC_B1, CODEC_INT4, CODEC_INT8):  # the Full gate (Full, B1Main, variants)
             N.check(self.lib.qg_gate_full_pairs(self.ptr, _ptr(prepared["rotated_residual"]),
                                                 _ptr(prepared["scalars"]), _ptr(qidx), _ptr(ids), n, _ptr(msb),
                                                 msb.shape[1], _ptr(factors), factors.shape[1], epsilon0, _ptr(out),

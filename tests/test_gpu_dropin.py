@@ -174,6 +174,15 @@ def test_b1main_distance_entry_points(lib, name, codec):
             out = np.zeros(n, np.float32)
             assert lib.rabitq_query_distance_b1_batch(sp, prep, _p(ids), n, _p(compact), compact.shape[1], _p(out))
             np.testing.assert_array_equal(bits(out), bits(v[f"{name}_distance_b1"][q]))
+            if codec == 4:  # B1Main gates with the FP32 Full gate (space_rabitq.h:4510-4531)
+                from quantization_graph_gb300 import _native as N
+
+                msb, factors = g["msb"], g["factors"]
+                est = (N.PaperEstimate * n)()
+                assert lib.rabitq_paper_estimate_batch_sidecar(sp, prep, _p(ids), n, _p(msb), msb.shape[1],
+                                                               _p(factors), factors.shape[1], C.c_float(1.9), est)
+                got = np.frombuffer(bytes(est), np.uint8).reshape(n, -1)
+                np.testing.assert_array_equal(got[:, :21], load_golden("full_codec")[f"{name}_gate"][q][:, :21])
     finally:
         lib.rabitq_space_delete(sp)
 

@@ -384,3 +384,26 @@ def test_gates_on_invalid_and_degenerate_rows_match_reference(oracle, codec):
                        (o.gate_encoded(ids, rec), r.gate_encoded(ids, rec))):
             np.testing.assert_array_equal(fo.view(np.uint8).reshape(n, -1)[:, :21],
                                           fr.view(np.uint8).reshape(n, -1)[:, :21])
+
+
+@pytest.mark.parametrize("name", ["kernels_d128", "kernels_d960", "kernels_d1536"])
+@pytest.mark.parametrize("codec", [4, 5, 6])
+def test_other_codecs_gate_with_the_full_gate(oracle, name, codec):
+    """compute_paper_prune_estimate_sidecar sends every codec but B1, Int4 and Int8 to the FP32 Full
+    gate (space_rabitq.h:4510-4531): a B1Main or Full-variant prepared query gates as Full does
+    (the reference's outputs for those codecs equal full_codec.npz's gates)."""
+    g = load_golden(name)
+    v = load_golden("full_codec")
+    dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+    _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+    o = oracle.Oracle(dim, g["center"], codec=codec)
+    ids = np.arange(n, dtype=np.uint32)
+    for qi in range(nq):
+        o.prepare(Q[qi])
+        est = o.gate(ids, g["msb"], g["factors"])
+        np.testing.assert_array_equal(est.view(np.uint8).reshape(n, -1)[:, :21], v[f"{name}_gate"][qi][:, :21])
+        if oracle.reference_available():
+            r = oracle.Reference(dim, g["center"], codec=codec)
+            r.prepare(Q[qi])
+            np.testing.assert_array_equal(r.gate(ids, g["msb"], g["factors"]).view(np.uint8).reshape(n, -1)[:, :21],
+                                          v[f"{name}_gate"][qi][:, :21])
