@@ -1003,21 +1003,26 @@ bool rabitq_full_residual_distance_batch(const void *space, const void *prepared
                                          const void *encoded_base, size_t encoded_stride,
                                          const void *residual_base, size_t residual_stride,
                                          RabitqDistanceInterval *out) {
+    // compute_full_residual_distance_intervals_batch_by_id: per record, the FP32 restore (mode 0)
+    // and the residual in the fused kernel's product order (space_rabitq.h:5700-5743); a record
+    // whose restore is not finite keeps its own result. +inf for every item when the call fails,
+    // as the reference's catch does for a batch.
     const float inf = std::numeric_limits<float>::infinity();
     try {
-        std::vector<uint8_t> modes(count, 0);
-        std::vector<float> zeros(count, 0.0f), longd(count, inf);
-        rabitq_query_distance_batch(space, prepared, ids, modes.data(), count, encoded_base,
-                                    encoded_stride, zeros.data(), longd.data());
-        bool any_inf = false;
-        for (float v : longd) any_inf |= !std::isfinite(v);
-        if (any_inf && count) {
-            for (size_t i = 0; i < count; ++i) out[i] = RabitqDistanceInterval{inf, inf, inf};
-            return true;
+        const Space *s = as_space(space);
+        bool ok = check_prepared(s, prepared) && ids && encoded_base && residual_base;
+        std::vector<float> longd(count, inf);
+        if (ok && count) {
+            std::vector<uint8_t> modes(count, 0);
+            ok = distance_host(s, ids, modes.data(), count, static_cast<const uint8_t *>(encoded_base), encoded_stride,
+                               nullptr, longd.data());
         }
-        // the residual in the fused kernel's product order (space_rabitq.h:5700-5743)
-        return residual_batch(space, prepared, ids, count, residual_base, residual_stride, longd.data(), out,
-                              true);
+        if (ok && count)
+            ok = residual_host(s, ids, count, static_cast<const uint8_t *>(residual_base), residual_stride,
+                               longd.data(), out, true);
+        if (!ok)
+            for (size_t i = 0; i < count; ++i) out[i] = RabitqDistanceInterval{inf, inf, inf};
+        return true;
     } catch (...) {
         for (size_t i = 0; i < count; ++i) out[i] = RabitqDistanceInterval{inf, inf, inf};
         return true;

@@ -323,3 +323,41 @@ def test_encoded_record_gate_entry_points(lib, name, codec):
             lib.rabitq_release_query(sp, prep)
     finally:
         lib.rabitq_space_delete(sp)
+
+
+def test_fused_rerank_keeps_per_record_results(lib, oracle):
+    """A record whose restore is not finite (NaN norm) keeps its own NaN interval and one with an
+    infinite long scale takes the invalid-record distance, while the others are unchanged: the
+    fused entry computes each record on its own, as the reference does (the oracle's fused
+    restatement matches the reference library on these rows)."""
+    from quantization_graph_gb300 import _native as N
+
+    g = load_golden("kernels_d128")
+    dim, n, nq = int(g["dim"]), int(g["n"]), int(g["nq"])
+    _, Q = kernel_inputs(dim, n, nq, int(g["seed"]))
+    compact = np.ascontiguousarray(g["compact"]).copy()
+    residual = np.ascontiguousarray(g["residual"])
+    f32 = compact[:, :16].copy().view(np.float32)
+    f32[3, 0], f32[9, 1] = np.nan, np.inf
+    compact[:, :16] = f32.view(np.uint8)
+    ids = np.arange(n, dtype=np.uint32)
+    o = oracle.Oracle(dim, g["center"])
+    sp = _space(lib, dim, g["center"])
+    try:
+        for q in range(2):
+            query = np.ascontiguousarray(Q[q])
+            prep = C.c_void_p(lib.rabitq_prepare_query(sp, _p(query)))
+            assert prep.value
+            iv = (N.DistanceInterval * n)()
+            assert lib.rabitq_full_residual_distance_batch(sp, prep, _p(ids), n, _p(compact), compact.shape[1],
+                                                           _p(residual), residual.shape[1], iv)
+            got = np.frombuffer(bytes(iv), np.float32).reshape(n, 3)
+            o.prepare(query)
+            want = o.full_residual(ids, compact, residual)
+            nan = np.isnan(want)
+            np.testing.assert_array_equal(np.isnan(got), nan)  # NaN payloads differ between CPU and GPU
+            np.testing.assert_array_equal(bits(got)[~nan], bits(want)[~nan])
+            assert nan[3].all() and not nan[9].any() and nan.sum() == 3
+            lib.rabitq_release_query(sp, prep)
+    finally:
+        lib.rabitq_space_delete(sp)
