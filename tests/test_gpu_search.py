@@ -224,50 +224,3 @@ def test_b1main_codec_search_matches_reference(cuda, name):
         np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), v[f"{name}_ids_L{L}"])
         np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(v[f"{name}_dists_L{L}"]))
         np.testing.assert_array_equal(stats_matrix(r.stats), v[f"{name}_stats_L{L}"])
-
-
-@pytest.mark.parametrize("name", list(SEARCH_CASES))
-@pytest.mark.parametrize("codec", [3, 2])
-def test_fused_int_rerank_search_matches_reference(cuda, name, codec):
-    """Int8 / Int4 searches with the fused rerank switched on (RABITQ_ENABLE_FUSED_INT_RERANK in
-    the reference) against the reference's kernels: ids, distance bits, counters."""
-    torch = cuda
-    from quantization_graph_gb300.index import OursIndex
-    from quantization_graph_gb300.space import RabitqSpace
-
-    g = load_golden(name)
-    v = load_golden("fused_rerank")
-    _, Q = SEARCH_CASES[name]()
-    sp = RabitqSpace(int(g["dim"]), g["center"], codec=codec)
-    ix = OursIndex(sp, g["compact"], g["residual"], g["msb"], g["factors"], g["degrees"], g["edges"])
-    q = torch.from_numpy(Q).cuda()
-    for L in (20, 40):
-        r = ix.search(q, k=10, l_value=L, with_stats=True, fused_int_rerank=True)
-        np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), v[f"{name}_c{codec}_ids_L{L}"])
-        np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(v[f"{name}_c{codec}_dists_L{L}"]))
-        np.testing.assert_array_equal(stats_matrix(r.stats), v[f"{name}_c{codec}_stats_L{L}"])
-
-
-@pytest.mark.parametrize("name", list(SEARCH_CASES))
-@pytest.mark.parametrize("codec", [0, 5, 6])
-def test_full_codec_search_matches_reference(cuda, name, codec):
-    """The Full codec through the batched GPU search (FP32 gate against the MSB plane, survivors
-    by the remaining bits with the gate's short ip, the rerank correcting those distances)
-    against the reference's kernels: ids, distance bits, counters. FullStaged (5) searches as Full;
-    FullRerankScalar (6) reranks in the per-record residual order."""
-    torch = cuda
-    from quantization_graph_gb300.index import OursIndex
-    from quantization_graph_gb300.space import RabitqSpace
-
-    g = load_golden(name)
-    v = load_golden("full_codec")
-    _, Q = SEARCH_CASES[name]()
-    sp = RabitqSpace(int(g["dim"]), g["center"], codec=codec)
-    ix = OursIndex(sp, g["compact"], g["residual"], g["msb"], g["factors"], g["degrees"], g["edges"])
-    q = torch.from_numpy(Q).cuda()
-    for L in (20, 40):
-        key = f"{name}_c{codec}" if f"{name}_c{codec}_ids_L{L}" in v else name
-        r = ix.search(q, k=10, l_value=L, with_stats=True)
-        np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), v[f"{key}_ids_L{L}"])
-        np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(v[f"{key}_dists_L{L}"]))
-        np.testing.assert_array_equal(stats_matrix(r.stats), v[f"{key}_stats_L{L}"])
