@@ -298,13 +298,22 @@ int qg_search_batch_ex(qg_index *index, const float *d_queries, size_t nq,
  * (warps x n_total x 2 bytes) must fit the array, else QG_ERR_INVALID with the reason in
  * qg_last_error(). All calls share the array: calls whose GPU work overlaps race, so serialise
  * them. The first call on a device looks up the array's address (make it before any stream
- * capture). Failed queries (bad neighbour ids) return UINT32_MAX ids; the status word is not
- * read back (no synchronisation). */
+ * capture). The call itself does not synchronise: failed queries (bad neighbour ids) return
+ * UINT32_MAX ids, and qg_search_noalloc_status reads the kernels' status word back. The visited
+ * tags limit the warps searching at once to about (64 MiB - prepared queries) / (2 * n_total):
+ * ~32 at 1M nodes; an index needs 2 * n_total <= ~64 MiB (about 33M nodes). */
 #define QG_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
 int qg_search_batch_noalloc(qg_index *index, const float *d_queries, size_t nq,
                             const qg_search_params *params, const int *d_k, const int *d_l,
                             size_t k_stride, uint32_t *d_ids, float *d_dists,
                             qg_search_stats *d_stats, void *stream);
+/* No counterpart in the reference. The status of the last qg_search_batch_noalloc call on the
+ * current device, read from the no-alloc scratch array on `stream` (synchronises it): QG_OK,
+ * QG_ERR_GRAPH (a neighbour id outside the graph; those queries returned no results),
+ * QG_ERR_TIMEOUT (the hop cap ended a search) or QG_ERR_INVALID (a per-query L above the
+ * call's pool capacity max(params->l_value, k) was clamped), as qg_search_status reports them
+ * for qg_search_batch. */
+int qg_search_noalloc_status(void *stream);
 /* Learned early termination (no counterpart in the reference: its search stops at fixed L or
  * by the kth / stall heuristics, ours_diskann.rs:1784-1809). A network 8 -> 64 -> 64 -> 1 with
  * BF16 weights reads 8 search-state features every `every` hops; the query stops expanding when

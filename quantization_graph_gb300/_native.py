@@ -107,6 +107,7 @@ _SIGS = {
     "qg_search_batch": (C.c_int, [P, P, SZ, P, P, P, SZ, P, P, P, P]),
     "qg_search_batch_ex": (C.c_int, [P, P, SZ, P, P, P, SZ, P, P, P, P, SZ, P]),
     "qg_search_batch_noalloc": (C.c_int, [P, P, SZ, P, P, P, SZ, P, P, P, P]),
+    "qg_search_noalloc_status": (C.c_int, [P]),
     "qg_search_batch_learned": (C.c_int, [P, P, SZ, P, P, P, SZ, P, P, P, P, P, P]),
     "qg_mlp_forward": (C.c_int, [P, SZ, P, P, P, P]),
     "qg_mlp_backward": (C.c_int, [P, P, SZ, P, P, P, P, P]),

@@ -351,6 +351,88 @@ void assemble_full(const Space *s, const uint8_t *compact, const uint8_t *residu
 
 void record_error(const std::string &msg) { set_error(msg); }
 
+// Warps per block and resident blocks per SM for a pool of l_cap entries: the caller's override
+// (qg_index_set_launch) clamped to what is resident, else the candidate with the most resident
+// warps (large pools need more shared memory per warp, where smaller blocks pack better).
+bool search_launch_geometry(const qg_index *index, int l_cap, bool stop_model, int *wpb_out, int *per_sm_out) {
+    const int D = static_cast<int>(index->space->code_dim);
+    int wpb = 0, per_sm = 0;
+    if (index->launch_wpb > 0) {
+        wpb = index->launch_wpb;
+        per_sm = search_blocks_per_sm(D, l_cap, wpb, stop_model);
+        if (index->launch_per_sm > 0 && index->launch_per_sm < per_sm) per_sm = index->launch_per_sm;
+    } else {
+        for (int cand : {8, 4, 2}) {
+            const int b = search_blocks_per_sm(D, l_cap, cand, stop_model);
+            if (b * cand > per_sm * wpb) {
+                wpb = cand;
+                per_sm = b;
+            }
+        }
+    }
+    if (per_sm <= 0 || wpb <= 0) {
+        set_error("search kernel cannot be resident with this pool size and launch shape");
+        return false;
+    }
+    *wpb_out = wpb;
+    *per_sm_out = per_sm;
+    return true;
+}
+
+int search_args_fill(const qg_index *index, size_t nq, const qg_search_params *params, const float *d_queries,
+                     const int *d_k, const int *d_l, size_t k_stride, uint32_t *d_ids, float *d_dists,
+                     qg_search_stats *d_stats, SearchArgs *out) {
+    if (!index || !params || !out || (nq && (!d_queries || !d_ids || !d_dists))) {
+        set_error("search: null argument");
+        return QG_ERR_INVALID;
+    }
+    if (nq > 0x7FFFFFFF) {
+        set_error("search: more than 2^31 - 1 queries in one batch");
+        return QG_ERR_INVALID;
+    }
+    const Space *s = index->space;
+    const int k_max = d_k ? static_cast<int>(k_stride) : params->k;
+    if (k_max <= 0 || (d_k == nullptr && k_stride != 0 && k_stride < static_cast<size_t>(params->k))) {
+        set_error("k must be positive and fit the output stride");
+        return QG_ERR_INVALID;
+    }
+    const int l_cap = std::max(params->l_value, k_max);
+    if (l_cap > 4096 || params->beam_width < 1 || params->beam_width > 8 || params->rerank_candidates < 0) {
+        set_error("L must be <= 4096 and beam width 1..8");
+        return QG_ERR_INVALID;
+    }
+    if (!space_query_bits(s)) {
+        set_error("the GPU query path implements the Full (0), B1 (1), Int4 (2), Int8 (3) and B1Main (4) "
+                  "query codecs");
+        return QG_ERR_INVALID;
+    }
+    SearchArgs a{};
+    a.ix = index->ix;
+    a.nq = static_cast<int>(nq);
+    a.k_default = params->k;
+    a.l_default = params->l_value;
+    a.k_per_q = d_k;
+    a.l_per_q = d_l;
+    a.k_stride = k_max;
+    a.l_cap = l_cap;
+    a.beam_width = params->beam_width;
+    a.eps = params->epsilon0;
+    a.rerank = params->rerank_candidates;
+    a.early_stop_hops = params->early_stop_hops;
+    a.kth_stop = params->kth_stop;
+    // the rerank residual in the fused kernel's order: the fused Int8 / Int4 rerank, or
+    // FullRerankScalar's per-record residual path
+    a.fused_rerank = ((space_search_mode(s) == 0 && params->fused_int_rerank != 0) || s->codec == 6) ? 1 : 0;
+    a.mode = space_search_mode(s);
+    a.ids_out = d_ids;
+    a.dists_out = d_dists;
+    a.stats_out = d_stats;
+    a.hop_cap = static_cast<int>(std::min<size_t>(static_cast<size_t>(index->ix.n_total) + 1, 0x7FFFFFFF));
+    a.stop_every = 1;
+    *out = a;
+    return QG_OK;
+}
+
 }  // namespace qg
 
 using namespace qg;
@@ -1005,8 +1087,10 @@ bool rabitq_full_residual_distance_batch(const void *space, const void *prepared
                                          RabitqDistanceInterval *out) {
     // compute_full_residual_distance_intervals_batch_by_id: per record, the FP32 restore (mode 0)
     // and the residual in the fused kernel's product order (space_rabitq.h:5700-5743); a record
-    // whose restore is not finite keeps its own result. +inf for every item when the call fails,
-    // as the reference's catch does for a batch.
+    // whose restore is not finite keeps its own result. The reference runs 64-record chunks and
+    // fills only a chunk that throws with +inf (rabitq_bridge.cpp:1044-1084); its chunks throw
+    // only on whole-call conditions (no space, no prepared query, null bases), which fail every
+    // chunk alike, so filling every item with +inf on a failure gives the same output.
     const float inf = std::numeric_limits<float>::infinity();
     try {
         const Space *s = as_space(space);
@@ -1392,34 +1476,6 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
                        const qg_stop_model *model, const qg_trace_request *trace, void *stream,
                        const int *d_nq = nullptr, bool allow_alloc = true);
 
-// Warps per block and resident blocks per SM for a pool of l_cap entries: the caller's override
-// (qg_index_set_launch) clamped to what is resident, else the candidate with the most resident
-// warps (large pools need more shared memory per warp, where smaller blocks pack better).
-static bool launch_geometry(const qg_index *index, int l_cap, bool stop_model, int *wpb_out, int *per_sm_out) {
-    const int D = static_cast<int>(index->space->code_dim);
-    int wpb = 0, per_sm = 0;
-    if (index->launch_wpb > 0) {
-        wpb = index->launch_wpb;
-        per_sm = search_blocks_per_sm(D, l_cap, wpb, stop_model);
-        if (index->launch_per_sm > 0 && index->launch_per_sm < per_sm) per_sm = index->launch_per_sm;
-    } else {
-        for (int cand : {8, 4, 2}) {
-            const int b = search_blocks_per_sm(D, l_cap, cand, stop_model);
-            if (b * cand > per_sm * wpb) {
-                wpb = cand;
-                per_sm = b;
-            }
-        }
-    }
-    if (per_sm <= 0 || wpb <= 0) {
-        set_error("search kernel cannot be resident with this pool size and launch shape");
-        return false;
-    }
-    *wpb_out = wpb;
-    *per_sm_out = per_sm;
-    return true;
-}
-
 int qg_index_set_launch(qg_index *index, int warps_per_block, int blocks_per_sm) {
     if (!index || warps_per_block < 0 || warps_per_block > 8 || blocks_per_sm < 0) return QG_ERR_INVALID;
     index->launch_wpb = warps_per_block;
@@ -1530,20 +1586,12 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
                        qg_search_stats *d_stats, uint32_t *d_expanded, size_t expanded_cap,
                        const qg_stop_model *model, const qg_trace_request *trace, void *stream,
                        const int *d_nq, bool allow_alloc) {
-    if (!index || !params || (nq && (!d_queries || !d_ids || !d_dists))) return QG_ERR_INVALID;
+    SearchArgs a{};
+    const int rc = search_args_fill(index, nq, params, d_queries, d_k, d_l, k_stride, d_ids, d_dists, d_stats, &a);
+    if (rc != QG_OK) return rc;
     if (d_expanded && (expanded_cap == 0 || expanded_cap > 0x7FFFFFFF)) return QG_ERR_INVALID;
-    if (nq > 0x7FFFFFFF) return QG_ERR_INVALID;
     const Space *s = index->space;
-    const int k_max = d_k ? static_cast<int>(k_stride) : params->k;
-    if (k_max <= 0 || (d_k == nullptr && k_stride != 0 && k_stride < static_cast<size_t>(params->k))) {
-        set_error("k must be positive and fit the output stride");
-        return QG_ERR_INVALID;
-    }
-    const int l_cap = std::max(params->l_value, k_max);
-    if (l_cap > 4096 || params->beam_width < 1 || params->beam_width > 8 || params->rerank_candidates < 0) {
-        set_error("L must be <= 4096 and beam width 1..8");
-        return QG_ERR_INVALID;
-    }
+    const int l_cap = a.l_cap;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // prepared-query workspace
     if (index->q_capacity < nq && !allow_alloc) {
@@ -1569,10 +1617,8 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
     }
     // persistent grid: warps per block and resident blocks per SM from the occupancy of
     // this pool size; one visited-tag row per warp slot
-    // warps per block: the candidate with the most resident warps per SM (large pools need
-    // more shared memory per warp, where smaller blocks pack better)
     int wpb = 0, per_sm = 0;
-    if (!launch_geometry(index, l_cap, model != nullptr, &wpb, &per_sm)) return QG_ERR_UNSUPPORTED;
+    if (!search_launch_geometry(index, l_cap, model != nullptr, &wpb, &per_sm)) return QG_ERR_UNSUPPORTED;
     int sms = qg_device_sm_count();
     if (sms <= 0) sms = 1;
     const int grid = sms * per_sm;
@@ -1599,11 +1645,6 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
     }
     if (nq == 0) return QG_OK;
     {
-        if (!space_query_bits(s)) {
-            set_error("the GPU query path implements the Full (0), B1 (1), Int4 (2), Int8 (3) and B1Main (4) "
-                      "query codecs");
-            return QG_ERR_INVALID;
-        }
         PrepArgs pa{d_queries, s->dim, static_cast<int>(nq), static_cast<int>(s->dim),
                     static_cast<int>(s->code_dim), s->d_signs, s->d_center, s->d_rotated_center,
                     s->d_center_norm, index->q.rr, index->q.codes, index->q.scal, index->q.csum, d_nq};
@@ -1613,40 +1654,17 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
     if (!cuda_ok(cudaMemsetAsync(index->counter, 0, 4, st), "counter reset") ||
         !cuda_ok(cudaMemsetAsync(index->status, 0, 4, st), "status reset"))
         return QG_ERR_CUDA;
-    SearchArgs a{};
-    a.ix = index->ix;
     a.rr = index->q.rr;
     a.codes = index->q.codes;
     a.scal = index->q.scal;
     a.csum = index->q.csum;
-    a.nq = static_cast<int>(nq);
-    a.k_default = params->k;
-    a.l_default = params->l_value;
-    a.k_per_q = d_k;
-    a.l_per_q = d_l;
-    a.k_stride = k_max;
-    a.l_cap = l_cap;
-    a.beam_width = params->beam_width;
-    a.eps = params->epsilon0;
-    a.rerank = params->rerank_candidates;
-    a.early_stop_hops = params->early_stop_hops;
-    a.kth_stop = params->kth_stop;
-    // the rerank residual in the fused kernel's order: the fused Int8 / Int4 rerank, or
-    // FullRerankScalar's per-record residual path
-    a.fused_rerank = ((space_search_mode(s) == 0 && params->fused_int_rerank != 0) || s->codec == 6) ? 1 : 0;
-    a.mode = space_search_mode(s);
-    a.ids_out = d_ids;
-    a.dists_out = d_dists;
-    a.stats_out = d_stats;
     a.tags = index->tags;
     a.epochs = index->epochs;
     a.counter = index->counter;
     a.status = index->status;
-    a.hop_cap = static_cast<int>(std::min<size_t>(index->ix.n_total + 1, 0x7FFFFFFF));
     a.nq_dev = d_nq;
     a.expanded_out = d_expanded;
     a.expanded_cap = static_cast<int>(expanded_cap);
-    a.stop_every = 1;
     if (model) {
         a.stop_w = model->d_weights;
         a.stop_norm = model->d_norm;

@@ -99,6 +99,18 @@ struct EncodeArgs {
 // Sets the message qg_last_error() returns on the calling thread.
 void record_error(const std::string &msg);
 
+// Checks the arguments of a batched search (qg_search_batch and its variants) and fills every
+// field of *out that does not name scratch memory: the prepared-query buffers, visited tags,
+// epochs, work counter and status word stay null for the caller to place. Returns QG_OK or a
+// QG_ERR_* status with the message recorded.
+int search_args_fill(const qg_index *index, size_t nq, const qg_search_params *params, const float *d_queries,
+                     const int *d_k, const int *d_l, size_t k_stride, uint32_t *d_ids, float *d_dists,
+                     qg_search_stats *d_stats, SearchArgs *out);
+// Warps per block and resident blocks per SM of the search kernel for a pool of l_cap entries:
+// the qg_index_set_launch override clamped to what is resident, else the shape with the most
+// resident warps. False (message recorded) when no block can be resident.
+bool search_launch_geometry(const qg_index *index, int l_cap, bool stop_model, int *wpb_out, int *per_sm_out);
+
 cudaError_t launch_prepare(const PrepArgs &a, cudaStream_t stream);
 cudaError_t launch_round_quotient_pairs(const float *x, const float *s, size_t n, int *out, uint8_t *undecided,
                                         cudaStream_t stream);

@@ -37,15 +37,6 @@ constexpr uint32_t kIdMask = 0x7FFFFFFFu;
 constexpr int kMaxFresh = 64;   // fresh neighbours per expanded node (max degree)
 constexpr int kMaxBeam = 8;
 
-#ifndef QG_GATE_PREFETCH
-#define QG_GATE_PREFETCH 0  // 0: every fresh MSB row to L1 at once; 1: one gate group ahead
-#endif
-#ifndef QG_TRAV_PREFETCH
-#define QG_TRAV_PREFETCH 0  // 0: every survivor code row to L1 at once; 1: L2, L1 one group ahead; 2: L2
-#endif
-#ifndef QG_GATE_ASYNC
-#define QG_GATE_ASYNC 0  // 1: gate MSB rows staged in shared memory by cp.async, two groups in flight
-#endif
 #ifndef QG_TRAV_GROUP_WIDE
 #define QG_TRAV_GROUP_WIDE 2  // code rows in flight per traversal group for D = 2048
 #endif
@@ -77,10 +68,7 @@ struct WarpSmem {
     float *sdist;
     float2 *shdr;
     uint32_t *frontier;
-    uint8_t *gstage;  // two gate groups of MSB rows (QG_GATE_ASYNC)
 };
-
-constexpr int kGateStageBytes = QG_GATE_ASYNC ? 2 * QG_GATE_GROUP * 128 : 0;
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~static_cast<size_t>(15); }
 
@@ -91,7 +79,6 @@ __host__ __device__ inline size_t warp_smem_bytes(int l_cap) {
     s += align16(kMaxFresh * 16);
     s += align16(kMaxFresh * 4) * 3 + align16(kMaxFresh * 8);
     s += align16(kMaxBeam * 4);
-    s += kGateStageBytes;
     return s;
 }
 
@@ -116,30 +103,7 @@ __device__ WarpSmem carve(unsigned char *base, int l_cap) {
     w.sdist = reinterpret_cast<float *>(take(kMaxFresh * 4));
     w.shdr = reinterpret_cast<float2 *>(take(kMaxFresh * 8));
     w.frontier = reinterpret_cast<uint32_t *>(take(kMaxBeam * 4));
-    w.gstage = take(kGateStageBytes);
     return w;
-}
-
-// 16-byte asynchronous copy global -> shared, cached in L2 only (cp.async.cg), and the
-// group bookkeeping around it.
-__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc) {
-    const unsigned int d = static_cast<unsigned int>(__cvta_generic_to_shared(smem_dst));
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gsrc) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
-#ifndef QG_STREAM_ROWS
-#define QG_STREAM_ROWS 0  // 1: gate and code rows read with the evict-first hint (each is read once)
-#endif
-template <typename T>
-__device__ __forceinline__ T row_load(const T *p) {
-#if QG_STREAM_ROWS
-    return __ldcs(p);
-#else
-    return __ldg(p);
-#endif
 }
 
 __device__ __forceinline__ void prefetch_l1(const void *p) {
@@ -477,66 +441,21 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             } else {
                 // ---- gate (paper-prune lower bound) for every fresh neighbour ----
                 // all MSB rows and factor rows are requested at once, then consumed group by group
-    #if QG_GATE_ASYNC
-                if constexpr (L::LPN != 32) prefetch_rows_l1(ix.msb, s.fid, F, D / 8, D / 8, lane);
-    #elif QG_GATE_PREFETCH == 0
                 prefetch_rows_l1(ix.msb, s.fid, F, D / 8, D / 8, lane);
-    #else
-                if constexpr (L::LPN == 32)
-                    prefetch_rows_l1(ix.msb, s.fid, F < L::GG ? F : L::GG, D / 8, D / 8, lane);
-                else
-                    prefetch_rows_l1(ix.msb, s.fid, F, D / 8, D / 8, lane);
-    #endif
                 prefetch_rows_l1(reinterpret_cast<const uint8_t *>(ix.pf), s.fid, F, 16, 16, lane);
                 for (int f = lane; f < F; f += 32) s.fpf[f] = ix.pf[s.fid[f]];
                 if constexpr (L::LPN == 32) {
                     constexpr int G = L::GG;
-    #if QG_GATE_ASYNC
-                    // rows of gate group `grp_i` to stage (grp_i & 1): G rows of D/8 bytes, 16-byte
-                    // pieces spread over the lanes; rows past F are not copied
-                    static_assert(G * (D / 8) <= QG_GATE_GROUP * 128, "gate stage size");
-                    auto stage_rows = [&](int gbase, int st) {
-                        constexpr int kPieces = G * (D / 8) / 16;
-                        uint8_t *dst = s.gstage + st * (QG_GATE_GROUP * 128);
-    #pragma unroll
-                        for (int c = lane; c < kPieces; c += 32) {
-                            const int r = c / (D / 128), off = (c % (D / 128)) * 16;
-                            if (gbase + r < F)
-                                cp_async16(dst + r * (D / 8) + off, ix.msb + static_cast<size_t>(s.fid[gbase + r]) * (D / 8) + off);
-                        }
-                        cp_async_commit();
-                    };
-                    stage_rows(0, 0);
-                    stage_rows(G, 1);
-    #endif
-                    for (int gb = 0, st = 0; gb < F; gb += G, st ^= 1) {
+                    for (int gb = 0; gb < F; gb += G) {
                         uint32_t w[G][L::CPL];
-    #if QG_GATE_ASYNC
-                        cp_async_wait<1>();
-                        __syncwarp();
-                        const uint32_t *stage = reinterpret_cast<const uint32_t *>(s.gstage + st * (QG_GATE_GROUP * 128));
-    #pragma unroll
-                        for (int g = 0; g < G; ++g) {
-    #pragma unroll
-                            for (int j = 0; j < L::CPL; ++j) w[g][j] = stage[g * (D / 32) + lane + 32 * j];
-                        }
-                        __syncwarp();
-                        stage_rows(gb + 2 * G, st);
-    #else
     #pragma unroll
                         for (int g = 0; g < G; ++g) {
                             const int f = gb + g < F ? gb + g : gb;
                             const uint32_t *row = reinterpret_cast<const uint32_t *>(
                                 ix.msb + static_cast<size_t>(s.fid[f]) * (D / 8));
     #pragma unroll
-                            for (int j = 0; j < L::CPL; ++j) w[g][j] = row_load(row + lane + 32 * j);
+                            for (int j = 0; j < L::CPL; ++j) w[g][j] = __ldg(row + lane + 32 * j);
                         }
-    #endif
-    #if QG_GATE_PREFETCH == 1
-                        if (gb + G < F)
-                            prefetch_rows_l1(ix.msb, s.fid + gb + G, F - gb - G < G ? F - gb - G : G, D / 8, D / 8,
-                                             lane);
-    #endif
                         int p[G];
     #pragma unroll
                         for (int g = 0; g < G; ++g) {
@@ -560,9 +479,6 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                             s.fval[f] = go.valid ? 1 : 0;
                         }
                     }
-    #if QG_GATE_ASYNC
-                    cp_async_wait<0>();  // nothing is left in flight (the last groups copy no rows)
-    #endif
                 } else {
                     constexpr int P = L::PG;
                     for (int fb = 0; fb < F; fb += P * L::NBP) {
@@ -620,14 +536,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             if (S == 0) continue;
 
             // ---- traversal distances of the survivors ----
-#if QG_TRAV_PREFETCH == 0
             prefetch_rows_l1(ix.codes, s.sid, S, D / 2, D / 2, lane);
-#else
-            prefetch_rows_l2(ix.codes, s.sid, S, D / 2, D / 2, lane);
-#if QG_TRAV_PREFETCH == 1
-            if constexpr (L::LPN == 32) prefetch_rows_l1(ix.codes, s.sid, S < L::GT ? S : L::GT, D / 2, D / 2, lane);
-#endif
-#endif
             prefetch_rows_l1(reinterpret_cast<const uint8_t *>(ix.hdr), s.sid, S, 16, 16, lane);
             // survivors are the likeliest next expansions: warm L2 with their adjacency rows
             prefetch_rows_l2(reinterpret_cast<const uint8_t *>(ix.edges), s.sid, S, ix.edge_stride * 4,
@@ -673,13 +582,8 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                             const uint4 *row = reinterpret_cast<const uint4 *>(
                                 ix.codes + static_cast<size_t>(s.sid[i]) * (D / 2));
     #pragma unroll
-                            for (int j = 0; j < L::CPL; ++j) c[g][j] = row_load(row + lane + 32 * j);
+                            for (int j = 0; j < L::CPL; ++j) c[g][j] = __ldg(row + lane + 32 * j);
                         }
-    #if QG_TRAV_PREFETCH == 1
-                        if (gb + G < S)
-                            prefetch_rows_l1(ix.codes, s.sid + gb + G, S - gb - G < G ? S - gb - G : G, D / 2, D / 2,
-                                             lane);
-    #endif
                         int p[G];
     #pragma unroll
                         for (int g = 0; g < G; ++g) {

@@ -19,6 +19,15 @@
 // Set-up: the first call on a device looks up the array's device address with
 // cudaGetSymbolAddress (host code cannot use the symbol itself: on the host it names a
 // stand-in, not device memory). Make that first call before any stream capture.
+//
+// Failures inside the kernels (a neighbour id outside the graph, the hop cap, a per-query L
+// above the pool capacity) are recorded in a status word in the same array;
+// qg_search_noalloc_status reads it back after the call, as qg_search_status does for
+// qg_search_batch. It is the status of the last call on the device.
+//
+// The visited tags take one row of 2 * n_total bytes per resident warp, so the number of warps
+// that search at once is about (64 MiB - prepared queries) / (2 * n_total): ~32 at 1M nodes,
+// ~300 at 100k (every resident warp, up to 152 SMs x 16, below ~27k nodes).
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -33,6 +42,8 @@ namespace {
 
 constexpr size_t kScratchBytes = QG_NOALLOC_SCRATCH_BYTES;
 constexpr int kMaxDevices = 64;
+constexpr size_t kCounterOffset = 0;   // the search's work counter
+constexpr size_t kStatusOffset = 256;  // the search's status word (qg_search_noalloc_status)
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -70,29 +81,20 @@ extern "C" int qg_search_batch_noalloc(qg_index *index, const float *d_queries, 
                                        size_t k_stride, uint32_t *d_ids, float *d_dists,
                                        qg_search_stats *d_stats, void *stream) {
     using namespace qg;
-    if (!index || !params || (nq && (!d_queries || !d_ids || !d_dists)))
-        return fail(QG_ERR_INVALID, "qg_search_batch_noalloc: null argument");
-    const Space *s = index->space;
-    const int k_max = d_k ? static_cast<int>(k_stride) : params->k;
-    if (k_max <= 0 || nq > 0x7FFFFFFF)
-        return fail(QG_ERR_INVALID, "qg_search_batch_noalloc: k must be positive");
-    const int l_cap = params->l_value > k_max ? params->l_value : k_max;
-    if (l_cap > 4096 || params->beam_width < 1 || params->beam_width > 8 || params->rerank_candidates < 0)
-        return fail(QG_ERR_INVALID, "qg_search_batch_noalloc: L must be <= 4096 and beam width 1..8");
+    SearchArgs a{};
+    const int rc = search_args_fill(index, nq, params, d_queries, d_k, d_l, k_stride, d_ids, d_dists, d_stats, &a);
+    if (rc != QG_OK) return rc;
     void *base = nullptr;
     cudaError_t e = scratch_address(&base);
     if (e != cudaSuccess)
         return fail(QG_ERR_CUDA, std::string("qg_search_batch_noalloc: scratch set-up: ") + cudaGetErrorString(e));
     if (nq == 0) return QG_OK;
 
+    const Space *s = index->space;
     const size_t D = s->code_dim;
     const size_t n_total = index->ix.n_total;
     // scratch layout: counter | status | prepared queries (rotated, codes, scalars, sums) | epochs | tags
-    size_t off = 0;
-    const size_t o_counter = off;
-    off += 256;
-    const size_t o_status = off;
-    off += 256;
+    size_t off = kStatusOffset + 256;
     const size_t o_rr = off;
     off += round256(nq * D * sizeof(float));
     const size_t o_codes = off;
@@ -104,32 +106,37 @@ extern "C" int qg_search_batch_noalloc(qg_index *index, const float *d_queries, 
     if (off > kScratchBytes)
         return fail(QG_ERR_INVALID, "qg_search_batch_noalloc: " + std::to_string(nq) +
                                         " queries do not fit the 64 MiB no-alloc scratch");
-    // warp slots: as many resident warps as the tag rows that still fit
-    int wpb = 8, per_sm = 0;
-    for (int cand : {8, 4, 2}) {
-        const int b = search_blocks_per_sm(static_cast<int>(D), l_cap, cand);
-        if (b * cand > per_sm * wpb) {
-            wpb = cand;
-            per_sm = b;
-        }
-    }
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (per_sm <= 0 || sms <= 0)
-        return fail(QG_ERR_UNSUPPORTED, "qg_search_batch_noalloc: search kernel cannot be resident");
+    // the launch shape qg_search_batch would take (with any qg_index_set_launch override) ...
+    int wpb = 0, per_sm = 0;
+    if (!search_launch_geometry(index, a.l_cap, false, &wpb, &per_sm)) return QG_ERR_UNSUPPORTED;
+    int sms = qg_device_sm_count();
+    if (sms <= 0) return fail(QG_ERR_CUDA, "qg_search_batch_noalloc: no device");
+    size_t max_slots = static_cast<size_t>(sms) * per_sm * wpb;
     const size_t row_bytes = n_total * sizeof(uint16_t);  // the kernel's tag rows are packed
-    const size_t epoch_bytes = round256(static_cast<size_t>(sms) * per_sm * wpb * sizeof(uint32_t));
+    const size_t epoch_bytes = round256(max_slots * sizeof(uint32_t));
     if (off + epoch_bytes > kScratchBytes)
         return fail(QG_ERR_INVALID, "qg_search_batch_noalloc: queries leave no room for visited tags");
+    // ... cut to the visited-tag rows that fit: one row of n_total tags per warp slot; a block
+    // narrower than wpb is taken when fewer than wpb rows fit
     const size_t room = kScratchBytes - off - epoch_bytes;
-    size_t slots = row_bytes ? room / row_bytes : 0;
-    const size_t max_slots = static_cast<size_t>(sms) * per_sm * wpb;
-    if (slots > max_slots) slots = max_slots;
+    size_t fit = row_bytes ? room / row_bytes : 0;
+    if (fit < static_cast<size_t>(wpb)) {
+        int narrow = 0;
+        for (int cand : {4, 2, 1})
+            if (cand < wpb && static_cast<size_t>(cand) <= fit) {
+                narrow = cand;
+                break;
+            }
+        if (narrow == 0)
+            return fail(QG_ERR_INVALID, "qg_search_batch_noalloc: index of " + std::to_string(n_total) +
+                                            " nodes is too large for the 64 MiB no-alloc scratch");
+        wpb = narrow;
+        per_sm = search_blocks_per_sm(static_cast<int>(D), a.l_cap, wpb);
+        if (per_sm <= 0) return fail(QG_ERR_UNSUPPORTED, "qg_search_batch_noalloc: search kernel cannot be resident");
+        max_slots = static_cast<size_t>(sms) * per_sm * wpb;
+    }
+    size_t slots = fit < max_slots ? fit : max_slots;
     slots -= slots % static_cast<size_t>(wpb);
-    if (slots == 0)
-        return fail(QG_ERR_INVALID, "qg_search_batch_noalloc: index of " + std::to_string(n_total) +
-                                        " nodes is too large for the 64 MiB no-alloc scratch");
     const size_t o_epochs = off;
     off += epoch_bytes;
     const size_t o_tags = off;
@@ -137,13 +144,11 @@ extern "C" int qg_search_batch_noalloc(qg_index *index, const float *d_queries, 
     unsigned char *sb = static_cast<unsigned char *>(base);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     // clear what must start at zero; tag rows are laid out for this call's node count
-    if ((e = cudaMemsetAsync(sb + o_counter, 0, 512, st)) != cudaSuccess ||
+    if ((e = cudaMemsetAsync(sb + kCounterOffset, 0, kStatusOffset + 256, st)) != cudaSuccess ||
         (e = cudaMemsetAsync(sb + o_epochs, 0, epoch_bytes, st)) != cudaSuccess ||
         (e = cudaMemsetAsync(sb + o_tags, 0, slots * row_bytes, st)) != cudaSuccess)
         return fail(QG_ERR_CUDA, std::string("qg_search_batch_noalloc: clear: ") + cudaGetErrorString(e));
 
-    if (!space_query_bits(s))
-        return fail(QG_ERR_INVALID, "qg_search_batch_noalloc: the Full (0), B1 (1), Int4 (2), Int8 (3) and B1Main (4) query codecs only");
     PrepArgs pa{d_queries, s->dim, static_cast<int>(nq), static_cast<int>(s->dim), static_cast<int>(D),
                 s->d_signs, s->d_center, s->d_rotated_center, s->d_center_norm,
                 reinterpret_cast<float *>(sb + o_rr), reinterpret_cast<int8_t *>(sb + o_codes),
@@ -152,39 +157,33 @@ extern "C" int qg_search_batch_noalloc(qg_index *index, const float *d_queries, 
     if ((e = launch_prepare(pa, st)) != cudaSuccess)
         return fail(QG_ERR_CUDA, std::string("qg_search_batch_noalloc: prepare: ") + cudaGetErrorString(e));
 
-    SearchArgs a{};
-    a.ix = index->ix;
     a.rr = pa.rr;
     a.codes = pa.codes;
     a.scal = pa.scal;
     a.csum = pa.csum;
-    a.nq = static_cast<int>(nq);
-    a.k_default = params->k;
-    a.l_default = params->l_value;
-    a.k_per_q = d_k;
-    a.l_per_q = d_l;
-    a.k_stride = k_max;
-    a.l_cap = l_cap;
-    a.beam_width = params->beam_width;
-    a.eps = params->epsilon0;
-    a.rerank = params->rerank_candidates;
-    a.early_stop_hops = params->early_stop_hops;
-    a.kth_stop = params->kth_stop;
-    // the rerank residual in the fused kernel's order: the fused Int8 / Int4 rerank, or
-    // FullRerankScalar's per-record residual path
-    a.fused_rerank = ((space_search_mode(s) == 0 && params->fused_int_rerank != 0) || s->codec == 6) ? 1 : 0;
-    a.mode = space_search_mode(s);
-    a.ids_out = d_ids;
-    a.dists_out = d_dists;
-    a.stats_out = d_stats;
     a.tags = reinterpret_cast<uint16_t *>(sb + o_tags);
     a.epochs = reinterpret_cast<uint32_t *>(sb + o_epochs);
-    a.counter = reinterpret_cast<unsigned int *>(sb + o_counter);
-    a.status = reinterpret_cast<int *>(sb + o_status);
-    a.hop_cap = static_cast<int>(n_total + 1 < 0x7FFFFFFF ? n_total + 1 : 0x7FFFFFFF);
-    a.expanded_out = nullptr;
-    a.expanded_cap = 0;
+    a.counter = reinterpret_cast<unsigned int *>(sb + kCounterOffset);
+    a.status = reinterpret_cast<int *>(sb + kStatusOffset);
     if ((e = launch_search(a, static_cast<int>(slots / static_cast<size_t>(wpb)), wpb, st)) != cudaSuccess)
         return fail(QG_ERR_CUDA, std::string("qg_search_batch_noalloc: search: ") + cudaGetErrorString(e));
+    return QG_OK;
+}
+
+extern "C" int qg_search_noalloc_status(void *stream) {
+    void *base = nullptr;
+    cudaError_t e = scratch_address(&base);
+    if (e != cudaSuccess)
+        return fail(QG_ERR_CUDA, std::string("qg_search_noalloc_status: scratch set-up: ") + cudaGetErrorString(e));
+    // the status word sits at a fixed offset of the array; the 4-byte copy lands in host stack memory
+    int h = 0;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if ((e = cudaMemcpyAsync(&h, static_cast<unsigned char *>(base) + kStatusOffset, sizeof(int),
+                             cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(st)) != cudaSuccess)
+        return fail(QG_ERR_CUDA, std::string("qg_search_noalloc_status: ") + cudaGetErrorString(e));
+    if (h & 1) return fail(QG_ERR_GRAPH, "a neighbour id outside the graph: the query returned no results");
+    if (h & 2) return fail(QG_ERR_TIMEOUT, "the hop cap ended a search");
+    if (h & 4) return fail(QG_ERR_INVALID, "a per-query L above the call's pool capacity was clamped");
     return QG_OK;
 }

@@ -16,7 +16,7 @@ import pytest
 
 from quantization_graph_gb300 import runio
 
-REF = "/root/reference"
+REF = os.environ.get("REF_ROOT", "/root/reference")
 
 
 def _ref_function(path, name, extra=None):

@@ -77,3 +77,48 @@ def test_no_alloc_search_rejects_sizes_beyond_its_scratch(cuda):
                                      _ptr(d), None, C.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert rc == 1  # QG_ERR_INVALID
     assert "do not fit" in N.last_error()
+
+
+def _noalloc_call(lib, N, index, q, k, params, torch, d_l=None):
+    nq = q.shape[0]
+    ids = torch.full((nq, k), 7, dtype=torch.int32, device="cuda")
+    d = torch.zeros((nq, k), dtype=torch.float32, device="cuda")
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rc = lib.qg_search_batch_noalloc(index.handle, _ptr(q), nq, C.byref(params), None, _ptr(d_l), k, _ptr(ids),
+                                     _ptr(d), None, stream)
+    assert rc == N.QG_OK, N.last_error()
+    return ids, d, lib.qg_search_noalloc_status(stream)
+
+
+def test_no_alloc_status_reports_what_the_kernels_saw(cuda):
+    """A neighbour id outside the graph gives UINT32_MAX ids and QG_ERR_GRAPH, a per-query L above
+    the call's pool capacity gives QG_ERR_INVALID, exactly as qg_search_batch + qg_search_status
+    report them; a clean call afterwards reads QG_OK again."""
+    torch = cuda
+    from quantization_graph_gb300 import _native as N
+    from quantization_graph_gb300.index import OursIndex
+    from quantization_graph_gb300.space import RabitqSpace
+
+    lib = N.load()
+    g = load_golden("search_c1")
+    _, Q = SEARCH_CASES["search_c1"]()
+    q = torch.from_numpy(Q[:32]).cuda()
+    space = RabitqSpace(128, g["center"])
+    params = N.SearchParams(10, 40, 1, 1.9, 100, 0, 0)
+
+    edges = g["edges"].copy()
+    edges[0, 0] = 10 ** 6  # node 0 (the start of every query) names a node outside the graph
+    bad = OursIndex(space, g["compact"], g["residual"], g["msb"], g["factors"], g["degrees"], edges)
+    ids, _, st = _noalloc_call(lib, N, bad, q, 10, params, torch)
+    assert st == 4, N.STATUS_NAMES.get(st)  # QG_ERR_GRAPH
+    assert (ids.cpu().numpy().astype(np.uint32) == np.uint32(0xFFFFFFFF)).all()
+    with pytest.raises(RuntimeError, match="QG_ERR_GRAPH"):  # the allocating path agrees
+        bad.search(q, k=10, l_value=40)
+
+    good = OursIndex(space, g["compact"], g["residual"], g["msb"], g["factors"], g["degrees"], g["edges"])
+    big_l = torch.full((q.shape[0],), 80, dtype=torch.int32, device="cuda")  # above params.l_value = 40
+    _, _, st = _noalloc_call(lib, N, good, q, 10, params, torch, d_l=big_l)
+    assert st == 1, N.STATUS_NAMES.get(st)  # QG_ERR_INVALID: clamped to 40
+    ids, d, st = _noalloc_call(lib, N, good, q, 10, params, torch)
+    assert st == N.QG_OK
+    np.testing.assert_array_equal(ids.cpu().numpy().astype(np.uint32), g["ids_L40_k10"][:32])
