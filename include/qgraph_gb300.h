@@ -316,22 +316,30 @@ int qg_search_batch_noalloc(qg_index *index, const float *d_queries, size_t nq,
 int qg_search_noalloc_status(void *stream);
 /* Learned early termination (no counterpart in the reference: its search stops at fixed L or
  * by the kth / stall heuristics, ours_diskann.rs:1784-1809). A network 8 -> 64 -> 64 -> 1 with
- * BF16 weights reads 8 search-state features every `every` hops; the query stops expanding when
- * sigmoid(logit) > threshold (never before min_hops) and reranks its current pool. Weight layout
+ * BF16 weights reads 8 search-state features every `every` hops (never before min_hops). As a
+ * stop classifier (kind 0) the query stops expanding when sigmoid(output) > threshold; as a hop
+ * budget (kind 1, after Li et al., "Improving Approximate Nearest Neighbor Search through Learned
+ * Adaptive Early Termination", SIGMOD 2020) the output predicts log(hops the query needs) and the
+ * query stops once its hops reach budget_scale * exp(output). Either way it then reranks its
+ * current pool. Weight layout
  * (matrices input-major, W[in][out]): W1[8][64] b1[64] W2[64][64] b2[64] w3[64] b3
  * (QG_MLP_PARAMS values); d_norm = mean[8], inv_std[8] of the features. */
 #define QG_MLP_PARAMS 4801
 typedef struct qg_stop_model {
     const uint16_t *d_weights;
     const float *d_norm;
-    float threshold;
+    float threshold;     /* kind 0: stop when sigmoid(output) > threshold */
     int every;
     int min_hops;
+    int kind;            /* 0: stop classifier; 1: hop budget (output = log of the hops needed) */
+    float budget_scale;  /* kind 1: stop once hops >= budget_scale * exp(output) */
+    int predict_once;    /* kind 1: predict at the first checkpoint only (else at every one) */
 } qg_stop_model;
 
-/* Training traces: at every `every`-th hop, the 8 features and the label 1 when the first
- * max(rerank, k) pool entries already contain all `truth_k` ids of d_truth (the final result of
- * the full fixed-L search), else 0; at most `cap` rows per query, d_counts[q] rows written. */
+/* Training traces: at every `every`-th hop, the 8 features and, as the label, how many of the
+ * `truth_k` ids of d_truth (for example the final result of the full fixed-L search) the first
+ * max(rerank, k) pool entries already contain; at most `cap` rows per query, d_counts[q] rows
+ * written. */
 typedef struct qg_trace_request {
     const uint32_t *d_truth;
     int truth_k;
@@ -348,13 +356,17 @@ int qg_search_batch_learned(qg_index *index, const float *d_queries, size_t nq,
                             size_t k_stride, uint32_t *d_ids, float *d_dists,
                             qg_search_stats *d_stats, const qg_stop_model *model,
                             const qg_trace_request *trace, void *stream);
-/* Network training kernels: logits of n feature rows; BCE loss and its gradient w.r.t. the
- * BF16 weights (FP32 accumulation; d_grad and d_loss are overwritten); one Adam step on the FP32
+/* Network training kernels: outputs of n feature rows; the loss and its gradient w.r.t. the
+ * BF16 weights (FP32 accumulation; d_grad and d_loss are overwritten) -- binary cross-entropy
+ * with logits for the stop classifier (qg_mlp_backward), half the squared error of the output
+ * for the hop budget (qg_mlp_backward_mse), both means over the rows; one Adam step on the FP32
  * master weights that also refreshes the BF16 copy (step counts from 1). */
 int qg_mlp_forward(const float *d_x, size_t n, const float *d_norm, const uint16_t *d_weights,
                    float *d_logits, void *stream);
 int qg_mlp_backward(const float *d_x, const float *d_y, size_t n, const float *d_norm,
                     const uint16_t *d_weights, float *d_grad, float *d_loss, void *stream);
+int qg_mlp_backward_mse(const float *d_x, const float *d_y, size_t n, const float *d_norm,
+                        const uint16_t *d_weights, float *d_grad, float *d_loss, void *stream);
 int qg_mlp_adam(float *d_master, uint16_t *d_weights, const float *d_grad, float *d_m, float *d_v,
                 float lr, float beta1, float beta2, float eps, int step, void *stream);
 /* Launch shape of the persistent search kernel: warps per block (2, 4 or 8) and an upper bound

@@ -3,7 +3,8 @@ for the GPU forward / backward / Adam kernels (quantization_graph_gb300/csrc/mlp
 
 Packed layout (weight matrices input-major): W1[8][64] b1[64] W2[64][64] b2[64] w3[64] b3,
 W[in][out]. Inputs are standardised with
-norm = (mean[8], inv_std[8]). Loss: mean binary cross-entropy with logits.
+norm = (mean[8], inv_std[8]). Loss: mean binary cross-entropy with logits (the stop classifier)
+or mean half squared error of the output (the hop budget).
 """
 from __future__ import annotations
 
@@ -39,13 +40,17 @@ def forward(w, norm, x):
     return h2 @ d + b3, (f, h1, h2)
 
 
-def loss_and_grad(w, norm, x, y):
+def loss_and_grad(w, norm, x, y, mse=False):
     a, b1, c, b2, d, b3 = unpack(w)
     z, (f, h1, h2) = forward(w, norm, x)
     y = np.asarray(y, np.float64)
     n = len(y)
-    loss = np.mean(np.maximum(z, 0) - z * y + np.log1p(np.exp(-np.abs(z))))
-    dz = (1.0 / (1.0 + np.exp(-z)) - y) / n
+    if mse:
+        loss = np.mean(0.5 * (z - y) ** 2)
+        dz = (z - y) / n
+    else:
+        loss = np.mean(np.maximum(z, 0) - z * y + np.log1p(np.exp(-np.abs(z))))
+        dz = (1.0 / (1.0 + np.exp(-z)) - y) / n
     g = np.zeros(PARAMS)
     g[B3] = dz.sum()
     g[W3:B3] = h2.T @ dz

@@ -43,7 +43,7 @@ class DistanceInterval(C.Structure):
 class StopModel(C.Structure):
     """qg_stop_model"""
     _fields_ = [("d_weights", C.c_void_p), ("d_norm", C.c_void_p), ("threshold", C.c_float), ("every", C.c_int),
-                ("min_hops", C.c_int)]
+                ("min_hops", C.c_int), ("kind", C.c_int), ("budget_scale", C.c_float), ("predict_once", C.c_int)]
 
 
 class TraceRequest(C.Structure):
@@ -111,6 +111,7 @@ _SIGS = {
     "qg_search_batch_learned": (C.c_int, [P, P, SZ, P, P, P, SZ, P, P, P, P, P, P]),
     "qg_mlp_forward": (C.c_int, [P, SZ, P, P, P, P]),
     "qg_mlp_backward": (C.c_int, [P, P, SZ, P, P, P, P, P]),
+    "qg_mlp_backward_mse": (C.c_int, [P, P, SZ, P, P, P, P, P]),
     "qg_mlp_adam": (C.c_int, [P, P, P, P, P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, P]),
     "qg_index_set_launch": (C.c_int, [P, C.c_int, C.c_int]),
     "qg_index_reserve": (C.c_int, [P, SZ, C.c_int, C.c_int]),

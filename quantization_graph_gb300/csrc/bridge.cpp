@@ -1510,14 +1510,25 @@ int qg_index_reserve(qg_index *index, size_t max_nq, int max_l, int max_k) {
     return QG_OK;
 }
 
+// A stop model needs weights, the normalisation block and every >= 1; a classifier (kind 0) a
+// threshold in (0, 1), a hop budget (kind 1) a positive finite scale.
+static bool stop_model_ok(const qg_stop_model *m) {
+    if (!m->d_weights || !m->d_norm || m->every < 1 || m->min_hops < 0) {
+        set_error("stop model needs weights, normalisation, every >= 1 and min_hops >= 0");
+        return false;
+    }
+    if (m->kind == 0 && (m->threshold > 0.0f && m->threshold < 1.0f)) return true;
+    if (m->kind == 1 && m->budget_scale > 0.0f && std::isfinite(m->budget_scale)) return true;
+    set_error("stop model: kind 0 needs 0 < threshold < 1, kind 1 a positive finite budget scale");
+    return false;
+}
+
 int qg_search_batch_graph(qg_index *index, const float *d_queries, size_t max_nq, const int *d_nq,
                           const qg_search_params *params, const int *d_k, const int *d_l, size_t k_stride,
                           uint32_t *d_ids, float *d_dists, qg_search_stats *d_stats,
                           const qg_stop_model *model, void *stream) {
     if (!d_nq) return QG_ERR_INVALID;
-    if (model && (!model->d_weights || !model->d_norm || model->every < 1 || !(model->threshold > 0.0f) ||
-                  !(model->threshold < 1.0f)))
-        return QG_ERR_INVALID;
+    if (model && !stop_model_ok(model)) return QG_ERR_INVALID;
     return search_impl(index, d_queries, max_nq, params, d_k, d_l, k_stride, d_ids, d_dists, d_stats, nullptr, 0,
                        model, nullptr, stream, d_nq, false);
 }
@@ -1534,11 +1545,7 @@ int qg_search_batch_learned(qg_index *index, const float *d_queries, size_t nq,
                             const qg_search_params *params, const int *d_k, const int *d_l,
                             size_t k_stride, uint32_t *d_ids, float *d_dists, qg_search_stats *d_stats,
                             const qg_stop_model *model, const qg_trace_request *trace, void *stream) {
-    if (model && (!model->d_weights || !model->d_norm || model->every < 1 || !(model->threshold > 0.0f) ||
-                  !(model->threshold < 1.0f))) {
-        set_error("stop model needs weights, normalisation, every >= 1 and 0 < threshold < 1");
-        return QG_ERR_INVALID;
-    }
+    if (model && !stop_model_ok(model)) return QG_ERR_INVALID;
     if (trace && (!trace->d_truth || trace->truth_k < 1 || trace->every < 1 || trace->cap < 1 ||
                   !trace->d_features || !trace->d_labels || !trace->d_counts)) {
         set_error("trace request needs truth ids, every >= 1, cap >= 1 and output buffers");
@@ -1567,6 +1574,16 @@ int qg_mlp_backward(const float *d_x, const float *d_y, size_t n, const float *d
     if (!cuda_ok(launch_mlp_backward(d_x, d_y, n, d_norm, d_weights, d_grad, d_loss,
                                      static_cast<cudaStream_t>(stream)),
                  "mlp backward"))
+        return QG_ERR_CUDA;
+    return QG_OK;
+}
+
+int qg_mlp_backward_mse(const float *d_x, const float *d_y, size_t n, const float *d_norm, const uint16_t *d_weights,
+                        float *d_grad, float *d_loss, void *stream) {
+    if (!d_grad || !d_loss || (n && (!d_x || !d_y || !d_norm || !d_weights))) return QG_ERR_INVALID;
+    if (!cuda_ok(launch_mlp_backward(d_x, d_y, n, d_norm, d_weights, d_grad, d_loss,
+                                     static_cast<cudaStream_t>(stream), true),
+                 "mlp backward (squared error)"))
         return QG_ERR_CUDA;
     return QG_OK;
 }
@@ -1668,7 +1685,10 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
     if (model) {
         a.stop_w = model->d_weights;
         a.stop_norm = model->d_norm;
-        a.stop_logit = std::log(model->threshold / (1.0f - model->threshold));
+        a.stop_kind = model->kind;
+        if (model->kind == 0) a.stop_logit = std::log(model->threshold / (1.0f - model->threshold));
+        a.stop_scale = model->budget_scale;
+        a.stop_once = model->predict_once;
         a.stop_every = model->every;
         a.stop_min_hops = model->min_hops;
     }

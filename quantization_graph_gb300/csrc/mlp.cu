@@ -4,7 +4,8 @@
 //
 // Training keeps FP32 master weights; forward and backward use their BF16 rounding (the
 // gradient is taken with respect to the rounded weights and applied to the masters), with FP32
-// accumulation. Loss: binary cross-entropy with logits, mean over the batch.
+// accumulation. Loss: binary cross-entropy with logits (the stop classifier) or half the
+// squared error of the output (the hop budget), mean over the batch.
 //
 // forward:  one warp per sample (the same warp-cooperative pass the search kernel runs).
 // backward: one warp per strided set of samples; each lane owns hidden units l and l+32, so its
@@ -42,6 +43,7 @@ __global__ void __launch_bounds__(128) mlp_forward_kernel(const float *X, size_t
 
 // per-warp gradients in shared memory, in the parameter layout itself: the weight matrices are
 // input-major, so lane j (output unit j) writes consecutive words
+template <bool kMse>
 __global__ void __launch_bounds__(kWarps * 32) mlp_backward_kernel(const float *X, const float *y, size_t n,
                                                                    const float *norm, const uint16_t *w,
                                                                    float *grad, float *loss) {
@@ -61,8 +63,14 @@ __global__ void __launch_bounds__(kWarps * 32) mlp_backward_kernel(const float *
         float h1a, h1b, h2a, h2b;
         const float z = mlp_forward_warp(f, w, lane, &h1a, &h1b, &h2a, &h2b);
         const float t = y[s];
-        wloss += fmaxf(z, 0.0f) - z * t + log1pf(expf(-fabsf(z)));
-        const float dz = (1.0f / (1.0f + expf(-z)) - t) * inv_n;
+        float dz;
+        if constexpr (kMse) {
+            wloss += 0.5f * (z - t) * (z - t);
+            dz = (z - t) * inv_n;
+        } else {
+            wloss += fmaxf(z, 0.0f) - z * t + log1pf(expf(-fabsf(z)));
+            dz = (1.0f / (1.0f + expf(-z)) - t) * inv_n;
+        }
         h1s[warp][lane] = h1a;
         h1s[warp][lane + 32] = h1b;
         // layer 3
@@ -134,14 +142,19 @@ cudaError_t launch_mlp_forward(const float *X, size_t n, const float *norm, cons
 }
 
 cudaError_t launch_mlp_backward(const float *X, const float *y, size_t n, const float *norm, const uint16_t *w,
-                                float *grad, float *loss, cudaStream_t stream) {
+                                float *grad, float *loss, cudaStream_t stream, bool mse) {
     cudaError_t e = cudaMemsetAsync(grad, 0, kMlpParams * sizeof(float), stream);
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(loss, 0, sizeof(float), stream);
     if (e != cudaSuccess || n == 0) return e;
     size_t blocks = (n + kWarps * 16 - 1) / (kWarps * 16);  // ~16 samples per warp
     if (blocks > 4096) blocks = 4096;
-    mlp_backward_kernel<<<static_cast<unsigned>(blocks), kWarps * 32, 0, stream>>>(X, y, n, norm, w, grad, loss);
+    if (mse)
+        mlp_backward_kernel<true><<<static_cast<unsigned>(blocks), kWarps * 32, 0, stream>>>(X, y, n, norm, w, grad,
+                                                                                            loss);
+    else
+        mlp_backward_kernel<false><<<static_cast<unsigned>(blocks), kWarps * 32, 0, stream>>>(X, y, n, norm, w, grad,
+                                                                                             loss);
     return cudaGetLastError();
 }
 

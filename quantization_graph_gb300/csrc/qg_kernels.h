@@ -64,15 +64,21 @@ struct SearchArgs {
     int hop_cap;
     uint32_t *expanded_out;  // optional [nq x expanded_cap]: expanded nodes in hop order
     int expanded_cap;
-    // learned early termination (optional): every stop_every hops the warp forms the 8 search-
-    // state features and evaluates the network; it stops when the logit exceeds stop_logit
+    // learned early termination (optional): every stop_every hops (from stop_min_hops on) the
+    // warp forms the 8 search-state features and evaluates the network. stop_kind 0: it stops
+    // when the logit exceeds stop_logit. stop_kind 1: the output is log(hops the query needs);
+    // the query stops once its hops reach stop_scale * exp(output) (re-predicted at every
+    // checkpoint, or only at the first one when stop_once)
     const uint16_t *stop_w;
     const float *stop_norm;
     float stop_logit;
     int stop_every;
     int stop_min_hops;
-    // trace collection (optional): features at every stop_every-th hop with the label "the
-    // first max(rerank, k) pool entries already hold every id of trace_truth"
+    int stop_kind;
+    float stop_scale;
+    int stop_once;
+    // trace collection (optional): features at every stop_every-th hop with the label "how many
+    // ids of trace_truth the first max(rerank, k) pool entries already hold"
     const uint32_t *trace_truth;  // [nq x trace_truth_k]
     int trace_truth_k;
     int trace_cap;
@@ -131,7 +137,7 @@ cudaError_t launch_encode(const EncodeArgs &a, cudaStream_t stream);
 cudaError_t launch_mlp_forward(const float *X, size_t n, const float *norm, const uint16_t *w, float *logits,
                                cudaStream_t stream);
 cudaError_t launch_mlp_backward(const float *X, const float *y, size_t n, const float *norm, const uint16_t *w,
-                                float *grad, float *loss, cudaStream_t stream);
+                                float *grad, float *loss, cudaStream_t stream, bool mse = false);
 cudaError_t launch_mlp_adam(float *master, uint16_t *w, const float *grad, float *m, float *v, float lr,
                             float beta1, float beta2, float eps, int step, cudaStream_t stream);
 cudaError_t launch_prune(int code_dim, const uint8_t *compact, size_t stride, int n, const uint32_t *cand,

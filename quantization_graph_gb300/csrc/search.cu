@@ -327,6 +327,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
     int n_expanded = 0;
     int last_topk = 0, last_topr = 0;  // last hop that inserted into the top k / top max(rerank, k)
     int fu = 0;                        // every pool entry before fu is expanded
+    float budget = 0.0f;               // learned hop budget (stop_kind 1; 0 = none yet)
     const int want_r_all = a.rerank > k ? a.rerank : k;
     bool failed = false;
     for (;;) {
@@ -373,18 +374,6 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                 row[h] = j < ix.edge_stride ? __ldg(adj + j) : 0xFFFFFFFFu;
             }
             const uint32_t deg = min(__ldg(ix.degrees + node), ix.edge_stride);
-            // speculative: the MSB and factor rows of every neighbour go to L2 while the
-            // visited tags are being read (about half of them turn out fresh)
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const uint32_t nb = row[h];
-                if (lane + 32 * h < static_cast<int>(deg) && nb < ix.n_total) {
-                    const uint8_t *m = ix.msb + static_cast<size_t>(nb) * (D / 8);
-#pragma unroll
-                    for (int l = 0; l < (D / 8 + 127) / 128; ++l) prefetch_l2(m + 128 * l);
-                    prefetch_l2(ix.pf + nb);
-                }
-            }
             // ---- fresh neighbours in adjacency order (VisitedScratch::try_mark) ----
             int F = 0;
             bool oob = false;
@@ -538,9 +527,6 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             // ---- traversal distances of the survivors ----
             prefetch_rows_l1(ix.codes, s.sid, S, D / 2, D / 2, lane);
             prefetch_rows_l1(reinterpret_cast<const uint8_t *>(ix.hdr), s.sid, S, 16, 16, lane);
-            // survivors are the likeliest next expansions: warm L2 with their adjacency rows
-            prefetch_rows_l2(reinterpret_cast<const uint8_t *>(ix.edges), s.sid, S, ix.edge_stride * 4,
-                             static_cast<int>(ix.edge_stride * 4), lane);
             for (int i = lane; i < S; i += 32) {
                 const float4 h = ix.hdr[s.sid[i]];
                 s.shdr[i] = make_float2(h.x, h.y);
@@ -749,7 +735,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                 if (a.trace_feat != nullptr) {
                     int row = a.trace_count[q];
                     if (row < a.trace_cap) {
-                        // label: every truth id already sits in the first max(rerank, k) entries
+                        // label: how many truth ids already sit in the first max(rerank, k) entries
                         const int want_r = a.rerank > k ? a.rerank : k;
                         const int lim = want_r < pn ? want_r : pn;
                         int found = 0;
@@ -768,21 +754,26 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                         if (lane < kMlpIn)
                             a.trace_feat[(static_cast<size_t>(q) * a.trace_cap + row) * kMlpIn + lane] = mine;
                         if (lane == 0) {
-                            a.trace_label[static_cast<size_t>(q) * a.trace_cap + row] =
-                                found == a.trace_truth_k ? 1.0f : 0.0f;
+                            a.trace_label[static_cast<size_t>(q) * a.trace_cap + row] = static_cast<float>(found);
                             a.trace_count[q] = row + 1;
                         }
                         __syncwarp();
                     }
                 }
-                if (a.stop_w != nullptr && hops_done >= a.stop_min_hops) {
+                if (a.stop_w != nullptr && hops_done >= a.stop_min_hops && !(a.stop_once && budget > 0.0f)) {
                     float f[kMlpIn];
 #pragma unroll
                     for (int i = 0; i < kMlpIn; ++i) f[i] = (feat[i] - a.stop_norm[i]) * a.stop_norm[kMlpIn + i];
                     const float z = mlp_forward_warp_smem(f, stop_smem, lane);
-                    if (z > a.stop_logit) break;
+                    if (a.stop_kind == 0) {
+                        if (z > a.stop_logit) break;
+                    } else {
+                        // the network's output is log(hops this query needs): the budget
+                        budget = expf(fminf(z, 30.0f)) * a.stop_scale;
+                    }
                 }
             }
+            if (budget > 0.0f && static_cast<float>(hops_done) >= budget) break;
         }
     }
 

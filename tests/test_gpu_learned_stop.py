@@ -18,6 +18,7 @@ def test_mlp_forward_backward_adam_match_fp64(cuda):
     rng = np.random.default_rng(0)
     x = rng.standard_normal((257, 8)).astype(np.float32) * 3 + 1
     y = (rng.random(257) < 0.4).astype(np.float32)
+    y_budget = (np.log(rng.integers(8, 900, 257)) + 0.0).astype(np.float32)
     norm = np.concatenate([x.mean(0), 1 / x.std(0)]).astype(np.float32)
     master = ls.init_weights(3)
     w = ls.to_bf16_bits(master)
@@ -34,6 +35,11 @@ def test_mlp_forward_backward_adam_match_fp64(cuda):
     g = grad.cpu().numpy()
     scale = np.abs(g_ref).max()
     np.testing.assert_allclose(g, g_ref, rtol=1e-3, atol=1e-5 * scale)
+    # the hop budget's squared-error loss and gradient
+    lm, gm = ls.loss_and_grad(w, tn, torch.from_numpy(x), torch.from_numpy(y_budget), kind=ls.KIND_BUDGET)
+    lm_ref, gm_ref = mlp_ref.loss_and_grad(wb, norm.astype(np.float64), x, y_budget, mse=True)
+    assert abs(float(lm) - lm_ref) < 1e-4 * max(1.0, abs(lm_ref))
+    np.testing.assert_allclose(gm.cpu().numpy(), gm_ref, rtol=1e-3, atol=1e-5 * np.abs(gm_ref).max())
     # one Adam step
     from quantization_graph_gb300 import _native as N
     import ctypes as C
@@ -72,10 +78,11 @@ def test_learned_stop_saves_hops_at_equal_recall(cuda, oracle):
     L = 80
     tq = torch.from_numpy(train_q).cuda()
     truth = ix.search(tq, k=10, l_value=L, with_stats=False).ids.to(torch.int32)
-    feats, labels = ls.collect_traces(ix, tq, truth, k=10, l_value=L, every=2)
-    assert feats.shape[0] == labels.shape[0] > 10_000
+    tr = ls.collect_traces(ix, tq, truth, k=10, l_value=L, every=2)
+    labels = tr.classifier_labels()
+    assert tr.features.shape[0] == labels.shape[0] > 10_000
     assert 0.05 < float(labels.mean()) < 0.95
-    model = ls.train(feats, labels, epochs=6, batch=4096, every=2, min_hops=4)
+    model = ls.train(tr.features, labels, epochs=6, batch=4096, every=2, min_hops=4)
     o = oracle.Oracle(128, g["center"])
     gt, _ = o.exact_knn(X, test_q, 10)
     qq = torch.from_numpy(test_q).cuda()
@@ -109,8 +116,8 @@ def test_in_kernel_stop_matches_standalone_forward(cuda):
     L, every, min_hops, thr = 80, 2, 4, 0.8
     tq = torch.from_numpy(train_q).cuda()
     truth = ix.search(tq, k=10, l_value=L, with_stats=False).ids.to(torch.int32)
-    feats, labels = ls.collect_traces(ix, tq, truth, k=10, l_value=L, every=every)
-    model = ls.train(feats, labels, epochs=2, batch=4096, every=every, min_hops=min_hops)
+    tr = ls.collect_traces(ix, tq, truth, k=10, l_value=L, every=every)
+    model = ls.train(tr.features, tr.classifier_labels(), epochs=2, batch=4096, every=every, min_hops=min_hops)
     qq = torch.from_numpy(test_q).cuda()
     truth_te = ix.search(qq, k=10, l_value=L, with_stats=False).ids.to(torch.int32)
     # per-checkpoint rows of the plain search, query by query
@@ -147,3 +154,65 @@ def test_in_kernel_stop_matches_standalone_forward(cuda):
     got = stats2[:, 2].cpu().numpy()
     assert (want < full_hops).sum() > 20, "the threshold should stop some queries early"
     np.testing.assert_array_equal(got, want)
+
+
+def test_in_kernel_budget_matches_standalone_forward(cuda):
+    """The hop budget in the search kernel: each query stops at the first hop h >= scale *
+    exp(output), the output re-predicted at every checkpoint (or taken at the first one only),
+    exactly as the standalone forward kernel over the plain search's trace says; the trace's
+    targets (log of the first hop whose rerank window holds the whole result) are consistent."""
+    torch = cuda
+    import ctypes as C
+
+    from quantization_graph_gb300 import _native as N
+    from quantization_graph_gb300 import learned_stop as ls
+    from quantization_graph_gb300 import synthetic
+    from quantization_graph_gb300.space import _ptr, _stream
+
+    g, ix = _index(torch)
+    _, cent = synthetic.gmm(1, 128, components=64, sigma=0.3, seed=11)
+    train_q, _ = synthetic.gmm(1500, 128, sigma=0.3, seed=301, centres=cent)
+    test_q, _ = synthetic.gmm(400, 128, sigma=0.3, seed=302, centres=cent)
+    L, every, min_hops, scale = 80, 2, 4, 0.9
+    tq = torch.from_numpy(train_q).cuda()
+    truth = ix.search(tq, k=10, l_value=L, with_stats=False).ids.to(torch.int32)
+    tr = ls.collect_traces(ix, tq, truth, k=10, l_value=L, every=every)
+    y = tr.budget_targets()
+    h = tr.hops_needed()
+    assert bool((h <= tr.final_hops).all()) and bool((h >= 1).all())
+    assert float((h < tr.final_hops).float().mean()) > 0.5  # most queries hold their result before the end
+    qq = torch.from_numpy(test_q).cuda()
+    truth_te = ix.search(qq, k=10, l_value=L, with_stats=False).ids.to(torch.int32)
+    te = ls.collect_traces(ix, qq, truth_te, k=10, l_value=L, every=every, cap=(4 * L) // every + 8)
+    nq = len(test_q)
+    for once in (False, True):
+        model = ls.train(tr.features, y, epochs=2, batch=4096, every=every, min_hops=min_hops,
+                         kind=ls.KIND_BUDGET, predict_once=once)
+        z = ls.forward(model.weights, model.norm, te.features).cpu().numpy()
+        full = te.final_hops.cpu().numpy()
+        rows_q = te.query.cpu().numpy()
+        rows_h = te.hop.cpu().numpy()
+        zq = {}
+        for r in range(len(z)):
+            zq[(rows_q[r], rows_h[r])] = z[r]
+        # replay the kernel's rule hop by hop: at a checkpoint (hop % every == 0, hop >= min_hops)
+        # the budget is (re)predicted, then the query stops at the first hop >= the budget
+        want = full.copy()
+        clear = np.ones(nq, bool)  # budgets within float rounding of the deciding hop are skipped
+        for q in range(nq):
+            budget = 0.0
+            for hop in range(1, int(full[q]) + 1):
+                if hop % every == 0 and hop >= min_hops and (q, hop) in zq and not (once and budget > 0):
+                    budget = float(np.float32(np.exp(np.float32(min(zq[(q, hop)], 30.0)))) * np.float32(scale))
+                if budget > 0 and abs(hop - budget) < 1e-3 * budget:
+                    clear[q] = False
+                if budget > 0 and hop >= budget:
+                    want[q] = hop
+                    break
+        stats = torch.empty((nq, 9), dtype=torch.int64, device="cuda")
+        ls.search(ix, qq, model, scale, k=10, l_value=L, stats_out=stats)
+        got = stats[:, 2].cpu().numpy()
+        assert clear.sum() > 0.9 * nq
+        want, got, full = want[clear], got[clear], full[clear]
+        assert (want < full).sum() > 20, "the budget should stop some queries early"
+        np.testing.assert_array_equal(got, want)

@@ -66,8 +66,8 @@ def test_graph_replay_with_learned_stop_matches_direct_call(cuda):
     tq, _ = synthetic.gmm(800, 128, sigma=0.3, seed=301, centres=cent)
     tq = torch.from_numpy(tq).cuda()
     truth = ix.search(tq, k=10, l_value=80, with_stats=False).ids.to(torch.int32)
-    feats, labels = ls.collect_traces(ix, tq, truth, k=10, l_value=80, every=4)
-    model = ls.train(feats, labels, epochs=2, batch=4096, every=4, min_hops=8)
+    tr = ls.collect_traces(ix, tq, truth, k=10, l_value=80, every=4)
+    model = ls.train(tr.features, tr.classifier_labels(), epochs=2, batch=4096, every=4, min_hops=8)
     _, Q = SEARCH_CASES["search_c1"]()
     q = torch.from_numpy(Q).cuda()
     gs = GraphSearcher(ix, 128, max_batch=64, max_k=10, max_l=80, model=model, threshold=0.8)
