@@ -81,9 +81,10 @@ def parse(argv=None):
     ap.add_argument("--stop-epochs", type=int, default=4)
     ap.add_argument("--stop-kind", default="both", choices=["classifier", "budget", "both"],
                     help="learned stop: a stop classifier, a hop budget (LAET-style), or both (the faster wins)")
-    ap.add_argument("--workload", default="dbpedia1536", choices=["dbpedia1536", "gist960", "stream"],
+    ap.add_argument("--workload", default="dbpedia1536", choices=["dbpedia1536", "gist960", "stream", "encode"],
                     help="gist960: 1M x 960 |x| with lambda_i ~ i^-1.2; stream: uneven batched stream over "
-                         "a 120k x 1024 clustered index")
+                         "a 120k x 1024 clustered index; encode: the GPU encode with the rotation on the tensor "
+                         "cores against the reference encoder")
     ap.add_argument("--stream-n", type=int, default=120_000)
     ap.add_argument("--stream-queries", type=int, default=200_000)
     ap.add_argument("--stream-thresholds", default="0.9,0.95,0.98",
@@ -481,6 +482,15 @@ def learned_stop_select(torch, w, args, L_fixed, rec_fixed, log):
                           every=args.stop_every, min_hops=min_hops, log=log, kind=ls.KIND_BUDGET)
         models["budget"] = budget
         models["budget-once"] = dataclasses.replace(budget, predict_once=True)
+        # how much of log(h*) the network explains: over all rows, and at the first prediction
+        y = tr.budget_targets()[keep]
+        z = ls.forward(budget.weights, budget.norm, tr.features[keep])
+        r2_rows = float(1.0 - ((z - y) ** 2).mean() / y.var())
+        first = keep & (tr.hop == min_hops)
+        y1 = tr.budget_targets()[first]
+        z1 = ls.forward(budget.weights, budget.norm, tr.features[first])
+        r2_first = float(1.0 - ((z1 - y1) ** 2).mean() / y1.var())
+        log(f"  hop budget: R^2 of log(h*) {r2_rows:.3f} over the checkpoints, {r2_first:.3f} at hop {min_hops}")
     t_train = time.time() - t0
     del tq, tr, truth
     knobs = {"classifier": (0.5, 0.7, 0.8, 0.9, 0.95, 0.98, 0.99),
@@ -516,6 +526,8 @@ def learned_stop_select(torch, w, args, L_fixed, rec_fixed, log):
                   dists_out=dists_out, stats_out=stats_out)
 
     info = {"oracle_stop_hop_fraction": round(oracle_frac, 4), "train_L": L_train}
+    if "budget" in models:
+        info.update(budget_r2_checkpoints=round(r2_rows, 4), budget_r2_first_prediction=round(r2_first, 4))
     return best, table, t_train, run, info
 
 
@@ -822,6 +834,100 @@ def main():
         sys.exit(3)
 
 
+def run_encode(args, log):
+    """GPU encode of the 1M x 1536 unit-norm base two ways: the reference's rotation (random
+    signs + fast Hadamard transform, bit-exact to the reference encoder) and the rotation as a
+    BF16x3 GEMM on the tcgen05 tensor cores (qg_encode_batch_gemm). Reports the GEMM's time and
+    throughput (useful FLOPs 2 N dim D, the three BF16 passes counted as overhead), the
+    code-mismatch rate and factor error of the GEMM path against the reference encoder over all
+    rows, and both rotations' error against an FP64 rotation on a row sample."""
+    import torch
+
+    from quantization_graph_gb300 import synthetic
+    from quantization_graph_gb300.space import RabitqSpace, train_global_center
+
+    base = synthetic.anisotropic_torch(args.n, args.dim, 0.8, seed=1, normalize=True)
+    space = RabitqSpace(args.dim, train_global_center(base))
+    D = space.code_dim
+    torch.cuda.synchronize()
+    t = time.time()
+    c_ref, r_ref = space.encode(base)
+    torch.cuda.synchronize()
+    t_fht = time.time() - t
+    t = time.time()
+    c_gem, r_gem = space.encode_gemm(base)
+    torch.cuda.synchronize()
+    t_gem = time.time() - t
+    # the rotation alone, device-timed over chunks of 131072 rows (the GEMM entry point's chunk)
+    chunk = min(args.n, 131072)
+    rows = base[:chunk]
+    for _ in range(max(1, args.warmup)):
+        space.rotate_gemm(rows)
+    ms = device_ms(torch, lambda: space.rotate_gemm(rows), max(1, args.steps))
+    kp = (args.dim + 63) // 64 * 64
+    useful = 2.0 * chunk * args.dim * D
+    issued = 2.0 * chunk * 3 * kp * D
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    codes_r = c_ref[:, 16:16 + D // 2]
+    codes_g = c_gem[:, 16:16 + D // 2]
+    nib_bad = int(((codes_r & 15) != (codes_g & 15)).sum() + ((codes_r >> 4) != (codes_g >> 4)).sum())
+    fr = c_ref[:, :16].contiguous().view(torch.float32).double()
+    fg = c_gem[:, :16].contiguous().view(torch.float32).double()
+    rel = (fr - fg).abs() / fr.abs().clamp_min(1e-30)
+    res_bad = int((r_ref != r_gem).any(1).sum())
+    # both rotations against FP64 on a sample of rows: exact u = r / |r|, exact +-1/sqrt(D) signs
+    sample = torch.arange(0, args.n, max(1, args.n // 256), device="cuda")[:256]
+    rot_g, norms = space.rotate_gemm(base[sample])
+    sgn = torch.from_numpy(space.signs()).cuda()
+    r32 = base[sample] - torch.from_numpy(space.center).cuda()[None, :]
+    u32 = r32 * (1.0 / norms)[:, None]  # the encoder's fl(r * fl(1 / |r|))
+    fht = torch.nn.functional.pad(u32 * sgn[None, :args.dim], (0, D - args.dim))
+    step = 1
+    while step < D:  # the reference's butterflies in FP32 (space_rabitq.h:944-988)
+        v = fht.view(-1, D // (2 * step), 2, step)
+        fht = torch.stack((v[:, :, 0] + v[:, :, 1], v[:, :, 0] - v[:, :, 1]), 2).reshape(-1, D)
+        step *= 2
+    j_ = torch.arange(D, device="cuda")
+    x = j_[:, None] & j_[None, :]
+    for sh in (16, 8, 4, 2, 1):
+        x = x ^ (x >> sh)
+    H = 1.0 - 2.0 * (x & 1).double()
+    r64 = r32.double() / r32.double().norm(dim=1, keepdim=True)
+    s64 = torch.where(sgn > 0, 1.0, -1.0).double() / float(np.sqrt(D))
+    exact = torch.nn.functional.pad(r64 * s64[None, :args.dim], (0, D - args.dim)) @ H.T
+    scale = exact.abs().max()
+    line = {"metric": "encode: rotation as a BF16x3 tcgen05 GEMM, 1M×1536 unit-norm (ExRaBitQ4 block16)",
+            "value": useful / (ms / 1000.0) / 1e12, "unit": "TFLOP/s (useful, 2*N*dim*D)", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16x3/f32", "data": "synthetic",
+            "config": {"workload": f"{args.n} x {args.dim} unit-norm anisotropic (lambda_i ~ i^-0.8), D={D}",
+                       "gemm_rows_per_step": chunk, "k": 3 * kp},
+            "roofline": {"bound": "tensor", "achieved": issued / (ms / 1000.0) / 1e12, "peak": peak,
+                         "unit": "TFLOP/s", "frac": issued / (ms / 1000.0) / 1e12 / peak, "traffic": None,
+                         "kernel": "rotate_gemm_kernel (+ rotate_split_kernel in the timed call)",
+                         "note": "achieved counts the three BF16 passes (issued FLOPs); value counts useful FLOPs",
+                         "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)" if peaks else "fallback"},
+            "encode": {"rows": args.n, "fht_encode_s": round(t_fht, 3), "gemm_encode_s": round(t_gem, 3),
+                       "code_mismatch_rate": nib_bad / (args.n * D),
+                       "compact_records_equal": int((c_ref == c_gem).all(1).sum()),
+                       "residual_records_differing": res_bad,
+                       "factor_rel_err": {"median": float(rel[:, 1:].median()), "max": float(rel[:, 1:].max()),
+                                          "norm_sqr_max": float(rel[:, 0].max())},
+                       "against": "the reference encoder (the FHT path, bit-exact to the reference)"},
+            "rotation_error_vs_fp64": {"rows": int(sample.numel()), "max_abs_value": float(scale),
+                                       "gemm_max_abs": float((rot_g.double() - exact).abs().max()),
+                                       "fht_max_abs": float((fht.double() - exact).abs().max()),
+                                       "gemm_vs_fht_max_abs": float((rot_g - fht).abs().max())}}
+    log(f"encode: FHT {t_fht:.2f}s, GEMM path {t_gem:.2f}s; rotation GEMM {ms:.2f} ms per {chunk} rows "
+        f"({line['value']:.0f} useful TFLOP/s); code mismatch {line['encode']['code_mismatch_rate']:.2e}")
+    print(json.dumps(line), flush=True)
+
+
 def run_stream(args, log):
     """Uneven batched stream: 200k queries over a 120k x 1024 clustered unit-norm index (16
     clusters, lambda_i ~ i^-1.0 within each), batch sizes log-uniform in [1, 4096], per-query
@@ -970,10 +1076,11 @@ def run_stream(args, log):
 
 if __name__ == "__main__":
     _args = parse()
-    if _args.workload == "stream":
+    if _args.workload in ("stream", "encode"):
         from quantization_graph_gb300 import build as _qb
 
         _qb.build()
-        run_stream(_args, lambda m: print(m, file=sys.stderr, flush=True))
+        (run_stream if _args.workload == "stream" else run_encode)(_args, lambda m: print(m, file=sys.stderr,
+                                                                                           flush=True))
     else:
         main()

@@ -291,17 +291,17 @@ int qg_search_batch_ex(qg_index *index, const float *d_queries, size_t nq,
 /* No counterpart in the reference. qg_search_batch for callers that cannot allocate device
  * memory -- code running while a CUDA graph is captured, or a serving process whose device
  * memory is fixed at start-up and may not call cudaMalloc on the request path. It allocates
- * nothing: its scratch (prepared queries, visited tags, epochs, counter, status) is one
- * file-scope device array of QG_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds
- * until exit. The index must already exist; queries and outputs are the caller's. Limits: the
- * prepared queries (nq x (5*D + 24) bytes) and at least one block of visited-tag rows
- * (warps x n_total x 2 bytes) must fit the array, else QG_ERR_INVALID with the reason in
- * qg_last_error(). All calls share the array: calls whose GPU work overlaps race, so serialise
- * them. The first call on a device looks up the array's address (make it before any stream
- * capture). The call itself does not synchronise: failed queries (bad neighbour ids) return
- * UINT32_MAX ids, and qg_search_noalloc_status reads the kernels' status word back. The visited
- * tags limit the warps searching at once to about (64 MiB - prepared queries) / (2 * n_total):
- * ~32 at 1M nodes; an index needs 2 * n_total <= ~64 MiB (about 33M nodes). */
+ * nothing: its scratch (prepared queries, visited rows, counter, status) is one file-scope
+ * device array of QG_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until exit.
+ * The index must already exist; queries and outputs are the caller's. Limits: the prepared
+ * queries (nq x (5*D + 24) bytes) and at least one visited row (a bit per graph node, n_total / 8
+ * bytes) must fit the array, else QG_ERR_INVALID with the reason in qg_last_error(). All calls
+ * share the array: calls whose GPU work overlaps race, so serialise them. The first call on a
+ * device looks up the array's address (make it before any stream capture). The call itself does
+ * not synchronise: failed queries (bad neighbour ids) return UINT32_MAX ids, and
+ * qg_search_noalloc_status reads the kernels' status word back. The visited rows limit the warps
+ * searching at once to about (64 MiB - prepared queries) / (n_total / 8): ~530 at 1M nodes;
+ * an index needs n_total / 8 <= ~64 MiB (about 500M nodes). */
 #define QG_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
 int qg_search_batch_noalloc(qg_index *index, const float *d_queries, size_t nq,
                             const qg_search_params *params, const int *d_k, const int *d_l,
@@ -396,6 +396,21 @@ int qg_center_mean(const float *d_data, size_t stride, size_t dim, const uint32_
  * f32 data into compact and residual records (device). */
 int qg_encode_batch(const void *space, const float *d_raw, size_t n, uint8_t *d_compact,
                     uint8_t *d_residual, void *stream);
+/* The encode rotation as a dense GEMM on the tensor cores (no counterpart in the reference,
+ * which runs a fast Hadamard transform, RaBitQSpace::rotate, space_rabitq.h:944-1000): row n of
+ * d_rotated [n x code_dim] = H diag(sgn) fl(c * (x_n - centre) / |x_n - centre|), c the stored
+ * 1/sqrt(code_dim), computed as one BF16 x BF16 -> FP32 tcgen05 GEMM over the exact three-term
+ * BF16 split of the scaled rows; d_norms [n] = |x_n - centre| (the encoder's sequential sum).
+ * Every product is exact; only the FP32 summation order differs from the butterflies. Needs a
+ * code dim that is a multiple of 256; allocates scratch and synchronises the stream;
+ * QG_ERR_TIMEOUT if a tile's wait ran out. */
+int qg_rotate_gemm(const void *space, const float *d_raw, size_t n, float *d_rotated, float *d_norms,
+                   void *stream);
+/* qg_encode_batch with the rotation from qg_rotate_gemm (same record layout). Codes equal the
+ * reference's except where the GEMM's summation order moves a rotated value across a code
+ * boundary; allocates scratch and synchronises the stream. */
+int qg_encode_batch_gemm(const void *space, const float *d_raw, size_t n, uint8_t *d_compact,
+                         uint8_t *d_residual, void *stream);
 /* GPU alpha robust prune for graph construction (this library's own builder; the reference
  * prunes on the host, vamana_prune.h:42-156). For each of n nodes, scores its K candidate ids
  * (device [n x K], UINT32_MAX = none; any order, duplicates allowed) with the symmetric 4-bit

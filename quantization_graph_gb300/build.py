@@ -22,7 +22,7 @@ LIB = os.path.join(BUILD, "libqgraph_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["query_prep.cu", "batch_kernels.cu", "search.cu", "encode.cu", "graph_build.cu", "mlp.cu",
-                "search_noalloc.cu", "vamana_build.cu"]
+                "search_noalloc.cu", "vamana_build.cu", "rotate_gemm.cu"]
 CXX_SOURCES = ["bridge.cpp"]
 
 

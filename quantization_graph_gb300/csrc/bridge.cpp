@@ -517,6 +517,7 @@ void rabitq_space_delete(void *space) {
     cudaFree(s->d_center);
     cudaFree(s->d_rotated_center);
     cudaFree(s->d_center_norm);
+    cudaFree(s->d_rot_gemm_b);
     delete s;
 }
 
@@ -557,6 +558,8 @@ bool qg_space_set_signs(void *space, const float *signs) {
         std::copy(signs, signs + s->code_dim, s->signs.begin());
         if (!cuda_ok(cudaMemcpy(s->d_signs, signs, s->code_dim * 4, cudaMemcpyHostToDevice), "signs upload"))
             return false;
+        cudaFree(s->d_rot_gemm_b);  // built from the signs: rebuilt on next use
+        s->d_rot_gemm_b = nullptr;
         if (s->center_set) {
             std::vector<float> c(s->center);
             return rabitq_space_set_center(space, c.data());
@@ -1148,6 +1151,109 @@ int qg_encode_batch(const void *space, const float *d_raw, size_t n, uint8_t *d_
     return QG_OK;
 }
 
+// The tensor-core rotation of rows [0, n) into d_rotated [n x code_dim] and d_norms [n], in chunks
+// of at most 2^17 rows through a scratch BF16 operand; builds the space's +-1 operand on first use.
+static int rotate_gemm_rows(Space *s, const float *d_raw, size_t n, float *d_rotated, float *d_norms,
+                            cudaStream_t st) {
+    const int dim = static_cast<int>(s->dim), D = static_cast<int>(s->code_dim);
+    if (!rotate_gemm_supported(D)) {
+        set_error("the tensor-core rotation needs a code dim that is a multiple of 256");
+        return QG_ERR_UNSUPPORTED;
+    }
+    const size_t kp3 = 3 * static_cast<size_t>(rotate_gemm_kp(dim));
+    if (!s->d_rot_gemm_b) {
+        s->d_rot_gemm_b = dev_alloc<uint16_t>(static_cast<size_t>(D) * kp3);
+        if (!s->d_rot_gemm_b) {
+            set_error("device allocation failed for the rotation operand");
+            return QG_ERR_OOM;
+        }
+        if (!cuda_ok(launch_r_matrix(s->d_signs, dim, D, s->d_rot_gemm_b, st), "rotation operand") ||
+            !cuda_ok(cudaStreamSynchronize(st), "rotation operand")) {
+            cudaFree(s->d_rot_gemm_b);
+            s->d_rot_gemm_b = nullptr;
+            return QG_ERR_CUDA;
+        }
+    }
+    const size_t chunk = std::min<size_t>(n, 1u << 17);
+    uint16_t *a3 = dev_alloc<uint16_t>(chunk * kp3);
+    int *status = dev_alloc<int>(1);
+    if (!a3 || !status) {
+        cudaFree(a3);
+        cudaFree(status);
+        set_error("device allocation failed for the rotation scratch");
+        return QG_ERR_OOM;
+    }
+    int rc = QG_OK;
+    const float c_abs = std::fabs(s->signs[0]);
+    if (!cuda_ok(cudaMemsetAsync(status, 0, 4, st), "rotation status")) rc = QG_ERR_CUDA;
+    for (size_t base = 0; base < n && rc == QG_OK; base += chunk) {
+        const int m = static_cast<int>(std::min(chunk, n - base));
+        if (!cuda_ok(launch_rotate_split(d_raw + base * s->dim, s->dim, m, dim, s->d_center, c_abs, a3,
+                                         d_norms + base, st), "rotation split") ||
+            !cuda_ok(launch_rotate_gemm(a3, s->d_rot_gemm_b, m, dim, D, d_rotated + base * D, status, st),
+                     "rotation gemm"))
+            rc = QG_ERR_CUDA;
+    }
+    int h = 0;
+    if (rc == QG_OK && (!cuda_ok(cudaMemcpyAsync(&h, status, 4, cudaMemcpyDeviceToHost, st), "rotation status") ||
+                        !cuda_ok(cudaStreamSynchronize(st), "rotation sync")))
+        rc = QG_ERR_CUDA;
+    if (rc == QG_OK && h) {
+        set_error("the rotation GEMM timed out waiting for its tiles");
+        rc = QG_ERR_TIMEOUT;
+    }
+    cudaStreamSynchronize(st);
+    cudaFree(a3);
+    cudaFree(status);
+    return rc;
+}
+
+int qg_rotate_gemm(const void *space, const float *d_raw, size_t n, float *d_rotated, float *d_norms, void *stream) {
+    Space *s = const_cast<Space *>(as_space(space));
+    if (!s || (n && (!d_raw || !d_rotated || !d_norms)) || n > 0x7FFFFFFF) return QG_ERR_INVALID;
+    if (!s->center_set) {
+        set_error("set the centre before encoding");
+        return QG_ERR_INVALID;
+    }
+    if (n == 0) return QG_OK;
+    return rotate_gemm_rows(s, d_raw, n, d_rotated, d_norms, static_cast<cudaStream_t>(stream));
+}
+
+int qg_encode_batch_gemm(const void *space, const float *d_raw, size_t n, uint8_t *d_compact, uint8_t *d_residual,
+                         void *stream) {
+    Space *s = const_cast<Space *>(as_space(space));
+    if (!s || (n && (!d_raw || !d_compact || !d_residual)) || n > 0x7FFFFFFF) return QG_ERR_INVALID;
+    if (!s->center_set) {
+        set_error("set the centre before encoding");
+        return QG_ERR_INVALID;
+    }
+    if (n == 0) return QG_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t chunk = std::min<size_t>(n, 1u << 17);
+    float *rot = dev_alloc<float>(chunk * s->code_dim);
+    float *norms = dev_alloc<float>(chunk);
+    if (!rot || !norms) {
+        cudaFree(rot);
+        cudaFree(norms);
+        set_error("device allocation failed for the rotated rows");
+        return QG_ERR_OOM;
+    }
+    int rc = QG_OK;
+    for (size_t base = 0; base < n && rc == QG_OK; base += chunk) {
+        const size_t m = std::min(chunk, n - base);
+        rc = rotate_gemm_rows(s, d_raw + base * s->dim, m, rot, norms, st);
+        if (rc != QG_OK) break;
+        EncodeArgs a{nullptr, s->dim, static_cast<int>(m), static_cast<int>(s->dim), static_cast<int>(s->code_dim),
+                     s->d_signs, s->d_center, d_compact + base * s->compact_bytes,
+                     d_residual + base * s->residual_bytes, s->compact_bytes, s->residual_bytes, rot, norms};
+        if (!cuda_ok(launch_encode(a, st), "encode kernel")) rc = QG_ERR_CUDA;
+    }
+    cudaStreamSynchronize(st);
+    cudaFree(rot);
+    cudaFree(norms);
+    return rc;
+}
+
 int qg_prune_candidates(const void *space, const uint8_t *d_compact, size_t compact_stride, size_t n,
                         const uint32_t *d_candidates, size_t k, size_t r, float alpha,
                         uint32_t *d_degrees, uint32_t *d_edges, size_t edge_stride, void *stream) {
@@ -1315,8 +1421,7 @@ int qg_residual_pairs(const void *space, const float *d_rotated, const float *d_
 static void index_free_all(qg_index *ix) {
     for (void *p : ix->owned) cudaFree(p);
     ix->owned.clear();
-    cudaFree(ix->tags);
-    cudaFree(ix->epochs);
+    cudaFree(ix->visited);
     cudaFree(ix->counter);
     cudaFree(ix->status);
     cudaFree(ix->q.rr);
@@ -1485,7 +1590,7 @@ int qg_index_set_launch(qg_index *index, int warps_per_block, int blocks_per_sm)
 
 int qg_index_reserve(qg_index *index, size_t max_nq, int max_l, int max_k) {
     if (!index || max_l < 1 || max_k < 1) return QG_ERR_INVALID;
-    // an ordinary search of an empty batch sizes the workspace and the visited tags
+    // an ordinary search of an empty batch sizes the workspace and the visited rows
     qg_search_params p{max_k, max_l, 1, 1.9f, 100, 0, 0};
     const int rc = search_impl(index, nullptr, 0, &p, nullptr, nullptr, static_cast<size_t>(max_k), nullptr,
                                nullptr, nullptr, nullptr, 0, nullptr, nullptr, nullptr);
@@ -1633,7 +1738,7 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
         index->q_capacity = cap;
     }
     // persistent grid: warps per block and resident blocks per SM from the occupancy of
-    // this pool size; one visited-tag row per warp slot
+    // this pool size; one visited row per warp slot
     int wpb = 0, per_sm = 0;
     if (!search_launch_geometry(index, l_cap, model != nullptr, &wpb, &per_sm)) return QG_ERR_UNSUPPORTED;
     int sms = qg_device_sm_count();
@@ -1645,19 +1750,14 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
         return QG_ERR_INVALID;
     }
     if (index->slots < slots) {
-        cudaFree(index->tags);
-        cudaFree(index->epochs);
-        index->tags = nullptr;
-        index->epochs = nullptr;
-        const size_t tag_bytes = static_cast<size_t>(slots) * index->ix.n_total * 2;
-        if (cudaMalloc(&index->tags, tag_bytes ? tag_bytes : 16) != cudaSuccess ||
-            cudaMalloc(&index->epochs, static_cast<size_t>(slots) * 4) != cudaSuccess) {
+        cudaFree(index->visited);
+        index->visited = nullptr;
+        const size_t bytes = static_cast<size_t>(slots) * visited_row_words(index->ix.n_total) * 4;
+        if (cudaMalloc(&index->visited, bytes) != cudaSuccess) {
             index->slots = 0;
-            set_error("device allocation failed for visited tags");
+            set_error("device allocation failed for the visited rows");
             return QG_ERR_OOM;
         }
-        cudaMemset(index->tags, 0, tag_bytes);
-        cudaMemset(index->epochs, 0, static_cast<size_t>(slots) * 4);
         index->slots = slots;
     }
     if (nq == 0) return QG_OK;
@@ -1675,8 +1775,7 @@ static int search_impl(qg_index *index, const float *d_queries, size_t nq, const
     a.codes = index->q.codes;
     a.scal = index->q.scal;
     a.csum = index->q.csum;
-    a.tags = index->tags;
-    a.epochs = index->epochs;
+    a.visited = index->visited;
     a.counter = index->counter;
     a.status = index->status;
     a.nq_dev = d_nq;

@@ -361,6 +361,9 @@ __device__ __forceinline__ void put_f32(uint8_t *dst, float v) {
     dst[3] = b >> 24;
 }
 
+// kRotated: the rotation was done elsewhere (the tensor-core GEMM, rotate_gemm.cu); row v of
+// a.rotated holds it and a.norms[v] the residual norm.
+template <bool kRotated>
 __global__ void __launch_bounds__(32) encode_kernel(EncodeArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int D = a.code_dim, dim = a.dim, lane = threadIdx.x;
@@ -375,26 +378,33 @@ __global__ void __launch_bounds__(32) encode_kernel(EncodeArgs a) {
 
     const int v = blockIdx.x;
     if (v >= a.n) return;
-    const float *raw = a.raw + static_cast<size_t>(v) * a.raw_stride;
-
-    // residual and its norm: sequential float sum of r*r (no contraction, space_rabitq.h:5856-5860)
-    for (int i = lane; i < D; i += 32) ru[i] = i < dim ? raw[i] - a.center[i] : 0.0f;
-    __syncwarp();
-    if (lane == 0) {
-        float rns = 0.0f;
-        for (int i = 0; i < dim; ++i) rns = rns + ru[i] * ru[i];
-        s_rn = sqrtf(rns);
+    float rn;
+    if constexpr (kRotated) {
+        const float *rot = a.rotated + static_cast<size_t>(v) * D;
+        for (int i = lane; i < D; i += 32) ru[i] = rot[i];
+        rn = a.norms[v];
+        __syncwarp();
+    } else {
+        const float *raw = a.raw + static_cast<size_t>(v) * a.raw_stride;
+        // residual and its norm: sequential float sum of r*r (no contraction, space_rabitq.h:5856-5860)
+        for (int i = lane; i < D; i += 32) ru[i] = i < dim ? raw[i] - a.center[i] : 0.0f;
+        __syncwarp();
+        if (lane == 0) {
+            float rns = 0.0f;
+            for (int i = 0; i < dim; ++i) rns = rns + ru[i] * ru[i];
+            s_rn = sqrtf(rns);
+        }
+        __syncwarp();
+        rn = s_rn;
+        if (rn > 0.0f) {
+            const float inv = 1.0f / rn;
+            for (int i = lane; i < dim; i += 32) ru[i] = ru[i] * inv;
+        }
+        __syncwarp();
+        for (int i = lane; i < dim; i += 32) ru[i] = ru[i] * a.signs[i];
+        __syncwarp();
+        fht_warp_local(ru, D, lane);
     }
-    __syncwarp();
-    const float rn = s_rn;
-    if (rn > 0.0f) {
-        const float inv = 1.0f / rn;
-        for (int i = lane; i < dim; i += 32) ru[i] = ru[i] * inv;
-    }
-    __syncwarp();
-    for (int i = lane; i < dim; i += 32) ru[i] = ru[i] * a.signs[i];
-    __syncwarp();
-    fht_warp_local(ru, D, lane);
 
     // ---- fastQuantizeAbs ----
     float mx = 0.0f;
@@ -541,10 +551,17 @@ cudaError_t launch_encode(const EncodeArgs &a, cudaStream_t stream) {
     if (a.n == 0) return cudaSuccess;
     if (a.code_dim > 2048 || a.code_dim < 64) return cudaErrorInvalidValue;
     const size_t smem = static_cast<size_t>(a.code_dim) * (8 + 4 + 1 + 1);
-    cudaError_t e = cudaFuncSetAttribute(encode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (a.rotated != nullptr) {
+        cudaError_t e = cudaFuncSetAttribute(encode_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+        encode_kernel<true><<<a.n, 32, smem, stream>>>(a);
+        return cudaGetLastError();
+    }
+    cudaError_t e = cudaFuncSetAttribute(encode_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    encode_kernel<<<a.n, 32, smem, stream>>>(a);
+    encode_kernel<false><<<a.n, 32, smem, stream>>>(a);
     return cudaGetLastError();
 }
 

@@ -57,8 +57,7 @@ struct SearchArgs {
     uint32_t *ids_out;
     float *dists_out;
     qg_search_stats *stats_out;
-    uint16_t *tags;      // [slots x n_total] visited tags
-    uint32_t *epochs;    // [slots]
+    uint32_t *visited;   // [slots x visited_row_words(n_total)] one bit per node, cleared per query
     unsigned int *counter;
     int *status;
     int hop_cap;
@@ -100,14 +99,19 @@ struct EncodeArgs {
     uint8_t *residual;     // [n x residual_bytes]
     size_t compact_bytes;
     size_t residual_bytes;
+    const float *rotated = nullptr;  // optional [n x code_dim]: rows already rotated (raw, signs unused)
+    const float *norms = nullptr;    // [n] residual norms, with `rotated`
 };
+
+// 32-bit words of one warp slot's visited row: a bit per graph node, rounded up to 16 bytes.
+__host__ __device__ inline size_t visited_row_words(size_t n_total) { return ((n_total + 31) / 32 + 3) & ~size_t(3); }
 
 // Sets the message qg_last_error() returns on the calling thread.
 void record_error(const std::string &msg);
 
 // Checks the arguments of a batched search (qg_search_batch and its variants) and fills every
-// field of *out that does not name scratch memory: the prepared-query buffers, visited tags,
-// epochs, work counter and status word stay null for the caller to place. Returns QG_OK or a
+// field of *out that does not name scratch memory: the prepared-query buffers, the visited
+// rows, the work counter and the status word stay null for the caller to place. Returns QG_OK or a
 // QG_ERR_* status with the message recorded.
 int search_args_fill(const qg_index *index, size_t nq, const qg_search_params *params, const float *d_queries,
                      const int *d_k, const int *d_l, size_t k_stride, uint32_t *d_ids, float *d_dists,
@@ -134,6 +138,16 @@ int search_blocks_per_sm(int code_dim, int l_cap, int warps_per_block, bool stop
 size_t search_block_smem(int l_cap, int warps_per_block, bool stop_model);
 int search_supported_dim(int code_dim);
 cudaError_t launch_encode(const EncodeArgs &a, cudaStream_t stream);
+// The encode rotation on the tensor cores (rotate_gemm.cu). Kp = dim rounded up to 64; a3 holds
+// n x 3 Kp BF16 (the rows' three exact BF16 terms), r3 code_dim x 3 Kp BF16 (the +-1 Hadamard-
+// sign matrix three times). status receives bit 0 when a CTA's wait timed out.
+int rotate_gemm_kp(int dim);
+bool rotate_gemm_supported(int code_dim);
+cudaError_t launch_rotate_split(const float *raw, size_t stride, int n, int dim, const float *center, float c_abs,
+                                void *a3, float *norms, cudaStream_t stream);
+cudaError_t launch_r_matrix(const float *signs, int dim, int code_dim, void *r3, cudaStream_t stream);
+cudaError_t launch_rotate_gemm(const void *a3, const void *r3, int n, int dim, int code_dim, float *out, int *status,
+                               cudaStream_t stream);
 cudaError_t launch_mlp_forward(const float *X, size_t n, const float *norm, const uint16_t *w, float *logits,
                                cudaStream_t stream);
 cudaError_t launch_mlp_backward(const float *X, const float *y, size_t n, const float *norm, const uint16_t *w,

@@ -36,6 +36,7 @@ struct Space {
     float *d_rotated_center = nullptr; // [D]
     float *d_center_norm = nullptr;    // [1] ||c||^2 as float (setCentroids)
     float center_norm_sqr = 0.0f;
+    void *d_rot_gemm_b = nullptr;      // the tensor-core rotation's +-1 operand (built on first use)
 };
 
 // Query code layout of a codec id: Int8 (3) -> 8, Int4 (2) -> 4 (integer codes), B1 (1) -> 1 (sign
@@ -81,9 +82,8 @@ struct qg_index {
     qg::DevIndex ix;
     const qg::Space *space = nullptr;
     int device = 0;
-    // search scratch: visited tags per warp slot, epochs, queue counter, status word
-    uint16_t *tags = nullptr;
-    uint32_t *epochs = nullptr;
+    // search scratch: a visited bit row per warp slot, queue counter, status word
+    uint32_t *visited = nullptr;
     unsigned int *counter = nullptr;
     int *status = nullptr;
     int slots = 0;

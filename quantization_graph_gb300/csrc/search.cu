@@ -18,8 +18,8 @@
 // loads in flight together, then reduced with a reduce-scatter butterfly that leaves each
 // neighbour's sum in one lane. The accept/insert pass is warp-serial over survivors in
 // adjacency order (the reference's result depends on that order); each insert is a
-// warp-parallel rank + shift of the pool in shared memory. The visited set is a per-warp-
-// slot array of 16-bit epoch tags in global memory (no per-query clearing).
+// warp-parallel rank + shift of the pool in shared memory. The visited set is one bit per
+// graph node in a per-warp-slot row of global memory, cleared at the start of each query.
 #include <cstdint>
 #include <map>
 #include <mutex>
@@ -257,7 +257,7 @@ __device__ __forceinline__ void load_query(QueryRegs<D> &r, const int8_t *codes,
 // remaining bits with the gate's short ip (mode 1), the others the FP32 restore (mode 0).
 template <int D, int kMode>
 __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int lane,
-                           uint16_t *tags, uint32_t tag, const uint32_t *stop_smem) {
+                           uint32_t *visited, const uint32_t *stop_smem) {
     using L = Lay<D>;
     const DevIndex &ix = a.ix;
     const int sub = lane % L::LPN;
@@ -308,7 +308,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
 
     int pn = 0;  // pool size (warp-uniform)
     if (ix.n_base != 0) {
-        if (lane == 0) tags[0] = static_cast<uint16_t>(tag);
+        if (lane == 0) visited[0] = 1u;
         const float4 h = ix.hdr[0];
         const float d0 = restore_distance_hw<D>(ix.codes, rr, h.x, h.y, half_sum, qn2, lane & 15);
         if (lane == 0) {
@@ -388,10 +388,9 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                 const bool leader = (__ffs(same) - 1) == lane;
                 bool fresh = false;
                 if (valid && !bad && leader) {
-                    if (tags[nb] != static_cast<uint16_t>(tag)) {
-                        tags[nb] = static_cast<uint16_t>(tag);
-                        fresh = true;
-                    }
+                    // distinct ids of this row may share a word: atomicOr serialises them
+                    const uint32_t bit = 1u << (nb & 31u);
+                    fresh = (atomicOr(visited + (nb >> 5), bit) & bit) == 0u;
                 }
                 if (__any_sync(0xffffffffu, bad)) oob = true;
                 const unsigned int fm = __ballot_sync(0xffffffffu, fresh);
@@ -883,22 +882,19 @@ __global__ void __launch_bounds__(QG_SEARCH_THREADS, QG_SEARCH_MINBLOCKS) search
     }
     const WarpSmem s = carve(smem + wsm + warp * warp_smem_bytes(a.l_cap), a.l_cap);
     const int slot = blockIdx.x * wpb + warp;
-    uint16_t *tags = a.tags + static_cast<size_t>(slot) * a.ix.n_total;
+    const size_t words = visited_row_words(a.ix.n_total);
+    uint32_t *visited = a.visited + static_cast<size_t>(slot) * words;
     const int nq = a.nq_dev != nullptr ? min(a.nq, *a.nq_dev) : a.nq;
     for (;;) {
         int q = 0;
         if (lane == 0) q = static_cast<int>(atomicAdd(a.counter, 1u));
         q = __shfl_sync(0xffffffffu, q, 0);
         if (q >= nq) break;
-        uint32_t e = a.epochs[slot] + 1;
-        if ((e & 0xFFFFu) == 0) {
-            // 16-bit tags wrapped: clear this slot's tags once every 65535 queries
-            for (size_t i = lane; i < a.ix.n_total; i += 32) tags[i] = 0;
-            __syncwarp();
-            e += 1;
-        }
-        if (lane == 0) a.epochs[slot] = e;
-        search_one<D, kMode>(a, s, q, lane, tags, e & 0xFFFFu, stop_smem);
+        // a clear visited row for every query (n_total / 8 bytes, 16-byte stores)
+        uint4 *row = reinterpret_cast<uint4 *>(visited);
+        for (size_t i = lane; i < words / 4; i += 32) row[i] = make_uint4(0u, 0u, 0u, 0u);
+        __syncwarp();
+        search_one<D, kMode>(a, s, q, lane, visited, stop_smem);
         __syncwarp();
     }
 }

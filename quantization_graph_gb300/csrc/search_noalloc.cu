@@ -4,16 +4,16 @@
 // request path).
 //
 // It runs the same two kernels as qg_search_batch (query preparation and the persistent
-// search), but every piece of scratch they need -- prepared queries, the visited-tag rows of
-// each warp slot, the per-slot epochs, the work counter and the status word -- lives in one
+// search), but every piece of scratch they need -- prepared queries, the visited rows of the
+// warp slots, the work counter and the status word -- lives in one
 // file-scope device array of QG_NOALLOC_SCRATCH_BYTES (64 MiB). Every GPU that loads this
 // library holds that array until the process exits. The caller passes the index (built
 // earlier), the queries and the outputs; nothing here calls cudaMalloc, cudaFree or any
 // allocating routine.
 //
 // The array is shared by all calls and keeps the last call's contents: each call clears the
-// parts that must start at zero (counter, status, epochs, the tag rows it uses) on its stream
-// before launching. Two calls whose GPU work overlaps (different streams, or different host
+// parts that must start at zero (counter, status) on its stream before launching; the search
+// kernel clears a visited row itself at the start of every query. Two calls whose GPU work overlaps (different streams, or different host
 // threads on one device) race on the array and give wrong results; serialise them.
 //
 // Set-up: the first call on a device looks up the array's device address with
@@ -25,9 +25,9 @@
 // qg_search_noalloc_status reads it back after the call, as qg_search_status does for
 // qg_search_batch. It is the status of the last call on the device.
 //
-// The visited tags take one row of 2 * n_total bytes per resident warp, so the number of warps
-// that search at once is about (64 MiB - prepared queries) / (2 * n_total): ~32 at 1M nodes,
-// ~300 at 100k (every resident warp, up to 152 SMs x 16, below ~27k nodes).
+// The visited set takes one row of n_total / 8 bytes (a bit per node) per resident warp, so the
+// number of warps that search at once is about (64 MiB - prepared queries) / (n_total / 8):
+// ~530 at 1M nodes, every resident warp (up to 152 SMs x 16) below ~220k nodes.
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -93,7 +93,7 @@ extern "C" int qg_search_batch_noalloc(qg_index *index, const float *d_queries, 
     const Space *s = index->space;
     const size_t D = s->code_dim;
     const size_t n_total = index->ix.n_total;
-    // scratch layout: counter | status | prepared queries (rotated, codes, scalars, sums) | epochs | tags
+    // scratch layout: counter | status | prepared queries (rotated, codes, scalars, sums) | visited rows
     size_t off = kStatusOffset + 256;
     const size_t o_rr = off;
     off += round256(nq * D * sizeof(float));
@@ -112,14 +112,11 @@ extern "C" int qg_search_batch_noalloc(qg_index *index, const float *d_queries, 
     int sms = qg_device_sm_count();
     if (sms <= 0) return fail(QG_ERR_CUDA, "qg_search_batch_noalloc: no device");
     size_t max_slots = static_cast<size_t>(sms) * per_sm * wpb;
-    const size_t row_bytes = n_total * sizeof(uint16_t);  // the kernel's tag rows are packed
-    const size_t epoch_bytes = round256(max_slots * sizeof(uint32_t));
-    if (off + epoch_bytes > kScratchBytes)
-        return fail(QG_ERR_INVALID, "qg_search_batch_noalloc: queries leave no room for visited tags");
-    // ... cut to the visited-tag rows that fit: one row of n_total tags per warp slot; a block
-    // narrower than wpb is taken when fewer than wpb rows fit
-    const size_t room = kScratchBytes - off - epoch_bytes;
-    size_t fit = row_bytes ? room / row_bytes : 0;
+    // ... cut to the visited rows that fit (one per warp slot); a block narrower than wpb is
+    // taken when fewer than wpb rows fit
+    const size_t row_bytes = visited_row_words(n_total) * 4;
+    const size_t room = kScratchBytes - off;
+    size_t fit = room / row_bytes;
     if (fit < static_cast<size_t>(wpb)) {
         int narrow = 0;
         for (int cand : {4, 2, 1})
@@ -137,16 +134,11 @@ extern "C" int qg_search_batch_noalloc(qg_index *index, const float *d_queries, 
     }
     size_t slots = fit < max_slots ? fit : max_slots;
     slots -= slots % static_cast<size_t>(wpb);
-    const size_t o_epochs = off;
-    off += epoch_bytes;
-    const size_t o_tags = off;
+    const size_t o_visited = off;
 
     unsigned char *sb = static_cast<unsigned char *>(base);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // clear what must start at zero; tag rows are laid out for this call's node count
-    if ((e = cudaMemsetAsync(sb + kCounterOffset, 0, kStatusOffset + 256, st)) != cudaSuccess ||
-        (e = cudaMemsetAsync(sb + o_epochs, 0, epoch_bytes, st)) != cudaSuccess ||
-        (e = cudaMemsetAsync(sb + o_tags, 0, slots * row_bytes, st)) != cudaSuccess)
+    if ((e = cudaMemsetAsync(sb + kCounterOffset, 0, kStatusOffset + 256, st)) != cudaSuccess)
         return fail(QG_ERR_CUDA, std::string("qg_search_batch_noalloc: clear: ") + cudaGetErrorString(e));
 
     PrepArgs pa{d_queries, s->dim, static_cast<int>(nq), static_cast<int>(s->dim), static_cast<int>(D),
@@ -161,8 +153,7 @@ extern "C" int qg_search_batch_noalloc(qg_index *index, const float *d_queries, 
     a.codes = pa.codes;
     a.scal = pa.scal;
     a.csum = pa.csum;
-    a.tags = reinterpret_cast<uint16_t *>(sb + o_tags);
-    a.epochs = reinterpret_cast<uint32_t *>(sb + o_epochs);
+    a.visited = reinterpret_cast<uint32_t *>(sb + o_visited);
     a.counter = reinterpret_cast<unsigned int *>(sb + kCounterOffset);
     a.status = reinterpret_cast<int *>(sb + kStatusOffset);
     if ((e = launch_search(a, static_cast<int>(slots / static_cast<size_t>(wpb)), wpb, st)) != cudaSuccess)

@@ -113,6 +113,36 @@ class RabitqSpace:
                 "qg_encode_batch")
         return compact, residual
 
+    def encode_gemm(self, data: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
+        """encode() with the rotation as a BF16x3 GEMM on the tensor cores (qg_encode_batch_gemm):
+        same layouts; codes equal the reference's except where the GEMM's FP32 summation order
+        moves a rotated value across a code boundary."""
+        data = _cuda(data, torch.float32)
+        n = data.shape[0]
+        compact = torch.empty((n, self.compact_record_bytes()), dtype=torch.uint8, device="cuda")
+        residual = torch.empty((n, self.residual_record_bytes()), dtype=torch.uint8, device="cuda")
+        N.check(self.lib.qg_encode_batch_gemm(self.ptr, _ptr(data), n, _ptr(compact), _ptr(residual), _stream()),
+                "qg_encode_batch_gemm")
+        return compact, residual
+
+    def rotate_gemm(self, data: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
+        """The encode rotation on the tensor cores (qg_rotate_gemm): ([n, code_dim] rotated
+        normalised residuals, [n] residual norms)."""
+        data = _cuda(data, torch.float32)
+        n = data.shape[0]
+        rot = torch.empty((n, self.code_dim), dtype=torch.float32, device="cuda")
+        norms = torch.empty(n, dtype=torch.float32, device="cuda")
+        N.check(self.lib.qg_rotate_gemm(self.ptr, _ptr(data), n, _ptr(rot), _ptr(norms), _stream()),
+                "qg_rotate_gemm")
+        return rot, norms
+
+    def signs(self) -> np.ndarray:
+        """The rotation's random signs, +-1/sqrt(code_dim) (setRandomRotation, space_rabitq.h:2900-2912)."""
+        out = np.empty(self.code_dim, np.float32)
+        if not self.lib.qg_space_signs(self.ptr, out.ctypes.data):
+            raise RuntimeError(f"qg_space_signs failed: {N.last_error()}")
+        return out
+
     def export_paper_sidecar(self, compact: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
         """MSB plane + 20-byte prune factors per record (rabitq_export_paper_sidecar,
         rabitq_bridge.cpp:317-343), on the GPU."""

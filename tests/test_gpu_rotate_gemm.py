@@ -1,0 +1,106 @@
+"""The encode rotation as a BF16x3 GEMM on the tcgen05 tensor cores (qg_rotate_gemm,
+qg_encode_batch_gemm) against FP64 arithmetic and against the reference encoder.
+
+The rotation's operands are exact (three BF16 terms of each scaled residual value, a +-1
+Hadamard-sign matrix), so the GEMM may differ from the exact product only by the FP32
+accumulation: at most 3 Kp * 2^-24 * sum|a| per value, whatever the summation order. Codes
+from the GEMM path are compared with the reference encoder's (the FHT path, bit-exact to the
+reference); they may differ only where the summation order moves a value across a boundary."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _hadamard_signs(D, dim, signs):
+    i = np.arange(dim)[None, :]
+    j = np.arange(D)[:, None]
+    pop = np.vectorize(lambda v: bin(v).count("1"))(i & j)
+    return np.where(pop & 1, -1.0, 1.0) * np.where(signs[:dim] > 0, 1.0, -1.0)[None, :]
+
+
+def _scaled_rows(x, center, c_abs):
+    """The split kernel's a = fl(fl(r * (1 / |r|)) * c) in float32, |r| by a sequential float32 sum."""
+    r = (x - center[None, :]).astype(np.float32)
+    rns = np.cumsum(r * r, axis=1, dtype=np.float32)[:, -1]
+    rn = np.sqrt(rns).astype(np.float32)
+    inv = (np.float32(1.0) / rn).astype(np.float32)
+    u = np.where(rn[:, None] > 0, (r * inv[:, None]).astype(np.float32), r)
+    return (u * np.float32(c_abs)).astype(np.float32), rn
+
+
+@pytest.mark.parametrize("dim,n", [(1536, 300), (960, 129), (200, 64)])
+def test_rotation_gemm_within_the_fp32_accumulation_bound(cuda, dim, n):
+    torch = cuda
+    from quantization_graph_gb300.space import RabitqSpace
+
+    rng = np.random.default_rng(dim)
+    x = rng.standard_normal((n, dim)).astype(np.float32)
+    center = rng.standard_normal(dim).astype(np.float32) * 0.1
+    x[3] = center  # a row on the centre: zero residual
+    sp = RabitqSpace(dim, center)
+    D = sp.code_dim
+    rot, norms = sp.rotate_gemm(torch.from_numpy(x))
+    rot = rot.cpu().numpy().astype(np.float64)
+    signs = sp.signs()
+    a, rn = _scaled_rows(x, center, abs(float(signs[0])))
+    np.testing.assert_array_equal(norms.cpu().numpy(), rn)  # the encoder's own norm, bit for bit
+    R = _hadamard_signs(D, dim, signs)
+    exact = a.astype(np.float64) @ R.T
+    kp = (dim + 63) // 64 * 64
+    bound = 3 * kp * 2.0 ** -24 * np.abs(a).astype(np.float64).sum(1)[:, None] + 1e-30
+    err = np.abs(rot - exact)
+    assert (err <= bound).all(), float((err / bound).max())
+    assert (rot[3] == 0).all()
+
+
+def test_rotation_gemm_close_to_the_reference_fht(cuda, oracle):
+    torch = cuda
+    from quantization_graph_gb300.space import RabitqSpace
+
+    rng = np.random.default_rng(7)
+    dim, n = 1536, 64
+    x = rng.standard_normal((n, dim)).astype(np.float32)
+    center = rng.standard_normal(dim).astype(np.float32) * 0.1
+    sp = RabitqSpace(dim, center)
+    rot, norms = sp.rotate_gemm(torch.from_numpy(x))
+    o = oracle.Oracle(dim, center)
+    np.testing.assert_array_equal(o.signs(), sp.signs())
+    rn = norms.cpu().numpy()
+    for v in range(n):  # the oracle rotates u = fl(r * (1 / |r|)) by signs and butterflies
+        fht = o.rotate(((x[v] - center).astype(np.float32) * (np.float32(1.0) / rn[v])).astype(np.float32))
+        assert np.abs(rot[v].cpu().numpy() - fht).max() < 1e-5, v
+
+
+def test_gemm_encode_matches_the_reference_encoder_but_for_rare_boundaries(cuda):
+    torch = cuda
+    from quantization_graph_gb300 import synthetic
+    from quantization_graph_gb300.space import RabitqSpace
+
+    dim, n = 1536, 3000
+    x = synthetic.anisotropic(n, dim, 0.8, seed=5, normalize=True)
+    center = x.mean(0).astype(np.float32)
+    sp = RabitqSpace(dim, center)
+    c_ref, r_ref = sp.encode(torch.from_numpy(x))       # the FHT path, bit-exact to the reference
+    c_gem, r_gem = sp.encode_gemm(torch.from_numpy(x))  # the tensor-core rotation
+    c_ref, c_gem = c_ref.cpu().numpy(), c_gem.cpu().numpy()
+    D = sp.code_dim
+    codes_r, codes_g = c_ref[:, 16:16 + D // 2], c_gem[:, 16:16 + D // 2]
+    bad = ((codes_r & 15) != (codes_g & 15)).sum() + ((codes_r >> 4) != (codes_g >> 4)).sum()
+    rate = bad / (n * D)
+    assert rate < 1e-3, rate
+    f_r = c_ref[:, :16].copy().view(np.float32).astype(np.float64)
+    f_g = c_gem[:, :16].copy().view(np.float32).astype(np.float64)
+    rel = np.abs(f_r - f_g) / np.maximum(np.abs(f_r), 1e-30)
+    assert rel[:, 0].max() == 0.0  # norm_sqr does not depend on the rotation
+    assert np.median(rel[:, 1:]) < 1e-6 and rel[:, 1:].max() < 1e-2
+    print(f"code mismatch rate {rate:.2e}, records equal {(c_ref == c_gem).all(1).mean():.4f}")
+
+
+def test_rotation_gemm_refuses_small_code_dims(cuda):
+    torch = cuda
+    from quantization_graph_gb300.space import RabitqSpace
+
+    sp = RabitqSpace(128, np.zeros(128, np.float32))
+    with pytest.raises(RuntimeError, match="QG_ERR_UNSUPPORTED"):
+        sp.rotate_gemm(torch.zeros((4, 128)))
