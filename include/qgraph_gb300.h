@@ -406,6 +406,11 @@ int qg_encode_batch(const void *space, const float *d_raw, size_t n, uint8_t *d_
  * QG_ERR_TIMEOUT if a tile's wait ran out. */
 int qg_rotate_gemm(const void *space, const float *d_raw, size_t n, float *d_rotated, float *d_norms,
                    void *stream);
+/* The GEMM of qg_rotate_gemm on operand planes given directly (kernel-level, for tests):
+ * d_a3 [n x 3 Kp] BF16 bits (Kp = dim rounded up to 64; three planes side by side along K),
+ * d_out [n x code_dim] = d_a3 times the space's +-1 operand (the Hadamard-sign matrix three
+ * times along K). */
+int qg_rotate_gemm_planes(const void *space, const uint16_t *d_a3, size_t n, float *d_out, void *stream);
 /* qg_encode_batch with the rotation from qg_rotate_gemm (same record layout). Codes equal the
  * reference's except where the GEMM's summation order moves a rotated value across a code
  * boundary; allocates scratch and synchronises the stream. */

@@ -145,6 +145,9 @@ struct qgo_prepared {
     const qgo_space *space = nullptr;
     std::vector<float> rotated_residual;  // q' = R q - R c
     std::vector<int8_t> int8_code;
+    // gate_tab[16 j + v]: sum of the integer codes of dims 4j..4j+3 whose bit is set in v (built
+    // with the codes; the gate's masked sum as one lookup per nibble of the MSB plane)
+    std::vector<int16_t> gate_tab;
     float query_norm_sqr = 0.0f;
     float query_norm = 0.0f;
     float half_sum = 0.0f;
@@ -374,9 +377,10 @@ float traversal_distance(const qgo_space &s, const qgo_prepared &q, const uint8_
     const float long_scale = get_f32(record + 4);
     if (!(long_scale > 0.0f) || !std::isfinite(long_scale)) return norm_sqr + q.query_norm_sqr;
     const uint8_t *code = record + s.off_code_compact();
-    int64_t dot = 0;
-    for (size_t i = 0; i < s.code_dim; ++i)
-        dot += static_cast<int64_t>(nib(code, i) & 7U) * q.int8_code[i];
+    int32_t dot = 0;  // |dot| <= 7 * 128 * D: an int32, exact in any order
+    const int8_t *x = q.int8_code.data();
+    for (size_t j = 0; j < s.code_dim / 2; ++j)
+        dot += static_cast<int32_t>(code[j] & 7U) * x[2 * j] + static_cast<int32_t>((code[j] >> 4U) & 7U) * x[2 * j + 1];
     return finish_traversal(q, norm_sqr, long_scale, short_ip, dot);
 }
 
@@ -451,9 +455,17 @@ qgo_paper_estimate gate_one(const qgo_space &s, const qgo_prepared &q, const uin
     if (!f.valid) return r;
     if (q.query_norm <= 0.0f || f.cross_scale <= 0.0f || !std::isfinite(f.cross_scale))
         return r;
-    int64_t selected = 0;
-    for (size_t i = 0; i < s.code_dim; ++i)
-        if ((msb[i >> 3U] >> (i & 7U)) & 1U) selected += q.int8_code[i];
+    int64_t selected = 0;  // integer sum: exact in any order
+    if (q.gate_tab.size() == s.code_dim / 4 * 16) {
+        const int16_t *t = q.gate_tab.data();
+        int32_t acc = 0;
+        for (size_t j = 0; j < s.code_dim / 8; ++j)
+            acc += t[32 * j + (msb[j] & 15U)] + t[32 * j + 16 + (msb[j] >> 4U)];
+        selected = acc;
+    } else {
+        for (size_t i = 0; i < s.code_dim; ++i)
+            if ((msb[i >> 3U] >> (i & 7U)) & 1U) selected += q.int8_code[i];
+    }
     const float short_ip =
         0.5f * q.int8_scale * static_cast<float>(static_cast<int64_t>(2) * selected - q.code_sum);
     return finish_gate(q, short_ip, f, eps);
@@ -850,6 +862,7 @@ int qgo_prepare(const qgo_space *sp, const float *query, qgo_prepared *p) {
     p->int8_scale = 1.0f;
     p->code_sum = 0;
     std::fill(p->int8_code.begin(), p->int8_code.end(), 0);
+    p->gate_tab.clear();
     if (s.query_bits == 32) return 0;  // Full: the FP32 residual only (space_rabitq.h:3489-3492)
     if (s.query_bits == 1) {  // B1: sign bits and the 1-bit estimator's scales (no integer codes)
         p->b1_code.assign(s.msb_bytes, 0);
@@ -896,6 +909,14 @@ int qgo_prepare(const qgo_space *sp, const float *query, qgo_prepared *p) {
             p->code_sum += x;
         }
     }
+    p->gate_tab.assign(D / 4 * 16, 0);
+    for (size_t j = 0; j < D / 4; ++j)
+        for (int v = 0; v < 16; ++v) {
+            int sum = 0;
+            for (int b = 0; b < 4; ++b)
+                if ((v >> b) & 1) sum += p->int8_code[4 * j + b];
+            p->gate_tab[16 * j + v] = static_cast<int16_t>(sum);
+        }
     return 0;
 }
 

@@ -121,6 +121,7 @@ _SIGS = {
     "qg_encode_batch": (C.c_int, [P, P, SZ, P, P, P]),
     "qg_rotate_gemm": (C.c_int, [P, P, SZ, P, P, P]),
     "qg_encode_batch_gemm": (C.c_int, [P, P, SZ, P, P, P]),
+    "qg_rotate_gemm_planes": (C.c_int, [P, P, SZ, P, P]),
     "qg_export_sidecar_device": (C.c_int, [P, P, SZ, SZ, P, P, P]),
     "qg_space_signs": (C.c_bool, [P, P]),
     "qg_space_set_signs": (C.c_bool, [P, P]),

@@ -1219,6 +1219,37 @@ int qg_rotate_gemm(const void *space, const float *d_raw, size_t n, float *d_rot
     return rotate_gemm_rows(s, d_raw, n, d_rotated, d_norms, static_cast<cudaStream_t>(stream));
 }
 
+int qg_rotate_gemm_planes(const void *space, const uint16_t *d_a3, size_t n, float *d_out, void *stream) {
+    Space *s = const_cast<Space *>(as_space(space));
+    if (!s || (n && (!d_a3 || !d_out)) || n > 0x7FFFFFFF) return QG_ERR_INVALID;
+    if (n == 0) return QG_OK;
+    // the space's +-1 operand, built on first use (the same one qg_rotate_gemm uses)
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int dim = static_cast<int>(s->dim), D = static_cast<int>(s->code_dim);
+    if (!rotate_gemm_supported(D)) {
+        set_error("the tensor-core rotation needs a code dim that is a multiple of 256");
+        return QG_ERR_UNSUPPORTED;
+    }
+    if (!s->d_rot_gemm_b) {
+        const size_t kp3 = 3 * static_cast<size_t>(rotate_gemm_kp(dim));
+        s->d_rot_gemm_b = dev_alloc<uint16_t>(static_cast<size_t>(D) * kp3);
+        if (!s->d_rot_gemm_b) return QG_ERR_OOM;
+        if (!cuda_ok(launch_r_matrix(s->d_signs, dim, D, s->d_rot_gemm_b, st), "rotation operand")) return QG_ERR_CUDA;
+    }
+    int *status = dev_alloc<int>(1);
+    if (!status) return QG_ERR_OOM;
+    int h = 0, rc = QG_OK;
+    if (!cuda_ok(cudaMemsetAsync(status, 0, 4, st), "status") ||
+        !cuda_ok(launch_rotate_gemm(d_a3, s->d_rot_gemm_b, static_cast<int>(n), dim, D, d_out, status, st), "gemm") ||
+        !cuda_ok(cudaMemcpyAsync(&h, status, 4, cudaMemcpyDeviceToHost, st), "status") ||
+        !cuda_ok(cudaStreamSynchronize(st), "sync"))
+        rc = QG_ERR_CUDA;
+    else if (h)
+        rc = QG_ERR_TIMEOUT;
+    cudaFree(status);
+    return rc;
+}
+
 int qg_encode_batch_gemm(const void *space, const float *d_raw, size_t n, uint8_t *d_compact, uint8_t *d_residual,
                          void *stream) {
     Space *s = const_cast<Space *>(as_space(space));

@@ -1,0 +1,431 @@
+// code_search.cuh -- fastQuantizeAbs (space_rabitq.h:867-942) for one vector held by one warp:
+// the search over the rescale factor t that the encoder runs on every rotated residual. Two
+// forms give the same t bit for bit: code_search_warp (all lanes; exact when the vector's double
+// sums are, which it checks) and code_search_lane0 (one lane, any vector). Shared by the encode
+// kernel and the host harness that runs them under a warp emulator (tests/native).
+//
+// Inputs, in shared memory: keys[D] = the dimensions sorted by (|v| descending, index ascending),
+// as (~bits(|v|) << 32 | index); ru[D] the rotated values; c0[D] the initial codes
+// floor(t_start |v| + 1e-5) (at most 2, t_start = 2 / max|v|); mx = max|v|.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "exact_fp.cuh"
+
+namespace qg {
+
+// Bitonic sort of n (a power of two) 64-bit keys in shared memory by one warp, ascending.
+__device__ inline void bitonic_sort_warp(unsigned long long *k, int n, int lane) {
+    for (int size = 2; size <= n; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int t = lane; t < n / 2; t += 32) {
+                const int lo = 2 * t - (t & (stride - 1));
+                const int hi = lo + stride;
+                const bool asc = (lo & size) == 0;
+                const unsigned long long a = k[lo], b = k[hi];
+                if ((a > b) == asc) {
+                    k[lo] = b;
+                    k[hi] = a;
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// The largest float not above the double 1e-5: a > 1e-5 (double) <=> a > kEpsBelowF.
+inline constexpr float kEpsBelowF = 9.99999974737875e-06f;
+
+// floor(RN53(t * a + 1e-5)) for t = th + tl (t a double split into two floats, a >= 0) in FP32:
+// ph + pl = th * a exactly, the rest is below 2^-16 and positive, so only the boundary above
+// can be crossed; decided unless the value lies within 2^-36 of it (`undecided`).
+__device__ __forceinline__ int floor_fma_eps(float th, float tl, float a, bool &undecided) {
+    const float ph = __fmul_rn(th, a);
+    const float pl = __fmaf_rn(th, a, -ph);
+    const float tail = __fadd_rn(__fadd_rn(__fadd_rn(pl, __fmul_rn(tl, a)), kEpsBelowF), 2.5262124e-13f);
+    const float n = floorf(ph);
+    const float d0 = __fsub_rn(ph, n);  // exact
+    int v = static_cast<int>(n);
+    if (d0 >= 0.5f) {
+        const float g = __fadd_rn(__fsub_rn(d0, 1.0f), tail);  // d0 - 1 exact for d0 >= 0.5
+        if (g > 0x1p-36f) v += 1;
+        else if (!(g < -0x1p-36f)) undecided = true;
+    } else if (!(tail > 0.0f)) {
+        undecided = true;  // cannot happen for a >= 0; keeps the decision honest
+    }
+    return v;
+}
+
+// sign of c1 / a1 - c2 / a2 for integers 1 <= c <= 17 and positive normal floats a, exactly:
+// the sign of c1 a2 - c2 a1, compared on the significands.
+__device__ __forceinline__ int ratio_cmp(int c1, float a1, int c2, float a2) {
+    const FloatParts p1 = split_float(a1), p2 = split_float(a2);
+    long long l = c1 * p2.m, r = c2 * p1.m;  // < 2^29
+    const int d = p2.e - p1.e;                 // l * 2^d against r
+    if (d > 30) return 1;
+    if (d < -30) return -1;
+    if (d > 0) l <<= d;
+    else r <<= -d;
+    return l < r ? -1 : (l > r ? 1 : 0);
+}
+
+// Truncation of a positive normal double to float (relative error below 2^-23), by bits.
+__device__ __forceinline__ float approx_float(double x) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
+    const int ex = static_cast<int>((b >> 52) & 0x7FF) - 1023 + 127;
+    if (ex <= 0) return 0.0f;
+    if (ex >= 255) return __int_as_float(0x7f800000);
+    return __uint_as_float((static_cast<uint32_t>(ex) << 23) | static_cast<uint32_t>((b >> 29) & 0x7FFFFFu));
+}
+
+// Heads of the seven level lists of fastQuantizeAbs's events: the next admissible dim of each
+// level in |v| order. Dim i is an event of level c when |v_i| > 1e-5, c > c0_i and
+// (c = c0_i + 1 or c / |v_i| < 17 / max|v|).
+struct LevelHead {
+    int ptr;
+    int id;   // -1 when the level is exhausted
+    float a;  // |v_id|
+    float t;  // RN24(c / a): orders heads unless two are equal
+};
+
+__device__ __forceinline__ void advance_level(LevelHead &h, int c, const unsigned long long *keys, const float *ru,
+                                              const unsigned char *c0, int D, float mx) {
+    while (h.ptr < D) {
+        const int i = static_cast<int>(keys[h.ptr] & 0xFFFFFFFFu);
+        const float ai = fabsf(ru[i]);
+        const int ci = c0[i];
+        if (ai > kEpsBelowF && c > ci && (c == ci + 1 || ratio_cmp(c, ai, 17, mx) < 0)) {
+            h.id = i;
+            h.a = ai;
+            h.t = __fdiv_rn(static_cast<float>(c), ai);
+            return;
+        }
+        ++h.ptr;
+    }
+    h.id = -1;
+}
+
+// event (c, h) before event (b, g): t ascending, ties by dim index; the float ratios decide
+// unless equal (rounding is monotone), then the exact comparison
+__device__ __forceinline__ bool event_before(int c, const LevelHead &h, int b, const LevelHead &g) {
+    if (h.t != g.t) return h.t < g.t;
+    const int r = ratio_cmp(c, h.a, b, g.a);
+    return r < 0 || (r == 0 && h.id < g.id);
+}
+
+// fastQuantizeAbs's search over the rescale factor t (space_rabitq.h:867-942), lane 0: the
+// (t, i) events of the seven levels in heap order (t = level / |v_i|, ties by i), running
+// num and sqr_den, t at the first maximum of ip = num / sqrt(sqr_den). Event order and the t_end
+// cut are decided by ratio comparisons (distinct level / |v| ratios differ by far more than a
+// double's rounding, so they order as their doubles do); num stays a double sum. The maximum is
+// screened in FP32 on squares, (ip_k / ip_best)^2 = num_k^2 sqr_den_best / (num_best^2 sqr_den_k)
+// (within 2^-20 of the float products): an event clearly above the running best (by more than
+// 2^-17) becomes the best, one clearly below is skipped, and only events inside that band are
+// compared exactly, in double, with the best (whose exact ip is computed once).
+__device__ inline double code_search_lane0(const unsigned long long *keys, const float *ru, const unsigned char *c0,
+                                    int D, float mx) {
+    long long sd4 = D;  // 4 * sqr_den
+    double num = 0.0;
+    for (int i = 0; i < D; ++i) {
+        const int c = c0[i];
+        sd4 += 4LL * (c * c + c);
+        num += (c + 0.5) * static_cast<double>(fabsf(ru[i]));
+    }
+    LevelHead hd[8];
+#pragma unroll
+    for (int c = 1; c <= 7; ++c) {
+        hd[c].ptr = 0;
+        advance_level(hd[c], c, keys, ru, c0, D, mx);
+    }
+    // the best so far: its ip is > 0 for every event, the reference starts from max_ip = 0
+    bool have = false, best_exact = false;
+    float best_n2 = 0.0f, best_sdf = 1.0f;  // num^2 and 4 sqr_den of the best, in float
+    double best_num = 0.0, best_ip = 0.0;
+    long long best_sd4 = 0;
+    int best_c = 0;
+    float best_a = 1.0f;
+    constexpr float kHi = 1.0f + 0x1p-17f, kLo = 1.0f - 0x1p-17f;
+    for (;;) {
+        int bc = 0;
+        LevelHead cur{0, -1, 0.0f, 0.0f};
+#pragma unroll
+        for (int c = 1; c <= 7; ++c)
+            if (hd[c].id >= 0 && (bc == 0 || event_before(c, hd[c], bc, cur))) {
+                bc = c;
+                cur = hd[c];
+            }
+        if (bc == 0) break;
+#pragma unroll
+        for (int c = 1; c <= 7; ++c)
+            if (c == bc) {
+                ++hd[c].ptr;
+                advance_level(hd[c], c, keys, ru, c0, D, mx);
+            }
+        sd4 += 8LL * bc;
+        num += static_cast<double>(cur.a);
+        const float nf = approx_float(num);
+        const float n2 = nf * nf, sdf = __ll2float_rn(sd4);  // sd4 < 2^24: exact
+        const float lhs = n2 * best_sdf, rhs = best_n2 * sdf;
+        bool take;
+        double ip = 0.0;
+        bool exact = false;
+        if (!have || lhs > rhs * kHi) {
+            take = true;
+        } else if (lhs < rhs * kLo) {
+            take = false;
+        } else {
+            if (!best_exact) {
+                best_ip = best_num / sqrt(static_cast<double>(best_sd4) * 0.25);
+                best_exact = true;
+            }
+            ip = num / sqrt(static_cast<double>(sd4) * 0.25);
+            exact = true;
+            take = ip > best_ip;
+        }
+        if (take) {
+            have = true;
+            best_n2 = n2;
+            best_sdf = sdf;
+            best_num = num;
+            best_sd4 = sd4;
+            best_c = bc;
+            best_a = cur.a;
+            best_exact = exact;
+            best_ip = ip;
+        }
+    }
+    return have ? static_cast<double>(best_c) / static_cast<double>(best_a) : 0.0;
+}
+
+// ---- fastQuantizeAbs across the warp ----------------------------------------------------
+//
+// The same search as code_search_lane0, with the event order and the running sums formed in
+// parallel; it applies when the double sums are exact (checked per vector), else the caller
+// runs code_search_lane0.
+//
+// Structure used: the dimensions sorted by (|v| descending, index ascending) give positions p;
+// the initial code c0 is non-increasing in p (one t_start for every dimension), and the events
+// of level c are exactly the dimensions with a_p > 1e-5, c0_p < c and (c0_p = c - 1 or
+// c / a_p < 17 / max), a contiguous range [lo_c, hi_c) of positions (each condition holds on a
+// prefix or a suffix), ordered by t = c / a_p as p grows. The heap's pop order is the merge of
+// the seven ranges by (t, index).
+//
+// Exactness: every term the reference adds to num ((c0 + 0.5) a for the start, a per event) is
+// a multiple of 2^E (E: the lowest set bit over all of them) and every partial sum lies below
+// 7.5 sum(a); when that bound is below 2^(E + 53) each partial sum is a double, so the running
+// double sum equals the exact sum in any order and prefix sums may replace the sequential loop.
+// sqr_den is an integer (times 1/4) throughout.
+//
+// Each lane takes a contiguous share of the events (levels one after another, positions within
+// a level) and walks it with one pointer per other level (the events of that level ordered
+// before the current one, found by binary search once per share, then advanced), so every
+// event's num, sqr_den and rank (events before it in pop order) are known. The maximum of
+// ip = num / sqrt(sqr_den) is located in two passes: an FP32 screen of ip^2 (relative error
+// below 2^-20) gives the warp maximum, then only events within 2^-18 of it compute ip exactly
+// in double; the first (smallest rank) of the largest is the reference's best t.
+
+// exponent of the lowest set bit of a positive finite float
+__device__ __forceinline__ int low_bit_exp(float a) {
+    const FloatParts p = split_float(a);
+    return p.e + __ffsll(p.m) - 1;
+}
+
+// (c1 / a1, i1) < (c2 / a2, i2) exactly: c1 a2 against c2 a1 as exact two-float products
+// (small integer times float: the FMA error term is exact), ties by index
+__device__ __forceinline__ bool ev_before(int c1, float a1, int i1, int c2, float a2, int i2) {
+    const float x = __fmul_rn(static_cast<float>(c1), a2), xl = __fmaf_rn(static_cast<float>(c1), a2, -x);
+    const float y = __fmul_rn(static_cast<float>(c2), a1), yl = __fmaf_rn(static_cast<float>(c2), a1, -y);
+    if (x != y) return x < y;
+    if (xl != yl) return xl < yl;
+    return i1 < i2;
+}
+
+struct SortedView {
+    const unsigned long long *keys;
+    const float *ru;
+    __device__ __forceinline__ int id(int p) const { return static_cast<int>(keys[p] & 0xFFFFFFFFu); }
+    __device__ __forceinline__ float a(int p) const { return fabsf(ru[id(p)]); }
+};
+
+// sum of a over sorted positions [0, p): the block prefix plus the rest of p's block
+__device__ __forceinline__ double prefix_a(const SortedView &sv, const double *blk, int p) {
+    const int b = p >> 5;
+    double s = blk[b];
+    for (int q = b << 5; q < p; ++q) s += static_cast<double>(sv.a(q));
+    return s;
+}
+
+// Returns false (all lanes) when the sums are not exact: run code_search_lane0 instead.
+__device__ inline bool code_search_warp(const unsigned long long *keys, const float *ru, const unsigned char *c0, int D,
+                                 float mx, double *blk, int lane, double *best_t_out) {
+    const SortedView sv{keys, ru};
+    // exactness bound, the starting num and 4 sqr_den
+    int emin = 1 << 30;
+    double tot = 0.0, num0 = 0.0;
+    long long sd4 = 0;
+    for (int i = lane; i < D; i += 32) {
+        const float ai = fabsf(ru[i]);
+        const int c = c0[i];
+        if (ai > 0.0f) emin = min(emin, low_bit_exp(ai) - 1);
+        tot += static_cast<double>(ai);
+        num0 += (c + 0.5) * static_cast<double>(ai);
+        sd4 += 4LL * (c * c + c);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        emin = min(emin, __shfl_xor_sync(0xffffffffu, emin, o));
+        tot += __shfl_xor_sync(0xffffffffu, tot, o);
+        num0 += __shfl_xor_sync(0xffffffffu, num0, o);
+        sd4 += __shfl_xor_sync(0xffffffffu, sd4, o);
+    }
+    sd4 += D;
+    if (!(7.5 * tot * (1.0 + 0x1p-30) < ldexp(1.0, emin + 53))) return false;
+
+    // level ranges: lanes 0-7 count c0 >= j, lanes 8-14 count c / a < 17 / max (c = lane - 7),
+    // lane 15 counts a > 1e-5; each predicate holds on a prefix of the positions
+    int cnt = 0;
+    if (lane < 16) {
+        int lo = 0, hi = D;  // first position where the predicate fails
+        while (lo < hi) {
+            const int m = (lo + hi) >> 1;
+            const float am = sv.a(m);
+            bool pr;
+            if (lane < 8) pr = c0[sv.id(m)] >= lane;
+            else if (lane < 15) pr = am > kEpsBelowF && ratio_cmp(lane - 7, am, 17, mx) < 0;
+            else pr = am > kEpsBelowF;
+            if (pr) lo = m + 1;
+            else hi = m;
+        }
+        cnt = lo;
+    }
+    int lo_c[8], hi_c[8], off_c[9];
+    const int r = __shfl_sync(0xffffffffu, cnt, 15);
+    off_c[0] = 0;
+    off_c[1] = 0;
+    lo_c[0] = hi_c[0] = 0;
+#pragma unroll
+    for (int c = 1; c <= 7; ++c) {
+        const int ge_c = __shfl_sync(0xffffffffu, cnt, c);
+        const int ge_prev = c == 1 ? D : __shfl_sync(0xffffffffu, cnt, c - 1);
+        const int q = __shfl_sync(0xffffffffu, cnt, 7 + c);
+        lo_c[c] = ge_c;
+        int h = min(max(ge_prev, q), r);
+        hi_c[c] = h > ge_c ? h : ge_c;
+        off_c[c + 1] = off_c[c] + (hi_c[c] - lo_c[c]);
+    }
+    const int n_ev = off_c[8];
+    // block prefix sums of a over positions (exact): blk[b] = sum of a over [0, 32 b)
+    const int nblk = D >> 5;
+    for (int b = lane; b < nblk; b += 32) {
+        double sb = 0.0;
+        for (int q = b << 5; q < (b << 5) + 32; ++q) sb += static_cast<double>(sv.a(q));
+        blk[b + 1] = sb;
+    }
+    __syncwarp();
+    if (lane == 0) {
+        blk[0] = 0.0;
+        for (int b = 1; b <= nblk; ++b) blk[b] += blk[b - 1];
+    }
+    __syncwarp();
+
+    const int e_begin = static_cast<int>((static_cast<long long>(n_ev) * lane) >> 5);
+    const int e_end = static_cast<int>((static_cast<long long>(n_ev) * (lane + 1)) >> 5);
+    float qmax = 0.0f;
+    double best_ip = -1.0;
+    int best_rank = 0x7FFFFFFF, best_c = 0;
+    float best_a = 1.0f;
+    for (int pass = 0; pass < 2; ++pass) {
+        const float thr = qmax * (1.0f - 0x1p-18f);
+        for (int c = 1; c <= 7; ++c) {
+            const int s0 = max(e_begin, off_c[c]), s1 = min(e_end, off_c[c + 1]);
+            if (s0 >= s1) continue;
+            const int pa = lo_c[c] + (s0 - off_c[c]), pb = lo_c[c] + (s1 - off_c[c]);
+            // pointers into the other levels: events ordered before (c, pa)
+            int ptr[8];
+            double acc = prefix_a(sv, blk, pa) - prefix_a(sv, blk, lo_c[c]);  // level c before pa
+            const float a0 = sv.a(pa);
+            const int i0 = sv.id(pa);
+#pragma unroll
+            for (int cc = 1; cc <= 7; ++cc) {
+                ptr[cc] = lo_c[cc];
+                if (cc == c) continue;
+                int lo = lo_c[cc], hi = hi_c[cc];
+                while (lo < hi) {
+                    const int m = (lo + hi) >> 1;
+                    if (ev_before(cc, sv.a(m), sv.id(m), c, a0, i0)) lo = m + 1;
+                    else hi = m;
+                }
+                ptr[cc] = lo;
+                acc += prefix_a(sv, blk, lo) - prefix_a(sv, blk, lo_c[cc]);
+            }
+            long long wsum = 0;  // sum over levels of level * (events of that level before)
+            int rank = 0;
+#pragma unroll
+            for (int cc = 1; cc <= 7; ++cc) {
+                if (cc == c) continue;
+                wsum += static_cast<long long>(cc) * (ptr[cc] - lo_c[cc]);
+                rank += ptr[cc] - lo_c[cc];
+            }
+            for (int p = pa; p < pb; ++p) {
+                const float ap = sv.a(p);
+                const int ip_ = sv.id(p);
+#pragma unroll
+                for (int cc = 1; cc <= 7; ++cc) {
+                    if (cc == c) continue;
+                    while (ptr[cc] < hi_c[cc]) {
+                        const int m = ptr[cc];
+                        const float am = sv.a(m);
+                        if (!ev_before(cc, am, sv.id(m), c, ap, ip_)) break;
+                        acc += static_cast<double>(am);
+                        wsum += cc;
+                        ++rank;
+                        ++ptr[cc];
+                    }
+                }
+                acc += static_cast<double>(ap);
+                const int before_c = p - lo_c[c];
+                const long long ev_sd4 = sd4 + 8LL * (wsum + static_cast<long long>(c) * (before_c + 1));
+                const double num = num0 + acc;
+                const int ev_rank = rank + before_c;
+                const float nf = approx_float(num);
+                const float qv = __fdiv_rn(nf * nf, __ll2float_rn(ev_sd4));
+                if (pass == 0) {
+                    qmax = fmaxf(qmax, qv);
+                } else if (qv >= thr) {
+                    const double ipx = num / sqrt(static_cast<double>(ev_sd4) * 0.25);
+                    if (ipx > best_ip || (ipx == best_ip && ev_rank < best_rank)) {
+                        best_ip = ipx;
+                        best_rank = ev_rank;
+                        best_c = c;
+                        best_a = ap;
+                    }
+                }
+            }
+        }
+        if (pass == 0) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) qmax = fmaxf(qmax, __shfl_xor_sync(0xffffffffu, qmax, o));
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double oip = __shfl_xor_sync(0xffffffffu, best_ip, o);
+        const int orank = __shfl_xor_sync(0xffffffffu, best_rank, o);
+        const int oc = __shfl_xor_sync(0xffffffffu, best_c, o);
+        const float oa = __shfl_xor_sync(0xffffffffu, best_a, o);
+        if (oip > best_ip || (oip == best_ip && orank < best_rank)) {
+            best_ip = oip;
+            best_rank = orank;
+            best_c = oc;
+            best_a = oa;
+        }
+    }
+    *best_t_out = best_c > 0 ? static_cast<double>(best_c) / static_cast<double>(best_a) : 0.0;
+    return true;
+}
+
+}  // namespace qg

@@ -14,6 +14,7 @@
 // order, and a 7-way merge by (t, i) replays the heap's pop sequence exactly.
 #include <cstdint>
 
+#include "code_search.cuh"
 #include "exact_fp.cuh"
 #include "qg_device.cuh"
 #include "qg_kernels.h"
@@ -158,24 +159,6 @@ __device__ __forceinline__ float quant_error(float rn, float r, float long_scale
     return out;
 }
 
-__device__ void bitonic_sort_warp(unsigned long long *k, int n, int lane) {
-    for (int size = 2; size <= n; size <<= 1) {
-        for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            for (int t = lane; t < n / 2; t += 32) {
-                const int lo = 2 * t - (t & (stride - 1));
-                const int hi = lo + stride;
-                const bool asc = (lo & size) == 0;
-                const unsigned long long a = k[lo], b = k[hi];
-                if ((a > b) == asc) {
-                    k[lo] = b;
-                    k[hi] = a;
-                }
-            }
-            __syncwarp();
-        }
-    }
-}
-
 __device__ void fht_warp_local(float *x, int D, int lane) {
     for (int step = 1; step < D; step <<= 1) {
         for (int b = lane; b < D / 2; b += 32) {
@@ -187,170 +170,6 @@ __device__ void fht_warp_local(float *x, int D, int lane) {
         }
         __syncwarp();
     }
-}
-
-// The largest float not above the double 1e-5: a > 1e-5 (double) <=> a > kEpsBelowF.
-constexpr float kEpsBelowF = 9.99999974737875e-06f;
-
-// floor(RN53(t * a + 1e-5)) for t = th + tl (t a double split into two floats, a >= 0) in FP32:
-// ph + pl = th * a exactly, the rest is below 2^-16 and positive, so only the boundary above
-// can be crossed; decided unless the value lies within 2^-36 of it (`undecided`).
-__device__ __forceinline__ int floor_fma_eps(float th, float tl, float a, bool &undecided) {
-    const float ph = __fmul_rn(th, a);
-    const float pl = __fmaf_rn(th, a, -ph);
-    const float tail = __fadd_rn(__fadd_rn(__fadd_rn(pl, __fmul_rn(tl, a)), kEpsBelowF), 2.5262124e-13f);
-    const float n = floorf(ph);
-    const float d0 = __fsub_rn(ph, n);  // exact
-    int v = static_cast<int>(n);
-    if (d0 >= 0.5f) {
-        const float g = __fadd_rn(__fsub_rn(d0, 1.0f), tail);  // d0 - 1 exact for d0 >= 0.5
-        if (g > 0x1p-36f) v += 1;
-        else if (!(g < -0x1p-36f)) undecided = true;
-    } else if (!(tail > 0.0f)) {
-        undecided = true;  // cannot happen for a >= 0; keeps the decision honest
-    }
-    return v;
-}
-
-// sign of c1 / a1 - c2 / a2 for integers 1 <= c <= 17 and positive normal floats a, exactly:
-// the sign of c1 a2 - c2 a1, compared on the significands.
-__device__ __forceinline__ int ratio_cmp(int c1, float a1, int c2, float a2) {
-    const FloatParts p1 = split_float(a1), p2 = split_float(a2);
-    long long l = c1 * p2.m, r = c2 * p1.m;  // < 2^29
-    const int d = p2.e - p1.e;                 // l * 2^d against r
-    if (d > 30) return 1;
-    if (d < -30) return -1;
-    if (d > 0) l <<= d;
-    else r <<= -d;
-    return l < r ? -1 : (l > r ? 1 : 0);
-}
-
-// Truncation of a positive normal double to float (relative error below 2^-23), by bits.
-__device__ __forceinline__ float approx_float(double x) {
-    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(x));
-    const int ex = static_cast<int>((b >> 52) & 0x7FF) - 1023 + 127;
-    if (ex <= 0) return 0.0f;
-    if (ex >= 255) return __int_as_float(0x7f800000);
-    return __uint_as_float((static_cast<uint32_t>(ex) << 23) | static_cast<uint32_t>((b >> 29) & 0x7FFFFFu));
-}
-
-// Heads of the seven level lists of fastQuantizeAbs's events: the next admissible dim of each
-// level in |v| order. Dim i is an event of level c when |v_i| > 1e-5, c > c0_i and
-// (c = c0_i + 1 or c / |v_i| < 17 / max|v|).
-struct LevelHead {
-    int ptr;
-    int id;   // -1 when the level is exhausted
-    float a;  // |v_id|
-    float t;  // RN24(c / a): orders heads unless two are equal
-};
-
-__device__ __forceinline__ void advance_level(LevelHead &h, int c, const unsigned long long *keys, const float *ru,
-                                              const unsigned char *c0, int D, float mx) {
-    while (h.ptr < D) {
-        const int i = static_cast<int>(keys[h.ptr] & 0xFFFFFFFFu);
-        const float ai = fabsf(ru[i]);
-        const int ci = c0[i];
-        if (ai > kEpsBelowF && c > ci && (c == ci + 1 || ratio_cmp(c, ai, 17, mx) < 0)) {
-            h.id = i;
-            h.a = ai;
-            h.t = __fdiv_rn(static_cast<float>(c), ai);
-            return;
-        }
-        ++h.ptr;
-    }
-    h.id = -1;
-}
-
-// event (c, h) before event (b, g): t ascending, ties by dim index; the float ratios decide
-// unless equal (rounding is monotone), then the exact comparison
-__device__ __forceinline__ bool event_before(int c, const LevelHead &h, int b, const LevelHead &g) {
-    if (h.t != g.t) return h.t < g.t;
-    const int r = ratio_cmp(c, h.a, b, g.a);
-    return r < 0 || (r == 0 && h.id < g.id);
-}
-
-// fastQuantizeAbs's search over the rescale factor t (space_rabitq.h:867-942), lane 0: the
-// (t, i) events of the seven levels in heap order (t = level / |v_i|, ties by i), running
-// num and sqr_den, t at the first maximum of ip = num / sqrt(sqr_den). Event order and the t_end
-// cut are decided by ratio comparisons (distinct level / |v| ratios differ by far more than a
-// double's rounding, so they order as their doubles do); num stays a double sum. The maximum is
-// screened in FP32 on squares, (ip_k / ip_best)^2 = num_k^2 sqr_den_best / (num_best^2 sqr_den_k)
-// (within 2^-20 of the float products): an event clearly above the running best (by more than
-// 2^-17) becomes the best, one clearly below is skipped, and only events inside that band are
-// compared exactly, in double, with the best (whose exact ip is computed once).
-__device__ double code_search_lane0(const unsigned long long *keys, const float *ru, const unsigned char *c0,
-                                    int D, float mx) {
-    long long sd4 = D;  // 4 * sqr_den
-    double num = 0.0;
-    for (int i = 0; i < D; ++i) {
-        const int c = c0[i];
-        sd4 += 4LL * (c * c + c);
-        num += (c + 0.5) * static_cast<double>(fabsf(ru[i]));
-    }
-    LevelHead hd[8];
-#pragma unroll
-    for (int c = 1; c <= 7; ++c) {
-        hd[c].ptr = 0;
-        advance_level(hd[c], c, keys, ru, c0, D, mx);
-    }
-    // the best so far: its ip is > 0 for every event, the reference starts from max_ip = 0
-    bool have = false, best_exact = false;
-    float best_n2 = 0.0f, best_sdf = 1.0f;  // num^2 and 4 sqr_den of the best, in float
-    double best_num = 0.0, best_ip = 0.0;
-    long long best_sd4 = 0;
-    int best_c = 0;
-    float best_a = 1.0f;
-    constexpr float kHi = 1.0f + 0x1p-17f, kLo = 1.0f - 0x1p-17f;
-    for (;;) {
-        int bc = 0;
-        LevelHead cur{0, -1, 0.0f, 0.0f};
-#pragma unroll
-        for (int c = 1; c <= 7; ++c)
-            if (hd[c].id >= 0 && (bc == 0 || event_before(c, hd[c], bc, cur))) {
-                bc = c;
-                cur = hd[c];
-            }
-        if (bc == 0) break;
-#pragma unroll
-        for (int c = 1; c <= 7; ++c)
-            if (c == bc) {
-                ++hd[c].ptr;
-                advance_level(hd[c], c, keys, ru, c0, D, mx);
-            }
-        sd4 += 8LL * bc;
-        num += static_cast<double>(cur.a);
-        const float nf = approx_float(num);
-        const float n2 = nf * nf, sdf = __ll2float_rn(sd4);  // sd4 < 2^24: exact
-        const float lhs = n2 * best_sdf, rhs = best_n2 * sdf;
-        bool take;
-        double ip = 0.0;
-        bool exact = false;
-        if (!have || lhs > rhs * kHi) {
-            take = true;
-        } else if (lhs < rhs * kLo) {
-            take = false;
-        } else {
-            if (!best_exact) {
-                best_ip = best_num / sqrt(static_cast<double>(best_sd4) * 0.25);
-                best_exact = true;
-            }
-            ip = num / sqrt(static_cast<double>(sd4) * 0.25);
-            exact = true;
-            take = ip > best_ip;
-        }
-        if (take) {
-            have = true;
-            best_n2 = n2;
-            best_sdf = sdf;
-            best_num = num;
-            best_sd4 = sd4;
-            best_c = bc;
-            best_a = cur.a;
-            best_exact = exact;
-            best_ip = ip;
-        }
-    }
-    return have ? static_cast<double>(best_c) / static_cast<double>(best_a) : 0.0;
 }
 
 __device__ __forceinline__ void put_f32(uint8_t *dst, float v) {
@@ -432,7 +251,14 @@ __global__ void __launch_bounds__(32) encode_kernel(EncodeArgs a) {
         }
         __syncwarp();
         bitonic_sort_warp(keys, D, lane);
-        if (lane == 0) s_best_t = code_search_lane0(keys, ru, c0, D, mx);
+        double bt = 0.0;
+        const bool par = code_search_warp(keys, ru, c0, D, mx, reinterpret_cast<double *>(rcode), lane, &bt);
+        __syncwarp();
+        if (par) {
+            if (lane == 0) s_best_t = bt;
+        } else if (lane == 0) {
+            s_best_t = code_search_lane0(keys, ru, c0, D, mx);
+        }
         __syncwarp();
         const double best_t = s_best_t;
         {

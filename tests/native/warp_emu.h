@@ -47,6 +47,39 @@ T shfl_down(unsigned mask, T v, unsigned delta, int width = 32) {
     return r;
 }
 
+template <class T>
+T shfl_xor(unsigned mask, T v, int lane_mask, int width = 32) {
+    static_assert(sizeof(T) <= 8, "shuffled values are at most 8 bytes");
+    (void)mask;
+    (void)width;
+    Warp &w = *g_warp;
+    uint64_t b = 0;
+    std::memcpy(&b, &v, sizeof(T));
+    w.slot[t_lane] = b;
+    w.bar.arrive_and_wait();
+    T r;
+    std::memcpy(&r, &w.slot[t_lane ^ lane_mask], sizeof(T));
+    w.bar.arrive_and_wait();
+    return r;
+}
+
+template <class T>
+T shfl_idx(unsigned mask, T v, int src, int width = 32) {
+    static_assert(sizeof(T) <= 8, "shuffled values are at most 8 bytes");
+    (void)mask;
+    Warp &w = *g_warp;
+    uint64_t b = 0;
+    std::memcpy(&b, &v, sizeof(T));
+    w.slot[t_lane] = b;
+    w.bar.arrive_and_wait();
+    T r;
+    std::memcpy(&r, &w.slot[t_lane / width * width + src % width], sizeof(T));
+    w.bar.arrive_and_wait();
+    return r;
+}
+
+inline void syncwarp() { g_warp->bar.arrive_and_wait(); }
+
 // fn(lane) on 32 threads as one warp; returns after every lane has finished.
 inline void run_warp(const std::function<void(int)> &fn) {
     Warp w;
@@ -65,6 +98,9 @@ inline void run_warp(const std::function<void(int)> &fn) {
 }  // namespace warp_emu
 
 #define __shfl_down_sync(...) warp_emu::shfl_down(__VA_ARGS__)
+#define __shfl_xor_sync(...) warp_emu::shfl_xor(__VA_ARGS__)
+#define __shfl_sync(...) warp_emu::shfl_idx(__VA_ARGS__)
+#define __syncwarp(...) warp_emu::syncwarp()
 
 inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }
 inline float __fmul_rn(float a, float b) { return a * b; }
@@ -96,4 +132,15 @@ inline int __float_as_int(float f) {
     return i;
 }
 inline int __popc(unsigned int x) { return __builtin_popcount(x); }
+inline float __fdiv_rn(float a, float b) { return a / b; }
+inline float __ll2float_rn(long long x) { return static_cast<float>(x); }
+inline int __ffsll(long long x) { return __builtin_ffsll(x); }
+inline int __clzll(long long x) { return x == 0 ? 64 : __builtin_clzll(static_cast<unsigned long long>(x)); }
+inline long long __double_as_longlong(double d) {
+    long long x;
+    std::memcpy(&x, &d, 8);
+    return x;
+}
 using std::isfinite;
+using std::max;
+using std::min;

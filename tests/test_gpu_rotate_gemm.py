@@ -43,7 +43,8 @@ def test_rotation_gemm_within_the_fp32_accumulation_bound(cuda, dim, n):
     rot, norms = sp.rotate_gemm(torch.from_numpy(x))
     rot = rot.cpu().numpy().astype(np.float64)
     signs = sp.signs()
-    a, rn = _scaled_rows(x, center, abs(float(signs[0])))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        a, rn = _scaled_rows(x, center, abs(float(signs[0])))
     np.testing.assert_array_equal(norms.cpu().numpy(), rn)  # the encoder's own norm, bit for bit
     R = _hadamard_signs(D, dim, signs)
     exact = a.astype(np.float64) @ R.T
@@ -93,7 +94,9 @@ def test_gemm_encode_matches_the_reference_encoder_but_for_rare_boundaries(cuda)
     f_g = c_gem[:, :16].copy().view(np.float32).astype(np.float64)
     rel = np.abs(f_r - f_g) / np.maximum(np.abs(f_r), 1e-30)
     assert rel[:, 0].max() == 0.0  # norm_sqr does not depend on the rotation
-    assert np.median(rel[:, 1:]) < 1e-6 and rel[:, 1:].max() < 1e-2
+    # the tensor cores' FP32 accumulation is coarser than the butterflies' rounded adds: the other
+    # factors move by a few parts per million (a handful more where a code changes)
+    assert np.median(rel[:, 1:]) < 2e-5 and rel[:, 1:].max() < 0.2
     print(f"code mismatch rate {rate:.2e}, records equal {(c_ref == c_gem).all(1).mean():.4f}")
 
 
@@ -104,3 +107,34 @@ def test_rotation_gemm_refuses_small_code_dims(cuda):
     sp = RabitqSpace(128, np.zeros(128, np.float32))
     with pytest.raises(RuntimeError, match="QG_ERR_UNSUPPORTED"):
         sp.rotate_gemm(torch.zeros((4, 128)))
+
+
+@pytest.mark.parametrize("plane", [0, 1, 2])
+def test_rotation_gemm_is_exact_where_the_sums_are_representable(cuda, plane):
+    """Operand planes of integers times a power of two (exact in BF16) whose every partial sum
+    fits 24 bits: the GEMM must return the exact product, from any one of the three planes."""
+    torch = cuda
+    import ctypes as C
+
+    from quantization_graph_gb300 import _native as N
+    from quantization_graph_gb300.space import RabitqSpace, _stream
+
+    dim, n = 1536, 200
+    sp = RabitqSpace(dim, np.zeros(dim, np.float32))
+    D = sp.code_dim
+    kp = (dim + 63) // 64 * 64
+    rng = np.random.default_rng(plane)
+    ints = rng.integers(-127, 128, (n, dim)).astype(np.int64)
+    scale = 2.0 ** (-7 - 8 * plane)
+    a3 = np.zeros((n, 3 * kp), np.float32)
+    a3[:, plane * kp:plane * kp + dim] = (ints * scale).astype(np.float32)
+    bits = (a3.view(np.uint32) >> 16).astype(np.uint16)  # exact: 8 significant bits at most
+    assert np.array_equal((bits.astype(np.uint32) << 16).view(np.float32), a3)
+    R = _hadamard_signs(D, dim, sp.signs()).astype(np.int64)
+    want = (ints @ R.T).astype(np.float64) * scale  # |sum| < 2^18 units: exact in FP32
+    out = torch.empty((n, D), dtype=torch.float32, device="cuda")
+    d_a3 = torch.from_numpy(bits.view(np.int16)).cuda()
+    lib = N.load()
+    N.check(lib.qg_rotate_gemm_planes(sp.ptr, C.c_void_p(d_a3.data_ptr()), n, C.c_void_p(out.data_ptr()), _stream()),
+            "qg_rotate_gemm_planes")
+    np.testing.assert_array_equal(out.cpu().numpy().astype(np.float64), want)
