@@ -99,7 +99,7 @@ def run_degree(args, degree: int, test_q: np.ndarray, test_gt: np.ndarray, base:
         evals = None
     else:
         d, e, evals = build_vamana(space, compact, r=degree, l_build=args.build_beam, alpha=args.alpha, beam=1,
-                                   batch=4096, refine=args.refine_passes, cap=256, stop_hops=2)
+                                   batch=args.build_batch_size, refine=args.refine_passes, cap=256, stop_hops=2)
         deg = d.cpu().numpy().view(np.uint32)
         edges = e.cpu().numpy().view(np.uint32)
         gfile.parent.mkdir(parents=True, exist_ok=True)
@@ -191,6 +191,9 @@ def parse(argv=None):
     ap.add_argument("--refine-passes", type=int, default=2, help="03 end-to-end keeps refine 2 (run_ours.py:198-200)")
     ap.add_argument("--build-beam", type=int, default=400)
     ap.add_argument("--alpha", type=float, default=1.2)
+    ap.add_argument("--build-batch-size", type=int, default=32768,
+                    help="nodes inserted per bulk batch (the runner's default, args.rs:63); a batch's searches see "
+                         "the graph as it was at the batch start, so a batch near n gives a poor graph on small data")
     ap.add_argument("--centroid-train-samples", type=int, default=100_000)
     args = ap.parse_args(argv)
     args.degrees = [int(v) for v in args.M.split(",") if v.strip()]

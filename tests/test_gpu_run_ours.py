@@ -13,8 +13,10 @@ pytestmark = pytest.mark.gpu
 def test_run_ours_writes_rows_and_reuses_its_graph(cuda, oracle, tmp_path):
     from quantization_graph_gb300 import run_ours, runio, synthetic
 
-    X, cent = synthetic.gmm(3000, 128, components=64, sigma=0.3, seed=41)
-    Q, _ = synthetic.gmm(260, 128, sigma=0.3, seed=42, centres=cent)
+    # one connected cloud (3,000 points in 64 far-apart clusters would leave the degree-32 graph
+    # in pieces that a search from node 0 cannot reach)
+    X = synthetic.anisotropic(3000, 128, 0.8, seed=41, normalize=True)
+    Q = synthetic.anisotropic(260, 128, 0.8, seed=42, normalize=True)
     gt, _ = oracle.Oracle(128, np.zeros(128, np.float32)).exact_knn(X, Q, 100)
     data = tmp_path / "data" / "tiny"
     data.mkdir(parents=True)
@@ -24,7 +26,7 @@ def test_run_ours_writes_rows_and_reuses_its_graph(cuda, oracle, tmp_path):
     out = tmp_path / "results"
     argv = ["--dataset", "tiny", "--M", "32", "--data-root", str(tmp_path / "data"), "--out-root", str(out),
             "--val-queries", "60", "--search-list-sizes", "20,40,80", "--repeats", "2", "--refine-passes", "1",
-            "--build-beam", "100"]
+            "--build-beam", "100", "--build-batch-size", "256"]
     assert run_ours.main(argv) == 0
     graph = run_ours.graph_path(out, "tiny", 32)
     assert graph.exists()
