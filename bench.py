@@ -61,6 +61,7 @@ def parse(argv=None):
     ap.add_argument("--k", type=int, default=10)
     ap.add_argument("--target-recall", type=float, default=0.95)
     ap.add_argument("--L", type=int, default=0, help="fixed L (0 = sweep)")
+    ap.add_argument("--tile", type=int, default=0, help="search tile shape (qg_index_set_tile, 0..4)")
     ap.add_argument("--parity-queries", type=int, default=1000,
                     help="queries re-run by the CPU restatement at the headline L and compared bit for bit")
     ap.add_argument("--encode-parity-rows", type=int, default=10_000,
@@ -284,6 +285,9 @@ def build_workload(torch, args, log):
     gt, gt_info = ground_truth(torch, base, queries, args.k)
     gt_info["seconds"] = round(time.time() - t3, 2)
     index = OursIndex(space, compact, residual, msb, factors, deg, edges)
+    if args.tile:
+        from quantization_graph_gb300 import _native as N
+        N.check(N.load().qg_index_set_tile(index.handle, args.tile), "qg_index_set_tile")
     torch.cuda.empty_cache()
     log(f"setup: data {t1 - t0:.1f}s encode {t_encode:.2f}s graph {t_graph:.1f}s reachable {reach:.4f} "
         f"index {index.device_bytes() / 1e9:.2f} GB; ground truth {gt_info['certified']} certified, "
@@ -725,7 +729,7 @@ def main():
     fixed = {"L": L, "recall@10": round(rec, 4), "qps": round(nq / fixed_ms * 1000.0, 1)}
 
     # learned stop
-    search_info = {"fixed_l": fixed, "mode": "fixed-L", "L": L}
+    search_info = {"fixed_l": fixed, "mode": "fixed-L", "L": L, "tile": args.tile}
     run_learned = None
     if not args.no_learned:
         best, table, t_train, run_learned, linfo = learned_stop_select(torch, w, args, L, rec, log)
@@ -1057,7 +1061,7 @@ def run_stream(args, log):
             "config": {"workload": (f"{n} x {dim} unit-norm 16-cluster mixture (lambda_i ~ i^-1.0, centre spread = "
                                     f"within-cluster spread), M={args.M}, {nq_total} queries in {len(sizes)} batches "
                                     "(log-uniform 1..4096), k in {1,10,100}, L ~ U[20,400]"),
-                       "launch": {"warps_per_block": best[0], "blocks_per_sm": best[1] or "max",
+                       "launch": {"warps_per_block": best[0], "blocks_per_sm": best[1] or "max", "tile": best[2],
                                   "tuned": [[list(s_), round(ms, 3)] for s_, ms in tune]},
                        "mode": "fixed per-query L" if not best_mode["threshold"] else
                                f"learned stop, threshold {best_mode['threshold']}",

@@ -354,16 +354,23 @@ void record_error(const std::string &msg) { set_error(msg); }
 // Warps per block and resident blocks per SM for a pool of l_cap entries: the caller's override
 // (qg_index_set_launch) clamped to what is resident, else the candidate with the most resident
 // warps (large pools need more shared memory per warp, where smaller blocks pack better).
+// The tile shape the search launches with: the index's for the Int8 / Int4 search at code dims of
+// 1024 and more (the instantiations that have shapes), else the default.
+static int search_tile(const qg_index *index) {
+    return (space_search_mode(index->space) == 0 && index->space->code_dim >= 1024) ? index->tile : 0;
+}
+
 bool search_launch_geometry(const qg_index *index, int l_cap, bool stop_model, int *wpb_out, int *per_sm_out) {
     const int D = static_cast<int>(index->space->code_dim);
+    const int tile = search_tile(index);
     int wpb = 0, per_sm = 0;
     if (index->launch_wpb > 0) {
         wpb = index->launch_wpb;
-        per_sm = search_blocks_per_sm(D, l_cap, wpb, stop_model);
+        per_sm = search_blocks_per_sm(D, l_cap, wpb, stop_model, tile);
         if (index->launch_per_sm > 0 && index->launch_per_sm < per_sm) per_sm = index->launch_per_sm;
     } else {
         for (int cand : {8, 4, 2}) {
-            const int b = search_blocks_per_sm(D, l_cap, cand, stop_model);
+            const int b = search_blocks_per_sm(D, l_cap, cand, stop_model, tile);
             if (b * cand > per_sm * wpb) {
                 wpb = cand;
                 per_sm = b;
@@ -416,6 +423,7 @@ int search_args_fill(const qg_index *index, size_t nq, const qg_search_params *p
     a.k_stride = k_max;
     a.l_cap = l_cap;
     a.beam_width = params->beam_width;
+    a.tile = search_tile(index);
     a.eps = params->epsilon0;
     a.rerank = params->rerank_candidates;
     a.early_stop_hops = params->early_stop_hops;
@@ -1616,6 +1624,15 @@ int qg_index_set_launch(qg_index *index, int warps_per_block, int blocks_per_sm)
     if (!index || warps_per_block < 0 || warps_per_block > 8 || blocks_per_sm < 0) return QG_ERR_INVALID;
     index->launch_wpb = warps_per_block;
     index->launch_per_sm = blocks_per_sm;
+    return QG_OK;
+}
+
+int qg_index_set_tile(qg_index *index, int tile) {
+    if (!index || tile < 0 || tile > 4) {
+        set_error("tile shape must be 0..4");
+        return QG_ERR_INVALID;
+    }
+    index->tile = tile;
     return QG_OK;
 }
 

@@ -1,12 +1,14 @@
 // code_search.cuh -- fastQuantizeAbs (space_rabitq.h:867-942) for one vector held by one warp:
 // the search over the rescale factor t that the encoder runs on every rotated residual. Two
-// forms give the same t bit for bit: code_search_warp (all lanes; exact when the vector's double
-// sums are, which it checks) and code_search_lane0 (one lane, any vector). Shared by the encode
-// kernel and the host harness that runs them under a warp emulator (tests/native).
+// forms give the same t bit for bit: code_search_warp (all lanes; for the vectors whose double
+// sums are exact, which exact_sum_unit decides) and code_search_lane0 (one lane, any vector).
+// Shared by the encode kernel and the host harness that runs them under a warp emulator
+// (tests/native).
 //
 // Inputs, in shared memory: keys[D] = the dimensions sorted by (|v| descending, index ascending),
-// as (~bits(|v|) << 32 | index); ru[D] the rotated values; c0[D] the initial codes
-// floor(t_start |v| + 1e-5) (at most 2, t_start = 2 / max|v|); mx = max|v|.
+// as (~bits(|v|) << 32 | index), which carry every |v| the search reads; c0[D] the initial codes
+// floor(t_start |v| + 1e-5) (at most 2, t_start = 2 / max|v|); mx = max|v|. The rotated values
+// themselves are read only before the keys are built (lane0_num_start, exact_sum_unit).
 #pragma once
 
 #include <cmath>
@@ -92,11 +94,12 @@ struct LevelHead {
     float t;  // RN24(c / a): orders heads unless two are equal
 };
 
-__device__ __forceinline__ void advance_level(LevelHead &h, int c, const unsigned long long *keys, const float *ru,
+__device__ __forceinline__ void advance_level(LevelHead &h, int c, const unsigned long long *keys,
                                               const unsigned char *c0, int D, float mx) {
     while (h.ptr < D) {
-        const int i = static_cast<int>(keys[h.ptr] & 0xFFFFFFFFu);
-        const float ai = fabsf(ru[i]);
+        const unsigned long long k = keys[h.ptr];
+        const int i = static_cast<int>(k & 0xFFFFFFFFu);
+        const float ai = __uint_as_float(0xFFFFFFFFu - static_cast<uint32_t>(k >> 32));
         const int ci = c0[i];
         if (ai > kEpsBelowF && c > ci && (c == ci + 1 || ratio_cmp(c, ai, 17, mx) < 0)) {
             h.id = i;
@@ -126,20 +129,27 @@ __device__ __forceinline__ bool event_before(int c, const LevelHead &h, int b, c
 // (within 2^-20 of the float products): an event clearly above the running best (by more than
 // 2^-17) becomes the best, one clearly below is skipped, and only events inside that band are
 // compared exactly, in double, with the best (whose exact ip is computed once).
-__device__ inline double code_search_lane0(const unsigned long long *keys, const float *ru, const unsigned char *c0,
-                                    int D, float mx) {
-    long long sd4 = D;  // 4 * sqr_den
+// The reference's starting num, sum of (c0_i + 0.5) |v_i| in dimension order in double (one lane).
+__device__ inline double lane0_num_start(const float *ru, const unsigned char *c0, int D) {
     double num = 0.0;
+    for (int i = 0; i < D; ++i) num += (c0[i] + 0.5) * static_cast<double>(fabsf(ru[i]));
+    return num;
+}
+
+// num_start: lane0_num_start of the vector.
+__device__ inline double code_search_lane0(const unsigned long long *keys, const unsigned char *c0, int D, float mx,
+                                           double num_start) {
+    long long sd4 = D;  // 4 * sqr_den
+    double num = num_start;
     for (int i = 0; i < D; ++i) {
         const int c = c0[i];
         sd4 += 4LL * (c * c + c);
-        num += (c + 0.5) * static_cast<double>(fabsf(ru[i]));
     }
     LevelHead hd[8];
 #pragma unroll
     for (int c = 1; c <= 7; ++c) {
         hd[c].ptr = 0;
-        advance_level(hd[c], c, keys, ru, c0, D, mx);
+        advance_level(hd[c], c, keys, c0, D, mx);
     }
     // the best so far: its ip is > 0 for every event, the reference starts from max_ip = 0
     bool have = false, best_exact = false;
@@ -163,7 +173,7 @@ __device__ inline double code_search_lane0(const unsigned long long *keys, const
         for (int c = 1; c <= 7; ++c)
             if (c == bc) {
                 ++hd[c].ptr;
-                advance_level(hd[c], c, keys, ru, c0, D, mx);
+                advance_level(hd[c], c, keys, c0, D, mx);
             }
         sd4 += 8LL * bc;
         num += static_cast<double>(cur.a);
@@ -218,15 +228,18 @@ __device__ inline double code_search_lane0(const unsigned long long *keys, const
 // a multiple of 2^E (E: the lowest set bit over all of them) and every partial sum lies below
 // 7.5 sum(a); when that bound is below 2^(E + 53) each partial sum is a double, so the running
 // double sum equals the exact sum in any order and prefix sums may replace the sequential loop.
-// sqr_den is an integer (times 1/4) throughout.
+// The sums are then kept as int64 multiples of 2^E (exact, and on the integer pipe: this part's
+// FP64 pipe is narrow). sqr_den is an integer (times 1/4) throughout.
 //
 // Each lane takes a contiguous share of the events (levels one after another, positions within
 // a level) and walks it with one pointer per other level (the events of that level ordered
-// before the current one, found by binary search once per share, then advanced), so every
-// event's num, sqr_den and rank (events before it in pop order) are known. The maximum of
-// ip = num / sqrt(sqr_den) is located in two passes: an FP32 screen of ip^2 (relative error
-// below 2^-20) gives the warp maximum, then only events within 2^-18 of it compute ip exactly
-// in double; the first (smallest rank) of the largest is the reference's best t.
+// before the current one, found by binary search once per level segment, then advanced), so
+// every event's num, sqr_den and rank (events before it in pop order) are known. Each lane keeps
+// its best event under an FP32 screen of ip^2 (relative error below 2^-20); events within 2^-17
+// of the running best are ordered by the exact integer cross products (ip_sq_order), and only
+// near-ties within 2^-33 compute ip = num / sqrt(sqr_den) in double as the reference does. The
+// lanes' bests are then compared exactly, and the first (smallest rank) of the largest is the
+// reference's t.
 
 // exponent of the lowest set bit of a positive finite float
 __device__ __forceinline__ int low_bit_exp(float a) {
@@ -244,46 +257,99 @@ __device__ __forceinline__ bool ev_before(int c1, float a1, int i1, int c2, floa
     return i1 < i2;
 }
 
+// the sorted keys hold ~bits(|v|) in the high word and the dimension in the low word
+__device__ __forceinline__ float key_a(unsigned long long k) {
+    return __uint_as_float(0xFFFFFFFFu - static_cast<uint32_t>(k >> 32));
+}
+__device__ __forceinline__ int key_id(unsigned long long k) { return static_cast<int>(k & 0xFFFFFFFFu); }
+
 struct SortedView {
     const unsigned long long *keys;
-    const float *ru;
-    __device__ __forceinline__ int id(int p) const { return static_cast<int>(keys[p] & 0xFFFFFFFFu); }
-    __device__ __forceinline__ float a(int p) const { return fabsf(ru[id(p)]); }
+    __device__ __forceinline__ int id(int p) const { return key_id(keys[p]); }
+    __device__ __forceinline__ float a(int p) const { return key_a(keys[p]); }
 };
 
-// sum of a over sorted positions [0, p): the block prefix plus the rest of p's block
-__device__ __forceinline__ double prefix_a(const SortedView &sv, const double *blk, int p) {
-    const int b = p >> 5;
-    double s = blk[b];
-    for (int q = b << 5; q < p; ++q) s += static_cast<double>(sv.a(q));
-    return s;
+// a (>= 0, a multiple of 2^E) as an integer count of 2^E: exact (E is at most a's lowest set bit)
+__device__ __forceinline__ long long units(float a, int E) {
+    const FloatParts p = split_float(a);
+    const int sh = p.e - E;
+    return sh >= 0 ? (p.m << sh) : (p.m >> -sh);
 }
 
-// Returns false (all lanes) when the sums are not exact: run code_search_lane0 instead.
-__device__ inline bool code_search_warp(const unsigned long long *keys, const float *ru, const unsigned char *c0, int D,
-                                 float mx, double *blk, int lane, double *best_t_out) {
-    const SortedView sv{keys, ru};
-    // exactness bound, the starting num and 4 sqr_den
+// 2^e as a float, for -126 <= e <= 127; as a double, for -1022 <= e <= 1023
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); }
+__device__ __forceinline__ double pow2d(int e) { return __longlong_as_double(static_cast<long long>(e + 1023) << 52); }
+
+// The exactness test above for the vector ru[0, D) (all lanes; the same answer in each): E = the
+// lowest set bit over the nonzero |v| minus one, and whether 7.5 sum|v| < 2^(E + 53) (sum in FP32
+// with a margin far above its rounding). Every double sum the encoder forms from (c + 0.5) |v|,
+// |v| or |v| / 2 is then exact in any order.
+__device__ inline bool exact_sum_unit(const float *ru, int D, int lane, int *E_out) {
     int emin = 1 << 30;
-    double tot = 0.0, num0 = 0.0;
-    long long sd4 = 0;
+    float tot = 0.0f;
     for (int i = lane; i < D; i += 32) {
         const float ai = fabsf(ru[i]);
-        const int c = c0[i];
         if (ai > 0.0f) emin = min(emin, low_bit_exp(ai) - 1);
-        tot += static_cast<double>(ai);
-        num0 += (c + 0.5) * static_cast<double>(ai);
-        sd4 += 4LL * (c * c + c);
+        tot += ai;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         emin = min(emin, __shfl_xor_sync(0xffffffffu, emin, o));
         tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    }
+    *E_out = emin;
+    if (emin < -120 || emin + 53 > 120 || !(tot < 0x1p40f)) return false;
+    return 7.5f * tot * 1.001f < pow2f(emin + 53);
+}
+
+// Order of num1^2 / sd1 against num2^2 / sd2 (the squared ips of two events; num < 2^53 and
+// 0 < sd < 2^24 integers): +1 or -1 when they differ by more than 2^-33 relative, else 0. The nums
+// keep their top 40 bits (exact below 2^40; truncation error under 2^-36 relative when the
+// smaller keeps at least 2^36, else 0 is returned), and the cross products a1^2 sd2 and a2^2 sd1
+// (below 2^104) are compared exactly in 128 bits with a 2^-32 margin.
+__device__ __forceinline__ int ip_sq_order(long long num1, long long sd1, long long num2, long long sd2) {
+    const unsigned long long n1 = static_cast<unsigned long long>(num1), n2 = static_cast<unsigned long long>(num2);
+    const unsigned long long big = n1 > n2 ? n1 : n2;
+    const int s = max(0, 64 - __clzll(static_cast<long long>(big)) - 40);
+    const unsigned long long a1 = n1 >> s, a2 = n2 >> s;
+    if (s > 0 && (a1 < (1ull << 36) || a2 < (1ull << 36))) return 0;
+    const unsigned __int128 x = static_cast<unsigned __int128>(a1) * a1 * static_cast<unsigned long long>(sd2);
+    const unsigned __int128 y = static_cast<unsigned __int128>(a2) * a2 * static_cast<unsigned long long>(sd1);
+    if (x > y + (y >> 32)) return 1;
+    if (y > x + (x >> 32)) return -1;
+    return 0;
+}
+
+// sum of a over sorted positions [0, p), in units of 2^E: the block prefix plus the rest of p's block
+__device__ __forceinline__ long long prefix_a(const SortedView &sv, const long long *blk, int p, int E) {
+    const int b = p >> 5;
+    long long s = blk[b];
+    for (int q = b << 5; q < p; ++q) s += units(sv.a(q), E);
+    return s;
+}
+
+// Call only when exact_sum_unit returned true (E its unit); blk holds D / 32 + 1 int64.
+__device__ inline void code_search_warp(const unsigned long long *keys, const unsigned char *c0, int D, float mx,
+                                        long long *blk, int E, int lane, double *best_t_out) {
+    const SortedView sv{keys};
+    // the starting num (in units of 2^E; (c + 0.5) a = (2c + 1) (a / 2), a / 2 a whole number of
+    // units) and 4 sqr_den, over the sorted positions (integer sums: any order)
+    long long num0 = 0;
+    long long sd4 = 0;
+    for (int p = lane; p < D; p += 32) {
+        const unsigned long long k = keys[p];
+        const int c = c0[key_id(k)];
+        num0 += static_cast<long long>(2 * c + 1) * (units(key_a(k), E) >> 1);
+        sd4 += 4LL * (c * c + c);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
         num0 += __shfl_xor_sync(0xffffffffu, num0, o);
         sd4 += __shfl_xor_sync(0xffffffffu, sd4, o);
     }
     sd4 += D;
-    if (!(7.5 * tot * (1.0 + 0x1p-30) < ldexp(1.0, emin + 53))) return false;
+    const float unit_f = pow2f(E);
+    const double unit_d = pow2d(E);
 
     // level ranges: lanes 0-7 count c0 >= j, lanes 8-14 count c / a < 17 / max (c = lane - 7),
     // lane 15 counts a > 1e-5; each predicate holds on a prefix of the positions
@@ -318,99 +384,133 @@ __device__ inline bool code_search_warp(const unsigned long long *keys, const fl
         off_c[c + 1] = off_c[c] + (hi_c[c] - lo_c[c]);
     }
     const int n_ev = off_c[8];
-    // block prefix sums of a over positions (exact): blk[b] = sum of a over [0, 32 b)
+    // block prefix sums of a over positions (exact, units of 2^E): blk[b] = sum over [0, 32 b)
     const int nblk = D >> 5;
     for (int b = lane; b < nblk; b += 32) {
-        double sb = 0.0;
-        for (int q = b << 5; q < (b << 5) + 32; ++q) sb += static_cast<double>(sv.a(q));
+        long long sb = 0;
+        for (int q = b << 5; q < (b << 5) + 32; ++q) sb += units(sv.a(q), E);
         blk[b + 1] = sb;
     }
     __syncwarp();
     if (lane == 0) {
-        blk[0] = 0.0;
+        blk[0] = 0;
         for (int b = 1; b <= nblk; ++b) blk[b] += blk[b - 1];
     }
     __syncwarp();
 
     const int e_begin = static_cast<int>((static_cast<long long>(n_ev) * lane) >> 5);
     const int e_end = static_cast<int>((static_cast<long long>(n_ev) * (lane + 1)) >> 5);
-    float qmax = 0.0f;
+    // the lane's best event: screened in FP32 on ip^2 as in code_search_lane0 (an event clearly
+    // above the best takes it, one clearly below is skipped, one inside the 2^-17 band is compared
+    // exactly), ties on the exact ip broken by rank (the reference keeps the first maximum)
+    constexpr float kHi = 1.0f + 0x1p-17f, kLo = 1.0f - 0x1p-17f;
+    bool have = false, best_exact = false;
+    float best_n2 = 0.0f, best_sdf = 1.0f;
+    long long best_num = 0, best_sd4 = 1;
     double best_ip = -1.0;
     int best_rank = 0x7FFFFFFF, best_c = 0;
     float best_a = 1.0f;
-    for (int pass = 0; pass < 2; ++pass) {
-        const float thr = qmax * (1.0f - 0x1p-18f);
-        for (int c = 1; c <= 7; ++c) {
-            const int s0 = max(e_begin, off_c[c]), s1 = min(e_end, off_c[c + 1]);
-            if (s0 >= s1) continue;
-            const int pa = lo_c[c] + (s0 - off_c[c]), pb = lo_c[c] + (s1 - off_c[c]);
-            // pointers into the other levels: events ordered before (c, pa)
-            int ptr[8];
-            double acc = prefix_a(sv, blk, pa) - prefix_a(sv, blk, lo_c[c]);  // level c before pa
-            const float a0 = sv.a(pa);
-            const int i0 = sv.id(pa);
+    // the lane's share as segments of one level each; the level is a run-time value, so every
+    // lane runs the same instructions whatever level its share lies in
+    for (int e = e_begin; e < e_end;) {
+        int c = 0, clo = 0, coff = 0, cend = 0;
+#pragma unroll
+        for (int cc = 1; cc <= 7; ++cc)
+            if (e >= off_c[cc] && e < off_c[cc + 1]) {
+                c = cc;
+                clo = lo_c[cc];
+                coff = off_c[cc];
+                cend = off_c[cc + 1];
+            }
+        const int s1 = min(e_end, cend);
+        const int pa = clo + (e - coff), pb = clo + (s1 - coff);
+        // pointers into the other levels: events ordered before (c, pa)
+        int ptr[8];
+        long long acc = prefix_a(sv, blk, pa, E) - prefix_a(sv, blk, clo, E);  // level c before pa
+        long long wsum = 0;  // sum over levels of level * (events of that level before)
+        int rank = 0;
+        {
+            const unsigned long long k0 = keys[pa];
+            const float a0 = key_a(k0);
+            const int i0 = key_id(k0);
 #pragma unroll
             for (int cc = 1; cc <= 7; ++cc) {
-                ptr[cc] = lo_c[cc];
-                if (cc == c) continue;
-                int lo = lo_c[cc], hi = hi_c[cc];
-                while (lo < hi) {
-                    const int m = (lo + hi) >> 1;
-                    if (ev_before(cc, sv.a(m), sv.id(m), c, a0, i0)) lo = m + 1;
-                    else hi = m;
+                int lo = lo_c[cc];
+                if (cc != c) {
+                    int hi = hi_c[cc];
+                    while (lo < hi) {
+                        const int m = (lo + hi) >> 1;
+                        const unsigned long long km = keys[m];
+                        if (ev_before(cc, key_a(km), key_id(km), c, a0, i0)) lo = m + 1;
+                        else hi = m;
+                    }
+                    acc += prefix_a(sv, blk, lo, E) - prefix_a(sv, blk, lo_c[cc], E);
+                    wsum += static_cast<long long>(cc) * (lo - lo_c[cc]);
+                    rank += lo - lo_c[cc];
                 }
                 ptr[cc] = lo;
-                acc += prefix_a(sv, blk, lo) - prefix_a(sv, blk, lo_c[cc]);
             }
-            long long wsum = 0;  // sum over levels of level * (events of that level before)
-            int rank = 0;
+        }
+        for (int p = pa; p < pb; ++p) {
+            const unsigned long long kp = keys[p];
+            const float ap = key_a(kp);
+            const int idp = key_id(kp);
 #pragma unroll
             for (int cc = 1; cc <= 7; ++cc) {
                 if (cc == c) continue;
-                wsum += static_cast<long long>(cc) * (ptr[cc] - lo_c[cc]);
-                rank += ptr[cc] - lo_c[cc];
-            }
-            for (int p = pa; p < pb; ++p) {
-                const float ap = sv.a(p);
-                const int ip_ = sv.id(p);
-#pragma unroll
-                for (int cc = 1; cc <= 7; ++cc) {
-                    if (cc == c) continue;
-                    while (ptr[cc] < hi_c[cc]) {
-                        const int m = ptr[cc];
-                        const float am = sv.a(m);
-                        if (!ev_before(cc, am, sv.id(m), c, ap, ip_)) break;
-                        acc += static_cast<double>(am);
-                        wsum += cc;
-                        ++rank;
-                        ++ptr[cc];
-                    }
-                }
-                acc += static_cast<double>(ap);
-                const int before_c = p - lo_c[c];
-                const long long ev_sd4 = sd4 + 8LL * (wsum + static_cast<long long>(c) * (before_c + 1));
-                const double num = num0 + acc;
-                const int ev_rank = rank + before_c;
-                const float nf = approx_float(num);
-                const float qv = __fdiv_rn(nf * nf, __ll2float_rn(ev_sd4));
-                if (pass == 0) {
-                    qmax = fmaxf(qmax, qv);
-                } else if (qv >= thr) {
-                    const double ipx = num / sqrt(static_cast<double>(ev_sd4) * 0.25);
-                    if (ipx > best_ip || (ipx == best_ip && ev_rank < best_rank)) {
-                        best_ip = ipx;
-                        best_rank = ev_rank;
-                        best_c = c;
-                        best_a = ap;
-                    }
+                while (ptr[cc] < hi_c[cc]) {
+                    const unsigned long long km = keys[ptr[cc]];
+                    const float am = key_a(km);
+                    if (!ev_before(cc, am, key_id(km), c, ap, idp)) break;
+                    acc += units(am, E);
+                    wsum += cc;
+                    ++rank;
+                    ++ptr[cc];
                 }
             }
+            acc += units(ap, E);
+            const int before_c = p - clo;
+            const long long ev_sd4 = sd4 + 8LL * (wsum + static_cast<long long>(c) * (before_c + 1));
+            const long long num = num0 + acc;  // units of 2^E, below 2^53
+            const int ev_rank = rank + before_c;
+            const float nf = __ll2float_rz(num) * unit_f;  // truncated: relative error below 2^-23
+            const float n2 = nf * nf, sdf = __ll2float_rn(ev_sd4);  // ev_sd4 < 2^24: exact
+            const float lhs = n2 * best_sdf, rhs = best_n2 * sdf;
+            bool take;
+            double ip = 0.0;
+            bool exact = false;
+            if (!have || lhs > rhs * kHi) {
+                take = true;
+            } else if (lhs < rhs * kLo) {
+                take = false;
+            } else if (const int o = ip_sq_order(num, ev_sd4, best_num, best_sd4); o != 0) {
+                take = o > 0;  // the doubles order as the exact values do
+            } else {
+                if (!best_exact) {
+                    best_ip = (__ll2double_rn(best_num) * unit_d) / sqrt(static_cast<double>(best_sd4) * 0.25);
+                    best_exact = true;
+                }
+                ip = (__ll2double_rn(num) * unit_d) / sqrt(static_cast<double>(ev_sd4) * 0.25);
+                exact = true;
+                take = ip > best_ip || (ip == best_ip && ev_rank < best_rank);
+            }
+            if (take) {
+                have = true;
+                best_n2 = n2;
+                best_sdf = sdf;
+                best_num = num;
+                best_sd4 = ev_sd4;
+                best_rank = ev_rank;
+                best_c = c;
+                best_a = ap;
+                best_exact = exact;
+                best_ip = ip;
+            }
         }
-        if (pass == 0) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) qmax = fmaxf(qmax, __shfl_xor_sync(0xffffffffu, qmax, o));
-        }
+        e = s1;
     }
+    if (have && !best_exact)
+        best_ip = (__ll2double_rn(best_num) * unit_d) / sqrt(static_cast<double>(best_sd4) * 0.25);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const double oip = __shfl_xor_sync(0xffffffffu, best_ip, o);
@@ -425,7 +525,6 @@ __device__ inline bool code_search_warp(const unsigned long long *keys, const fl
         }
     }
     *best_t_out = best_c > 0 ? static_cast<double>(best_c) / static_cast<double>(best_a) : 0.0;
-    return true;
 }
 
 }  // namespace qg

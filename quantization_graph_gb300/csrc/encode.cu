@@ -2,10 +2,11 @@
 // space_rabitq.h:5845-5999, one centroid) writing compact and residual records in the
 // reference layouts (copyCompactPayloadFromFull / copyResidualRecordFromFull, :6005-6029).
 //
-// One warp per vector. Parallel parts (rotation, code search set-up, block scales) use all
-// lanes; every floating-point accumulation whose rounding depends on order (the reference
-// accumulates sequentially) runs in one lane in the reference order, so codes and factors
-// are bit-identical to the reference.
+// One warp per vector, codes and factors bit-identical to the reference. The reference
+// accumulates its floating-point sums sequentially; here a sum is formed across the lanes only
+// where the result provably equals the sequential one (exact in fixed point: multiples of 2^E
+// whose partial sums fit 53 bits; or a float decided within a rigorous bound on the sequential
+// rounding), otherwise one lane runs it in the reference order.
 //
 // fastQuantizeAbs (:867-942) pops (t, i) events from a min-heap; the pop order equals the
 // ascending (t, i) order of all events, since every pushed event of a dimension is larger
@@ -180,41 +181,31 @@ __device__ __forceinline__ void put_f32(uint8_t *dst, float v) {
     dst[3] = b >> 24;
 }
 
-// kRotated: the rotation was done elsewhere (the tensor-core GEMM, rotate_gemm.cu); row v of
-// a.rotated holds it and a.norms[v] the residual norm.
-template <bool kRotated>
-__global__ void __launch_bounds__(32) encode_kernel(EncodeArgs a) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const int D = a.code_dim, dim = a.dim, lane = threadIdx.x;
-    unsigned long long *keys = reinterpret_cast<unsigned long long *>(smem);   // [D]
-    float *ru = reinterpret_cast<float *>(keys + D);                            // [D]
-    unsigned char *c0 = reinterpret_cast<unsigned char *>(ru + D);              // [D] initial code / final magnitude
-    signed char *rcode = reinterpret_cast<signed char *>(c0 + D);               // [D]
-    float *qerr = reinterpret_cast<float *>(keys);                              // reuses keys after the scan
-    __shared__ float s_rn;
-    __shared__ double s_best_t, s_num2;
-    __shared__ float s_sc[128];  // stored block scales (D/16 <= 128)
-
-    const int v = blockIdx.x;
-    if (v >= a.n) return;
-    float rn;
+// The rotated residual of row v into ru[0, D): the residual, its norm (a sequential float sum of
+// r * r, no contraction, space_rabitq.h:5856-5860; written to *rn_out when kNorm), normalised,
+// times the random signs, then the Hadamard transform. kRotated: the rotation was done elsewhere
+// (the tensor-core GEMM, rotate_gemm.cu); row v of a.rotated holds it and a.norms[v] the norm.
+template <bool kRotated, bool kNorm>
+__device__ void rotated_row(const EncodeArgs &a, int v, float *ru, int lane, float *s_rn, float rn_known) {
+    const int D = a.code_dim, dim = a.dim;
     if constexpr (kRotated) {
         const float *rot = a.rotated + static_cast<size_t>(v) * D;
         for (int i = lane; i < D; i += 32) ru[i] = rot[i];
-        rn = a.norms[v];
+        if (kNorm && lane == 0) *s_rn = a.norms[v];
         __syncwarp();
     } else {
         const float *raw = a.raw + static_cast<size_t>(v) * a.raw_stride;
-        // residual and its norm: sequential float sum of r*r (no contraction, space_rabitq.h:5856-5860)
         for (int i = lane; i < D; i += 32) ru[i] = i < dim ? raw[i] - a.center[i] : 0.0f;
         __syncwarp();
-        if (lane == 0) {
-            float rns = 0.0f;
-            for (int i = 0; i < dim; ++i) rns = rns + ru[i] * ru[i];
-            s_rn = sqrtf(rns);
+        if constexpr (kNorm) {
+            if (lane == 0) {
+                float rns = 0.0f;
+                for (int i = 0; i < dim; ++i) rns = rns + ru[i] * ru[i];
+                *s_rn = sqrtf(rns);
+            }
+            __syncwarp();
         }
-        __syncwarp();
-        rn = s_rn;
+        const float rn = kNorm ? *s_rn : rn_known;
         if (rn > 0.0f) {
             const float inv = 1.0f / rn;
             for (int i = lane; i < dim; i += 32) ru[i] = ru[i] * inv;
@@ -224,6 +215,34 @@ __global__ void __launch_bounds__(32) encode_kernel(EncodeArgs a) {
         __syncwarp();
         fht_warp_local(ru, D, lane);
     }
+}
+
+// Shared memory, 10 bytes per dimension: an 8D-byte region that holds the rotated row (floats
+// [0, D)) until the sort keys are built over it in place, the keys through the code search, then
+// the rotated row again (re-derived from the input) and the quantisation errors (floats [D, 2D));
+// the codes c0[D]; the residual codes rcode[D] (the code search's block prefix sums before them).
+template <bool kRotated>
+__global__ void __launch_bounds__(32) encode_kernel(EncodeArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int D = a.code_dim, lane = threadIdx.x;
+    unsigned long long *keys = reinterpret_cast<unsigned long long *>(smem);   // [D]
+    float *ru = reinterpret_cast<float *>(smem);                                // [D], outside the keys' lifetime
+    float *qerr = ru + D;                                                       // [D], after the keys
+    unsigned char *c0 = smem + 8 * static_cast<size_t>(D);                      // [D] initial code / final magnitude
+    signed char *rcode = reinterpret_cast<signed char *>(c0 + D);               // [D]
+    __shared__ float s_rn;
+    __shared__ double s_best_t, s_num2, s_num_start;
+    __shared__ float s_sc[128];  // stored block scales (D/16 <= 128)
+
+    const int v = blockIdx.x;
+    if (v >= a.n) return;
+    rotated_row<kRotated, true>(a, v, ru, lane, &s_rn, 0.0f);
+    const float rn = s_rn;
+
+    // whether the encoder's double sums over |v| are exact in any order, and their unit 2^E
+    int E = 0;
+    const bool exact = exact_sum_unit(ru, D, lane, &E);
+    long long *lblk = reinterpret_cast<long long *>(rcode);  // scratch until the residual codes
 
     // ---- fastQuantizeAbs ----
     float mx = 0.0f;
@@ -231,8 +250,8 @@ __global__ void __launch_bounds__(32) encode_kernel(EncodeArgs a) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     const double max_o = static_cast<double>(mx);
-    float ip_norm = 1.0f;
-    if (!(mx > kEpsBelowF)) {  // max_o <= kEps
+    const bool search = mx > kEpsBelowF;  // else max_o <= kEps: every code is 0
+    if (!search) {
         for (int i = lane; i < D; i += 32) c0[i] = 0;
     } else {
         const double t_start = 2.0 / max_o;  // t_end = 17 / max_o is applied as an exact ratio test
@@ -245,35 +264,60 @@ __global__ void __launch_bounds__(32) encode_kernel(EncodeArgs a) {
                 int c = floor_fma_eps(th, tl, ai, und);
                 if (und) c = static_cast<int>(__fma_rn(t_start, static_cast<double>(ai), kEps));
                 c0[i] = static_cast<unsigned char>(min(c, 7));
-                keys[i] = (static_cast<unsigned long long>(0xFFFFFFFFu - __float_as_uint(ai)) << 32) |
-                          static_cast<unsigned int>(i);
             }
         }
         __syncwarp();
-        bitonic_sort_warp(keys, D, lane);
-        double bt = 0.0;
-        const bool par = code_search_warp(keys, ru, c0, D, mx, reinterpret_cast<double *>(rcode), lane, &bt);
+        if (!exact && lane == 0) s_num_start = lane0_num_start(ru, c0, D);
+        // the keys over the rotated row in place, from the top: chunk [j, j + 32) is read before
+        // it is written, and its keys cover floats [2j, 2j + 64), none of them below j
+        for (int base = D - 32; base >= 0; base -= 32) {
+            const int j = base + lane;
+            const float aj = fabsf(ru[j]);
+            __syncwarp();
+            keys[j] = (static_cast<unsigned long long>(0xFFFFFFFFu - __float_as_uint(aj)) << 32) |
+                      static_cast<unsigned int>(j);
+        }
         __syncwarp();
-        if (par) {
+        bitonic_sort_warp(keys, D, lane);
+        if (exact) {
+            double bt = 0.0;
+            code_search_warp(keys, c0, D, mx, lblk, E, lane, &bt);
             if (lane == 0) s_best_t = bt;
         } else if (lane == 0) {
-            s_best_t = code_search_lane0(keys, ru, c0, D, mx);
+            s_best_t = code_search_lane0(keys, c0, D, mx, s_num_start);
         }
         __syncwarp();
         const double best_t = s_best_t;
         {
             const float th = __double2float_rn(best_t);
             const float tl = __double2float_rn(best_t - static_cast<double>(th));
-            for (int i = lane; i < D; i += 32) {
-                const float ai = fabsf(ru[i]);
+            for (int p = lane; p < D; p += 32) {
+                const unsigned long long k = keys[p];
+                const float ai = key_a(k);
                 bool und = false;
                 int c = floor_fma_eps(th, tl, ai, und);
                 if (und) c = static_cast<int>(__fma_rn(best_t, static_cast<double>(ai), kEps));
-                c0[i] = static_cast<unsigned char>(min(c, 7));
+                c0[key_id(k)] = static_cast<unsigned char>(min(c, 7));
             }
         }
         __syncwarp();
-        if (lane == 0) {
+        if (exact) {  // the same exact sum, across the lanes in units of 2^E
+            long long k = 0;
+            for (int p = lane; p < D; p += 32) {
+                const unsigned long long kp = keys[p];
+                k += static_cast<long long>(2 * c0[key_id(kp)] + 1) * (units(key_a(kp), E) >> 1);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+            if (lane == 0) s_num2 = __ll2double_rn(k) * pow2d(E);
+        }
+        __syncwarp();
+    }
+    // the rotated row again, over the keys (the same operations give the same floats)
+    rotated_row<kRotated, false>(a, v, ru, lane, &s_rn, rn);
+    float ip_norm = 1.0f;
+    if (search) {
+        if (!exact && lane == 0) {
             double num = 0.0;
             for (int i = 0; i < D; ++i) num += (c0[i] + 0.5) * static_cast<double>(fabsf(ru[i]));
             s_num2 = num;
@@ -298,29 +342,62 @@ __global__ void __launch_bounds__(32) encode_kernel(EncodeArgs a) {
     }
     if (lane == 0) cp[16 + D / 2] = 0;  // centroid id
 
-    // o_obar (FMA chain) and half L1 norm, sequential in dimension order (:5893-5912)
-    if (lane == 0) {
-        double o_obar = 0.0, half_l1 = 0.0;
+    // o_obar (FMA chain) and half L1 norm, sequential in dimension order (:5893-5912). With exact
+    // sums: half_l1 and S = sum|v| across the lanes; o_obar = S / sqrt(D) exactly when sqrt(D) is
+    // a power of two, else the chain lies within (D + 2) 2^-53 o of RN(S / sqrt(D)) (each FMA
+    // rounds once, every partial sum is at most o) and error_scale, monotone in o, is decided
+    // when both ends of that interval give the same float; otherwise lane 0 runs the chain.
+    {
         const double inv_sqrt_d = 1.0 / sqrt(static_cast<double>(D));
-        for (int i = 0; i < D; ++i) {
-            const double sign = ru[i] > 0.0f ? 1.0 : -1.0;
-            o_obar = __fma_rn(static_cast<double>(ru[i]) * sign, inv_sqrt_d, o_obar);
-            half_l1 += 0.5 * fabs(static_cast<double>(ru[i]));
+        const double fac = 0.359375 / sqrt(static_cast<double>(D));  // ldexp(5.75, -4) / sqrt(D)
+        auto error_of = [&](double o) {
+            if (!isfinite(o)) o = 0.8;
+            o = fmin(0.999999, fmax(1e-6, o));
+            const double o2 = o * o;
+            return static_cast<float>(sqrt(fmax(0.0, (1.0 - o2) / o2)) * fac * 2.0 * static_cast<double>(rn));
+        };
+        bool done = false;
+        double half_l1 = 0.0;
+        float error_scale = 0.0f;
+        if (exact) {
+            long long k = 0;
+            for (int i = lane; i < D; i += 32) k += units(fabsf(ru[i]), E);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) k += __shfl_xor_sync(0xffffffffu, k, o);
+            const double S = __ll2double_rn(k) * pow2d(E);
+            half_l1 = __ll2double_rn(k >> 1) * pow2d(E);  // k is even: |v| / 2 is a whole number of units
+            const double o_par = S * inv_sqrt_d;
+            if ((D & 0x55555555) != 0) {  // D = 4^j: 1 / sqrt(D) is a power of two, every step exact
+                error_scale = error_of(o_par);
+                done = true;
+            } else {
+                const double d = (static_cast<double>(D) + 4.0) * 0x1p-53 * o_par;
+                const float e_lo = error_of(o_par + d), e_hi = error_of(o_par - d);
+                if (e_lo == e_hi) {
+                    error_scale = e_lo;
+                    done = true;
+                }
+            }
         }
-        float short_scale = 0.0f, error_scale = 0.0f;
-        if (rn > 0.0f && half_l1 > 1e-12) {
-            short_scale = static_cast<float>(2.0 * static_cast<double>(rn) / half_l1);
-            if (!isfinite(o_obar)) o_obar = 0.8;
-            o_obar = fmin(0.999999, fmax(1e-6, o_obar));
-            const double o2 = o_obar * o_obar;
-            const double fac = 0.359375 / sqrt(static_cast<double>(D));  // ldexp(5.75, -4) / sqrt(D)
-            error_scale = static_cast<float>(sqrt(fmax(0.0, (1.0 - o2) / o2)) * fac * 2.0 *
-                                             static_cast<double>(rn));
+        if (lane == 0) {
+            if (!done) {
+                double o_obar = 0.0, hl = 0.0;
+                for (int i = 0; i < D; ++i) {
+                    const double sign = ru[i] > 0.0f ? 1.0 : -1.0;
+                    o_obar = __fma_rn(static_cast<double>(ru[i]) * sign, inv_sqrt_d, o_obar);
+                    hl += 0.5 * fabs(static_cast<double>(ru[i]));
+                }
+                half_l1 = hl;
+                error_scale = error_of(o_obar);
+            }
+            float short_scale = 0.0f;
+            if (rn > 0.0f && half_l1 > 1e-12) short_scale = static_cast<float>(2.0 * static_cast<double>(rn) / half_l1);
+            else error_scale = 0.0f;
+            put_f32(cp, norm_sqr);
+            put_f32(cp + 4, long_scale);
+            put_f32(cp + 8, short_scale);
+            put_f32(cp + 12, error_scale);
         }
-        put_f32(cp, norm_sqr);
-        put_f32(cp + 4, long_scale);
-        put_f32(cp + 8, short_scale);
-        put_f32(cp + 12, error_scale);
     }
     __syncwarp();
 
@@ -355,19 +432,53 @@ __global__ void __launch_bounds__(32) encode_kernel(EncodeArgs a) {
         const uint32_t hi = static_cast<uint32_t>(rcode[2 * j + 1]) & 0xFu;
         rp[8 + D / 8 + j] = static_cast<uint8_t>(lo | (hi << 4));
     }
-    if (lane == 0) {
-        double dec_norm = 0.0, x4_ip = 0.0;
-        for (int i = 0; i < D; ++i) {
+    // the residual record's norm and inner product (:5984-5991): sums of per-dim double products,
+    // sequential in dimension order, stored as floats. Across the lanes in another order: each
+    // order lies within gamma_{D-1} sum|t| of the exact sum of the same rounded terms t (Higham
+    // 2002, section 3.1), so the two orders differ by at most twice that, and the float is
+    // decided when both ends of that interval give the same float; otherwise lane 0 runs the loop.
+    {
+        double s1 = 0.0, s2 = 0.0, a2 = 0.0;
+        for (int i = lane; i < D; i += 32) {
             const float stored = s_sc[i >> 4];
             if (stored == 0.0f || !isfinite(stored)) continue;
             const int code = ru[i] > 0.0f ? 8 + c0[i] : 7 - c0[i];
             const double dec = static_cast<double>(stored) * static_cast<double>(rcode[i]);
             const double x4 = 0.5 * static_cast<double>(long_scale) * (static_cast<double>(code) - 7.5);
-            dec_norm += dec * dec;
-            x4_ip += x4 * dec;
+            const double t1 = dec * dec, t2 = x4 * dec;
+            s1 += t1;
+            s2 += t2;
+            a2 += fabs(t2);
         }
-        put_f32(rp, static_cast<float>(dec_norm));
-        put_f32(rp + 4, static_cast<float>(x4_ip));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+            s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+            a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+        }
+        const double g = 2.0 * (static_cast<double>(D) * 0x1p-53) / (1.0 - static_cast<double>(D) * 0x1p-53) * 1.0001;
+        const double d1 = g * s1 + 4.0 * 0x1p-53 * s1, d2 = g * a2 + 4.0 * 0x1p-53 * fabs(s2);
+        const bool ok1 = isfinite(s1) && static_cast<float>(s1 - d1) == static_cast<float>(s1 + d1);
+        const bool ok2 = isfinite(s2) && static_cast<float>(s2 - d2) == static_cast<float>(s2 + d2);
+        if (lane == 0) {
+            float f1 = static_cast<float>(s1), f2 = static_cast<float>(s2);
+            if (!ok1 || !ok2) {
+                double dec_norm = 0.0, x4_ip = 0.0;
+                for (int i = 0; i < D; ++i) {
+                    const float stored = s_sc[i >> 4];
+                    if (stored == 0.0f || !isfinite(stored)) continue;
+                    const int code = ru[i] > 0.0f ? 8 + c0[i] : 7 - c0[i];
+                    const double dec = static_cast<double>(stored) * static_cast<double>(rcode[i]);
+                    const double x4 = 0.5 * static_cast<double>(long_scale) * (static_cast<double>(code) - 7.5);
+                    dec_norm += dec * dec;
+                    x4_ip += x4 * dec;
+                }
+                f1 = static_cast<float>(dec_norm);
+                f2 = static_cast<float>(x4_ip);
+            }
+            put_f32(rp, f1);
+            put_f32(rp + 4, f2);
+        }
     }
 }
 
@@ -376,7 +487,7 @@ __global__ void __launch_bounds__(32) encode_kernel(EncodeArgs a) {
 cudaError_t launch_encode(const EncodeArgs &a, cudaStream_t stream) {
     if (a.n == 0) return cudaSuccess;
     if (a.code_dim > 2048 || a.code_dim < 64) return cudaErrorInvalidValue;
-    const size_t smem = static_cast<size_t>(a.code_dim) * (8 + 4 + 1 + 1);
+    const size_t smem = static_cast<size_t>(a.code_dim) * (8 + 1 + 1);
     if (a.rotated != nullptr) {
         cudaError_t e = cudaFuncSetAttribute(encode_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              static_cast<int>(smem));

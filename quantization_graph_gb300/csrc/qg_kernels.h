@@ -48,6 +48,7 @@ struct SearchArgs {
                      // 2 B1Main (+-1 codes, no gate, every fresh neighbour by the 4-bit x 1-bit distance);
                      // 3 Full (FP32 gate, survivors by the remaining bits with the gate's short ip)
     int beam_width;
+    int tile;        // tile shape of the Int8 / Int4 search at D >= 1024 (0..4; search.cu, Tile), else 0
     float eps;
     int rerank;
     int early_stop_hops;
@@ -134,7 +135,7 @@ cudaError_t launch_search(const SearchArgs &a, int grid, int warps_per_block, cu
 size_t search_smem_per_warp(int code_dim, int l_cap);
 // Resident blocks per SM and dynamic shared memory of one search block; a stop model adds
 // the staged network weights to every block.
-int search_blocks_per_sm(int code_dim, int l_cap, int warps_per_block, bool stop_model = false);
+int search_blocks_per_sm(int code_dim, int l_cap, int warps_per_block, bool stop_model = false, int tile = 0);
 size_t search_block_smem(int l_cap, int warps_per_block, bool stop_model);
 int search_supported_dim(int code_dim);
 cudaError_t launch_encode(const EncodeArgs &a, cudaStream_t stream);

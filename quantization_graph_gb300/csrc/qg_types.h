@@ -95,5 +95,6 @@ struct qg_index {
     size_t device_bytes = 0;
     int launch_wpb = 0;      // qg_index_set_launch override (0 = automatic)
     int launch_per_sm = 0;
+    int tile = 0;            // qg_index_set_tile: the search's tile shape
     std::vector<void *> owned;
 };

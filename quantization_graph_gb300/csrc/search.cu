@@ -37,21 +37,36 @@ constexpr uint32_t kIdMask = 0x7FFFFFFFu;
 constexpr int kMaxFresh = 64;   // fresh neighbours per expanded node (max degree)
 constexpr int kMaxBeam = 8;
 
-#ifndef QG_TRAV_GROUP_WIDE
-#define QG_TRAV_GROUP_WIDE 2  // code rows in flight per traversal group for D = 2048
-#endif
-#ifndef QG_GATE_GROUP
-#define QG_GATE_GROUP 16  // 32-dim MSB chunks in flight per lane in the gate (neighbours x chunks)
-#endif
 template <int D>
 struct Lay {
     static constexpr int CH = D / 32;
     static constexpr int LPN = CH < 32 ? CH : 32;   // lanes per neighbour
     static constexpr int CPL = CH / LPN;            // 32-dim chunks per lane
     static constexpr int NBP = 32 / LPN;            // neighbours per pass
-    static constexpr int GG = QG_GATE_GROUP / CPL;  // gate group (LPN == 32)
-    static constexpr int GT = CPL == 1 ? 8 : QG_TRAV_GROUP_WIDE;  // traversal group (LPN == 32)
     static constexpr int PG = 4;                    // passes per batch (LPN < 32)
+};
+
+#ifndef QG_SEARCH_MINBLOCKS
+#define QG_SEARCH_MINBLOCKS 2  // 128 registers per thread
+#endif
+#ifndef QG_SEARCH_THREADS
+#define QG_SEARCH_THREADS 256
+#endif
+
+// Tile shape of the gate and traversal loops when one neighbour spans the warp (D >= 1024): how
+// many neighbours' rows a lane keeps in flight, and the registers per thread. Shape 0 (the
+// default; measured fastest at 200k x 1536): 16 MSB chunks per lane in the gate, 2 code rows
+// (8 at D = 1024) in the traversal, 128 registers (16 warps per SM); 1: 8 chunks; 2: 32 chunks;
+// 3: twice the traversal rows; 4: 8 chunks compiled for three 8-warp blocks per SM (at most 85
+// registers, 24 warps per SM). Shapes 1-4 exist for the Int8 / Int4 search at D = 1024 and 2048,
+// chosen per index (qg_index_set_tile, the autotuner).
+template <int D, int kTile>
+struct Tile {
+    static constexpr int CPL = Lay<D>::CPL;
+    static constexpr int chunks = (kTile == 1 || kTile == 4) ? 8 : (kTile == 2 ? 32 : 16);
+    static constexpr int GG = chunks / CPL > 0 ? chunks / CPL : 1;                 // gate group
+    static constexpr int GT = (CPL == 1 ? 8 : 2) * (kTile == 3 ? 2 : 1);           // traversal group
+    static constexpr int min_blocks = kTile == 4 ? 3 * 256 / QG_SEARCH_THREADS : QG_SEARCH_MINBLOCKS;
 };
 
 struct WarpSmem {
@@ -255,10 +270,11 @@ __device__ __forceinline__ void load_query(QueryRegs<D> &r, const int8_t *codes,
 // kMode 3, Full: the FP32 rotated residual against the MSB plane (16 lanes over dimensions and
 // the reduce tree, half a warp per neighbour) gates; survivors with a valid gate take the
 // remaining bits with the gate's short ip (mode 1), the others the FP32 restore (mode 0).
-template <int D, int kMode>
+template <int D, int kMode, int kTile>
 __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int lane,
                            uint32_t *visited, const uint32_t *stop_smem) {
     using L = Lay<D>;
+    using T = Tile<D, kTile>;
     const DevIndex &ix = a.ix;
     const int sub = lane % L::LPN;
     const int grp = lane / L::LPN;
@@ -433,7 +449,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                 prefetch_rows_l1(reinterpret_cast<const uint8_t *>(ix.pf), s.fid, F, 16, 16, lane);
                 for (int f = lane; f < F; f += 32) s.fpf[f] = ix.pf[s.fid[f]];
                 if constexpr (L::LPN == 32) {
-                    constexpr int G = L::GG;
+                    constexpr int G = T::GG;
                     for (int gb = 0; gb < F; gb += G) {
                         uint32_t w[G][L::CPL];
     #pragma unroll
@@ -558,7 +574,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
             } else {
                 bool any_full = false;
                 if constexpr (L::LPN == 32) {
-                    constexpr int G = L::GT;
+                    constexpr int G = T::GT;
                     for (int gb = 0; gb < S; gb += G) {
                         uint4 c[G][L::CPL];
     #pragma unroll
@@ -862,14 +878,8 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
     }
 }
 
-#ifndef QG_SEARCH_MINBLOCKS
-#define QG_SEARCH_MINBLOCKS 2  // 128 registers per thread; 80 (3 blocks) spills and measured slower
-#endif
-#ifndef QG_SEARCH_THREADS
-#define QG_SEARCH_THREADS 256
-#endif
-template <int D, int kMode>
-__global__ void __launch_bounds__(QG_SEARCH_THREADS, QG_SEARCH_MINBLOCKS) search_kernel(SearchArgs a) {
+template <int D, int kMode, int kTile>
+__global__ void __launch_bounds__(QG_SEARCH_THREADS, (Tile<D, kTile>::min_blocks)) search_kernel(SearchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
@@ -894,7 +904,7 @@ __global__ void __launch_bounds__(QG_SEARCH_THREADS, QG_SEARCH_MINBLOCKS) search
         uint4 *row = reinterpret_cast<uint4 *>(visited);
         for (size_t i = lane; i < words / 4; i += 32) row[i] = make_uint4(0u, 0u, 0u, 0u);
         __syncwarp();
-        search_one<D, kMode>(a, s, q, lane, visited, stop_smem);
+        search_one<D, kMode, kTile>(a, s, q, lane, visited, stop_smem);
         __syncwarp();
     }
 }
@@ -911,13 +921,13 @@ int search_supported_dim(int code_dim) {
            code_dim == 1024 || code_dim == 2048;
 }
 
-template <int D, int kMode>
+template <int D, int kMode, int kTile = 0>
 static cudaError_t launch_dc(const SearchArgs &a, int grid, int wpb, cudaStream_t stream) {
     const size_t smem = search_block_smem(a.l_cap, wpb, a.stop_w != nullptr);
-    cudaError_t e = cudaFuncSetAttribute(search_kernel<D, kMode>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(search_kernel<D, kMode, kTile>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    search_kernel<D, kMode><<<grid, wpb * 32, smem, stream>>>(a);
+    search_kernel<D, kMode, kTile><<<grid, wpb * 32, smem, stream>>>(a);
     return cudaGetLastError();
 }
 
@@ -927,54 +937,70 @@ static cudaError_t launch_d(const SearchArgs &a, int grid, int wpb, cudaStream_t
         case 1: return launch_dc<D, 1>(a, grid, wpb, stream);
         case 2: return launch_dc<D, 2>(a, grid, wpb, stream);
         case 3: return launch_dc<D, 3>(a, grid, wpb, stream);
-        default: return launch_dc<D, 0>(a, grid, wpb, stream);
+        default: break;
     }
+    if constexpr (D >= 1024) {
+        switch (a.tile) {
+            case 1: return launch_dc<D, 0, 1>(a, grid, wpb, stream);
+            case 2: return launch_dc<D, 0, 2>(a, grid, wpb, stream);
+            case 3: return launch_dc<D, 0, 3>(a, grid, wpb, stream);
+            case 4: return launch_dc<D, 0, 4>(a, grid, wpb, stream);
+            default: break;
+        }
+    }
+    return launch_dc<D, 0>(a, grid, wpb, stream);
 }
 
 size_t search_block_smem(int l_cap, int wpb, bool stop_model) {
     return warp_smem_bytes(l_cap) * static_cast<size_t>(wpb) + (stop_model ? kMlpSmemBytes : 0);
 }
 
-template <int D>
-static int blocks_per_sm_d(int l_cap, int wpb, bool stop_model) {
+template <typename K>
+static int blocks_per_sm_k(K kernel, int l_cap, int wpb, bool stop_model) {
     const size_t smem = search_block_smem(l_cap, wpb, stop_model);
-    // the B1, B1Main and Full instantiations share the launch bounds and shared memory of the Int8 one
-    if (cudaFuncSetAttribute(search_kernel<D, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(smem)) != cudaSuccess)
-        return 0;
-    int blocks = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, search_kernel<D, 0>, wpb * 32, smem) !=
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
         cudaSuccess)
         return 0;
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, wpb * 32, smem) != cudaSuccess) return 0;
     return blocks;
 }
 
-static int blocks_per_sm_uncached(int code_dim, int l_cap, int wpb, bool stop_model) {
+// Every codec mode and tile shapes 0-3 share the launch bounds and shared memory of
+// search_kernel<D, 0, 0>; shape 4 has its own launch bounds.
+template <int D>
+static int blocks_per_sm_d(int l_cap, int wpb, bool stop_model, int tile) {
+    if constexpr (D >= 1024)
+        if (tile == 4) return blocks_per_sm_k(search_kernel<D, 0, 4>, l_cap, wpb, stop_model);
+    return blocks_per_sm_k(search_kernel<D, 0, 0>, l_cap, wpb, stop_model);
+}
+
+static int blocks_per_sm_uncached(int code_dim, int l_cap, int wpb, bool stop_model, int tile) {
     switch (code_dim) {
-        case 64: return blocks_per_sm_d<64>(l_cap, wpb, stop_model);
-        case 128: return blocks_per_sm_d<128>(l_cap, wpb, stop_model);
-        case 256: return blocks_per_sm_d<256>(l_cap, wpb, stop_model);
-        case 512: return blocks_per_sm_d<512>(l_cap, wpb, stop_model);
-        case 1024: return blocks_per_sm_d<1024>(l_cap, wpb, stop_model);
-        case 2048: return blocks_per_sm_d<2048>(l_cap, wpb, stop_model);
+        case 64: return blocks_per_sm_d<64>(l_cap, wpb, stop_model, tile);
+        case 128: return blocks_per_sm_d<128>(l_cap, wpb, stop_model, tile);
+        case 256: return blocks_per_sm_d<256>(l_cap, wpb, stop_model, tile);
+        case 512: return blocks_per_sm_d<512>(l_cap, wpb, stop_model, tile);
+        case 1024: return blocks_per_sm_d<1024>(l_cap, wpb, stop_model, tile);
+        case 2048: return blocks_per_sm_d<2048>(l_cap, wpb, stop_model, tile);
         default: return 0;
     }
 }
 
 // Occupancy queries cost host time on every call; their answers depend only on the device and
 // the launch parameters, so they are kept.
-int search_blocks_per_sm(int code_dim, int l_cap, int wpb, bool stop_model) {
+int search_blocks_per_sm(int code_dim, int l_cap, int wpb, bool stop_model, int tile) {
     static std::mutex mu;
-    static std::map<std::tuple<int, int, int, int, bool>, int> cache;
+    static std::map<std::tuple<int, int, int, int, bool, int>, int> cache;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 0;
-    const auto key = std::make_tuple(dev, code_dim, l_cap, wpb, stop_model);
+    const auto key = std::make_tuple(dev, code_dim, l_cap, wpb, stop_model, tile);
     {
         std::lock_guard<std::mutex> lock(mu);
         const auto it = cache.find(key);
         if (it != cache.end()) return it->second;
     }
-    const int b = blocks_per_sm_uncached(code_dim, l_cap, wpb, stop_model);
+    const int b = blocks_per_sm_uncached(code_dim, l_cap, wpb, stop_model, tile);
     std::lock_guard<std::mutex> lock(mu);
     cache[key] = b;
     return b;

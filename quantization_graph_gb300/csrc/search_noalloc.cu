@@ -128,7 +128,7 @@ extern "C" int qg_search_batch_noalloc(qg_index *index, const float *d_queries, 
             return fail(QG_ERR_INVALID, "qg_search_batch_noalloc: index of " + std::to_string(n_total) +
                                             " nodes is too large for the 64 MiB no-alloc scratch");
         wpb = narrow;
-        per_sm = search_blocks_per_sm(static_cast<int>(D), a.l_cap, wpb);
+        per_sm = search_blocks_per_sm(static_cast<int>(D), a.l_cap, wpb, false, a.tile);
         if (per_sm <= 0) return fail(QG_ERR_UNSUPPORTED, "qg_search_batch_noalloc: search kernel cannot be resident");
         max_slots = static_cast<size_t>(sms) * per_sm * wpb;
     }

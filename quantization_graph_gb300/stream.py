@@ -7,7 +7,9 @@ the captured buffers and replays the graph. The kernels read the batch size on t
 nothing is re-captured and nothing is allocated per batch.
 
 autotune() times the persistent kernel's launch shapes (warps per block, resident blocks per
-SM) on a sample of the workload and keeps the fastest on the index.
+SM) and, for code dims of 1024 and more, the tile shapes of its gate and traversal loops
+(qg_index_set_tile) on a sample of the workload and keeps the fastest on the index. Every shape
+returns the same results; only the speed differs.
 """
 from __future__ import annotations
 
@@ -20,16 +22,23 @@ from . import _native as N
 from .space import _cuda, _ptr
 
 
-def autotune(index, queries: torch.Tensor, k: int, l_value: int, shapes=None, repeats: int = 3, log=None):
-    """Pick (warps_per_block, blocks_per_sm) for this index and pool size; returns the timings."""
+def autotune(index, queries: torch.Tensor, k: int, l_value: int, shapes=None, tiles=None, repeats: int = 3,
+             log=None):
+    """Pick (warps_per_block, blocks_per_sm, tile) for this index and pool size; returns the timings.
+
+    Launch shapes are timed with the default tile; the tile shapes (only where the code dim is at
+    least 1024, where they exist) are then timed with the best launch shape."""
     lib = N.load()
     shapes = shapes or [(8, 0), (4, 0), (2, 0), (8, 1), (4, 2), (4, 1)]
+    if tiles is None:
+        tiles = [0, 1, 2, 3, 4] if index.space.code_dim >= 1024 else [0]
     q = _cuda(queries, torch.float32)
     ids = torch.empty((q.shape[0], k), dtype=torch.int32, device="cuda")
     dists = torch.empty((q.shape[0], k), dtype=torch.float32, device="cuda")
-    results = []
-    for wpb, per_sm in shapes:
+
+    def timed(wpb, per_sm, tile):
         N.check(lib.qg_index_set_launch(index.handle, wpb, per_sm), "qg_index_set_launch")
+        N.check(lib.qg_index_set_tile(index.handle, tile), "qg_index_set_tile")
         index.search_into(q, ids, dists, k=k, l_value=l_value)
         torch.cuda.synchronize()
         start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -38,11 +47,17 @@ def autotune(index, queries: torch.Tensor, k: int, l_value: int, shapes=None, re
             index.search_into(q, ids, dists, k=k, l_value=l_value)
         end.record()
         torch.cuda.synchronize()
-        results.append(((wpb, per_sm), start.elapsed_time(end) / repeats))
+        ms = start.elapsed_time(end) / repeats
         if log:
-            log(f"  launch {wpb} warps/block, <= {per_sm or 'max'} blocks/SM: {results[-1][1]:.3f} ms")
+            log(f"  launch {wpb} warps/block, <= {per_sm or 'max'} blocks/SM, tile {tile}: {ms:.3f} ms")
+        return ms
+
+    results = [((wpb, per_sm, 0), timed(wpb, per_sm, 0)) for wpb, per_sm in shapes]
+    wpb, per_sm, _ = min(results, key=lambda r: r[1])[0]
+    results += [((wpb, per_sm, t), timed(wpb, per_sm, t)) for t in tiles if t != 0]
     best = min(results, key=lambda r: r[1])[0]
     N.check(lib.qg_index_set_launch(index.handle, best[0], best[1]), "qg_index_set_launch")
+    N.check(lib.qg_index_set_tile(index.handle, best[2]), "qg_index_set_tile")
     return best, results
 
 

@@ -72,17 +72,20 @@ extern "C" int qcs_run(int D, const float *ru, double *t_heap, double *t_lane0, 
     }
     std::sort(keys.begin(), keys.end());
     *t_heap = heap_search(a, c0, max_o);
-    std::vector<double> blk(D / 32 + 2);
+    std::vector<long long> blk(D / 32 + 2);
     double t0 = 0.0, tw = 0.0;
     bool ok = false;
     std::vector<float> ruv(ru, ru + D);
     warp_emu::run_warp([&](int lane) {
-        if (lane == 0) t0 = qg::code_search_lane0(keys.data(), ruv.data(), c0b.data(), D, mx);
+        if (lane == 0)
+            t0 = qg::code_search_lane0(keys.data(), c0b.data(), D, mx, qg::lane0_num_start(ruv.data(), c0b.data(), D));
+        int E = 0;
+        const bool exact = qg::exact_sum_unit(ruv.data(), D, lane, &E);
         double t = 0.0;
-        const bool k = qg::code_search_warp(keys.data(), ruv.data(), c0b.data(), D, mx, blk.data(), lane, &t);
+        if (exact) qg::code_search_warp(keys.data(), c0b.data(), D, mx, blk.data(), E, lane, &t);
         if (lane == 0) {
             tw = t;
-            ok = k;
+            ok = exact;
         }
     });
     *t_lane0 = t0;

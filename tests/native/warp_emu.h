@@ -136,6 +136,19 @@ inline float __fdiv_rn(float a, float b) { return a / b; }
 inline float __ll2float_rn(long long x) { return static_cast<float>(x); }
 inline int __ffsll(long long x) { return __builtin_ffsll(x); }
 inline int __clzll(long long x) { return x == 0 ? 64 : __builtin_clzll(static_cast<unsigned long long>(x)); }
+inline double __longlong_as_double(long long x) {
+    double d;
+    std::memcpy(&d, &x, 8);
+    return d;
+}
+inline float __ll2float_rz(long long x) {
+    // round toward zero: the nearest float, stepped back toward zero when it overshoots
+    float f = static_cast<float>(x);
+    if (static_cast<long double>(f) > static_cast<long double>(x) && x > 0) f = std::nextafter(f, 0.0f);
+    if (static_cast<long double>(f) < static_cast<long double>(x) && x < 0) f = std::nextafter(f, 0.0f);
+    return f;
+}
+inline double __ll2double_rn(long long x) { return static_cast<double>(x); }
 inline long long __double_as_longlong(double d) {
     long long x;
     std::memcpy(&x, &d, 8);

@@ -165,6 +165,41 @@ def test_other_code_dims_match_oracle(cuda, oracle, dim):
         np.testing.assert_array_equal(stats_matrix(r.stats), stats_matrix(os_))
 
 
+@pytest.mark.parametrize("dim", [700, 1536])
+def test_tile_shapes_match_oracle(cuda, oracle, dim):
+    """Every tile shape of the gate / traversal loops (qg_index_set_tile) at D = 1024 and 2048
+    returns the oracle's ids, distance bits and counters."""
+    torch = cuda
+    from quantization_graph_gb300 import _native as N
+    from quantization_graph_gb300.graph_build import build_graph
+    from quantization_graph_gb300.index import OursIndex
+    from quantization_graph_gb300.space import RabitqSpace
+
+    rng = np.random.default_rng(dim + 7)
+    X = (rng.standard_normal((1200, dim)) * rng.uniform(0.2, 2.0, dim)).astype(np.float32)
+    Q = (rng.standard_normal((24, dim)) * rng.uniform(0.2, 2.0, dim)).astype(np.float32)
+    c = X.mean(0).astype(np.float32)
+    sp = RabitqSpace(dim, c)
+    xd = torch.from_numpy(X).cuda()
+    compact, residual = sp.encode(xd)
+    msb, factors = sp.export_paper_sidecar(compact)
+    deg, edges = build_graph(sp, xd, compact, r=32, knn=64, alpha=1.2, reverse=32, refine_rounds=1, refine_l=64,
+                             residual=residual, msb=msb, factors=factors)
+    ix = OursIndex(sp, compact, residual, msb, factors, deg, edges)
+    gi = dict(compact=compact.cpu().numpy(), residual=residual.cpu().numpy(), msb=msb.cpu().numpy(),
+              factors=factors.cpu().numpy(), degrees=deg.cpu().numpy().view(np.uint32),
+              edges=edges.cpu().numpy().view(np.uint32), total_points=1200, base_points=1200)
+    oi, od, os_ = oracle.Oracle(dim, c).search(Q, gi, k=10, L=48)
+    lib = N.load()
+    for tile in (0, 1, 2, 3, 4):
+        N.check(lib.qg_index_set_tile(ix.handle, tile), "qg_index_set_tile")
+        r = ix.search(torch.from_numpy(Q).cuda(), k=10, l_value=48)
+        np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), oi)
+        np.testing.assert_array_equal(bits(r.distances.cpu().numpy()), bits(od))
+        np.testing.assert_array_equal(stats_matrix(r.stats), stats_matrix(os_))
+    assert lib.qg_index_set_tile(ix.handle, 5) != 0
+
+
 def test_int4_codec_search_matches_reference(cuda):
     """The Int4 query codec (an ablation in the reference: scale max/8, codes in [-8, 7], the
     second dither draw) through the batched GPU search, against the reference's own kernels."""

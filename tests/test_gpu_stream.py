@@ -49,7 +49,7 @@ def test_autotuner_keeps_results(cuda):
     _, Q = SEARCH_CASES["search_c1"]()
     q = torch.from_numpy(Q).cuda()
     best, results = autotune(ix, q, k=10, l_value=40, repeats=1)
-    assert best in [r[0] for r in results]
+    assert best in [r[0] for r in results] and len(best) == 3
     r = ix.search(q, k=10, l_value=40)
     np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), g["ids_L40_k10"])
 
