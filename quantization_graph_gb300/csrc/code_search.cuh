@@ -320,34 +320,120 @@ __device__ __forceinline__ int ip_sq_order(long long num1, long long sd1, long l
     return 0;
 }
 
-// sum of a over sorted positions [0, p), in units of 2^E: the block prefix plus the rest of p's block
+// sum of a over sorted positions [0, p), in units of 2^E: the prefix of p's 16-position block
+// plus the rest of it
 __device__ __forceinline__ long long prefix_a(const SortedView &sv, const long long *blk, int p, int E) {
-    const int b = p >> 5;
-    long long s = blk[b];
-    for (int q = b << 5; q < p; ++q) s += units(sv.a(q), E);
+    long long s = blk[p >> 4];
+    for (int q = p & ~15; q < p; ++q) s += units(sv.a(q), E);
     return s;
 }
 
-// Call only when exact_sum_unit returned true (E its unit); blk holds D / 32 + 1 int64.
+// c / a < T exactly (c a small integer, a > 0, T > 0 finite): c against the exact product
+// T a = h + l (FMA error term); c - h is exact wherever the comparison is close (Sterbenz)
+__device__ __forceinline__ bool t_below(int c, float a, float T) {
+    const float h = __fmul_rn(T, a);
+    const float l = __fmaf_rn(T, a, -h);
+    return __fsub_rn(static_cast<float>(c), h) < l;
+}
+
+// Sign of num1^2 sd2 - num2^2 sd1 (the order of two events' ip^2 = 4 num^2 / sd), exactly:
+// num < 2^53 and 0 < sd < 2^20 keep both products below 2^126.
+__device__ __forceinline__ unsigned __int128 sq_times(long long num, long long sd) {
+    const unsigned long long n = static_cast<unsigned long long>(num);
+    return static_cast<unsigned __int128>(n) * n * static_cast<unsigned long long>(sd);
+}
+
+// The state of the search after every event with t < T (T = +inf: after all events): num (units
+// of 2^E), 4 sqr_den, the number of events (rank of the next) and each level's count.
+struct CutState {
+    long long num, sd4;
+    int rank;
+    int cnt[8];  // [1..7]
+};
+
+__device__ __forceinline__ void cut_state(const SortedView &sv, const int (&lo_c)[8], const int (&hi_c)[8],
+                                          const long long (&base)[8], const long long *blk, int E, float T, bool all,
+                                          long long num0, long long sd40, CutState &st) {
+    long long acc = 0, w = 0;
+    int r = 0;
+#pragma unroll
+    for (int c = 1; c <= 7; ++c) {
+        int lo = lo_c[c], hi = hi_c[c];
+        if (all) {
+            lo = hi;
+        } else {
+            while (lo < hi) {
+                const int m = (lo + hi) >> 1;
+                if (t_below(c, sv.a(m), T)) lo = m + 1;
+                else hi = m;
+            }
+        }
+        const int n = lo - lo_c[c];
+        st.cnt[c] = n;
+        acc += prefix_a(sv, blk, lo, E) - base[c];
+        w += static_cast<long long>(c) * n;
+        r += n;
+    }
+    st.num = num0 + acc;
+    st.sd4 = sd40 + 8 * w;
+    st.rank = r;
+}
+
+__device__ __forceinline__ void shfl_state(CutState &d, const CutState &s, int src) {
+    d.num = __shfl_sync(0xffffffffu, s.num, src);
+    d.sd4 = __shfl_sync(0xffffffffu, s.sd4, src);
+    d.rank = __shfl_sync(0xffffffffu, s.rank, src);
+#pragma unroll
+    for (int c = 1; c <= 7; ++c) d.cnt[c] = __shfl_sync(0xffffffffu, s.cnt[c], src);
+}
+
+// index of the n-th (from 0) set bit of mask (n < popc(mask))
+__device__ __forceinline__ int nth_set_bit(unsigned int mask, int n) {
+    for (int k = 0; k < n; ++k) mask &= mask - 1u;
+    return __ffs(static_cast<int>(mask)) - 1;
+}
+
+// The warp's best achieved (num, sd4) by exact ip^2 order (any one of equal values).
+__device__ __forceinline__ void warp_max_ip(long long &num, long long &sd4) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const long long on = __shfl_xor_sync(0xffffffffu, num, o);
+        const long long os = __shfl_xor_sync(0xffffffffu, sd4, o);
+        if (sq_times(on, sd4) > sq_times(num, os)) {
+            num = on;
+            sd4 = os;
+        }
+    }
+}
+
+// Call only when exact_sum_unit returned true (E its unit); blk holds D / 16 + 1 int64.
+//
+// Branch and bound over t. An interval [A, B) of t holds the events with A <= t < B; the states at
+// its ends come from cut_state, and the last event inside achieves exactly num(B), sd4(B). Every
+// event inside has |v| <= level / A, which bounds its ip^2 (see the drop test); an interval whose
+// bound is below the best achieved ip^2 by more than 2^-36 (far above the double rounding of the
+// reference's ip) cannot hold the maximum and is dropped. Starting from [0, inf), each round splits
+// the surviving intervals geometrically among the 32 lanes and drops again; the survivors of the
+// last round are walked event by event in (t, index) order, a lane each.
 __device__ inline void code_search_warp(const unsigned long long *keys, const unsigned char *c0, int D, float mx,
                                         long long *blk, int E, int lane, double *best_t_out) {
     const SortedView sv{keys};
     // the starting num (in units of 2^E; (c + 0.5) a = (2c + 1) (a / 2), a / 2 a whole number of
     // units) and 4 sqr_den, over the sorted positions (integer sums: any order)
     long long num0 = 0;
-    long long sd4 = 0;
+    long long sd40 = 0;
     for (int p = lane; p < D; p += 32) {
         const unsigned long long k = keys[p];
         const int c = c0[key_id(k)];
         num0 += static_cast<long long>(2 * c + 1) * (units(key_a(k), E) >> 1);
-        sd4 += 4LL * (c * c + c);
+        sd40 += 4LL * (c * c + c);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         num0 += __shfl_xor_sync(0xffffffffu, num0, o);
-        sd4 += __shfl_xor_sync(0xffffffffu, sd4, o);
+        sd40 += __shfl_xor_sync(0xffffffffu, sd40, o);
     }
-    sd4 += D;
+    sd40 += D;
     const float unit_f = pow2f(E);
     const double unit_d = pow2d(E);
 
@@ -368,10 +454,8 @@ __device__ inline void code_search_warp(const unsigned long long *keys, const un
         }
         cnt = lo;
     }
-    int lo_c[8], hi_c[8], off_c[9];
+    int lo_c[8], hi_c[8];
     const int r = __shfl_sync(0xffffffffu, cnt, 15);
-    off_c[0] = 0;
-    off_c[1] = 0;
     lo_c[0] = hi_c[0] = 0;
 #pragma unroll
     for (int c = 1; c <= 7; ++c) {
@@ -381,14 +465,12 @@ __device__ inline void code_search_warp(const unsigned long long *keys, const un
         lo_c[c] = ge_c;
         int h = min(max(ge_prev, q), r);
         hi_c[c] = h > ge_c ? h : ge_c;
-        off_c[c + 1] = off_c[c] + (hi_c[c] - lo_c[c]);
     }
-    const int n_ev = off_c[8];
-    // block prefix sums of a over positions (exact, units of 2^E): blk[b] = sum over [0, 32 b)
-    const int nblk = D >> 5;
+    // prefix sums of a over positions in blocks of 16 (exact, units of 2^E): blk[b] = sum over [0, 16 b)
+    const int nblk = D >> 4;
     for (int b = lane; b < nblk; b += 32) {
         long long sb = 0;
-        for (int q = b << 5; q < (b << 5) + 32; ++q) sb += units(sv.a(q), E);
+        for (int q = b << 4; q < (b << 4) + 16; ++q) sb += units(sv.a(q), E);
         blk[b + 1] = sb;
     }
     __syncwarp();
@@ -397,12 +479,108 @@ __device__ inline void code_search_warp(const unsigned long long *keys, const un
         for (int b = 1; b <= nblk; ++b) blk[b] += blk[b - 1];
     }
     __syncwarp();
+    long long base[8];  // prefix at each level's first position
+    {
+        const long long mine = lane >= 1 && lane <= 7 ? prefix_a(sv, blk, lo_c[lane], E) : 0;
+        base[0] = 0;
+#pragma unroll
+        for (int c = 1; c <= 7; ++c) base[c] = __shfl_sync(0xffffffffu, mine, c);
+    }
+    // spacing of the cuts: events lie in [1 / max, t_top]
+    const float t_lo = __frcp_rn(mx);
+    float t_top = t_lo;
+#pragma unroll
+    for (int c = 1; c <= 7; ++c)
+        if (hi_c[c] > lo_c[c]) t_top = fmaxf(t_top, __fdiv_rn(static_cast<float>(c), sv.a(hi_c[c] - 1)));
 
-    const int e_begin = static_cast<int>((static_cast<long long>(n_ev) * lane) >> 5);
-    const int e_end = static_cast<int>((static_cast<long long>(n_ev) * (lane + 1)) >> 5);
-    // the lane's best event: screened in FP32 on ip^2 as in code_search_lane0 (an event clearly
-    // above the best takes it, one clearly below is skipped, one inside the 2^-17 band is compared
-    // exactly), ties on the exact ip broken by rank (the reference keeps the first maximum)
+    // the lane's interval [A, B): A = 0 or B = +inf flagged; S, E the states at its ends
+    float A = 0.0f, B = 0.0f;
+    bool a_zero = true, b_inf = true;
+    CutState S, Ee;
+    S.num = num0;
+    S.sd4 = sd40;
+    S.rank = 0;
+#pragma unroll
+    for (int c = 1; c <= 7; ++c) S.cnt[c] = 0;
+    cut_state(sv, lo_c, hi_c, base, blk, E, 0.0f, true, num0, sd40, Ee);
+    unsigned int surv = 1u;  // lanes holding a surviving interval: lane 0 holds [0, inf)
+    long long lb_num = Ee.num, lb_sd4 = Ee.sd4;  // the best achieved so far: the last event
+    for (int round = 0; round < 4; ++round) {
+        const int K = __popc(surv), L = 32 / K;
+        const int i = lane / L, m = lane - i * L;
+        const bool act = i < K;
+        const int src = nth_set_bit(surv, act ? i : 0);
+        const float sA = __shfl_sync(0xffffffffu, A, src), sB = __shfl_sync(0xffffffffu, B, src);
+        const bool sAz = __shfl_sync(0xffffffffu, a_zero ? 1 : 0, src) != 0;
+        const bool sBi = __shfl_sync(0xffffffffu, b_inf ? 1 : 0, src) != 0;
+        CutState sS, sE;
+        shfl_state(sS, S, src);
+        shfl_state(sE, Ee, src);
+        // this lane's piece m of L: end cut geometric between the survivor's ends
+        const float ga = sAz ? t_lo : sA, gb = sBi ? t_top * 1.0001f : sB;
+        float T = ga * exp2f(__log2f(gb / ga) * static_cast<float>(m + 1) / static_cast<float>(L));
+        if (!sAz) T = fmaxf(T, sA);
+        if (!sBi) T = fminf(T, sB);
+        const bool last = !act || m == L - 1;
+        CutState nE;
+        if (!last) cut_state(sv, lo_c, hi_c, base, blk, E, T, false, num0, sd40, nE);
+        else nE = sE;
+        float nB = last ? sB : T;
+        bool nBi = last ? sBi : false;
+        // start: the previous piece's end, or the survivor's start
+        CutState nS;
+        shfl_state(nS, nE, (lane + 31) & 31);
+        float nA = __shfl_sync(0xffffffffu, nB, (lane + 31) & 31);
+        bool nAz = false;
+        if (m == 0) {
+            nS = sS;
+            nA = sA;
+            nAz = sAz;
+        }
+        const bool nonempty = act && nE.rank > nS.rank;
+        // the best achieved: the pieces' last events
+        long long cn = nonempty ? nE.num : lb_num, cs = nonempty ? nE.sd4 : lb_sd4;
+        if (sq_times(cn, lb_sd4) > sq_times(lb_num, cs)) {
+            lb_num = cn;
+            lb_sd4 = cs;
+        }
+        warp_max_ip(lb_num, lb_sd4);
+        // drop the pieces whose bound is below the best by the margin
+        bool keep = false;
+        int n_in = 0;
+        if (nonempty) {
+            // every event inside has a <= c / A: after events of levels summing to x, num <=
+            // min(n0 + k x, nE) (k = 1 / (A 2^E)) and sd4 = s0 + 8 x; (n0 + k x)^2 / (s0 + 8 x) is
+            // quasi-convex in x, so the bound is its value at x = 1 or where n0 + k x reaches nE.
+            // Double evaluation (relative error below 2^-48) against a 2^-36 margin.
+            const double a_eff = nAz ? 1.0 / static_cast<double>(mx) * (1.0 - 0x1p-40) : static_cast<double>(nA);
+            const double kk = 1.0 / (a_eff * unit_d);
+            const double n0 = __ll2double_rn(nS.num), ne = __ll2double_rn(nE.num), s0 = __ll2double_rn(nS.sd4);
+            const double b1 = (n0 + kk) * (n0 + kk) / (s0 + 8.0);
+            const double xc = fmax(1.0, (ne - n0) / kk);
+            const double b2 = ne * ne / (s0 + 8.0 * xc);
+            const double lbn = __ll2double_rn(lb_num);
+            const double lbd = lbn * lbn / __ll2double_rn(lb_sd4);
+            keep = !(fmax(fmin(b1, ne * ne / (s0 + 8.0)), b2) * (1.0 + 0x1p-36) < lbd);
+            n_in = nE.rank - nS.rank;
+        }
+        surv = __ballot_sync(0xffffffffu, keep);
+        A = nA;
+        B = nB;
+        a_zero = nAz;
+        b_inf = nBi;
+        S = nS;
+        Ee = nE;
+        int most = keep ? n_in : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) most = max(most, __shfl_xor_sync(0xffffffffu, most, o));
+        if (most <= 24 || L == 1) break;
+    }
+
+    // walk the surviving intervals: a 7-way merge of the levels' events in (t, index) order; each
+    // lane keeps its best under an FP32 screen of ip^2 (relative error below 2^-20): events within
+    // 2^-17 of the best are ordered by the exact cross products, and only near-ties within 2^-33
+    // compute ip = num / sqrt(sqr_den) in double as the reference does
     constexpr float kHi = 1.0f + 0x1p-17f, kLo = 1.0f - 0x1p-17f;
     bool have = false, best_exact = false;
     float best_n2 = 0.0f, best_sdf = 1.0f;
@@ -410,104 +588,79 @@ __device__ inline void code_search_warp(const unsigned long long *keys, const un
     double best_ip = -1.0;
     int best_rank = 0x7FFFFFFF, best_c = 0;
     float best_a = 1.0f;
-    // the lane's share as segments of one level each; the level is a run-time value, so every
-    // lane runs the same instructions whatever level its share lies in
-    for (int e = e_begin; e < e_end;) {
-        int c = 0, clo = 0, coff = 0, cend = 0;
+    const bool walk = (surv >> lane) & 1u;
+    int pk[8], ek[8], ik[8];
+    float ak[8];
 #pragma unroll
-        for (int cc = 1; cc <= 7; ++cc)
-            if (e >= off_c[cc] && e < off_c[cc + 1]) {
-                c = cc;
-                clo = lo_c[cc];
-                coff = off_c[cc];
-                cend = off_c[cc + 1];
-            }
-        const int s1 = min(e_end, cend);
-        const int pa = clo + (e - coff), pb = clo + (s1 - coff);
-        // pointers into the other levels: events ordered before (c, pa)
-        int ptr[8];
-        long long acc = prefix_a(sv, blk, pa, E) - prefix_a(sv, blk, clo, E);  // level c before pa
-        long long wsum = 0;  // sum over levels of level * (events of that level before)
-        int rank = 0;
-        {
-            const unsigned long long k0 = keys[pa];
-            const float a0 = key_a(k0);
-            const int i0 = key_id(k0);
-#pragma unroll
-            for (int cc = 1; cc <= 7; ++cc) {
-                int lo = lo_c[cc];
-                if (cc != c) {
-                    int hi = hi_c[cc];
-                    while (lo < hi) {
-                        const int m = (lo + hi) >> 1;
-                        const unsigned long long km = keys[m];
-                        if (ev_before(cc, key_a(km), key_id(km), c, a0, i0)) lo = m + 1;
-                        else hi = m;
-                    }
-                    acc += prefix_a(sv, blk, lo, E) - prefix_a(sv, blk, lo_c[cc], E);
-                    wsum += static_cast<long long>(cc) * (lo - lo_c[cc]);
-                    rank += lo - lo_c[cc];
-                }
-                ptr[cc] = lo;
-            }
+    for (int c = 1; c <= 7; ++c) {
+        pk[c] = lo_c[c] + S.cnt[c];
+        ek[c] = walk ? lo_c[c] + Ee.cnt[c] : pk[c];
+        ak[c] = 0.0f;
+        ik[c] = 0;
+        if (pk[c] < ek[c]) {
+            const unsigned long long k0 = keys[pk[c]];
+            ak[c] = key_a(k0);
+            ik[c] = key_id(k0);
         }
-        for (int p = pa; p < pb; ++p) {
-            const unsigned long long kp = keys[p];
-            const float ap = key_a(kp);
-            const int idp = key_id(kp);
+    }
+    long long num = S.num, sd4 = S.sd4;
+    const int n_walk = walk ? Ee.rank - S.rank : 0;
+    for (int k = 0; k < n_walk; ++k) {
+        int cm = 0, im = 0;
+        float am = 0.0f;
 #pragma unroll
-            for (int cc = 1; cc <= 7; ++cc) {
-                if (cc == c) continue;
-                while (ptr[cc] < hi_c[cc]) {
-                    const unsigned long long km = keys[ptr[cc]];
-                    const float am = key_a(km);
-                    if (!ev_before(cc, am, key_id(km), c, ap, idp)) break;
-                    acc += units(am, E);
-                    wsum += cc;
-                    ++rank;
-                    ++ptr[cc];
+        for (int c = 1; c <= 7; ++c)
+            if (pk[c] < ek[c] && (cm == 0 || ev_before(c, ak[c], ik[c], cm, am, im))) {
+                cm = c;
+                am = ak[c];
+                im = ik[c];
+            }
+#pragma unroll
+        for (int c = 1; c <= 7; ++c)
+            if (c == cm) {
+                ++pk[c];
+                if (pk[c] < ek[c]) {
+                    const unsigned long long kn = keys[pk[c]];
+                    ak[c] = key_a(kn);
+                    ik[c] = key_id(kn);
                 }
             }
-            acc += units(ap, E);
-            const int before_c = p - clo;
-            const long long ev_sd4 = sd4 + 8LL * (wsum + static_cast<long long>(c) * (before_c + 1));
-            const long long num = num0 + acc;  // units of 2^E, below 2^53
-            const int ev_rank = rank + before_c;
-            const float nf = __ll2float_rz(num) * unit_f;  // truncated: relative error below 2^-23
-            const float n2 = nf * nf, sdf = __ll2float_rn(ev_sd4);  // ev_sd4 < 2^24: exact
-            const float lhs = n2 * best_sdf, rhs = best_n2 * sdf;
-            bool take;
-            double ip = 0.0;
-            bool exact = false;
-            if (!have || lhs > rhs * kHi) {
-                take = true;
-            } else if (lhs < rhs * kLo) {
-                take = false;
-            } else if (const int o = ip_sq_order(num, ev_sd4, best_num, best_sd4); o != 0) {
-                take = o > 0;  // the doubles order as the exact values do
-            } else {
-                if (!best_exact) {
-                    best_ip = (__ll2double_rn(best_num) * unit_d) / sqrt(static_cast<double>(best_sd4) * 0.25);
-                    best_exact = true;
-                }
-                ip = (__ll2double_rn(num) * unit_d) / sqrt(static_cast<double>(ev_sd4) * 0.25);
-                exact = true;
-                take = ip > best_ip || (ip == best_ip && ev_rank < best_rank);
+        num += units(am, E);
+        sd4 += 8LL * cm;
+        const int ev_rank = S.rank + k;
+        const float nf = __ll2float_rz(num) * unit_f;  // truncated: relative error below 2^-23
+        const float n2 = nf * nf, sdf = __ll2float_rn(sd4);  // sd4 < 2^24: exact
+        const float lhs = n2 * best_sdf, rhs = best_n2 * sdf;
+        bool take;
+        double ip = 0.0;
+        bool exact = false;
+        if (!have || lhs > rhs * kHi) {
+            take = true;
+        } else if (lhs < rhs * kLo) {
+            take = false;
+        } else if (const int o = ip_sq_order(num, sd4, best_num, best_sd4); o != 0) {
+            take = o > 0;  // the doubles order as the exact values do
+        } else {
+            if (!best_exact) {
+                best_ip = (__ll2double_rn(best_num) * unit_d) / sqrt(static_cast<double>(best_sd4) * 0.25);
+                best_exact = true;
             }
-            if (take) {
-                have = true;
-                best_n2 = n2;
-                best_sdf = sdf;
-                best_num = num;
-                best_sd4 = ev_sd4;
-                best_rank = ev_rank;
-                best_c = c;
-                best_a = ap;
-                best_exact = exact;
-                best_ip = ip;
-            }
+            ip = (__ll2double_rn(num) * unit_d) / sqrt(static_cast<double>(sd4) * 0.25);
+            exact = true;
+            take = ip > best_ip || (ip == best_ip && ev_rank < best_rank);
         }
-        e = s1;
+        if (take) {
+            have = true;
+            best_n2 = n2;
+            best_sdf = sdf;
+            best_num = num;
+            best_sd4 = sd4;
+            best_rank = ev_rank;
+            best_c = cm;
+            best_a = am;
+            best_exact = exact;
+            best_ip = ip;
+        }
     }
     if (have && !best_exact)
         best_ip = (__ll2double_rn(best_num) * unit_d) / sqrt(static_cast<double>(best_sd4) * 0.25);

@@ -77,12 +77,12 @@ __device__ float mse_scale16_f64(const float *e) {
     return scale;
 }
 
-// The same scale without FP64. Each q = round(e / scale) is decided in FP32
-// (round_away_quotient); n = sum e_i q_i is summed exactly in integers on the grid of the
-// smallest term, which equals the reference's double sum whenever every partial sum fits 53
-// bits there (the products e_i q_i are exact in double); next = float(n / d) is rounded from
-// the exact quotient (128-bit division by the integer d) through 53 and then 24 bits. Returns
-// false when any of those conditions fails; the caller then takes mse_scale16_f64.
+// The same scale with one FP64 operation per iteration. Each q = round(e / scale) is decided in
+// FP32 (round_away_quotient, one reciprocal per iteration); n = sum e_i q_i is summed exactly in
+// int64 on the grid of the smallest term, which equals the reference's double sum whenever every
+// partial sum fits 53 bits there (the products e_i q_i are exact in double); n is then that
+// double exactly, and next = float(n / d) is the reference's own double division and rounding.
+// Returns false when a condition fails; the caller then takes mse_scale16_f64.
 __device__ bool mse_scale16_exact(const float *e, float *out) {
     float m = 0.0f;
     for (int i = 0; i < 16; ++i) m = fmaxf(m, fabsf(e[i]));
@@ -95,37 +95,39 @@ __device__ bool mse_scale16_exact(const float *e, float *out) {
         *out = scale;
         return true;
     }
+    constexpr long long kLim = 1LL << 53;
     for (int iter = 0; iter < 8; ++iter) {
         if (!(scale >= 0x1p-100f)) return false;
+        const float inv = __frcp_rn(scale);
         int d = 0, G = 1 << 30;
         int qv[16];
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
             bool und = false;
-            int q = round_away_quotient(e[i], scale, und);
+            int q = round_away_quotient(e[i], scale, inv, und);
             if (und) q = max(-7, min(7, round_away(static_cast<double>(e[i]) / static_cast<double>(scale))));
             qv[i] = q;
             d += q * q;
             if (q != 0 && e[i] != 0.0f) G = min(G, split_float(e[i]).e);
         }
         if (d <= 0) break;
-        __int128 N = 0;
+        long long N = 0;
         if (G != (1 << 30)) {
             for (int i = 0; i < 16; ++i) {
                 if (qv[i] == 0 || e[i] == 0.0f) continue;
                 const FloatParts p = split_float(e[i]);
                 const int sh = p.e - G;
-                if (sh > 60) return false;
-                N += static_cast<__int128>(p.m * qv[i]) << sh;
-                const __int128 a = N < 0 ? -N : N;
-                if (a >= (static_cast<__int128>(1) << 53)) return false;  // a partial sum may have rounded
+                if (sh > 36) return false;
+                const long long term = (p.m * qv[i]) * (1LL << sh);  // |p.m q| < 2^27: below 2^63
+                if (term >= kLim || term <= -kLim) return false;
+                N += term;
+                if (N >= kLim || N <= -kLim) return false;  // a partial sum may have rounded
             }
         }
         if (N == 0) break;  // next = 0: the reference stops
-        bool ok = true;
-        const unsigned long long mag = static_cast<unsigned long long>(N < 0 ? -N : N);
-        const float next = float_via_double(N < 0, div_shift64_sticky(mag, static_cast<uint32_t>(d)), G - 65, ok);
-        if (!ok) return false;
+        if (G < -1000 || G > 1000) return false;
+        const double n = __ll2double_rn(N) * pow2d(G);  // exact
+        const float next = __double2float_rn(__ddiv_rn(n, static_cast<double>(d)));
         if (next <= 0.0f || !isfinite(next)) break;
         if (fabsf(next - scale) <= 1e-6f * fmaxf(1.0f, scale)) {
             scale = next;
@@ -161,10 +163,10 @@ __device__ __forceinline__ float quant_error(float rn, float r, float long_scale
 }
 
 __device__ void fht_warp_local(float *x, int D, int lane) {
-    for (int step = 1; step < D; step <<= 1) {
+    for (int sh = 0; (1 << sh) < D; ++sh) {
+        const int step = 1 << sh;
         for (int b = lane; b < D / 2; b += 32) {
-            const int block = b / step, i = b - block * step;
-            const int ia = block * 2 * step + i, ib = ia + step;
+            const int ia = ((b >> sh) << (sh + 1)) + (b & (step - 1)), ib = ia + step;
             const float a = x[ia], c = x[ib];
             x[ia] = a + c;
             x[ib] = a - c;
@@ -416,11 +418,12 @@ __global__ void __launch_bounds__(32) encode_kernel(EncodeArgs a) {
         rp[9 + 2 * b] = static_cast<uint8_t>(h >> 8);
         const float stored = half_to_float_ref(h);
         s_sc[b] = stored;
+        const float inv_stored = __frcp_rn(stored);
         for (int i = 16 * b; i < 16 * b + 16; ++i) {
             int q = 0;
             if (stored != 0.0f && isfinite(stored)) {
                 bool und = !(stored >= 0x1p-100f) || !isfinite(qerr[i]);
-                if (!und) q = round_away_quotient(qerr[i], stored, und);
+                if (!und) q = round_away_quotient(qerr[i], stored, inv_stored, und);
                 if (und) q = max(-7, min(7, round_away(static_cast<double>(qerr[i]) / static_cast<double>(stored))));
             }
             rcode[i] = static_cast<signed char>(q);

@@ -96,38 +96,25 @@ __device__ __forceinline__ float float_via_double(bool neg, unsigned __int128 ma
     return __uint_as_float((neg ? 0x80000000u : 0u) | (static_cast<uint32_t>(ex + 127) << 23) | sig);
 }
 
-// (num << 64) / d for num < 2^64 and 0 < d < 2^32, with a sticky bit appended: the result
-// r satisfies num / d = (r >> 1 + frac) * 2^-64, r & 1 = (remainder != 0).
-__device__ __forceinline__ unsigned __int128 div_shift64_sticky(unsigned long long num, uint32_t d) {
-    unsigned __int128 q = 0;
-    unsigned long long rem = 0;
-    const uint32_t limbs[4] = {0u, 0u, static_cast<uint32_t>(num), static_cast<uint32_t>(num >> 32)};
-#pragma unroll
-    for (int i = 3; i >= 0; --i) {
-        const unsigned long long cur = (rem << 32) | limbs[i];
-        const unsigned long long qq = cur / d;
-        rem = cur - qq * d;
-        q |= static_cast<unsigned __int128>(qq) << (32 * i);
-    }
-    return (q << 1) | (rem != 0 ? 1u : 0u);
-}
-
 // std::round(double(x) / double(s)) clamped to [-7, 7] (round half away from zero), decided in
-// FP32: y + c approximates |x| / s within 2^-44 (FMA remainder of the float quotient) and the
-// double quotient is within 2^-50 of it; the rounding is decided unless the quotient lies
-// within 2^-36 of a half-integer, in which case `undecided` is set and the caller evaluates
-// the double expression. Requires finite x and a normal s >= 2^-100.
-__device__ __forceinline__ int round_away_quotient(float x, float s, bool &undecided) {
+// FP32 with the caller's inv_s = RN(1/s) (one reciprocal serves a block of quotients). With
+// q = |x| / s: y = RN(|x| inv_s) is within 2^-20 of q (two roundings, q < 7.25); the FMA remainder
+// r = RN(|x| - y s) times inv_s gives c with |y + c - q| < 2^-42; the double quotient is within
+// 2^-50 of q. Near a half-integer, g = RN((f - 0.5) + c) (f = y - floor(y), f - 0.5 exact there)
+// is within 2^-37.8 of q - floor(y) - 0.5, so the rounding is decided unless that lies within
+// 2^-36 of zero, where `undecided` is set and the caller evaluates the double expression.
+// Requires finite x and a normal s >= 2^-100.
+__device__ __forceinline__ int round_away_quotient(float x, float s, float inv_s, bool &undecided) {
     const float ax = fabsf(x);
-    const float y = __fdiv_rn(ax, s);
-    if (!(y < 7.25f)) return x < 0.0f ? -7 : 7;  // rounds to 7 or more either way
-    const float r = __fmaf_rn(-y, s, ax);
-    const float c = __fdiv_rn(r, s);
+    const float y = __fmul_rn(ax, inv_s);
+    if (!(y < 7.25f)) return x < 0.0f ? -7 : 7;  // q > 7.24: rounds to 7 or more either way
     const float n = floorf(y);
     const float f = __fsub_rn(y, n);  // exact
     int q = static_cast<int>(n) + (f > 0.5f ? 1 : 0);
     if (fabsf(__fsub_rn(f, 0.5f)) < 0x1p-14f) {
-        const float g = __fadd_rn(__fsub_rn(f, 0.5f), c);  // f - 0.5 exact for f in [0.25, 0.75]
+        const float r = __fmaf_rn(-y, s, ax);
+        const float c = __fmul_rn(r, inv_s);
+        const float g = __fadd_rn(__fsub_rn(f, 0.5f), c);
         if (g > 0x1p-36f) q = static_cast<int>(n) + 1;
         else if (g < -0x1p-36f) q = static_cast<int>(n);
         else undecided = true;

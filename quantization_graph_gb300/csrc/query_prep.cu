@@ -445,7 +445,7 @@ __global__ void round_quotient_kernel(const float *x, const float *s, size_t n, 
     const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     bool und = !(s[i] >= 0x1p-100f) || !isfinite(x[i]);
-    int q = und ? 0 : round_away_quotient(x[i], s[i], und);
+    int q = und ? 0 : round_away_quotient(x[i], s[i], __frcp_rn(s[i]), und);
     if (und) q = max(-7, min(7, static_cast<int>(round(static_cast<double>(x[i]) / static_cast<double>(s[i])))));
     out[i] = q;
     if (undecided) undecided[i] = und ? 1 : 0;

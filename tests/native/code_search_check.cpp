@@ -72,7 +72,7 @@ extern "C" int qcs_run(int D, const float *ru, double *t_heap, double *t_lane0, 
     }
     std::sort(keys.begin(), keys.end());
     *t_heap = heap_search(a, c0, max_o);
-    std::vector<long long> blk(D / 32 + 2);
+    std::vector<long long> blk(D / 16 + 2);
     double t0 = 0.0, tw = 0.0;
     bool ok = false;
     std::vector<float> ruv(ru, ru + D);

@@ -80,6 +80,18 @@ T shfl_idx(unsigned mask, T v, int src, int width = 32) {
 
 inline void syncwarp() { g_warp->bar.arrive_and_wait(); }
 
+inline unsigned int ballot(unsigned mask, int pred) {
+    (void)mask;
+    Warp &w = *g_warp;
+    w.slot[t_lane] = pred != 0 ? 1u : 0u;
+    w.bar.arrive_and_wait();
+    unsigned int r = 0;
+    for (int l = 0; l < 32; ++l)
+        if (w.slot[l]) r |= 1u << l;
+    w.bar.arrive_and_wait();
+    return r;
+}
+
 // fn(lane) on 32 threads as one warp; returns after every lane has finished.
 inline void run_warp(const std::function<void(int)> &fn) {
     Warp w;
@@ -101,9 +113,11 @@ inline void run_warp(const std::function<void(int)> &fn) {
 #define __shfl_xor_sync(...) warp_emu::shfl_xor(__VA_ARGS__)
 #define __shfl_sync(...) warp_emu::shfl_idx(__VA_ARGS__)
 #define __syncwarp(...) warp_emu::syncwarp()
+#define __ballot_sync(...) warp_emu::ballot(__VA_ARGS__)
 
 inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }
 inline float __fmul_rn(float a, float b) { return a * b; }
+inline float __frcp_rn(float a) { return 1.0f / a; }
 inline float __fadd_rn(float a, float b) { return a + b; }
 inline float __fsub_rn(float a, float b) { return a - b; }
 inline double __fma_rn(double a, double b, double c) { return std::fma(a, b, c); }
@@ -135,6 +149,8 @@ inline int __popc(unsigned int x) { return __builtin_popcount(x); }
 inline float __fdiv_rn(float a, float b) { return a / b; }
 inline float __ll2float_rn(long long x) { return static_cast<float>(x); }
 inline int __ffsll(long long x) { return __builtin_ffsll(x); }
+inline int __ffs(int x) { return __builtin_ffs(x); }
+inline float __log2f(float x) { return std::log2(x); }
 inline int __clzll(long long x) { return x == 0 ? 64 : __builtin_clzll(static_cast<unsigned long long>(x)); }
 inline double __longlong_as_double(long long x) {
     double d;
