@@ -62,6 +62,9 @@ def parse(argv=None):
     ap.add_argument("--target-recall", type=float, default=0.95)
     ap.add_argument("--L", type=int, default=0, help="fixed L (0 = sweep)")
     ap.add_argument("--tile", type=int, default=0, help="search tile shape (qg_index_set_tile, 0..4)")
+    ap.add_argument("--codecs", default="int4,b1,b1main,full",
+                    help="query codecs measured beside the Int8 headline on the same index (empty: none)")
+    ap.add_argument("--codec-parity-queries", type=int, default=200)
     ap.add_argument("--parity-queries", type=int, default=1000,
                     help="queries re-run by the CPU restatement at the headline L and compared bit for bit")
     ap.add_argument("--encode-parity-rows", type=int, default=10_000,
@@ -350,6 +353,61 @@ def oracle_index(w, n):
     return dict(compact=host(w["compact"]), residual=host(w["residual"]), msb=host(w["msb"]),
                 factors=host(w["factors"]), degrees=host(w["deg"]).view(np.uint32),
                 edges=host(w["edges"]).view(np.uint32), total_points=n, base_points=n)
+
+
+def codec_ablation(torch, w, args, log):
+    """The reference's ablation query codecs (rabitq_set_query_coarse_codec: Int4, B1, B1Main,
+    Full) through the same index and queries as the Int8 headline: for each, the smallest L
+    reaching the recall target (the headline's sweep), its device-timed QPS, and parity with the
+    oracle searching with that codec on a sample of the queries (ids, distance bits, counters)."""
+    from quantization_graph_gb300.space import CODEC_B1, CODEC_B1MAIN, CODEC_FULL, CODEC_INT4, CODEC_INT8
+
+    codes = {"int4": CODEC_INT4, "b1": CODEC_B1, "b1main": CODEC_B1MAIN, "full": CODEC_FULL}
+    names = [c.strip() for c in args.codecs.split(",") if c.strip()]
+    if not names:
+        return {}
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+
+    oracle_py.build()
+    space, index, q = w["space"], w["index"], w["queries"]
+    nq = q.shape[0]
+    sweep_args = argparse.Namespace(**{**vars(args), "L": 0})
+    ids = torch.empty((nq, args.k), dtype=torch.int32, device="cuda")
+    dists = torch.empty((nq, args.k), dtype=torch.float32, device="cuda")
+    stats = torch.empty((nq, 9), dtype=torch.int64, device="cuda")
+    center = space.center.cpu().numpy() if hasattr(space.center, "cpu") else space.center
+    oindex = oracle_index(w, args.n)
+    out = {}
+    try:
+        for name in names:
+            space.set_query_coarse_codec(codes[name])
+            log(f"codec {name}:")
+            L, rec, _ = pick_l(torch, w, sweep_args, log)
+            index.search_into(q, ids, dists, k=args.k, l_value=L, stats_out=stats)
+            torch.cuda.synchronize()
+            for _ in range(args.warmup):
+                index.search_into(q, ids, dists, k=args.k, l_value=L)
+            ms = device_ms(torch, lambda: index.search_into(q, ids, dists, k=args.k, l_value=L), args.steps)
+            count = min(nq, args.codec_parity_queries)
+            sample = np.linspace(0, nq - 1, count).astype(np.int64)
+            o = oracle_py.Oracle(args.dim, center, codec=codes[name])
+            oi, od, ost = o.search(q.cpu().numpy()[sample], oindex, k=args.k, L=L, threads=os.cpu_count() or 1)
+            gi = ids.cpu().numpy().view(np.uint32)[sample]
+            gd = dists.cpu().numpy()[sample]
+            gs = stats_struct(stats, nq)[sample]
+            c_bad = np.zeros(count, bool)
+            for f in gs.dtype.names:
+                c_bad |= gs[f] != ost[f]
+            out[name] = {"L": int(L), "recall@10": round(float(rec), 4), "qps": round(nq / ms * 1000.0, 1),
+                         "ms_per_batch": round(ms, 3),
+                         "parity": {"queries": int(count), "id_mismatch": int((~(gi == oi).all(1)).sum()),
+                                    "dist_bit_mismatch": int((~(gd.view(np.uint32) == od.view(np.uint32)).all(1)).sum()),
+                                    "counter_mismatch": int(c_bad.sum())}}
+            log(f"  codec {name}: L={L} recall {rec:.4f}, {out[name]['qps']:.0f} QPS, parity {out[name]['parity']}")
+    finally:
+        space.set_query_coarse_codec(CODEC_INT8)
+    return out
 
 
 def cpu_parity(w, args, L, gpu_ids, gpu_dists, gpu_stats, log):
@@ -810,6 +868,8 @@ def main():
     if rank == 0 and not args.skip_cpu:
         parity, cpu = cpu_parity(w, args, L, fixed_ids, fixed_d, fixed_stats, log)
         enc = encode_parity(w, args, log)
+        if world == 1 and args.codecs:
+            search_info["codecs"] = codec_ablation(torch, w, args, log)
     search_info.update({"recall@10": round(final_recall, 4), "recall@10_gathered_shards": round(sharded_recall, 4),
                         "queries_per_rank": nl, "l_sweep": {str(k_): round(v, 4) for k_, v in sweep.items()}})
     line = {"metric": metric, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
@@ -831,6 +891,9 @@ def main():
     if rank == 0:
         print(json.dumps(line), flush=True)
     bad = parity is not None and (parity["id_mismatch"] or parity["dist_bit_mismatch"] or parity["counter_mismatch"])
+    for c in search_info.get("codecs", {}).values():
+        p_ = c["parity"]
+        bad = bad or bool(p_["id_mismatch"] or p_["dist_bit_mismatch"] or p_["counter_mismatch"])
     if world > 1:
         dist.destroy_process_group()
     if bad:
