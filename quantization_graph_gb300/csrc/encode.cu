@@ -78,11 +78,13 @@ __device__ float mse_scale16_f64(const float *e) {
 }
 
 // The same scale with one FP64 operation per iteration. Each q = round(e / scale) is decided in
-// FP32 (round_away_quotient, one reciprocal per iteration); n = sum e_i q_i is summed exactly in
-// int64 on the grid of the smallest term, which equals the reference's double sum whenever every
-// partial sum fits 53 bits there (the products e_i q_i are exact in double); n is then that
-// double exactly, and next = float(n / d) is the reference's own double division and rounding.
-// Returns false when a condition fails; the caller then takes mse_scale16_f64.
+// FP32 (round_away_quotient, one reciprocal per iteration). n = sum e_i q_i is summed exactly in
+// int64 on the grid 2^G of the block's smallest nonzero e (at least as fine as the grid of the
+// terms the reference adds), which equals the reference's double sum whenever every partial sum
+// fits 53 bits there (the products e_i q_i are exact in double): checked once per block from
+// sum 7 |e_i| when that is enough, else per partial sum. n is then that double exactly, and
+// next = float(n / d) is the reference's own double division and rounding. Returns false when a
+// condition fails; the caller then takes mse_scale16_f64.
 __device__ bool mse_scale16_exact(const float *e, float *out) {
     float m = 0.0f;
     for (int i = 0; i < 16; ++i) m = fmaxf(m, fabsf(e[i]));
@@ -96,36 +98,43 @@ __device__ bool mse_scale16_exact(const float *e, float *out) {
         return true;
     }
     constexpr long long kLim = 1LL << 53;
+    // the errors as integers on the common grid: e_i = u_i 2^G
+    int G = 1 << 30;
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+        if (e[i] != 0.0f) G = min(G, split_float(e[i]).e);
+    if (G < -1000) return false;
+    long long u[16];
+    long long mag = 0;  // sum |u_i|, bounded by 16 * 2^60 below
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        u[i] = 0;
+        if (e[i] == 0.0f) continue;
+        const FloatParts p = split_float(e[i]);
+        const int sh = p.e - G;
+        if (sh > 36) return false;  // |u_i| < 2^60
+        u[i] = p.m * (1LL << sh);
+        mag += u[i] < 0 ? -u[i] : u[i];
+    }
+    const bool safe = mag < kLim / 7;  // |q| <= 7: no partial sum can reach 2^53
     for (int iter = 0; iter < 8; ++iter) {
         if (!(scale >= 0x1p-100f)) return false;
         const float inv = __frcp_rn(scale);
-        int d = 0, G = 1 << 30;
-        int qv[16];
+        int d = 0;
+        long long N = 0;
+        bool ok = true;
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
             bool und = false;
             int q = round_away_quotient(e[i], scale, inv, und);
             if (und) q = max(-7, min(7, round_away(static_cast<double>(e[i]) / static_cast<double>(scale))));
-            qv[i] = q;
             d += q * q;
-            if (q != 0 && e[i] != 0.0f) G = min(G, split_float(e[i]).e);
+            N += u[i] * q;  // |u_i q| < 2^63
+            if (!safe) ok = ok && N < kLim && N > -kLim;
         }
+        if (!ok) return false;  // a partial sum may have rounded
         if (d <= 0) break;
-        long long N = 0;
-        if (G != (1 << 30)) {
-            for (int i = 0; i < 16; ++i) {
-                if (qv[i] == 0 || e[i] == 0.0f) continue;
-                const FloatParts p = split_float(e[i]);
-                const int sh = p.e - G;
-                if (sh > 36) return false;
-                const long long term = (p.m * qv[i]) * (1LL << sh);  // |p.m q| < 2^27: below 2^63
-                if (term >= kLim || term <= -kLim) return false;
-                N += term;
-                if (N >= kLim || N <= -kLim) return false;  // a partial sum may have rounded
-            }
-        }
         if (N == 0) break;  // next = 0: the reference stops
-        if (G < -1000 || G > 1000) return false;
         const double n = __ll2double_rn(N) * pow2d(G);  // exact
         const float next = __double2float_rn(__ddiv_rn(n, static_cast<double>(d)));
         if (next <= 0.0f || !isfinite(next)) break;
@@ -224,7 +233,7 @@ __device__ void rotated_row(const EncodeArgs &a, int v, float *ru, int lane, flo
 // the rotated row again (re-derived from the input) and the quantisation errors (floats [D, 2D));
 // the codes c0[D]; the residual codes rcode[D] (the code search's block prefix sums before them).
 template <bool kRotated>
-__global__ void __launch_bounds__(32) encode_kernel(EncodeArgs a) {
+__global__ void __launch_bounds__(32, 10) encode_kernel(EncodeArgs a) {  // 10 per SM: the shared-memory limit at D = 2048
     extern __shared__ __align__(16) unsigned char smem[];
     const int D = a.code_dim, lane = threadIdx.x;
     unsigned long long *keys = reinterpret_cast<unsigned long long *>(smem);   // [D]
