@@ -162,19 +162,26 @@ __device__ __forceinline__ int gate_chunk(uint32_t w, const int (&xg)[8], int ac
     return acc;
 }
 
+// Unsigned bytes of a times signed bytes of b, summed into c.
+__device__ __forceinline__ int dp4a_us(uint32_t a, int b, int c) {
+    int d;
+    asm("dp4a.u32.s32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
 // Integer traversal partial over one 32-dim chunk: sum of (code & 7) * x, or of the whole 4-bit
-// code times x (kFull: the B1Main distance, x = +-1).
+// code times x (kFull: the B1Main distance, x = +-1). Both nibbles are masked in place: the low
+// ones sum into lo, the high ones (byte values 16 * code) into hi, and the row's sum is
+// lo + hi / 16 (exact: hi is a multiple of 16), formed once per row by the caller.
 template <bool kFull = false>
-__device__ __forceinline__ int trav_chunk(const uint4 c, const int (&xe)[4], const int (&xo)[4],
-                                          int acc) {
+__device__ __forceinline__ void trav_chunk(const uint4 c, const int (&xe)[4], const int (&xo)[4], int &lo, int &hi) {
     constexpr uint32_t kMask = kFull ? 0x0F0F0F0Fu : 0x07070707u;
     const uint32_t w[4] = {c.x, c.y, c.z, c.w};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        acc = __dp4a(static_cast<int>(w[k] & kMask), xe[k], acc);
-        acc = __dp4a(static_cast<int>((w[k] >> 4) & kMask), xo[k], acc);
+        lo = dp4a_us(w[k] & kMask, xe[k], lo);
+        hi = dp4a_us(w[k] & (kMask << 4), xo[k], hi);
     }
-    return acc;
 }
 
 // Reduce-scatter of N per-lane partial sums across the warp (N = 32, 16, 8 or 4): on return
@@ -588,10 +595,10 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                         int p[G];
     #pragma unroll
                         for (int g = 0; g < G; ++g) {
-                            int acc = 0;
+                            int lo = 0, hi = 0;
     #pragma unroll
-                            for (int j = 0; j < L::CPL; ++j) acc = trav_chunk<kMode == 2>(c[g][j], qr.xe[j], qr.xo[j], acc);
-                            p[g] = acc;
+                            for (int j = 0; j < L::CPL; ++j) trav_chunk<kMode == 2>(c[g][j], qr.xe[j], qr.xo[j], lo, hi);
+                            p[g] = lo + (hi >> 4);
                         }
                         const int tot = reduce_scatter<G>(p, lane);
                         const int i = gb + lane;
@@ -611,7 +618,9 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                         }
     #pragma unroll
                         for (int pp = 0; pp < P; ++pp) {
-                            int acc = trav_chunk<kMode == 2>(c[pp], qr.xe[0], qr.xo[0], 0);
+                            int lo = 0, hi = 0;
+                            trav_chunk<kMode == 2>(c[pp], qr.xe[0], qr.xo[0], lo, hi);
+                            int acc = lo + (hi >> 4);
     #pragma unroll
                             for (int o = 1; o < L::LPN; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
                             const int i = ib + pp * L::NBP + grp;
