@@ -90,6 +90,41 @@ __device__ __forceinline__ float restore_distance_hw(const uint8_t *__restrict__
     return out;
 }
 
+// restore_distance_hw for two records at once (r0, r1): the same operations in the same order for
+// each, as two independent chains per lane.
+template <int D>
+__device__ __forceinline__ void restore_distance_hw2(const uint8_t *__restrict__ c0, const uint8_t *__restrict__ c1,
+                                                     const float *__restrict__ rr, float4 h0, float4 h1,
+                                                     float half_sum, float qn2, int t, float *d0, float *d1) {
+    constexpr int kPairs = D / 2;
+    float sel0 = 0.0f, rem0 = 0.0f, sel1 = 0.0f, rem1 = 0.0f;
+#pragma unroll 8
+    for (int base = 0; base < kPairs; base += 16) {
+        const int pair = base + t;
+        const uint32_t p0 = c0[pair], p1 = c1[pair];
+        const float2 q = *reinterpret_cast<const float2 *>(rr + 2 * pair);
+        const uint32_t lo0 = p0 & 0x0Fu, hi0 = p0 >> 4, lo1 = p1 & 0x0Fu, hi1 = p1 >> 4;
+        rem0 = __fmaf_rn(static_cast<float>(lo0 & 7u), q.x, rem0);
+        rem1 = __fmaf_rn(static_cast<float>(lo1 & 7u), q.x, rem1);
+        rem0 = __fmaf_rn(static_cast<float>(hi0 & 7u), q.y, rem0);
+        rem1 = __fmaf_rn(static_cast<float>(hi1 & 7u), q.y, rem1);
+        if (lo0 > 7u) sel0 = sel0 + q.x;
+        if (lo1 > 7u) sel1 = sel1 + q.x;
+        if (hi0 > 7u) sel0 = sel0 + q.y;
+        if (hi1 > 7u) sel1 = sel1 + q.y;
+    }
+    sel0 = reduce16_tree(sel0);
+    rem0 = reduce16_tree(rem0);
+    sel1 = reduce16_tree(sel1);
+    rem1 = reduce16_tree(rem1);
+    float o0 = finish_long(h0.x, h0.y, sel0 - half_sum, rem0, half_sum, qn2);
+    float o1 = finish_long(h1.x, h1.y, sel1 - half_sum, rem1, half_sum, qn2);
+    if (!(h0.y > 0.0f) || !f_isfinite(h0.y)) o0 = h0.x + qn2;
+    if (!(h1.y > 0.0f) || !f_isfinite(h1.y)) o1 = h1.x + qn2;
+    *d0 = o0;
+    *d1 = o1;
+}
+
 // The Full codec's survivor distance: the restore's 16-lane sums with the gate's FP32 short ip
 // reused when `reuse` (query_distance_with_paper_msb, space_rabitq.h:3961-3966, 1609-1619; its
 // remaining-bit sum, dotRemainingUint8FloatAvx512 :1052-1073, has the restore's lanes and
@@ -339,6 +374,49 @@ __device__ __forceinline__ void residual_interval_thread(const uint16_t *__restr
     *est = distance;
     *lo_out = distance - err;
     *hi_out = distance + err;
+}
+
+// The estimate of residual_interval_thread for two records at once (a, b): the same operations
+// in the same order for each, as independent chains sharing the query loads.
+template <int D>
+__device__ __forceinline__ void residual_estimate_thread2(const uint16_t *__restrict__ sa, const uint8_t *__restrict__ ca,
+                                                          float long_a, const uint16_t *__restrict__ sb,
+                                                          const uint8_t *__restrict__ cb, float long_b,
+                                                          const float *__restrict__ rr, bool fused, float *est_a,
+                                                          float *est_b) {
+    constexpr int kBlocks = D / 16;
+    float ipa = 0.0f, ipb = 0.0f;
+    for (int b = 0; b < kBlocks; ++b) {
+        const float sca = __half2float(__ushort_as_half(sa[b])), scb = __half2float(__ushort_as_half(sb[b]));
+        const uint2 pa = *reinterpret_cast<const uint2 *>(ca + 8 * b);
+        const uint2 pb = *reinterpret_cast<const uint2 *>(cb + 8 * b);
+        const float4 *q4 = reinterpret_cast<const float4 *>(rr + 16 * b);
+        float bia = 0.0f, bib = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const float4 q = q4[j >> 1];
+            const float qe = (j & 1) ? q.z : q.x;
+            const float qo = (j & 1) ? q.w : q.y;
+            const uint32_t bya = ((j < 4 ? pa.x : pa.y) >> (8 * (j & 3))) & 0xFFu;
+            const uint32_t byb = ((j < 4 ? pb.x : pb.y) >> (8 * (j & 3))) & 0xFFu;
+            int la = static_cast<int>(bya & 0x0Fu), ha = static_cast<int>(bya >> 4);
+            int lb = static_cast<int>(byb & 0x0Fu), hb = static_cast<int>(byb >> 4);
+            la -= (la > 7) ? 16 : 0;
+            ha -= (ha > 7) ? 16 : 0;
+            lb -= (lb > 7) ? 16 : 0;
+            hb -= (hb > 7) ? 16 : 0;
+            const float fla = static_cast<float>(la), fha = static_cast<float>(ha);
+            const float flb = static_cast<float>(lb), fhb = static_cast<float>(hb);
+            const float pra = fused ? __fmaf_rn(fla, qe, __fmul_rn(fha, qo)) : __fmaf_rn(fha, qo, __fmul_rn(fla, qe));
+            const float prb = fused ? __fmaf_rn(flb, qe, __fmul_rn(fhb, qo)) : __fmaf_rn(fhb, qo, __fmul_rn(flb, qe));
+            bia = bia + pra;
+            bib = bib + prb;
+        }
+        if (sca != 0.0f && f_isfinite(sca)) ipa = __fmaf_rn(sca, bia, ipa);
+        if (scb != 0.0f && f_isfinite(scb)) ipb = __fmaf_rn(scb, bib, ipb);
+    }
+    *est_a = long_a - 2.0f * ipa;
+    *est_b = long_b - 2.0f * ipb;
 }
 
 // Byte masks of four MSB bits: nibble b3..b0 -> bytes (b0, b1, b2, b3), each 0 or 1. The

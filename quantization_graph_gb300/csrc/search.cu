@@ -169,6 +169,24 @@ __device__ __forceinline__ int dp4a_us(uint32_t a, int b, int c) {
     return d;
 }
 
+// The gate partial over a lane's CPL >= 2 chunks of one row, without the shifts: w & (0x01010101
+// << k) has byte values 2^k per set bit, so acc_k = 2^k (the sum of group k) exactly, and the row's
+// sum is sum_k acc_k >> k (exact: acc_k is a multiple of 2^k), formed once per row.
+template <int CPL>
+__device__ __forceinline__ int gate_row(const uint32_t (&w)[CPL], const int (&xg)[CPL][8]) {
+    int acc[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc[k] = 0;
+#pragma unroll
+    for (int j = 0; j < CPL; ++j)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) acc[k] = dp4a_us(w[j] & (0x01010101u << k), xg[j][k], acc[k]);
+    int sum = acc[0];
+#pragma unroll
+    for (int k = 1; k < 8; ++k) sum += acc[k] >> k;
+    return sum;
+}
+
 // Integer traversal partial over one 32-dim chunk: sum of (code & 7) * x, or of the whole 4-bit
 // code times x (kFull: the B1Main distance, x = +-1). Both nibbles are masked in place: the low
 // ones sum into lo, the high ones (byte values 16 * code) into hi, and the row's sum is
@@ -471,12 +489,16 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
     #pragma unroll
                         for (int g = 0; g < G; ++g) {
                             int acc = 0;
+                            if constexpr (!kB1 && L::CPL >= 2) {
+                                acc = gate_row<L::CPL>(w[g], qr.xg);
+                            } else {
     #pragma unroll
-                            for (int j = 0; j < L::CPL; ++j) {
-                                if constexpr (kB1)
-                                    acc += __popc(w[g][j] ^ static_cast<uint32_t>(qr.xg[j][0]));
-                                else
-                                    acc = gate_chunk(w[g][j], qr.xg[j], acc);
+                                for (int j = 0; j < L::CPL; ++j) {
+                                    if constexpr (kB1)
+                                        acc += __popc(w[g][j] ^ static_cast<uint32_t>(qr.xg[j][0]));
+                                    else
+                                        acc = gate_chunk(w[g][j], qr.xg[j], acc);
+                                }
                             }
                             p[g] = acc;
                         }
@@ -845,25 +867,34 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
     // nothing); B1Main's and Full's residuals correct the distances in the pool (4-bit x 1-bit,
     // mode 1) (ours_diskann.rs:1849-1883).
     if constexpr (kMode <= 1) {
-        for (int base = 0; base < m; base += 2) {
-            const int e = base + (lane >> 4);
-            const int ee = e < m ? e : base;
-            const uint32_t id = s.pid[ee];
-            const float4 h = ix.hdr[id];
-            const float d = restore_distance_hw<D>(ix.codes + static_cast<size_t>(id) * (D / 2), rr,
-                                                   h.x, h.y, half_sum, qn2, lane & 15);
-            if ((lane & 15) == 0 && e < m) s.pd[e] = d;
+        // four records per pass: e and e + 2 on each half-warp
+        for (int base = 0; base < m; base += 4) {
+            const int e0 = base + (lane >> 4), e1 = e0 + 2;
+            const uint32_t id0 = s.pid[e0 < m ? e0 : base], id1 = s.pid[e1 < m ? e1 : base];
+            float d0, d1;
+            restore_distance_hw2<D>(ix.codes + static_cast<size_t>(id0) * (D / 2),
+                                    ix.codes + static_cast<size_t>(id1) * (D / 2), rr, ix.hdr[id0], ix.hdr[id1],
+                                    half_sum, qn2, lane & 15, &d0, &d1);
+            if ((lane & 15) == 0) {
+                if (e0 < m) s.pd[e0] = d0;
+                if (e1 < m) s.pd[e1] = d1;
+            }
         }
         __syncwarp();
     }
-    // residual correction, one record per lane
-    for (int e = lane; e < m; e += 32) {
-        const uint32_t id = s.pid[e];
-        float est, lo, hi;
-        residual_interval_thread<D>(ix.res_scales + static_cast<size_t>(id) * (D / 16),
-                                    ix.res_codes + static_cast<size_t>(id) * (D / 2), rr, s.pd[e],
-                                    qn, a.fused_rerank != 0, &est, &lo, &hi);
-        s.plb[e] = est;
+    // residual correction: records e and e + 32 on each lane
+    (void)qn;
+    for (int e0 = lane; e0 < m; e0 += 64) {
+        const int e1 = e0 + 32 < m ? e0 + 32 : e0;
+        const uint32_t id0 = s.pid[e0], id1 = s.pid[e1];
+        float est0, est1;
+        residual_estimate_thread2<D>(ix.res_scales + static_cast<size_t>(id0) * (D / 16),
+                                     ix.res_codes + static_cast<size_t>(id0) * (D / 2), s.pd[e0],
+                                     ix.res_scales + static_cast<size_t>(id1) * (D / 16),
+                                     ix.res_codes + static_cast<size_t>(id1) * (D / 2), s.pd[e1], rr,
+                                     a.fused_rerank != 0, &est0, &est1);
+        s.plb[e0] = est0;
+        if (e1 != e0) s.plb[e1] = est1;
     }
     __syncwarp();
     // top-k by (estimate, id): rank of each candidate among all candidates
