@@ -91,6 +91,7 @@ def parse(argv=None):
                          "cores against the reference encoder")
     ap.add_argument("--stream-n", type=int, default=120_000)
     ap.add_argument("--stream-queries", type=int, default=200_000)
+    ap.add_argument("--stream-inflight", type=int, default=8, help="batches in flight (SearchPool)")
     ap.add_argument("--stream-thresholds", default="0.9,0.95,0.98",
                     help="learned-stop thresholds tried on the stream ('' = fixed per-query L only)")
     ap.add_argument("--setup-cache", default="", help=argparse.SUPPRESS)  # internal: the reference arm's set-up
@@ -999,7 +1000,8 @@ def run_stream(args, log):
     """Uneven batched stream: 200k queries over a 120k x 1024 clustered unit-norm index (16
     clusters, lambda_i ~ i^-1.0 within each), batch sizes log-uniform in [1, 4096], per-query
     k in {1, 10, 100} and L uniform in [20, 400]; every batch is one replay of the captured
-    CUDA graph (GraphSearcher) with the autotuned launch shape. Reports QPS over the whole
+    CUDA graph (GraphSearcher, several in flight through SearchPool) with the autotuned launch
+    shape. Reports QPS over the whole
     stream and p50/p99 batch latency, measured end to end from pinned host buffers (queries,
     k and L copied in, ids copied out, per batch)."""
     import torch
@@ -1009,7 +1011,7 @@ def run_stream(args, log):
     from quantization_graph_gb300.graph_build import build_graph, build_vamana, reachable_fraction
     from quantization_graph_gb300.index import OursIndex
     from quantization_graph_gb300.space import RabitqSpace, train_global_center
-    from quantization_graph_gb300.stream import GraphSearcher, autotune
+    from quantization_graph_gb300.stream import SearchPool, autotune
 
     dim, n, nq_total = 1024, args.stream_n, args.stream_queries
     t0 = time.time()
@@ -1070,31 +1072,15 @@ def run_stream(args, log):
     k1 = torch.from_numpy(kq == 1)
     gtc = gt.cpu()
 
+    bounds = np.concatenate([[0], np.cumsum(sizes)])
+    batches = [(hq[a:b], hk[a:b], hl[a:b]) for a, b in zip(bounds[:-1], bounds[1:])]
+
     def measure(thr):
-        gs = GraphSearcher(index, dim, max_batch=4096, max_k=100, max_l=400, model=model if thr else None,
-                           threshold=thr)
-
-        def run():
-            lat = []
-            start = 0
-            t_all = time.perf_counter()
-            for b in sizes:
-                tb = time.perf_counter()
-                with torch.cuda.stream(gs.stream):
-                    dq = hq[start:start + b].to("cuda", non_blocking=True)
-                    dk = hk[start:start + b].to("cuda", non_blocking=True)
-                    dl = hl[start:start + b].to("cuda", non_blocking=True)
-                ids, _ = gs.search(dq, dk, dl)
-                with torch.cuda.stream(gs.stream):
-                    out[start:start + b].copy_(ids, non_blocking=True)
-                gs.synchronize()
-                lat.append((time.perf_counter() - tb) * 1000.0)
-                start += b
-            return lat, time.perf_counter() - t_all
-
-        run()  # warm-up pass over the whole stream
+        pool = SearchPool(index, dim, max_batch=4096, max_k=100, max_l=400, inflight=args.stream_inflight,
+                          model=model if thr else None, threshold=thr)
+        pool.run(batches, out)  # warm-up pass over the whole stream
         with ClockSampler(0) as clocks:
-            lat, elapsed = run()
+            lat, elapsed = pool.run(batches, out)
         ids_all = out.to(torch.int64)
         hit = (ids_all[k10][:, :10, None] == gtc[k10][:, None, :10]).any(-1).sum().item()
         rec10 = hit / (int(k10.sum()) * 10)
@@ -1108,7 +1094,7 @@ def run_stream(args, log):
         log(f"  stream {'fixed L' if not thr else f'learned stop t={thr}'}: {r['qps']:.0f} qps, "
             f"recall@10 {rec10:.4f}, recall@1 {rec1:.4f}, p50 {r['batch_latency_ms']['p50']:.2f} ms, "
             f"p99 {r['batch_latency_ms']['p99']:.2f} ms")
-        del gs
+        del pool
         return r
 
     fixed = measure(None)
@@ -1132,7 +1118,11 @@ def run_stream(args, log):
                        "recall@1 (k=1 queries)": best_mode["recall@1 (k=1 queries)"],
                        "batch_latency_ms": best_mode["batch_latency_ms"],
                        "modes": [{k_: v for k_, v in m.items() if k_ != "clocks"} for m in modes],
-                       "timing": "host wall clock per batch: pinned H2D of queries/k/L, graph replay, D2H of ids"},
+                       "inflight": args.stream_inflight,
+                       "timing": (f"up to {args.stream_inflight} batches in flight (SearchPool: a handle and a stream "
+                                  "each); QPS = queries / wall time of the whole stream; batch latency = device "
+                                  "time on the batch's stream from its pinned H2D of queries/k/L through the graph "
+                                  "replay to the D2H of its ids")},
             "e2e": {"value": best_mode["qps"], "unit": "queries/s",
                     "h2d_bytes_per_step": int(nq_total * (dim * 4 + 8) / len(sizes)),
                     "d2h_bytes_per_step": int(nq_total * 400 / len(sizes))},

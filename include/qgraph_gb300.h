@@ -269,6 +269,11 @@ int qg_index_upload_device(const void *space, const void *d_compact, size_t comp
                            size_t edge_stride, size_t base_points, size_t total_points,
                            void *stream, qg_index **out);
 void qg_index_free(qg_index *index);
+/* No counterpart in the reference. A second handle on src's resident payload and adjacency (no
+ * copy) with its own search scratch, so that searches through different handles may run at the
+ * same time on different streams (searches through one handle must not overlap). The payload is
+ * freed with the last handle; launch and tile settings are copied, later changes are per handle. */
+int qg_index_share(const qg_index *src, qg_index **out);
 /* Device bytes held by the index (payload + adjacency + search scratch). */
 size_t qg_index_device_bytes(const qg_index *index);
 

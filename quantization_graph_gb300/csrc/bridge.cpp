@@ -1458,8 +1458,7 @@ int qg_residual_pairs(const void *space, const float *d_rotated, const float *d_
 }
 
 static void index_free_all(qg_index *ix) {
-    for (void *p : ix->owned) cudaFree(p);
-    ix->owned.clear();
+    ix->payload.reset();
     cudaFree(ix->visited);
     cudaFree(ix->counter);
     cudaFree(ix->status);
@@ -1489,13 +1488,14 @@ int qg_index_upload_device(const void *space, const void *d_compact, size_t comp
     }
     auto *ix = new (std::nothrow) qg_index();
     if (!ix) return QG_ERR_OOM;
+    ix->payload = std::make_shared<DeviceBlocks>();
     ix->space = s;
     cudaGetDevice(&ix->device);
     const size_t D = s->code_dim, nb = base_points, nt = total_points;
     auto own = [&](size_t bytes) -> void * {
         void *p = nullptr;
         if (cudaMalloc(&p, bytes ? bytes : 16) != cudaSuccess) return nullptr;
-        ix->owned.push_back(p);
+        ix->payload->ptrs.push_back(p);
         ix->device_bytes += bytes;
         return p;
     };
@@ -1583,6 +1583,33 @@ int qg_index_upload_host(const void *space, const void *compact, size_t compact_
                                     edge_stride, base_points, total_points, nullptr, out);
     for (void *p : tmp) cudaFree(p);
     return rc;
+}
+
+int qg_index_share(const qg_index *src, qg_index **out) {
+    if (!src || !out || !src->payload) {
+        set_error("qg_index_share: null argument");
+        return QG_ERR_INVALID;
+    }
+    auto *ix = new (std::nothrow) qg_index();
+    if (!ix) return QG_ERR_OOM;
+    ix->ix = src->ix;
+    ix->space = src->space;
+    ix->device = src->device;
+    ix->device_bytes = src->device_bytes;
+    ix->launch_wpb = src->launch_wpb;
+    ix->launch_per_sm = src->launch_per_sm;
+    ix->tile = src->tile;
+    ix->payload = src->payload;
+    ix->counter = dev_alloc<unsigned int>(1);
+    ix->status = dev_alloc<int>(1);
+    if (!ix->counter || !ix->status || cudaMemset(ix->status, 0, 4) != cudaSuccess) {
+        set_error("qg_index_share: device allocation failed");
+        index_free_all(ix);
+        delete ix;
+        return QG_ERR_OOM;
+    }
+    *out = ix;
+    return QG_OK;
 }
 
 void qg_index_free(qg_index *index) {

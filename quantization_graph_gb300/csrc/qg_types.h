@@ -3,6 +3,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <memory>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -78,6 +79,19 @@ struct DevQueries {
 
 }  // namespace qg
 
+namespace qg {
+// Device allocations freed together when the last owner lets go.
+struct DeviceBlocks {
+    std::vector<void *> ptrs;
+    DeviceBlocks() = default;
+    DeviceBlocks(const DeviceBlocks &) = delete;
+    DeviceBlocks &operator=(const DeviceBlocks &) = delete;
+    ~DeviceBlocks() {
+        for (void *p : ptrs) cudaFree(p);
+    }
+};
+}  // namespace qg
+
 struct qg_index {
     qg::DevIndex ix;
     const qg::Space *space = nullptr;
@@ -96,5 +110,7 @@ struct qg_index {
     int launch_wpb = 0;      // qg_index_set_launch override (0 = automatic)
     int launch_per_sm = 0;
     int tile = 0;            // qg_index_set_tile: the search's tile shape
-    std::vector<void *> owned;
+    // the payload and adjacency allocations, shared by the handles qg_index_share makes and freed
+    // with the last of them; the scratch above belongs to this handle alone
+    std::shared_ptr<qg::DeviceBlocks> payload;
 };

@@ -70,6 +70,18 @@ class OursIndex:
     def device_bytes(self) -> int:
         return self.lib.qg_index_device_bytes(self.handle)
 
+    def share(self) -> "OursIndex":
+        """A second handle on this index's resident payload (qg_index_share: no copy, its own
+        search scratch), for searches that run at the same time on another stream."""
+        other = object.__new__(OursIndex)
+        other.space, other.lib = self.space, self.lib
+        other.base_points, other.total_points, other.max_degree = self.base_points, self.total_points, self.max_degree
+        other._source = self  # keeps the space and the first handle alive
+        handle = C.c_void_p()
+        N.check(self.lib.qg_index_share(self.handle, C.byref(handle)), "qg_index_share")
+        other.handle = handle
+        return other
+
     def search_into(self, queries: torch.Tensor, ids_out: torch.Tensor, dists_out: torch.Tensor,
                     k: int = 10, l_value: int = 100, beam_width: int = 1, epsilon0: float = 1.9,
                     rerank_candidates: int = 100, early_stop_hops: int = 0, kth_stop: bool = False,

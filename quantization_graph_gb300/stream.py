@@ -6,6 +6,9 @@ the maximum, any mix of per-query k and L -- only copies its queries, k, L and b
 the captured buffers and replays the graph. The kernels read the batch size on the device, so
 nothing is re-captured and nothing is allocated per batch.
 
+SearchPool keeps several batches in flight over one resident index (a searcher per handle from
+OursIndex.share, a stream each), so small batches share the GPU instead of queueing.
+
 autotune() times the persistent kernel's launch shapes (warps per block, resident blocks per
 SM) and, for code dims of 1024 and more, the tile shapes of its gate and traversal loops
 (qg_index_set_tile) on a sample of the workload and keeps the fastest on the index. Every shape
@@ -112,6 +115,58 @@ class GraphSearcher:
 
     def synchronize(self):
         self.stream.synchronize()
+
+
+class SearchPool:
+    """Several batches in flight over one resident index: `inflight` GraphSearchers, each on a
+    handle of its own (OursIndex.share: the same payload, separate scratch) and a stream of its
+    own, take the batches in turn. A searcher is reused only after its previous batch completes,
+    so the results of a batch stay valid until `inflight` more batches have been submitted."""
+
+    def __init__(self, index, dim: int, max_batch: int, max_k: int, max_l: int, inflight: int = 4, model=None,
+                 threshold: float | None = None, rerank: int = 100):
+        self.handles = [index] + [index.share() for _ in range(max(1, inflight) - 1)]
+        self.searchers = [GraphSearcher(h, dim, max_batch, max_k, max_l, model=model, threshold=threshold,
+                                        rerank=rerank) for h in self.handles]
+        self.next = 0
+        self.busy = [None] * len(self.searchers)  # per searcher: (start, end) events of its batch
+
+    def run(self, batches, out_ids=None):
+        """Serve (queries, k, L) batches (host or device tensors) in order with up to `inflight` in
+        flight; out_ids (pinned host [sum of batch sizes x max_k], optional) receives the ids.
+        Returns per-batch device latencies (ms, start of the batch's copies to the end of its
+        result copy, on its stream) and the elapsed wall seconds."""
+        lat = []
+        t_all = time.perf_counter()
+        row = 0
+        for qb, kb, lb in batches:
+            i = self.next
+            self.next = (i + 1) % len(self.searchers)
+            gs = self.searchers[i]
+            if self.busy[i] is not None:
+                s, e = self.busy[i]
+                e.synchronize()
+                lat.append(s.elapsed_time(e))
+            n = qb.shape[0]
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(gs.stream):
+                s.record()
+                gs.q[:n].copy_(qb, non_blocking=True)  # from pinned host memory: one H2D copy each
+                gs.k[:n].copy_(kb, non_blocking=True)
+                gs.l[:n].copy_(lb, non_blocking=True)
+                gs.nq.fill_(n)
+                gs.graph.replay()
+                if out_ids is not None:
+                    out_ids[row:row + n].copy_(gs.ids[:n], non_blocking=True)
+                e.record()
+            self.busy[i] = (s, e)
+            row += n
+        for i, b in enumerate(self.busy):
+            if b is not None:
+                b[1].synchronize()
+                lat.append(b[0].elapsed_time(b[1]))
+                self.busy[i] = None
+        return lat, time.perf_counter() - t_all
 
 
 def serve(searcher: GraphSearcher, batches, log=None):

@@ -79,3 +79,35 @@ def test_graph_replay_with_learned_stop_matches_direct_call(cuda):
     torch.cuda.synchronize()
     np.testing.assert_array_equal(ids.cpu().numpy(), ref_ids.cpu().numpy())
     np.testing.assert_array_equal(dists.cpu().numpy().view(np.uint32), ref_d.cpu().numpy().view(np.uint32))
+
+
+def test_search_pool_in_flight_matches_plain_search(cuda):
+    """Several batches in flight over shared handles of one index (SearchPool, qg_index_share)
+    return exactly what the ordinary search returns, batch by batch; a share searches on its own
+    after the pool's handles are gone."""
+    torch = cuda
+    from quantization_graph_gb300.stream import SearchPool
+
+    g, ix = _index(torch)
+    _, Q = SEARCH_CASES["search_c1"]()
+    rng = np.random.default_rng(9)
+    sizes = [1, 64, 7, 33, 2, 64, 13, 50, 3, 64]
+    bounds = np.concatenate([[0], np.cumsum(sizes)])
+    allq = np.concatenate([Q] * (int(bounds[-1]) // len(Q) + 1))
+    kq = rng.choice([1, 10, 100], size=bounds[-1]).astype(np.int32)
+    lq = rng.integers(10, 160, size=bounds[-1]).astype(np.int32)
+    hq = torch.from_numpy(allq[:bounds[-1]].copy()).pin_memory()
+    hk, hl = torch.from_numpy(kq).pin_memory(), torch.from_numpy(lq).pin_memory()
+    batches = [(hq[a:b], hk[a:b], hl[a:b]) for a, b in zip(bounds[:-1], bounds[1:])]
+    out = torch.empty((bounds[-1], 100), dtype=torch.int32).pin_memory()
+    pool = SearchPool(ix, 128, max_batch=64, max_k=100, max_l=160, inflight=3)
+    lat, elapsed = pool.run(batches, out)
+    assert len(lat) == len(sizes) and elapsed > 0
+    for a, b in zip(bounds[:-1], bounds[1:]):
+        ref = ix.search(hq[a:b].cuda(), k=100, l_value=160, k_per_query=hk[a:b], l_per_query=hl[a:b],
+                        with_stats=False)
+        np.testing.assert_array_equal(out[a:b].numpy().astype(np.uint32), ref.ids.cpu().numpy().astype(np.uint32))
+    share = ix.share()
+    del pool
+    r = share.search(torch.from_numpy(Q).cuda(), k=10, l_value=40)
+    np.testing.assert_array_equal(r.ids.cpu().numpy().astype(np.uint32), g["ids_L40_k10"])
