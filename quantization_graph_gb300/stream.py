@@ -148,6 +148,8 @@ class SearchPool:
                 e.synchronize()
                 lat.append(s.elapsed_time(e))
             n = qb.shape[0]
+            if n > gs.max_batch:
+                raise ValueError("batch larger than the captured maximum")
             s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             with torch.cuda.stream(gs.stream):
                 s.record()
