@@ -62,7 +62,7 @@ def parse(argv=None):
     ap.add_argument("--target-recall", type=float, default=0.95)
     ap.add_argument("--L", type=int, default=0, help="fixed L (0 = sweep)")
     ap.add_argument("--tile", type=int, default=0, help="search tile shape (qg_index_set_tile, 0..4)")
-    ap.add_argument("--codecs", default="int4,b1,b1main,full",
+    ap.add_argument("--codecs", default="int4,b1,b1main,full,int8_fused",
                     help="query codecs measured beside the Int8 headline on the same index (empty: none)")
     ap.add_argument("--codec-parity-queries", type=int, default=200)
     ap.add_argument("--parity-queries", type=int, default=1000,
@@ -358,12 +358,14 @@ def oracle_index(w, n):
 
 def codec_ablation(torch, w, args, log):
     """The reference's ablation query codecs (rabitq_set_query_coarse_codec: Int4, B1, B1Main,
-    Full) through the same index and queries as the Int8 headline: for each, the smallest L
+    Full) and the Int8 search with the opt-in fused rerank (RABITQ_ENABLE_FUSED_INT_RERANK)
+    through the same index and queries as the Int8 headline: for each, the smallest L
     reaching the recall target (the headline's sweep), its device-timed QPS, and parity with the
     oracle searching with that codec on a sample of the queries (ids, distance bits, counters)."""
     from quantization_graph_gb300.space import CODEC_B1, CODEC_B1MAIN, CODEC_FULL, CODEC_INT4, CODEC_INT8
 
-    codes = {"int4": CODEC_INT4, "b1": CODEC_B1, "b1main": CODEC_B1MAIN, "full": CODEC_FULL}
+    codes = {"int4": CODEC_INT4, "b1": CODEC_B1, "b1main": CODEC_B1MAIN, "full": CODEC_FULL,
+             "int8_fused": CODEC_INT8}  # the Int8 search with the opt-in fused restore + residual rerank
     names = [c.strip() for c in args.codecs.split(",") if c.strip()]
     if not names:
         return {}
@@ -383,17 +385,24 @@ def codec_ablation(torch, w, args, log):
     try:
         for name in names:
             space.set_query_coarse_codec(codes[name])
+            fused = name.endswith("_fused")
             log(f"codec {name}:")
             L, rec, _ = pick_l(torch, w, sweep_args, log)
-            index.search_into(q, ids, dists, k=args.k, l_value=L, stats_out=stats)
+            index.search_into(q, ids, dists, k=args.k, l_value=L, stats_out=stats, fused_int_rerank=fused)
             torch.cuda.synchronize()
+            if fused:
+                rec = recall_at(ids.to(torch.int64), w["gt"], args.k)
             for _ in range(args.warmup):
-                index.search_into(q, ids, dists, k=args.k, l_value=L)
-            ms = device_ms(torch, lambda: index.search_into(q, ids, dists, k=args.k, l_value=L), args.steps)
+                index.search_into(q, ids, dists, k=args.k, l_value=L, fused_int_rerank=fused)
+            ms = device_ms(torch, lambda: index.search_into(q, ids, dists, k=args.k, l_value=L,
+                                                            fused_int_rerank=fused), args.steps)
+            index.search_into(q, ids, dists, k=args.k, l_value=L, stats_out=stats, fused_int_rerank=fused)
+            torch.cuda.synchronize()
             count = min(nq, args.codec_parity_queries)
             sample = np.linspace(0, nq - 1, count).astype(np.int64)
             o = oracle_py.Oracle(args.dim, center, codec=codes[name])
-            oi, od, ost = o.search(q.cpu().numpy()[sample], oindex, k=args.k, L=L, threads=os.cpu_count() or 1)
+            oi, od, ost = o.search(q.cpu().numpy()[sample], oindex, k=args.k, L=L, threads=os.cpu_count() or 1,
+                                   fused=fused)
             gi = ids.cpu().numpy().view(np.uint32)[sample]
             gd = dists.cpu().numpy()[sample]
             gs = stats_struct(stats, nq)[sample]
