@@ -377,10 +377,14 @@ int qg_mlp_adam(float *d_master, uint16_t *d_weights, const float *d_grad, float
 /* Launch shape of the persistent search kernel: warps per block (2, 4 or 8) and an upper bound
  * on resident blocks per SM; 0 restores the automatic choice. Used by the autotuner. */
 int qg_index_set_launch(qg_index *index, int warps_per_block, int blocks_per_sm);
+/* The widest search block, in warps, of the kernel this index searches with (its code dim and
+ * tile shape): qg_index_set_launch's warps_per_block (at most 8) is capped to it. */
+int qg_index_max_block_warps(const qg_index *index);
 /* Tile shape of the search's gate and traversal loops for the Int8 / Int4 codecs at code dims
  * 1024 and 2048 (how many neighbours' rows each lane keeps in flight): 0 (the default) 16 MSB
  * chunks per lane and 2 code rows (8 at D = 1024); 1: 8 chunks; 2: 32 chunks; 3: twice the code
- * rows; 4: 8 chunks with fewer registers per thread and more resident warps. Results are
+ * rows; 4: shape 0 at the other residency (8-warp blocks at 128 registers where shape 0 has
+ * 7-warp blocks at 80, as at 2048, and the reverse at 1024). Results are
  * identical for every shape; only the speed differs. Other codecs and dims ignore it. Used by
  * the autotuner. Returns QG_ERR_INVALID outside 0..4. */
 int qg_index_set_tile(qg_index *index, int tile);

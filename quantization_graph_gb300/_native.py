@@ -115,6 +115,7 @@ _SIGS = {
     "qg_mlp_adam": (C.c_int, [P, P, P, P, P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, P]),
     "qg_index_set_launch": (C.c_int, [P, C.c_int, C.c_int]),
     "qg_index_set_tile": (C.c_int, [P, C.c_int]),
+    "qg_index_max_block_warps": (C.c_int, [P]),
     "qg_index_share": (C.c_int, [P, C.POINTER(C.c_void_p)]),
     "qg_index_reserve": (C.c_int, [P, SZ, C.c_int, C.c_int]),
     "qg_search_batch_graph": (C.c_int, [P, P, SZ, P, P, P, P, SZ, P, P, P, P, P]),

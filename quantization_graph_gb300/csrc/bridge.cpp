@@ -364,12 +364,14 @@ bool search_launch_geometry(const qg_index *index, int l_cap, bool stop_model, i
     const int D = static_cast<int>(index->space->code_dim);
     const int tile = search_tile(index);
     int wpb = 0, per_sm = 0;
+    const int wmax = search_max_block_warps(D, tile);
     if (index->launch_wpb > 0) {
-        wpb = index->launch_wpb;
+        wpb = std::min(index->launch_wpb, wmax);  // the override, within this instantiation's block
         per_sm = search_blocks_per_sm(D, l_cap, wpb, stop_model, tile);
         if (index->launch_per_sm > 0 && index->launch_per_sm < per_sm) per_sm = index->launch_per_sm;
     } else {
-        for (int cand : {8, 4, 2}) {
+        for (int cand : {wmax, wmax / 2, wmax / 4}) {
+            if (cand < 1) continue;
             const int b = search_blocks_per_sm(D, l_cap, cand, stop_model, tile);
             if (b * cand > per_sm * wpb) {
                 wpb = cand;
@@ -1652,6 +1654,11 @@ int qg_index_set_launch(qg_index *index, int warps_per_block, int blocks_per_sm)
     index->launch_wpb = warps_per_block;
     index->launch_per_sm = blocks_per_sm;
     return QG_OK;
+}
+
+int qg_index_max_block_warps(const qg_index *index) {
+    if (!index) return 0;
+    return search_max_block_warps(static_cast<int>(index->space->code_dim), search_tile(index));
 }
 
 int qg_index_set_tile(qg_index *index, int tile) {

@@ -46,27 +46,28 @@ struct Lay {
     static constexpr int PG = 4;                    // passes per batch (LPN < 32)
 };
 
-#ifndef QG_SEARCH_MINBLOCKS
-#define QG_SEARCH_MINBLOCKS 2  // 128 registers per thread
-#endif
-#ifndef QG_SEARCH_THREADS
-#define QG_SEARCH_THREADS 256
-#endif
-
 // Tile shape of the gate and traversal loops when one neighbour spans the warp (D >= 1024): how
-// many neighbours' rows a lane keeps in flight, and the registers per thread. Shape 0 (the
-// default; measured fastest at 200k x 1536): 16 MSB chunks per lane in the gate, 2 code rows
-// (8 at D = 1024) in the traversal, 128 registers (16 warps per SM); 1: 8 chunks; 2: 32 chunks;
-// 3: twice the traversal rows; 4: 8 chunks compiled for three 8-warp blocks per SM (at most 85
-// registers, 24 warps per SM). Shapes 1-4 exist for the Int8 / Int4 search at D = 1024 and 2048,
+// many neighbours' rows a lane keeps in flight, and the block size and residency the kernel is
+// compiled for. Shape 0 (the default): 16 MSB chunks per lane in the gate, 2 code rows (8 at
+// D = 1024) in the traversal; 1: 8 chunks; 2: 32 chunks; 3: twice the traversal rows; 4: shape 0
+// at the other residency. Shapes 1-4 exist for the Int8 / Int4 search at D = 1024 and 2048,
 // chosen per index (qg_index_set_tile, the autotuner).
+//
+// Residency: "wide" = blocks of 7 warps, at least 3 per SM, which the compiler meets with 80
+// registers (small spills), 21 warps per SM; otherwise blocks of 8 warps, 2 per SM, 128
+// registers, 16 warps. Measured (10k queries): at D = 2048 (1M x 1536, L = 384) wide is 5.6 %
+// faster (capping the registers with __maxnreg__ instead, at 96 / 88 with the same 21 warps:
+// -2 % / -26 %); at D = 1024 (the 120k x 1024 stream, 4,096-query batch) it is 20 % slower. So
+// shape 0 is wide at D = 2048 only and shape 4 takes the other residency.
 template <int D, int kTile>
 struct Tile {
     static constexpr int CPL = Lay<D>::CPL;
-    static constexpr int chunks = (kTile == 1 || kTile == 4) ? 8 : (kTile == 2 ? 32 : 16);
+    static constexpr int chunks = kTile == 1 ? 8 : (kTile == 2 ? 32 : 16);
     static constexpr int GG = chunks / CPL > 0 ? chunks / CPL : 1;                 // gate group
     static constexpr int GT = (CPL == 1 ? 8 : 2) * (kTile == 3 ? 2 : 1);           // traversal group
-    static constexpr int min_blocks = kTile == 4 ? 3 * 256 / QG_SEARCH_THREADS : QG_SEARCH_MINBLOCKS;
+    static constexpr bool wide = D >= 1024 && ((D == 2048) != (kTile == 4));
+    static constexpr int threads = wide ? 224 : 256;
+    static constexpr int min_blocks = wide ? 3 : 2;
 };
 
 struct WarpSmem {
@@ -919,7 +920,7 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
 }
 
 template <int D, int kMode, int kTile>
-__global__ void __launch_bounds__(QG_SEARCH_THREADS, (Tile<D, kTile>::min_blocks)) search_kernel(SearchArgs a) {
+__global__ void __launch_bounds__((Tile<D, kTile>::threads), (Tile<D, kTile>::min_blocks)) search_kernel(SearchArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
@@ -989,6 +990,12 @@ static cudaError_t launch_d(const SearchArgs &a, int grid, int wpb, cudaStream_t
         }
     }
     return launch_dc<D, 0>(a, grid, wpb, stream);
+}
+
+int search_max_block_warps(int code_dim, int tile) {
+    if (code_dim == 2048) return (tile == 4 ? Tile<2048, 4>::threads : Tile<2048, 0>::threads) / 32;
+    if (code_dim == 1024) return (tile == 4 ? Tile<1024, 4>::threads : Tile<1024, 0>::threads) / 32;
+    return Tile<512, 0>::threads / 32;
 }
 
 size_t search_block_smem(int l_cap, int wpb, bool stop_model) {

@@ -27,12 +27,12 @@ from .space import _cuda, _ptr
 
 def autotune(index, queries: torch.Tensor, k: int, l_value: int, shapes=None, tiles=None, repeats: int = 3,
              log=None):
-    """Pick (warps_per_block, blocks_per_sm, tile) for this index and pool size; returns the timings.
+    """Pick (tile, warps_per_block, blocks_per_sm) for this index and pool size; returns the timings.
 
-    Launch shapes are timed with the default tile; the tile shapes (only where the code dim is at
-    least 1024, where they exist) are then timed with the best launch shape."""
+    The tile shapes (where the code dim is at least 1024, where they exist) are timed with the
+    automatic launch shape, then the launch shapes with the best tile (its block width from
+    qg_index_max_block_warps)."""
     lib = N.load()
-    shapes = shapes or [(8, 0), (4, 0), (2, 0), (8, 1), (4, 2), (4, 1)]
     if tiles is None:
         tiles = [0, 1, 2, 3, 4] if index.space.code_dim >= 1024 else [0]
     q = _cuda(queries, torch.float32)
@@ -40,8 +40,8 @@ def autotune(index, queries: torch.Tensor, k: int, l_value: int, shapes=None, ti
     dists = torch.empty((q.shape[0], k), dtype=torch.float32, device="cuda")
 
     def timed(wpb, per_sm, tile):
-        N.check(lib.qg_index_set_launch(index.handle, wpb, per_sm), "qg_index_set_launch")
         N.check(lib.qg_index_set_tile(index.handle, tile), "qg_index_set_tile")
+        N.check(lib.qg_index_set_launch(index.handle, wpb, per_sm), "qg_index_set_launch")
         index.search_into(q, ids, dists, k=k, l_value=l_value)
         torch.cuda.synchronize()
         start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -52,15 +52,18 @@ def autotune(index, queries: torch.Tensor, k: int, l_value: int, shapes=None, ti
         torch.cuda.synchronize()
         ms = start.elapsed_time(end) / repeats
         if log:
-            log(f"  launch {wpb} warps/block, <= {per_sm or 'max'} blocks/SM, tile {tile}: {ms:.3f} ms")
+            log(f"  tile {tile}, launch {wpb or 'auto'} warps/block, <= {per_sm or 'max'} blocks/SM: {ms:.3f} ms")
         return ms
 
-    results = [((wpb, per_sm, 0), timed(wpb, per_sm, 0)) for wpb, per_sm in shapes]
-    wpb, per_sm, _ = min(results, key=lambda r: r[1])[0]
-    results += [((wpb, per_sm, t), timed(wpb, per_sm, t)) for t in tiles if t != 0]
+    results = [((0, 0, t), timed(0, 0, t)) for t in tiles]
+    tile = min(results, key=lambda r: r[1])[0][2]
+    N.check(lib.qg_index_set_tile(index.handle, tile), "qg_index_set_tile")
+    w = lib.qg_index_max_block_warps(index.handle)
+    shapes = shapes or [(w, 0), (max(1, w // 2), 0), (w, 1), (w, 2), (max(1, w // 2), 2)]
+    results += [((wpb, per_sm, tile), timed(wpb, per_sm, tile)) for wpb, per_sm in shapes]
     best = min(results, key=lambda r: r[1])[0]
-    N.check(lib.qg_index_set_launch(index.handle, best[0], best[1]), "qg_index_set_launch")
     N.check(lib.qg_index_set_tile(index.handle, best[2]), "qg_index_set_tile")
+    N.check(lib.qg_index_set_launch(index.handle, best[0], best[1]), "qg_index_set_launch")
     return best, results
 
 
