@@ -61,7 +61,8 @@ def parse(argv=None):
     ap.add_argument("--k", type=int, default=10)
     ap.add_argument("--target-recall", type=float, default=0.95)
     ap.add_argument("--L", type=int, default=0, help="fixed L (0 = sweep)")
-    ap.add_argument("--tile", type=int, default=0, help="search tile shape (qg_index_set_tile, 0..4)")
+    ap.add_argument("--tile", type=int, default=-1, help="search tile shape (qg_index_set_tile: -1 by index size, 0..4)")
+    ap.add_argument("--launch", default="", help="warps per block and blocks per SM, e.g. 7,3 (qg_index_set_launch)")
     ap.add_argument("--codecs", default="int4,b1,b1main,full,int8_fused",
                     help="query codecs measured beside the Int8 headline on the same index (empty: none)")
     ap.add_argument("--codec-parity-queries", type=int, default=200)
@@ -289,9 +290,12 @@ def build_workload(torch, args, log):
     gt, gt_info = ground_truth(torch, base, queries, args.k)
     gt_info["seconds"] = round(time.time() - t3, 2)
     index = OursIndex(space, compact, residual, msb, factors, deg, edges)
-    if args.tile:
+    if args.tile != -1 or args.launch:
         from quantization_graph_gb300 import _native as N
         N.check(N.load().qg_index_set_tile(index.handle, args.tile), "qg_index_set_tile")
+        if args.launch:
+            wpb, per_sm = (int(x) for x in args.launch.split(","))
+            N.check(N.load().qg_index_set_launch(index.handle, wpb, per_sm), "qg_index_set_launch")
     torch.cuda.empty_cache()
     log(f"setup: data {t1 - t0:.1f}s encode {t_encode:.2f}s graph {t_graph:.1f}s reachable {reach:.4f} "
         f"index {index.device_bytes() / 1e9:.2f} GB; ground truth {gt_info['certified']} certified, "
@@ -797,7 +801,7 @@ def main():
     fixed = {"L": L, "recall@10": round(rec, 4), "qps": round(nq / fixed_ms * 1000.0, 1)}
 
     # learned stop
-    search_info = {"fixed_l": fixed, "mode": "fixed-L", "L": L, "tile": args.tile}
+    search_info = {"fixed_l": fixed, "mode": "fixed-L", "L": L, "tile": args.tile, "launch": args.launch or "auto"}
     run_learned = None
     if not args.no_learned:
         best, table, t_train, run_learned, linfo = learned_stop_select(torch, w, args, L, rec, log)

@@ -384,9 +384,10 @@ int qg_index_max_block_warps(const qg_index *index);
  * 1024 and 2048 (how many neighbours' rows each lane keeps in flight): 0 (the default) 16 MSB
  * chunks per lane and 2 code rows (8 at D = 1024); 1: 8 chunks; 2: 32 chunks; 3: twice the code
  * rows; 4: shape 0 at the other residency (8-warp blocks at 128 registers where shape 0 has
- * 7-warp blocks at 80, as at 2048, and the reverse at 1024). Results are
+ * 7-warp blocks at 80, as at 2048, and the reverse at 1024); -1 (the default): shape 0, except
+ * shape 4 for an index at code dim 2048 of at most four times the L2 size. Results are
  * identical for every shape; only the speed differs. Other codecs and dims ignore it. Used by
- * the autotuner. Returns QG_ERR_INVALID outside 0..4. */
+ * the autotuner. Returns QG_ERR_INVALID outside -1..4. */
 int qg_index_set_tile(qg_index *index, int tile);
 /* Allocate the prepared-query workspace for max_nq queries and the visited tags for the launch
  * shape of pools up to max(max_l, max_k), so that qg_search_batch_graph never allocates. */

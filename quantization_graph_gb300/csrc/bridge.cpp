@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <mutex>
 #include <new>
 #include <random>
@@ -354,10 +355,28 @@ void record_error(const std::string &msg) { set_error(msg); }
 // Warps per block and resident blocks per SM for a pool of l_cap entries: the caller's override
 // (qg_index_set_launch) clamped to what is resident, else the candidate with the most resident
 // warps (large pools need more shared memory per warp, where smaller blocks pack better).
+static size_t l2_bytes(int device) {
+    static std::mutex mu;
+    static std::map<int, size_t> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    const auto it = cache.find(device);
+    if (it != cache.end()) return it->second;
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrL2CacheSize, device) != cudaSuccess) v = 0;
+    cache[device] = static_cast<size_t>(v);
+    return static_cast<size_t>(v);
+}
+
 // The tile shape the search launches with: the index's for the Int8 / Int4 search at code dims of
-// 1024 and more (the instantiations that have shapes), else the default.
+// 1024 and more (the instantiations that have shapes), else the default. Unset (-1) at D = 2048:
+// shape 0 (80 registers, 24 warps per SM) for an index of more than four times the L2, where the
+// extra warps hide the DRAM latency (1M x 1536: +6 % over shape 4); shape 4 (128 registers, 16
+// warps) for a smaller one, which the L2 mostly holds (100k x 1536: +30 % over shape 0).
 static int search_tile(const qg_index *index) {
-    return (space_search_mode(index->space) == 0 && index->space->code_dim >= 1024) ? index->tile : 0;
+    if (space_search_mode(index->space) != 0 || index->space->code_dim < 1024) return 0;
+    if (index->tile >= 0) return index->tile;
+    if (index->space->code_dim == 2048) return index->device_bytes > 4 * l2_bytes(index->device) ? 0 : 4;
+    return 0;
 }
 
 bool search_launch_geometry(const qg_index *index, int l_cap, bool stop_model, int *wpb_out, int *per_sm_out) {
@@ -1662,8 +1681,8 @@ int qg_index_max_block_warps(const qg_index *index) {
 }
 
 int qg_index_set_tile(qg_index *index, int tile) {
-    if (!index || tile < 0 || tile > 4) {
-        set_error("tile shape must be 0..4");
+    if (!index || tile < -1 || tile > 4) {
+        set_error("tile shape must be -1 (by index size) or 0..4");
         return QG_ERR_INVALID;
     }
     index->tile = tile;

@@ -109,7 +109,7 @@ struct qg_index {
     size_t device_bytes = 0;
     int launch_wpb = 0;      // qg_index_set_launch override (0 = automatic)
     int launch_per_sm = 0;
-    int tile = 0;            // qg_index_set_tile: the search's tile shape
+    int tile = -1;           // qg_index_set_tile: the search's tile shape (-1: chosen by index size)
     // the payload and adjacency allocations, shared by the handles qg_index_share makes and freed
     // with the last of them; the scratch above belongs to this handle alone
     std::shared_ptr<qg::DeviceBlocks> payload;

@@ -53,12 +53,14 @@ struct Lay {
 // at the other residency. Shapes 1-4 exist for the Int8 / Int4 search at D = 1024 and 2048,
 // chosen per index (qg_index_set_tile, the autotuner).
 //
-// Residency: "wide" = blocks of 7 warps, at least 3 per SM, which the compiler meets with 80
-// registers (small spills), 21 warps per SM; otherwise blocks of 8 warps, 2 per SM, 128
-// registers, 16 warps. Measured (10k queries): at D = 2048 (1M x 1536, L = 384) wide is 5.6 %
-// faster (capping the registers with __maxnreg__ instead, at 96 / 88 with the same 21 warps:
-// -2 % / -26 %); at D = 1024 (the 120k x 1024 stream, 4,096-query batch) it is 20 % slower. So
-// shape 0 is wide at D = 2048 only and shape 4 takes the other residency.
+// Residency: "wide" = compiled for blocks of up to 7 warps with at least 3 resident per SM, which
+// the compiler meets with 80 registers (small spills); the launch geometry then packs 3-warp
+// blocks 8 to an SM, 24 warps. Otherwise blocks of up to 8 warps, 2 per SM, 128 registers, 16
+// warps. Measured (10k queries at 1M x 1536, L = 384): wide with 3-warp blocks 259k QPS, wide
+// with 7-warp blocks (21 warps) 234k, the other 244k; capping the registers with __maxnreg__
+// instead, at 96 / 88 with 21 warps: 240k / 181k. On indexes the L2 mostly holds (100k x 1536,
+// and the 120k x 1024 stream) the 128-register build is 20-30 % faster. So shape 0 is wide at
+// D = 2048 only, shape 4 takes the other residency, and an unset shape is chosen by index size.
 template <int D, int kTile>
 struct Tile {
     static constexpr int CPL = Lay<D>::CPL;
