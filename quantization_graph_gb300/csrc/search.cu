@@ -61,6 +61,13 @@ struct Lay {
 // instead, at 96 / 88 with 21 warps: 240k / 181k. On indexes the L2 mostly holds (100k x 1536,
 // and the 120k x 1024 stream) the 128-register build is 20-30 % faster. So shape 0 is wide at
 // D = 2048 only, shape 4 takes the other residency, and an unset shape is chosen by index size.
+#ifndef QG_WIDE_THREADS
+#define QG_WIDE_THREADS 224
+#endif
+#ifndef QG_WIDE_MINBLOCKS
+#define QG_WIDE_MINBLOCKS 3
+#endif
+
 template <int D, int kTile>
 struct Tile {
     static constexpr int CPL = Lay<D>::CPL;
@@ -68,8 +75,8 @@ struct Tile {
     static constexpr int GG = chunks / CPL > 0 ? chunks / CPL : 1;                 // gate group
     static constexpr int GT = (CPL == 1 ? 8 : 2) * (kTile == 3 ? 2 : 1);           // traversal group
     static constexpr bool wide = D >= 1024 && ((D == 2048) != (kTile == 4));
-    static constexpr int threads = wide ? 224 : 256;
-    static constexpr int min_blocks = wide ? 3 : 2;
+    static constexpr int threads = wide ? QG_WIDE_THREADS : 256;
+    static constexpr int min_blocks = wide ? QG_WIDE_MINBLOCKS : 2;
 };
 
 struct WarpSmem {
