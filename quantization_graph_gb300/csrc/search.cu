@@ -48,9 +48,9 @@ struct Lay {
 
 // Tile shape of the gate and traversal loops when one neighbour spans the warp (D >= 1024): how
 // many neighbours' rows a lane keeps in flight, and the block size and residency the kernel is
-// compiled for. Shape 0 (the default): 16 MSB chunks per lane in the gate, 2 code rows (8 at
-// D = 1024) in the traversal; 1: 8 chunks; 2: 32 chunks; 3: twice the traversal rows; 4: shape 0
-// at the other residency. Shapes 1-4 exist for the Int8 / Int4 search at D = 1024 and 2048,
+// compiled for. Shape 0 (the default): 16 MSB chunks per lane in the gate, 2 code rows in the
+// traversal (4 in the wide build at D = 2048, 8 at D = 1024); 1: 8 chunks; 2: 32 chunks; 3: twice
+// the traversal rows; 4: shape 0 at the other residency. Shapes 1-4 exist for the Int8 / Int4 search at D = 1024 and 2048,
 // chosen per index (qg_index_set_tile, the autotuner).
 //
 // Residency: "wide" = compiled for blocks of up to 7 warps with at least 3 resident per SM, which
@@ -73,8 +73,9 @@ struct Tile {
     static constexpr int CPL = Lay<D>::CPL;
     static constexpr int chunks = kTile == 1 ? 8 : (kTile == 2 ? 32 : 16);
     static constexpr int GG = chunks / CPL > 0 ? chunks / CPL : 1;                 // gate group
-    static constexpr int GT = (CPL == 1 ? 8 : 2) * (kTile == 3 ? 2 : 1);           // traversal group
     static constexpr bool wide = D >= 1024 && ((D == 2048) != (kTile == 4));
+    // traversal group: 4 code rows in the wide build at D = 2048 (1 % faster there than 2)
+    static constexpr int GT = (CPL == 1 ? 8 : (wide ? 4 : 2)) * (kTile == 3 ? 2 : 1);
     static constexpr int threads = wide ? QG_WIDE_THREADS : 256;
     static constexpr int min_blocks = wide ? QG_WIDE_MINBLOCKS : 2;
 };
