@@ -63,6 +63,10 @@ def parse(argv=None):
     ap.add_argument("--L", type=int, default=0, help="fixed L (0 = sweep)")
     ap.add_argument("--tile", type=int, default=-1, help="search tile shape (qg_index_set_tile: -1 by index size, 0..4)")
     ap.add_argument("--launch", default="", help="warps per block and blocks per SM, e.g. 7,3 (qg_index_set_launch)")
+    ap.add_argument("--inflight", type=int, default=2,
+                    help="timed steps in flight: step s runs on handle s mod N (qg_index_share: the same resident "
+                         "index, search scratch of its own) and a stream of its own, so the next batch takes the "
+                         "SMs the last queries of the previous one leave idle; 1 = one step after another")
     ap.add_argument("--codecs", default="int4,b1,b1main,full,int8_fused",
                     help="query codecs measured beside the Int8 headline on the same index (empty: none)")
     ap.add_argument("--codec-parity-queries", type=int, default=200)
@@ -516,6 +520,27 @@ def device_ms(torch, fn, steps):
     return start.elapsed_time(end) / steps
 
 
+def pipelined_ms(torch, fns, streams, steps):
+    """Mean device time per step, step s issued by fns[s % n] on streams[s % n]: CUDA events on the
+    current stream, which every stream waits on before the first step and which waits on every
+    stream after the last, so the region covers all steps of all streams."""
+    cur = torch.cuda.current_stream()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record(cur)
+    for st in streams:
+        st.wait_event(start)
+    for i in range(steps):
+        j = i % len(fns)
+        with torch.cuda.stream(streams[j]):
+            fns[j]()
+    for st in streams:
+        cur.wait_stream(st)
+    end.record(cur)
+    torch.cuda.synchronize()
+    return start.elapsed_time(end) / steps
+
+
 def stats_struct(stats, nq):
     names = ("visited_nodes", "distance_computations", "hops", "paper_checked", "paper_would_prune",
              "paper_not_pruned", "paper_full_saved", "paper_msb_kernel_calls", "paper_remaining_kernel_calls")
@@ -597,8 +622,8 @@ def learned_stop_select(torch, w, args, L_fixed, rec_fixed, log):
                 f"{r_['knob']}: {r_['recall']:.4f}/{r_['qps']:.0f}" for r_ in table
                 if r_["L"] == L and r_["model"] == name))
 
-    def run(qq, ids_out, dists_out, stats_out=None):
-        ls.search(index, qq, models[best["model"]], best["knob"], k=args.k, l_value=best["L"], ids_out=ids_out,
+    def run(qq, ids_out, dists_out, stats_out=None, idx=index):
+        ls.search(idx, qq, models[best["model"]], best["knob"], k=args.k, l_value=best["L"], ids_out=ids_out,
                   dists_out=dists_out, stats_out=stats_out)
 
     info = {"oracle_stop_hop_fraction": round(oracle_frac, 4), "train_L": L_train}
@@ -820,11 +845,11 @@ def main():
         if search_info["mode"] != "learned-stop":
             run_learned = None
 
-    def step(qq, ids_out, dists_out, stats_out=None):
+    def step(qq, ids_out, dists_out, stats_out=None, idx=index):
         if run_learned is not None:
-            run_learned(qq, ids_out, dists_out, stats_out)
+            run_learned(qq, ids_out, dists_out, stats_out, idx=idx)
         else:
-            index.search_into(qq, ids_out, dists_out, k=args.k, l_value=L, stats_out=stats_out)
+            idx.search_into(qq, ids_out, dists_out, k=args.k, l_value=L, stats_out=stats_out)
 
     # counters of the chosen mode over the whole batch, for the algorithmic bytes and the recall
     step(q, ids, dists, stats)
@@ -832,36 +857,55 @@ def main():
     final_recall = recall_at(ids.to(torch.int64), w["gt"], args.k)
     alg_bytes = algorithmic_bytes(stats_struct(stats, nq), D, args.M, 100, args.k)
 
-    # the timed region: this rank's query range
-    ids_l = torch.empty((nl, args.k), dtype=torch.int32, device="cuda")
-    d_l = torch.empty((nl, args.k), dtype=torch.float32, device="cuda")
-    for _ in range(args.warmup):
-        step(ql, ids_l, d_l)
-    prep_ms = device_ms(torch, lambda: w["space"].prepare(ql), args.steps)
+    # the timed region: this rank's query range, `inflight` batches in flight (a handle on the
+    # same resident index, outputs and a stream per slot)
+    nf = max(1, args.inflight)
+    handles = [index] + [index.share() for _ in range(nf - 1)]
+    streams = [torch.cuda.Stream() for _ in range(nf)]
+    ids_l = [torch.empty((nl, args.k), dtype=torch.int32, device="cuda") for _ in range(nf)]
+    d_l = [torch.empty((nl, args.k), dtype=torch.float32, device="cuda") for _ in range(nf)]
     hq = ql.cpu().pin_memory()
-    hid = torch.empty((nl, args.k), dtype=torch.int32).pin_memory()
-    hd = torch.empty((nl, args.k), dtype=torch.float32).pin_memory()
-    dq = torch.empty_like(ql)
+    hid = [torch.empty((nl, args.k), dtype=torch.int32).pin_memory() for _ in range(nf)]
+    hd = [torch.empty((nl, args.k), dtype=torch.float32).pin_memory() for _ in range(nf)]
+    dq = [torch.empty_like(ql) for _ in range(nf)]
 
-    def e2e_step():
-        dq.copy_(hq, non_blocking=True)
-        step(dq, ids_l, d_l)
-        hid.copy_(ids_l, non_blocking=True)
-        hd.copy_(d_l, non_blocking=True)
+    def device_step(j):
+        return lambda: step(ql, ids_l[j], d_l[j], idx=handles[j])
+
+    def e2e_step(j):
+        def fn():
+            dq[j].copy_(hq, non_blocking=True)
+            step(dq[j], ids_l[j], d_l[j], idx=handles[j])
+            hid[j].copy_(ids_l[j], non_blocking=True)
+            hd[j].copy_(d_l[j], non_blocking=True)
+        return fn
+
+    dev_fns = [device_step(j) for j in range(nf)]
+    e2e_fns = [e2e_step(j) for j in range(nf)]
+    for fns in (dev_fns, e2e_fns):  # every handle's scratch settled before the timed region
+        pipelined_ms(torch, fns, streams, max(args.warmup, nf))
+    for _ in range(args.warmup):
+        step(ql, ids_l[0], d_l[0])
+    prep_ms = device_ms(torch, lambda: w["space"].prepare(ql), args.steps)
 
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
-        step_ms = device_ms(torch, lambda: step(ql, ids_l, d_l), args.steps)
-        e2e_ms = device_ms(torch, e2e_step, args.steps)
+        # one launch at a time: the search kernel's own duration, for the roofline
+        seq_ms = device_ms(torch, dev_fns[0], args.steps)
+        step_ms = pipelined_ms(torch, dev_fns, streams, args.steps)
+        e2e_ms = pipelined_ms(torch, e2e_fns, streams, args.steps)
     if world > 1:
         dist.barrier()
+    seq_ms = replica_aggregate(seq_ms, seq_ms, nq, world)[0]
     step_ms, e2e_ms, value, e2e_value = replica_aggregate(step_ms, e2e_ms, nq, world)
-    ok = bool((hid.to(torch.int64).cuda() == ids_l.to(torch.int64)).all())
+    ok = all(bool((hid[j].to(torch.int64).cuda() == ids_l[j].to(torch.int64)).all()) and
+             bool((ids_l[j] == ids_l[0]).all()) for j in range(min(nf, args.steps)))
+    ids_l = ids_l[0]
     gathered = gather_shards(ids_l, nq, world)
     sharded_recall = recall_at(gathered.to(torch.int64), w["gt"], args.k)
-    search_ms = max(step_ms - prep_ms, 1e-6)
+    search_ms = max(seq_ms - prep_ms, 1e-6)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -885,7 +929,12 @@ def main():
         if world == 1 and args.codecs:
             search_info["codecs"] = codec_ablation(torch, w, args, log)
     search_info.update({"recall@10": round(final_recall, 4), "recall@10_gathered_shards": round(sharded_recall, 4),
-                        "queries_per_rank": nl, "l_sweep": {str(k_): round(v, 4) for k_, v in sweep.items()}})
+                        "queries_per_rank": nl, "l_sweep": {str(k_): round(v, 4) for k_, v in sweep.items()},
+                        "inflight": nf,
+                        "one_at_a_time": {"ms_per_step": round(seq_ms, 3), "qps": round(nq / seq_ms * 1000.0, 1)},
+                        "timing": (f"value and e2e: {args.steps} steps of {nl} queries, {nf} in flight (a handle on "
+                                   "the same resident index and a stream each, step s on slot s mod "
+                                   f"{nf}); the roofline's kernel time: the same steps one at a time")})
     line = {"metric": metric, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int8/f32", "data": "synthetic", "config": config,
