@@ -673,8 +673,10 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                 }
                 __syncwarp();
                 // survivors whose gate was invalid use the full FP32 restore (mode 0)
-                if constexpr (kMode != 2)
-                    for (int i = 0; i < S; ++i) any_full |= s.fval[s.sslot[i]] == 0;
+                if constexpr (kMode != 2) {
+                    for (int i = lane; i < S; i += 32) any_full |= s.fval[s.sslot[i]] == 0;
+                    any_full = __any_sync(0xffffffffu, any_full);
+                }
                 if (any_full) {
                     for (int i = 0; i < S; ++i) {
                         if (s.fval[s.sslot[i]]) continue;
@@ -738,6 +740,9 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                     pos = sb + 1024;
                 }
                 const int newn = pn + 1 < lval ? pn + 1 : lval;
+                // shift (pos, newn) up by one, 32 entries per pass from the top: a pass reads
+                // (top - 32, top - 1] and writes (top - 31, top]; the next pass writes entry top - 32
+                // only after its own __syncwarp, which every lane reaches after this pass's reads
                 for (int top = newn - 1; top > pos; top -= 32) {
                     const int e = top - lane;
                     float vd = 0.0f, vl = 0.0f;
@@ -754,8 +759,8 @@ __device__ void search_one(const SearchArgs &a, const WarpSmem &s, int q, int la
                         s.pid[e] = vi;
                         s.plb[e] = vl;
                     }
-                    __syncwarp();
                 }
+                __syncwarp();
                 if (lane == 0) {
                     s.pd[pos] = d;
                     s.pid[pos] = id;
