@@ -244,6 +244,10 @@ def graph_desc(args) -> str:
 def workload_config(args) -> dict:
     """The workload both arms run (identical in their JSON lines): data, index and search knobs."""
     metric = METRIC
+    if (args.n, args.dim) != (1_000_000, 1536):  # another size: the metric names it
+        size = f"{args.n // 1_000_000}M" if args.n % 1_000_000 == 0 else (
+            f"{args.n // 1000}k" if args.n % 1000 == 0 else str(args.n))
+        metric = METRIC.replace("1M×1536", f"{size}×{args.dim}")
     data_desc = f"{args.n} x {args.dim} unit-norm anisotropic (lambda_i ~ i^-0.8)"
     if args.workload == "gist960":
         metric = "QPS@recall10=0.95, 1M×960 4-bit, fixed-L beam, 1 GB300"
