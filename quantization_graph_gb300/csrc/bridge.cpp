@@ -389,7 +389,8 @@ bool search_launch_geometry(const qg_index *index, int l_cap, bool stop_model, i
         per_sm = search_blocks_per_sm(D, l_cap, wpb, stop_model, tile);
         if (index->launch_per_sm > 0 && index->launch_per_sm < per_sm) per_sm = index->launch_per_sm;
     } else {
-        for (int cand : {wmax, wmax / 2, wmax / 4}) {
+        // the most warps per SM; a tie keeps the earlier candidate
+        for (int cand : {search_first_block_warps(D, tile), wmax, wmax / 2, wmax / 4}) {
             if (cand < 1) continue;
             const int b = search_blocks_per_sm(D, l_cap, cand, stop_model, tile);
             if (b * cand > per_sm * wpb) {

@@ -138,6 +138,8 @@ size_t search_smem_per_warp(int code_dim, int l_cap);
 int search_blocks_per_sm(int code_dim, int l_cap, int warps_per_block, bool stop_model = false, int tile = 0);
 // The widest block the search kernel for this code dim and tile shape is compiled for, in warps.
 int search_max_block_warps(int code_dim, int tile);
+// The block width the automatic launch shape tries first (0: none), ahead of the widest.
+int search_first_block_warps(int code_dim, int tile);
 size_t search_block_smem(int l_cap, int warps_per_block, bool stop_model);
 int search_supported_dim(int code_dim);
 cudaError_t launch_encode(const EncodeArgs &a, cudaStream_t stream);

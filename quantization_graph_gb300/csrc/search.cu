@@ -1013,6 +1013,12 @@ int search_max_block_warps(int code_dim, int tile) {
     return Tile<512, 0>::threads / 32;
 }
 
+// Block width the automatic launch shape tries first: 2 warps for the 24-warp build at D = 2048.
+// It ties with 3-warp blocks on warps per SM, and with a second launch queued behind this one a
+// smaller block frees its slots sooner (1M x 1536, two 10k-query launches in flight: 273k QPS
+// against 268k; one launch at a time the same; 1-warp blocks 251k). 0 (none) otherwise.
+int search_first_block_warps(int code_dim, int tile) { return code_dim == 2048 && tile != 4 ? 2 : 0; }
+
 size_t search_block_smem(int l_cap, int wpb, bool stop_model) {
     return warp_smem_bytes(l_cap) * static_cast<size_t>(wpb) + (stop_model ? kMlpSmemBytes : 0);
 }
