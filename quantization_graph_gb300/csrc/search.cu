@@ -54,8 +54,8 @@ struct Lay {
 // chosen per index (qg_index_set_tile, the autotuner).
 //
 // Residency: "wide" = compiled for blocks of up to 7 warps with at least 3 resident per SM, which
-// the compiler meets with 80 registers (small spills); the launch geometry then packs 3-warp
-// blocks 8 to an SM, 24 warps. Otherwise blocks of up to 8 warps, 2 per SM, 128 registers, 16
+// the compiler meets with 80 registers (small spills); the launch geometry then packs 24 warps
+// to an SM (2-warp blocks at D = 2048, see search_first_block_warps). Otherwise blocks of up to 8 warps, 2 per SM, 128 registers, 16
 // warps. Measured (10k queries at 1M x 1536, L = 384): wide with 3-warp blocks 259k QPS, wide
 // with 7-warp blocks (21 warps) 234k, the other 244k; capping the registers with __maxnreg__
 // instead, at 96 / 88 with 21 warps: 240k / 181k. On indexes the L2 mostly holds (100k x 1536,
