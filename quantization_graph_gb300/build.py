@@ -50,7 +50,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(INCLUDE, "qgraph_gb300.h"))
-    common = ["-std=c++17", "-O3", "-I", INCLUDE, "-I", CSRC] + os.environ.get("QG_NVCC_DEFINES", "").split()
+    common = ["-std=c++17", "-O3", "-I", INCLUDE, "-I", CSRC]
     jobs = []
     objs = []
     for src in CUDA_SOURCES:

@@ -55,19 +55,12 @@ struct Lay {
 //
 // Residency: "wide" = compiled for blocks of up to 7 warps with at least 3 resident per SM, which
 // the compiler meets with 80 registers (small spills); the launch geometry then packs 24 warps
-// to an SM (2-warp blocks at D = 2048, see search_first_block_warps). Otherwise blocks of up to 8 warps, 2 per SM, 128 registers, 16
-// warps. Measured (10k queries at 1M x 1536, L = 384): wide with 3-warp blocks 259k QPS, wide
+// to an SM (2-warp blocks at D = 2048, see search_first_block_warps). Otherwise blocks of up to
+// 8 warps, 2 per SM, 128 registers, 16 warps. Measured (10k queries at 1M x 1536, L = 384): wide with 3-warp blocks 259k QPS, wide
 // with 7-warp blocks (21 warps) 234k, the other 244k; capping the registers with __maxnreg__
 // instead, at 96 / 88 with 21 warps: 240k / 181k. On indexes the L2 mostly holds (100k x 1536,
 // and the 120k x 1024 stream) the 128-register build is 20-30 % faster. So shape 0 is wide at
 // D = 2048 only, shape 4 takes the other residency, and an unset shape is chosen by index size.
-#ifndef QG_WIDE_THREADS
-#define QG_WIDE_THREADS 224
-#endif
-#ifndef QG_WIDE_MINBLOCKS
-#define QG_WIDE_MINBLOCKS 3
-#endif
-
 template <int D, int kTile>
 struct Tile {
     static constexpr int CPL = Lay<D>::CPL;
@@ -76,8 +69,8 @@ struct Tile {
     static constexpr bool wide = D >= 1024 && ((D == 2048) != (kTile == 4));
     // traversal group: 4 code rows in the wide build at D = 2048 (1 % faster there than 2)
     static constexpr int GT = (CPL == 1 ? 8 : (wide ? 4 : 2)) * (kTile == 3 ? 2 : 1);
-    static constexpr int threads = wide ? QG_WIDE_THREADS : 256;
-    static constexpr int min_blocks = wide ? QG_WIDE_MINBLOCKS : 2;
+    static constexpr int threads = wide ? 224 : 256;
+    static constexpr int min_blocks = wide ? 3 : 2;
 };
 
 struct WarpSmem {
